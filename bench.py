@@ -1,0 +1,331 @@
+"""Benchmark of the GB300 WCSPH step (one JSON line on stdout).
+
+Workload: ``obstacle_1m`` — 1,048,576 FP32 particles (128 x 128 x 64 jittered lattice, spacing
+0.0075 m, h = 0.015 m) in a 2 x 1 x 1 m box with a sphere obstacle (r = 0.2 m, 128^3 volume map),
+dt = 1e-4. A step is one WCSPH substep of every particle (key, sort, cells + reorder, boundary +
+density, pressure + viscosity + integration).
+
+* ``value``  particle-steps/s with the state resident in HBM, device-timed with CUDA events per
+  step on the launching stream; L2 is flushed (256 MiB write) between timed steps.
+* ``e2e``    the same metric through the public C ABI with host buffers: per step the state is
+  uploaded from pinned memory (set_particle_state), one substep runs, and positions, velocities
+  and densities are read back (copy_data_buffers); wall-clock over the K steps.
+* ``roofline`` the dominant kernel's algorithmic bytes per launch / its mean event-timed duration
+  against the measured HBM copy bandwidth.
+* ``cpu_baseline`` the oracle (the project's restatement of the reference's shader math) on the
+  host's cores, on a bounded sample of the same workload.
+
+``--impl reference`` times that CPU restatement alone, on every host thread (the reference's own
+Vulkan pipeline has no runnable form here: no Vulkan stack or software renderer exists).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "particle-steps/s @1M (plain vs batched vs fwd+adjoint, 1e-5 rel), % HBM roofline"
+UNIT = "particle-steps/s"
+# Algorithmic HBM bytes per particle-step and per pass (compulsory traffic between the passes'
+# global dependencies, float3 fields): key 16, sort 12, cell starts 8, reorder 52,
+# density + boundary 28, force + integrate 64.
+B_STEP = 180
+B_PHASE = {"keys": 16, "sort": 12, "cells_reorder": 60, "density": 28, "force": 64}
+FLUSH_BYTES = 256 << 20
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.out = self.proc.communicate(timeout=5)[0]
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                self.out = ""
+        else:
+            self.out = ""
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in (self.out or "").splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def oracle_for_workload(w, model=None):
+    """CPU oracle of the workload; boundary grids from the GPU model or built on the CPU."""
+    from oracle import binding as ob
+
+    o = ob.OracleModel(ob.params_from(w.sim, w.sph, w.wcsph), w.n)
+    if model is not None:
+        for i in range(model.n_boundary_objects):
+            o.add_object(model.get_boundary_object(i))
+    else:
+        for a in w.objects:
+            bs, bp, sdf, vm = ob.volume_map(a.shape, a.params, w.sim.smooth_radius, a.resolution,
+                                            np.float32(8.0 * w.sim.smooth_radius))
+            T = np.eye(4, dtype=np.float32)
+            T[:3, 3] = -np.asarray(a.position, np.float32)
+            o.add_object(type("Obj", (), dict(
+                transform=T.T.ravel(), rotation=np.eye(4, dtype=np.float32).ravel(),
+                box_size=bs, box_pos=bp, resolution=tuple(a.resolution), sdf=sdf,
+                volume_map=vm)))
+    o.set_state(w.pos, w.vel)
+    return o
+
+
+def time_cpu(w, model=None, budget_s=12.0, max_steps=200, threads=None):
+    from oracle import binding as ob
+
+    if threads:
+        ob.set_threads(threads)
+    o = oracle_for_workload(w, model)
+    o.substeps(1)  # warm-up
+    steps, t0 = 0, time.perf_counter()
+    while steps < max_steps:
+        o.substeps(1)
+        steps += 1
+        if time.perf_counter() - t0 >= budget_s and steps >= 2:
+            break
+    dt = time.perf_counter() - t0
+    return {"value": w.n * steps / dt, "unit": UNIT, "cores": ob.get_threads(), "kind": "port",
+            "sample": f"{w.name}: {steps} substeps of {w.n} particles after 1 warm-up substep "
+                      f"({dt:.1f} s wall)"}
+
+
+def run_reference(args):
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return
+    from vkfluidsim_gb300 import workloads as W
+
+    w = W.obstacle_1m()
+    cpu = time_cpu(w, None, budget_s=args.cpu_budget, threads=os.cpu_count())
+    line = {"metric": METRIC, "value": cpu["value"], "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * w.n / cpu["value"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic: seeded jittered lattice", "impl": "reference",
+            "config": {"workload": w.name, "particles": w.n},
+            "cpu_baseline": cpu,
+            "e2e": {"value": cpu["value"], "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0},
+            "note": "the reference's own compute path is Vulkan/Slang and cannot run on this box "
+                    "(no Vulkan stack or software renderer); this is the project's CPU restatement "
+                    "of its shader math (oracle), OpenMP on all host threads"}
+    print(json.dumps(line), flush=True)
+
+
+def run_gpu(args):
+    import torch
+
+    from vkfluidsim_gb300 import workloads as W
+
+    world, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    w = W.obstacle_1m(seed=1 + rank)
+    m = W.build_model(w)
+    m.set_stream(stream.cuda_stream)
+    n = w.n
+    flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            import torch.distributed as dist
+
+            dist.barrier()
+
+    # Warm-up (graph capture happens in the first substep).
+    for _ in range(args.warmup):
+        m.substeps(1)
+    barrier()
+
+    # ---- value: device-timed substeps, L2 flushed between steps.
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    with ClockSampler(local) as clk:
+        t_wall0 = time.perf_counter()
+        for k in range(args.steps):
+            flush.zero_()
+            starts[k].record(stream)
+            m.substeps(1)
+            ends[k].record(stream)
+        barrier()
+        t_wall = time.perf_counter() - t_wall0
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    total_ms = sum(step_ms)
+    if world > 1:
+        import torch.distributed as dist
+
+        t = torch.tensor([total_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = world * n * args.steps / (total_ms / 1e3)
+    ms_per_step = total_ms / args.steps
+
+    # ---- per-kernel timing (same stream, CUDA events between the passes).
+    prof = m.profile_substeps(max(3, min(args.steps, 10)))
+    digits, items, passes = m.get_sort_config()
+    kernel_phases = {k: v for k, v in prof.items() if k in B_PHASE}
+    dom = max(kernel_phases, key=kernel_phases.get)
+    hbm, peak_kind = peaks()
+    achieved = B_PHASE[dom] * n / (kernel_phases[dom] * 1e-3) / 1e9
+    traffic = None
+    tfile = ROOT / "profiles" / "ncu_traffic.json"
+    if tfile.exists():
+        t = json.loads(tfile.read_text())
+        per = t.get("bytes_per_particle", {}).get(dom)
+        if per is not None:
+            traffic = per * n
+
+    # ---- e2e through the C ABI with pinned host buffers.
+    s0 = m.copy_data_buffers()
+    hp = torch.empty((n, 3), dtype=torch.float32, pin_memory=True)
+    hv = torch.empty((n, 3), dtype=torch.float32, pin_memory=True)
+    hd = torch.empty((n,), dtype=torch.float32, pin_memory=True)
+    hp.numpy()[:] = s0["positions"]
+    hv.numpy()[:] = s0["velocities"]
+    lib = m._lib
+    import ctypes as C
+
+    fp = lambda t_: C.cast(C.c_void_p(t_.data_ptr()), C.POINTER(C.c_float))  # noqa: E731
+    from vkfluidsim_gb300._abi import check
+
+    for _ in range(2):
+        check(lib.vfs_model_set_particle_state(m._h, fp(hp), fp(hv), 0, n))
+        check(lib.vfs_model_substeps(m._h, 1))
+        check(lib.vfs_model_copy_data_buffers(m._h, fp(hp), fp(hv), fp(hd), None))
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        check(lib.vfs_model_set_particle_state(m._h, fp(hp), fp(hv), 0, n))
+        check(lib.vfs_model_substeps(m._h, 1))
+        check(lib.vfs_model_copy_data_buffers(m._h, fp(hp), fp(hv), fp(hd), None))
+    barrier()
+    e2e_s = time.perf_counter() - t0
+    if world > 1:
+        import torch.distributed as dist
+
+        t = torch.tensor([e2e_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e = {"value": world * n * args.steps / e2e_s, "unit": UNIT,
+           "h2d_bytes_per_step": 24 * n, "d2h_bytes_per_step": 28 * n}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cpu = time_cpu(w, m, budget_s=args.cpu_budget)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic: seeded jittered lattice (no dataset exists for this path)",
+            "config": {"workload": w.name, "particles": n, "h": w.sim.smooth_radius,
+                       "dt": w.sph.fixed_dt, "boundary": "sphere r=0.2, 128^3 volume map",
+                       "l2": "flushed between timed steps (256 MiB write)",
+                       "sort": {"digit_bits": digits, "tile_items": items, "passes": passes},
+                       "cuda_graph": True, "parallelism": f"replicas x{world}"},
+            "e2e": e2e,
+            "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm,
+                         "unit": "GB/s", "frac": achieved / hbm, "peak_kind": peak_kind,
+                         "algorithmic_bytes_per_launch": B_PHASE[dom] * n, "traffic": traffic},
+            "step_roofline": {"bytes_per_particle_step": B_STEP,
+                              "achieved_gbs": B_STEP * n / (ms_per_step * 1e-3) / 1e9,
+                              "frac": B_STEP * n / (ms_per_step * 1e-3) / 1e9 / hbm},
+            "phase_ms": prof,
+            "gpu_launches": (4 + passes) * args.steps,
+            "clocks": clk.summary(),
+            "wall_s_timed_region": t_wall,
+        }
+        if cpu:
+            line["cpu_baseline"] = cpu
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--cpu-budget", type=float, default=12.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,215 @@
+/* vfs_cuda.h — C ABI of the GB300-native WCSPH step (VkFluidSim's WCSPHWithBoundaryModel).
+ *
+ * Plain C types only: host pointers, sizes, an opaque handle and an int status. No call throws.
+ * Every entry point names the reference interface it replaces (paths are relative to the
+ * VkFluidSim source tree). One handle serves one host thread at a time; work is enqueued on the
+ * handle's CUDA stream (vfs_model_set_stream) and host-visible results are returned after the
+ * stream has been synchronised.
+ *
+ * Vectors on the host are packed float3 (12 bytes per particle, the reference's scalar layout).
+ * Particle arrays are in the model's current (sorted) order; ids[] map them back to the order in
+ * which they were first set (the reference permutes positions and velocities in place every
+ * substep and keeps no ids: src/models/model.cpp:210-223).
+ */
+#ifndef VFS_CUDA_H
+#define VFS_CUDA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes (the reference aborts through VK_CHECK, src/gfx/common.h:20-29) ---- */
+#define VFS_OK 0
+#define VFS_ERR_INVALID_ARGUMENT 1
+#define VFS_ERR_CUDA 2
+#define VFS_ERR_OUT_OF_MEMORY 3
+#define VFS_ERR_IO 4
+#define VFS_ERR_PARSE 5
+#define VFS_ERR_CAPACITY 6
+#define VFS_ERR_DEVICE_CHECK 7 /* a kernel reported an error word (e.g. look-back timeout) */
+#define VFS_ERR_NOT_READY 8
+
+typedef struct vfs_model vfs_model;
+
+/* SimulationParameters, src/simulation.h:10-13 (defaults g = (0,-9.81,0), h = 0.2,
+ * src/simulation.cpp:20-27). */
+typedef struct vfs_sim_params {
+    float gravity[3];
+    float smooth_radius;
+} vfs_sim_params;
+
+/* SPHModel::Parameters, src/models/model.h:14-21 (gfx::BoundingBox is {size, pos},
+ * src/gfx/mesh.h:13-16). n_particles is the model capacity. */
+typedef struct vfs_sph_params {
+    float time_scale;
+    int32_t iterations;
+    int32_t n_particles;
+    float fixed_dt;
+    float target_density;
+    float bbox_size[3];
+    float bbox_pos[3];
+} vfs_sph_params;
+
+/* WCSPHWithBoundaryModel::Parameters, src/models/wcsph_with_boundary_model.h:26-33
+ * (defaults 1e4, 1000, 7, 0.01: src/models/wcsph_with_boundary_model.cpp:27-36). */
+typedef struct vfs_wcsph_params {
+    float wall_stiffness;
+    float stiffness;
+    float expoent;
+    float viscosity_strenght;
+} vfs_wcsph_params;
+
+/* WCSPHWithBoundaryModel::BoundaryObjectInfo, src/models/wcsph_with_boundary_model.h:16-24:
+ * transform = inverse of the object's world matrix, rotation = mat4 of its rotation, both glm
+ * column-major (element (row r, column c) at [c*4 + r]); the grids are host arrays of
+ * resolution[0]*resolution[1]*resolution[2] floats indexed x + nx*(y + ny*z) and are copied. */
+typedef struct vfs_boundary_object {
+    float transform[16];
+    float rotation[16];
+    float box_size[3];
+    float box_pos[3];
+    uint32_t resolution[3];
+    const float* sdf_grid;
+    const float* volume_map_grid;
+} vfs_boundary_object;
+
+/* An analytic boundary shape whose SDF grid and volume map the library builds on the GPU, in
+ * place of the reference's OBJ mesh -> MeshSDF -> GenerateVolumeMap chain
+ * (src/scenes/generic_scene.cpp:88-124, src/util/volume_map.cpp:9-54). The placement fields are
+ * the scene JSON's boundaryObjects[] keys (src/util/scene_loader.cpp:59-95). */
+#define VFS_SHAPE_SPHERE 0    /* params[0] = radius */
+#define VFS_SHAPE_BOX 1       /* params[0..2] = half extents, solid */
+#define VFS_SHAPE_CONTAINER 2 /* params[0..2] = half extents, fluid inside (inverted box) */
+typedef struct vfs_analytic_object {
+    int32_t shape;
+    double params[3];
+    float position[3];
+    float rotation_angle_deg;
+    float rotation_axis[3];
+    float scale[3];
+    uint32_t resolution[3];
+} vfs_analytic_object;
+
+/* Thread-local message of the last failing call on this thread. */
+const char* vfs_last_error(void);
+/* Library version string. */
+const char* vfs_version(void);
+/* Number of CUDA devices visible to the library (0 when there is none or no driver). */
+int vfs_device_count(void);
+
+/* ---- model lifecycle: SPHModel / WCSPHWithBoundaryModel (src/models/model.h:58-64) ---- */
+
+/* WCSPHWithBoundaryModel(sph, wcsph) + Init (src/models/wcsph_with_boundary_model.cpp:39-79,
+ * src/models/model.cpp:82-98): allocates every device buffer for sph->n_particles particles. */
+int vfs_model_create(const vfs_sim_params* sim, const vfs_sph_params* sph,
+                     const vfs_wcsph_params* wcsph, vfs_model** out);
+/* SPHModel::Clear (src/models/model.cpp:102-111). */
+int vfs_model_destroy(vfs_model* m);
+/* The CUDA stream (a cudaStream_t passed as void*) all later work is enqueued on; NULL selects
+ * the handle's own non-blocking stream. */
+int vfs_model_set_stream(vfs_model* m, void* stream);
+/* Simulation::SetGlobalParameters (src/simulation.cpp:46-50) and the parameter edits of
+ * DrawDebugUI (src/models/model.cpp:236-263, wcsph_with_boundary_model.cpp:119-141). Any
+ * argument may be NULL. n_particles is ignored (the capacity is fixed at create). */
+int vfs_model_set_parameters(vfs_model* m, const vfs_sim_params* sim, const vfs_sph_params* sph,
+                             const vfs_wcsph_params* wcsph);
+int vfs_model_get_parameters(const vfs_model* m, vfs_sim_params* sim, vfs_sph_params* sph,
+                             vfs_wcsph_params* wcsph);
+uint32_t vfs_model_num_particles(const vfs_model* m);
+
+/* GenericScene::AddBoundaryObject + CreateBoundaryObjectBuffer
+ * (src/scenes/generic_scene.cpp:88-145), from prepared grids. */
+int vfs_model_add_boundary_object(vfs_model* m, const vfs_boundary_object* obj);
+/* The same from an analytic shape: SDF grid and 16^3-point Gauss-Legendre volume map are
+ * generated on the GPU over the shape's box grown by a margin of 8h
+ * (src/util/mesh_sdf.cpp:69-86 with margin 8h from generic_scene.cpp:101). */
+int vfs_model_add_analytic_object(vfs_model* m, const vfs_analytic_object* obj);
+uint32_t vfs_model_num_boundary_objects(const vfs_model* m);
+/* Reads back boundary object idx: matrices and box into *info (grid pointers set to NULL), and
+ * the grids into sdf_out / vm_out when they are not NULL. */
+int vfs_model_get_boundary_object(const vfs_model* m, uint32_t idx, vfs_boundary_object* info,
+                                  float* sdf_out, float* vm_out);
+
+/* ---- state: SPHModel::SetParticleState / SetParticlesInBox / CopyDataBuffers ---- */
+
+/* SetParticleState (src/models/model.h:77-81, model.cpp:139-147): writes count particles at
+ * offset (count < 0: all from offset); densities of those particles are zeroed. ids are set to
+ * offset + i. */
+int vfs_model_set_particle_state(vfs_model* m, const float* pos, const float* vel,
+                                 uint32_t offset, int64_t count);
+/* SetParticlesInBox in Compact mode (src/models/model.cpp:117-137, 35-66): a lattice with
+ * spacing cbrt(1 / target_density), zero velocity. mode 1 (Random) draws uniform positions from
+ * a seeded generator (the reference seeds from std::random_device). */
+int vfs_model_set_particles_in_box(vfs_model* m, const float box_size[3], const float box_pos[3],
+                                   uint32_t offset, int64_t count, int32_t mode, uint64_t seed);
+/* SPHModel::CopyDataBuffers (src/models/model.cpp:158-170), into host arrays; any may be NULL.
+ * acc is the acceleration of the last substep (recorded only while field recording is on). */
+int vfs_model_copy_data_buffers(vfs_model* m, float* pos, float* vel, float* dens, float* acc);
+int vfs_model_get_ids(vfs_model* m, uint32_t* ids);
+/* Neighbour arrays of the last substep: SpatialHash keys / sorted_indices / spatial_offsets
+ * (src/compute/spatial_hash.h:15-17; offsets hold N for empty keys). Any may be NULL. */
+int vfs_model_get_neighbor_arrays(vfs_model* m, uint32_t* keys, uint32_t* sorted_indices,
+                                  uint32_t* offsets);
+/* Boundary density Psi_b and gradient of the last substep (VolumeMapBuffers,
+ * src/models/wcsph_with_boundary_model.cpp:19-22). */
+int vfs_model_get_boundary_fields(vfs_model* m, float* boundary_density,
+                                  float* boundary_gradient);
+/* Keep the per-particle acceleration of every substep for copy_data_buffers (off by default:
+ * the fused force pass otherwise never stores it). */
+int vfs_model_record_fields(vfs_model* m, int32_t enable);
+
+/* ---- stepping: WCSPHWithBoundaryModel::Step (src/models/wcsph_with_boundary_model.cpp:81-117) */
+
+/* One Simulation::Step: `iterations` substeps of dt = time_scale * fixed_dt / iterations. */
+int vfs_model_step(vfs_model* m);
+/* count substeps. */
+int vfs_model_substeps(vfs_model* m, int32_t count);
+/* Capture each substep as a CUDA graph (default on). */
+int vfs_model_use_graph(vfs_model* m, int32_t enable);
+/* Waits for the stream and reads the device error word; VFS_ERR_DEVICE_CHECK if set. */
+int vfs_model_synchronize(vfs_model* m);
+/* count substeps without graphs, with events between passes; phase_ms[6] receives the mean
+ * milliseconds per substep of: key+histogram, radix sort, cell ranges+reorder, density,
+ * force+integrate, scratch clear. */
+int vfs_model_profile_substeps(vfs_model* m, int32_t count, float* phase_ms);
+/* Sort tuning: digit width in bits (4..8) and items per thread of a onesweep tile (8, 12, 16). */
+int vfs_model_set_sort_config(vfs_model* m, int32_t digit_bits, int32_t tile_items);
+int vfs_model_get_sort_config(const vfs_model* m, int32_t* digit_bits, int32_t* tile_items,
+                              int32_t* passes);
+/* Device pointers of the current state: float4 (x, y, z, id bits) and (vx, vy, vz, 0). */
+int vfs_model_device_state(vfs_model* m, void** pos4, void** vel4);
+
+/* ---- scene: LoadScene / GenericScene (src/util/scene_loader.cpp:113-140,
+ * src/scenes/generic_scene.cpp:10-57) ---- */
+
+/* Parses a scene JSON, creates the model (N = sum of fluid-block sizes), adds its boundary
+ * objects (resourcePath resolved against resources_dir) and spawns the fluid blocks
+ * (GenericScene::Reset). */
+int vfs_scene_load(const char* json_path, const char* resources_dir, vfs_model** out);
+/* GenericScene::Reset (src/scenes/generic_scene.cpp:42-57): re-spawns the fluid blocks of a
+ * model created by vfs_scene_load. */
+int vfs_scene_reset(vfs_model* m);
+
+/* ---- seeded synthetic inputs (counter-based generator; identical on every host) ---- */
+
+/* Jittered lattice: positions origin + spacing * (i + 0.5, j + 0.5, k + 0.5) + U(-jitter,
+ * +jitter) * spacing per component, i fastest. */
+int vfs_generate_lattice(const uint32_t dims[3], const float origin[3], float spacing,
+                         float jitter, uint64_t seed, float* pos_out);
+/* n_uniform points uniform in [lo, hi) followed by n_blob Gaussian points around center. */
+int vfs_generate_uniform_blob(uint64_t n_uniform, const float lo[3], const float hi[3],
+                              uint64_t n_blob, const float center[3], float sigma, uint64_t seed,
+                              float* pos_out);
+/* Smooth velocity field: sum of `modes` random Fourier modes, scaled so the largest speed over
+ * the given positions equals amplitude. */
+int vfs_generate_fourier_velocity(uint64_t n, const float* pos, int32_t modes, float amplitude,
+                                  uint64_t seed, float* vel_out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* VFS_CUDA_H */

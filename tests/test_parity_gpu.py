@@ -1,0 +1,268 @@
+"""GPU parity tests: the CUDA path (through the C ABI) against the CPU oracle on identical inputs.
+
+Bars: sort keys, sorted_indices (permutation) and spatial offsets bit-exact; boundary terms,
+densities, accelerations, velocities and positions within RTOL = 1e-5 normwise relative error
+(tests/helpers.py); the FP32-vs-FP64 error of the same step is printed beside it.
+"""
+from __future__ import annotations
+
+import json
+from dataclasses import replace
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import vkfluidsim_gb300 as vfs
+from tests.helpers import RTOL, by_id, normwise_rel, oracle_for
+from vkfluidsim_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+GOLDEN = Path(__file__).resolve().parent / "golden"
+M32 = np.uint64(0xFFFFFFFF)
+
+
+def np_keys(pos, h, n):
+    """Vectorised HashCell3D(floor(x / h)) % n (spatial_hash_3d.slang:16-32)."""
+    c = np.floor(pos.astype(np.float32) / np.float32(h)).astype(np.int64)
+    u = (c + 25) & 0xFFFFFFFF
+    loc, blk = u % 50, u // 50
+    bh = (blk[:, 0] * 15823 + blk[:, 1] * 9737333 + blk[:, 2] * 440817757) & 0xFFFFFFFF
+    hsh = (loc[:, 0] + 50 * (loc[:, 1] + 50 * loc[:, 2]) + bh) & 0xFFFFFFFF
+    return (hsh % n).astype(np.uint32)
+
+
+def compare_step(model, oracle, label="", fp64_oracle=None, check_fields=True):
+    """Runs one substep on both and checks the bars; returns the error table."""
+    model.record_fields(True)
+    model.substeps(1)
+    oracle.substeps(1)
+    gk, gp, go = model.get_neighbor_arrays()
+    ok, op, oo = oracle.neighbors()
+    assert np.array_equal(gk, ok), f"{label}: sorted keys differ"
+    assert np.array_equal(gp, op), f"{label}: permutation differs"
+    assert np.array_equal(go, oo), f"{label}: spatial offsets differ"
+    g = model.copy_data_buffers(with_acc=True)
+    o = oracle.state()
+    assert np.array_equal(model.get_ids(), o["ids"])
+    errs = {}
+    if check_fields:
+        bd, bg = model.get_boundary_fields()
+        f = oracle.fields()
+        errs["boundary_density"] = normwise_rel(bd, f["boundary_density"])
+        errs["boundary_gradient"] = normwise_rel(bg, f["boundary_gradient"])
+        errs["accelerations"] = normwise_rel(g["accelerations"], f["accelerations"])
+    errs["densities"] = normwise_rel(g["densities"], o["densities"])
+    errs["velocities"] = normwise_rel(g["velocities"], o["velocities"])
+    errs["positions"] = normwise_rel(g["positions"], o["positions"])
+    if fp64_oracle is not None:
+        fp64_oracle.substeps(1)
+        d = fp64_oracle.state()
+        for k in ("densities", "velocities", "positions"):
+            ref = by_id(d[k], d["ids"])
+            errs[f"gpu_vs_fp64_{k}"] = normwise_rel(by_id(g[k], o["ids"]), ref)
+            errs[f"oracle32_vs_fp64_{k}"] = normwise_rel(by_id(o[k], o["ids"]), ref)
+    print(label, json.dumps({k: float(f"{v:.3g}") for k, v in errs.items()}))
+    for k, v in errs.items():
+        if not k.startswith(("gpu_vs_fp64", "oracle32_vs_fp64")):
+            assert v <= RTOL, f"{label}: {k} normwise error {v:.3g} > {RTOL}"
+    return errs
+
+
+@pytest.fixture(scope="module")
+def dam():
+    w = W.dam_break(dims=(24, 24, 24), map_res=32, stiffness=200.0)
+    w.pos[:, 2] -= 0.005  # some particles start below the floor: wall penalty is exercised
+    return w
+
+
+def test_first_substep_parity_dam_break(dam):
+    m = W.build_model(dam)
+    o = oracle_for(dam, m)
+    o64 = oracle_for(dam, m, fp64=True)
+    errs = compare_step(m, o, "dam_break_13824", fp64_oracle=o64)
+    bd, _ = m.get_boundary_fields()
+    assert (bd > 0).sum() > 100, "the volume map must contribute"
+    # The GPU's FP32 error against FP64 stays at the oracle's own FP32 error level.
+    for k in ("densities", "velocities", "positions"):
+        assert errs[f"gpu_vs_fp64_{k}"] <= max(4 * errs[f"oracle32_vs_fp64_{k}"], 1e-6)
+
+
+def test_per_step_parity_from_identical_state(dam):
+    """Advance 40 substeps on the GPU, load that state into the oracle, compare one substep."""
+    m = W.build_model(dam)
+    m.substeps(40)
+    s = m.copy_data_buffers()
+    ids = m.get_ids()
+    o = oracle_for(dam, m, pos=s["positions"], vel=s["velocities"], ids=ids)
+    errs = compare_step(m, o, "dam_break_after_40")
+    assert np.abs(s["velocities"]).max() > 1e-3
+
+
+def test_multistep_drift_is_bounded():
+    w = W.dam_break(dims=(16, 16, 16), map_res=24, stiffness=200.0)
+    m = W.build_model(w)
+    o = oracle_for(w, m)
+    m.substeps(200)
+    o.substeps(200)
+    g, r = m.copy_data_buffers(), o.state()
+    gi, ri = m.get_ids(), r["ids"]
+    drift = np.abs(by_id(g["positions"], gi) - by_id(r["positions"], ri)).max()
+    travel = np.abs(by_id(g["positions"], gi) - w.pos).max()
+    print("drift after 200 substeps:", drift, "max travel:", travel)
+    assert travel > 1e-3
+    assert drift < 1e-4
+
+
+def test_sphere_obstacle_rotated_and_scaled():
+    w = W.dam_break(dims=(20, 20, 12), spacing=0.02, map_res=0, stiffness=100.0)
+    rng = np.random.default_rng(11)
+    w.pos[:] = (rng.random(w.pos.shape) * (0.6, 0.6, 0.4) + (0.1, 0.1, 0.0)).astype(np.float32)
+    w.vel[:] = ((rng.random(w.vel.shape) - 0.5) * 0.5).astype(np.float32)
+    w.objects = [
+        vfs.AnalyticObject(vfs.SHAPE_SPHERE, (0.12,), position=(0.4, 0.4, 0.15),
+                           rotation_angle_deg=30.0, rotation_axis=(1.0, 1.0, 0.0),
+                           scale=(1.0, 1.0, 1.0), resolution=(40, 40, 40)),
+        vfs.AnalyticObject(vfs.SHAPE_BOX, (0.1, 0.05, 0.08), position=(0.2, 0.6, 0.1),
+                           rotation_angle_deg=-90.0, rotation_axis=(0.0, 1.0, 0.0),
+                           scale=(1.0, 2.0, 1.0), resolution=(24, 24, 24)),
+    ]
+    m = W.build_model(w)
+    o = oracle_for(w, m)
+    compare_step(m, o, "two_objects")
+    bd, _ = m.get_boundary_fields()
+    assert (bd > 0).sum() > 20
+
+
+@pytest.mark.parametrize("n", [29, 57])
+def test_tiny_tables_with_colliding_keys(n):
+    w = W.dam_break(dims=(2, 2, 2), map_res=0)
+    rng = np.random.default_rng(n)
+    pos = (rng.random((n, 3)) * 0.12).astype(np.float32)
+    w.pos, w.vel = pos, ((rng.random((n, 3)) - 0.5) * 0.1).astype(np.float32)
+    w.sph = replace(w.sph, n_particles=n)
+    m = W.build_model(w)
+    o = oracle_for(w, m)
+    for _ in range(3):
+        compare_step(m, o, f"tiny_{n}")
+
+
+@pytest.mark.parametrize("n", [0, 1, 2, 255, 4097])
+def test_edge_sizes(n):
+    w = W.dam_break(dims=(2, 2, 2), map_res=0)
+    rng = np.random.default_rng(100 + n)
+    w.pos = (rng.random((n, 3)) * 0.3).astype(np.float32)
+    w.vel = np.zeros((n, 3), np.float32)
+    w.sph = replace(w.sph, n_particles=n)
+    m = W.build_model(w)
+    if n == 0:
+        m.substeps(2)
+        m.synchronize()
+        assert m.copy_data_buffers()["positions"].shape == (0, 3)
+        return
+    o = oracle_for(w, m)
+    compare_step(m, o, f"n={n}")
+
+
+@pytest.mark.parametrize("digits,items", [(4, 8), (5, 12), (6, 16), (7, 8), (8, 12), (8, 16)])
+def test_sort_configurations_are_bit_exact(digits, items):
+    w = W.stress_4m(n_uniform=60000, n_blob=9000, map_res=0)
+    rng = np.random.default_rng(digits * 31 + items)
+    w.pos = w.pos[rng.permutation(w.n)]
+    m = W.build_model(w)
+    m.set_sort_config(digits, items)
+    o = oracle_for(w, m)
+    compare_step(m, o, f"sort_{digits}_{items}", check_fields=False)
+
+
+def test_graph_and_stream_launch_agree_bitwise(dam):
+    a, b = W.build_model(dam), W.build_model(dam)
+    b.use_graph(False)
+    a.substeps(5)
+    b.substeps(5)
+    sa, sb = a.copy_data_buffers(), b.copy_data_buffers()
+    for k in sa:
+        assert np.array_equal(sa[k], sb[k]), k
+
+
+def test_full_size_one_million_particles():
+    """BASELINE's plain configuration at full size: 1,048,576 particles with the sphere map."""
+    w = W.obstacle_1m(map_res=128)
+    m = W.build_model(w)
+    m.substeps(1)
+    keys, perm, offs = m.get_neighbor_arrays()
+    expected = np_keys(w.pos, w.sim.smooth_radius, w.n)
+    assert np.array_equal(np.sort(perm), np.arange(w.n, dtype=np.uint32))
+    assert np.array_equal(keys, expected[perm])
+    same = keys[1:] == keys[:-1]
+    assert np.all(np.diff(keys.astype(np.int64)) >= 0) and np.all(perm[1:][same] > perm[:-1][same])
+    first = np.searchsorted(keys, np.arange(w.n, dtype=np.uint32))
+    present = np.zeros(w.n, bool)
+    present[keys] = True
+    assert np.array_equal(offs, np.where(present, first, w.n).astype(np.uint32))
+    # Full parity of one substep from that identical state.
+    s = m.copy_data_buffers()
+    o = oracle_for(w, m, pos=s["positions"], vel=s["velocities"], ids=m.get_ids())
+    compare_step(m, o, "obstacle_1m")
+
+
+def test_volume_map_generation_matches_oracle():
+    from oracle import binding as ob
+
+    h = 0.015
+    for shape, prm, res in ((vfs.SHAPE_SPHERE, (0.2,), (48, 48, 48)),
+                            (vfs.SHAPE_CONTAINER, (0.5, 0.25, 0.25), (40, 24, 24)),
+                            (vfs.SHAPE_BOX, (0.1, 0.2, 0.05), (20, 30, 16))):
+        w = W.dam_break(dims=(2, 2, 2), map_res=0)
+        w.sim = replace(w.sim, smooth_radius=h)
+        w.objects = [vfs.AnalyticObject(shape, prm, resolution=res)]
+        m = W.build_model(w)
+        info = m.get_boundary_object(0)
+        bs, bp, sdf, vm = ob.volume_map(shape, prm, h, res, np.float32(8.0 * h))
+        assert np.array_equal(info.box_size, bs) and np.array_equal(info.box_pos, bp)
+        assert np.array_equal(info.sdf, sdf)
+        assert normwise_rel(info.volume_map, vm) < 1e-6
+        assert (vm > 0).sum() > 100
+
+
+def test_reference_dam_break_scene():
+    """The reference's assets/scenes/dam_break.json: 75,000 particles, 3 iterations per step."""
+    m = vfs.load_scene(str(GOLDEN / "scenes" / "dam_break.json"))
+    counts = json.loads((GOLDEN / "scenes" / "expected_counts.json").read_text())
+    assert m.n_particles == counts["dam_break.json"]
+    sim, sph, wc = m.get_parameters()
+    assert sph.iterations == 3 and abs(sim.smooth_radius - 0.2) < 1e-7
+    s0 = m.copy_data_buffers()
+    diam = np.cbrt(np.float32(1) / np.float32(1000.0)).astype(np.float32)
+    assert np.allclose(s0["positions"][1] - s0["positions"][0], (0, 0, diam), atol=1e-6)
+    assert np.allclose(s0["positions"][0], (0.0, 0.0, 1.5))
+    from oracle import binding as ob
+
+    o = ob.OracleModel(ob.params_from(sim, sph, wc), m.n_particles)
+    o.set_state(s0["positions"], s0["velocities"])
+    m.record_fields(True)
+    m.step()
+    o.step()
+    assert np.array_equal(m.get_neighbor_arrays()[0], o.neighbors()[0])
+    g, r = m.copy_data_buffers(), o.state()
+    for k in ("positions", "velocities", "densities"):
+        assert normwise_rel(g[k], r[k]) <= RTOL, k
+    m.reset()
+    assert np.array_equal(m.copy_data_buffers()["positions"], s0["positions"])
+
+
+def test_partial_state_update_and_profile():
+    w = W.dam_break(dims=(12, 12, 12), map_res=16)
+    m = W.build_model(w)
+    newp = w.pos[:100] + np.float32(0.01)
+    m.set_particle_state(newp, np.ones((100, 3), np.float32), offset=500, count=100)
+    s = m.copy_data_buffers()
+    assert np.array_equal(s["positions"][500:600], newp)
+    assert np.array_equal(s["positions"][:500], w.pos[:500])
+    assert np.all(s["densities"][500:600] == 0)
+    assert np.array_equal(m.get_ids()[500:600], np.arange(500, 600))
+    prof = m.profile_substeps(3)
+    assert all(v > 0 for k, v in prof.items() if k != "clear"), prof
+    m.synchronize()
+    with pytest.raises(vfs.VfsError):
+        m.set_particle_state(newp, newp, offset=w.n - 10, count=100)

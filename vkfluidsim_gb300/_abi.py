@@ -1,0 +1,151 @@
+"""ctypes declarations of ``include/vfs_cuda.h`` (the C ABI of the CUDA library).
+
+Loading fails loudly when the in-tree library has not been built: there is no fallback path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libvfs_cuda.so"
+
+VFS_OK = 0
+STATUS_NAMES = {
+    1: "VFS_ERR_INVALID_ARGUMENT",
+    2: "VFS_ERR_CUDA",
+    3: "VFS_ERR_OUT_OF_MEMORY",
+    4: "VFS_ERR_IO",
+    5: "VFS_ERR_PARSE",
+    6: "VFS_ERR_CAPACITY",
+    7: "VFS_ERR_DEVICE_CHECK",
+    8: "VFS_ERR_NOT_READY",
+}
+
+SHAPE_SPHERE, SHAPE_BOX, SHAPE_CONTAINER = 0, 1, 2
+
+
+class VfsError(RuntimeError):
+    def __init__(self, code: int, message: str):
+        super().__init__(f"{STATUS_NAMES.get(code, code)}: {message}")
+        self.code = code
+
+
+class SimParams(C.Structure):
+    _fields_ = [("gravity", C.c_float * 3), ("smooth_radius", C.c_float)]
+
+
+class SphParams(C.Structure):
+    _fields_ = [
+        ("time_scale", C.c_float),
+        ("iterations", C.c_int32),
+        ("n_particles", C.c_int32),
+        ("fixed_dt", C.c_float),
+        ("target_density", C.c_float),
+        ("bbox_size", C.c_float * 3),
+        ("bbox_pos", C.c_float * 3),
+    ]
+
+
+class WcsphParams(C.Structure):
+    _fields_ = [
+        ("wall_stiffness", C.c_float),
+        ("stiffness", C.c_float),
+        ("expoent", C.c_float),
+        ("viscosity_strenght", C.c_float),
+    ]
+
+
+class BoundaryObject(C.Structure):
+    _fields_ = [
+        ("transform", C.c_float * 16),
+        ("rotation", C.c_float * 16),
+        ("box_size", C.c_float * 3),
+        ("box_pos", C.c_float * 3),
+        ("resolution", C.c_uint32 * 3),
+        ("sdf_grid", C.POINTER(C.c_float)),
+        ("volume_map_grid", C.POINTER(C.c_float)),
+    ]
+
+
+class AnalyticObject(C.Structure):
+    _fields_ = [
+        ("shape", C.c_int32),
+        ("params", C.c_double * 3),
+        ("position", C.c_float * 3),
+        ("rotation_angle_deg", C.c_float),
+        ("rotation_axis", C.c_float * 3),
+        ("scale", C.c_float * 3),
+        ("resolution", C.c_uint32 * 3),
+    ]
+
+
+_P = C.c_void_p
+_F = C.POINTER(C.c_float)
+_U = C.POINTER(C.c_uint32)
+_I = C.c_int
+_U32 = C.c_uint32
+
+# name -> (restype, argtypes)
+SIGNATURES = {
+    "vfs_last_error": (C.c_char_p, []),
+    "vfs_version": (C.c_char_p, []),
+    "vfs_device_count": (_I, []),
+    "vfs_model_create": (_I, [C.POINTER(SimParams), C.POINTER(SphParams), C.POINTER(WcsphParams), C.POINTER(_P)]),
+    "vfs_model_destroy": (_I, [_P]),
+    "vfs_model_set_stream": (_I, [_P, _P]),
+    "vfs_model_set_parameters": (_I, [_P, C.POINTER(SimParams), C.POINTER(SphParams), C.POINTER(WcsphParams)]),
+    "vfs_model_get_parameters": (_I, [_P, C.POINTER(SimParams), C.POINTER(SphParams), C.POINTER(WcsphParams)]),
+    "vfs_model_num_particles": (_U32, [_P]),
+    "vfs_model_add_boundary_object": (_I, [_P, C.POINTER(BoundaryObject)]),
+    "vfs_model_add_analytic_object": (_I, [_P, C.POINTER(AnalyticObject)]),
+    "vfs_model_num_boundary_objects": (_U32, [_P]),
+    "vfs_model_get_boundary_object": (_I, [_P, _U32, C.POINTER(BoundaryObject), _F, _F]),
+    "vfs_model_set_particle_state": (_I, [_P, _F, _F, _U32, C.c_int64]),
+    "vfs_model_set_particles_in_box": (_I, [_P, _F, _F, _U32, C.c_int64, C.c_int32, C.c_uint64]),
+    "vfs_model_copy_data_buffers": (_I, [_P, _F, _F, _F, _F]),
+    "vfs_model_get_ids": (_I, [_P, _U]),
+    "vfs_model_get_neighbor_arrays": (_I, [_P, _U, _U, _U]),
+    "vfs_model_get_boundary_fields": (_I, [_P, _F, _F]),
+    "vfs_model_record_fields": (_I, [_P, C.c_int32]),
+    "vfs_model_step": (_I, [_P]),
+    "vfs_model_substeps": (_I, [_P, C.c_int32]),
+    "vfs_model_use_graph": (_I, [_P, C.c_int32]),
+    "vfs_model_synchronize": (_I, [_P]),
+    "vfs_model_profile_substeps": (_I, [_P, C.c_int32, _F]),
+    "vfs_model_set_sort_config": (_I, [_P, C.c_int32, C.c_int32]),
+    "vfs_model_get_sort_config": (_I, [_P, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
+    "vfs_model_device_state": (_I, [_P, C.POINTER(_P), C.POINTER(_P)]),
+    "vfs_scene_load": (_I, [C.c_char_p, C.c_char_p, C.POINTER(_P)]),
+    "vfs_scene_reset": (_I, [_P]),
+    "vfs_generate_lattice": (_I, [_U, _F, C.c_float, C.c_float, C.c_uint64, _F]),
+    "vfs_generate_uniform_blob": (_I, [C.c_uint64, _F, _F, C.c_uint64, _F, C.c_float, C.c_uint64, _F]),
+    "vfs_generate_fourier_velocity": (_I, [C.c_uint64, _F, C.c_int32, C.c_float, C.c_uint64, _F]),
+}
+
+_lib = None
+
+
+def load_library(path: Path | None = None) -> C.CDLL:
+    """Loads libvfs_cuda.so and binds every declared symbol; raises when it is missing."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise ImportError(
+            f"{p} is missing: the CUDA library must be built first "
+            "(python -c 'import __graft_entry__ as g; g.build()')")
+    lib = C.CDLL(str(p))
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    if path is None:
+        _lib = lib
+    return lib
+
+
+def check(code: int) -> None:
+    if code != VFS_OK:
+        msg = load_library().vfs_last_error()
+        raise VfsError(code, msg.decode() if msg else "")

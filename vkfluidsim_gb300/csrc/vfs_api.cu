@@ -1,0 +1,802 @@
+// Host runtime behind include/vfs_cuda.h: the GB300 counterpart of VkFluidSim's SPHModel /
+// WCSPHWithBoundaryModel host classes (src/models/model.cpp, wcsph_with_boundary_model.cpp) and
+// of the compute primitives they drive (src/compute/spatial_hash.cpp, sort.cpp).
+//
+// The reference records 20 dispatches and 2 buffer copies per substep, each behind a full
+// compute barrier. Here one substep is five kernels plus one memset on one stream
+// (keys+histogram, 2-4 onesweep passes, cells+reorder, density, force), captured once as a CUDA
+// graph and replayed. State ping-pongs between two float4 buffer pairs: the reorder writes the
+// sorted copy into the spare pair and the force pass writes the integrated state back into the
+// original pair, so the substep is graph-stable.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "vfs_cuda.h"
+#include "vfs_internal.h"
+#include "vfs_model.h"
+#include "vfs_volume_map.h"
+
+namespace vfs {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string& msg) {
+    g_last_error = msg;
+    return code;
+}
+
+#define VFS_CUDA_TRY(expr)                                                               \
+    do {                                                                                 \
+        cudaError_t e_ = (expr);                                                         \
+        if (e_ != cudaSuccess)                                                           \
+            return ::vfs::fail(VFS_ERR_CUDA, std::string(#expr) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+namespace {
+
+__global__ void k_expand_state(uint32_t offset, uint32_t count, const float* __restrict__ pos3,
+                               const float* __restrict__ vel3, float4* __restrict__ pos,
+                               float4* __restrict__ vel, float4* __restrict__ aux) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    const uint32_t d = offset + i;
+    pos[d] = make_float4(pos3[3 * i], pos3[3 * i + 1], pos3[3 * i + 2], __uint_as_float(d));
+    vel[d] = make_float4(vel3[3 * i], vel3[3 * i + 1], vel3[3 * i + 2], 0.0f);
+    aux[d].z = 0.0f;  // SetParticleState zeroes the densities it covers (model.cpp:146)
+}
+
+__global__ void k_compact_state(uint32_t n, const float4* __restrict__ pos,
+                                const float4* __restrict__ vel, const float4* __restrict__ aux,
+                                float* __restrict__ pos3, float* __restrict__ vel3,
+                                float* __restrict__ dens, uint32_t* __restrict__ ids) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 p = pos[i];
+    const float4 v = vel[i];
+    pos3[3 * i] = p.x;
+    pos3[3 * i + 1] = p.y;
+    pos3[3 * i + 2] = p.z;
+    vel3[3 * i] = v.x;
+    vel3[3 * i + 1] = v.y;
+    vel3[3 * i + 2] = v.z;
+    dens[i] = aux[i].z;
+    ids[i] = __float_as_uint(p.w);
+}
+
+double pi_d() { return 3.14159265358979323846; }
+
+// Gauss-Legendre rule on [-1, 1] by Newton iteration on the Legendre recurrence.
+void gauss_legendre_nodes(int n, double* x, double* w) {
+    for (int i = 0; i < n; i++) {
+        double z = std::cos(pi_d() * (i + 0.75) / (n + 0.5));
+        for (int it = 0; it < 100; it++) {
+            double p0 = 1.0, p1 = z;
+            for (int k = 2; k <= n; k++) {
+                const double pk = ((2.0 * k - 1.0) * z * p1 - (k - 1.0) * p0) / k;
+                p0 = p1;
+                p1 = pk;
+            }
+            const double dp = n * (z * p1 - p0) / (z * z - 1.0);
+            const double dz = p1 / dp;
+            z -= dz;
+            if (std::fabs(dz) < 1e-16) break;
+        }
+        double p0 = 1.0, p1 = z;
+        for (int k = 2; k <= n; k++) {
+            const double pk = ((2.0 * k - 1.0) * z * p1 - (k - 1.0) * p0) / k;
+            p0 = p1;
+            p1 = pk;
+        }
+        const double dp = n * (z * p1 - p0) / (z * z - 1.0);
+        x[i] = -z;
+        w[i] = 2.0 / ((1.0 - z * z) * dp * dp);
+    }
+}
+
+// 4x4 double matrices, column-major like glm.
+struct M4 {
+    double a[16];
+};
+M4 m4_identity() {
+    M4 m{};
+    m.a[0] = m.a[5] = m.a[10] = m.a[15] = 1.0;
+    return m;
+}
+M4 m4_mul(const M4& A, const M4& B) {
+    M4 C{};
+    for (int c = 0; c < 4; c++)
+        for (int r = 0; r < 4; r++) {
+            double s = 0.0;
+            for (int k = 0; k < 4; k++) s += A.a[k * 4 + r] * B.a[c * 4 + k];
+            C.a[c * 4 + r] = s;
+        }
+    return C;
+}
+bool m4_inverse(const M4& M, M4& out) {
+    // Gauss-Jordan on a row-major copy.
+    double a[4][8];
+    for (int r = 0; r < 4; r++)
+        for (int c = 0; c < 4; c++) {
+            a[r][c] = M.a[c * 4 + r];
+            a[r][c + 4] = r == c ? 1.0 : 0.0;
+        }
+    for (int col = 0; col < 4; col++) {
+        int piv = col;
+        for (int r = col + 1; r < 4; r++)
+            if (std::fabs(a[r][col]) > std::fabs(a[piv][col])) piv = r;
+        if (std::fabs(a[piv][col]) < 1e-300) return false;
+        if (piv != col)
+            for (int c = 0; c < 8; c++) std::swap(a[piv][c], a[col][c]);
+        const double inv = 1.0 / a[col][col];
+        for (int c = 0; c < 8; c++) a[col][c] *= inv;
+        for (int r = 0; r < 4; r++) {
+            if (r == col) continue;
+            const double f = a[r][col];
+            for (int c = 0; c < 8; c++) a[r][c] -= f * a[col][c];
+        }
+    }
+    for (int r = 0; r < 4; r++)
+        for (int c = 0; c < 4; c++) out.a[c * 4 + r] = a[r][c + 4];
+    return true;
+}
+
+// Rotation of `angle_deg` about `axis` (the scene JSON's rotation {angle, axis},
+// src/util/scene_loader.cpp:83-88), as a column-major 4x4.
+M4 m4_rotation(float angle_deg, const float axis[3]) {
+    M4 m = m4_identity();
+    const double ax = axis[0], ay = axis[1], az = axis[2];
+    const double len = std::sqrt(ax * ax + ay * ay + az * az);
+    if (angle_deg == 0.0f || len == 0.0) return m;
+    const double x = ax / len, y = ay / len, z = az / len;
+    const double t = (double)angle_deg * pi_d() / 180.0;
+    const double c = std::cos(t), s = std::sin(t), C = 1.0 - c;
+    const double R[3][3] = {{c + x * x * C, x * y * C - z * s, x * z * C + y * s},
+                            {y * x * C + z * s, c + y * y * C, y * z * C - x * s},
+                            {z * x * C - y * s, z * y * C + x * s, c + z * z * C}};
+    for (int r = 0; r < 3; r++)
+        for (int cc = 0; cc < 3; cc++) m.a[cc * 4 + r] = R[r][cc];
+    return m;
+}
+
+void to_rowmajor34(const float* colmajor16, float* out12) {
+    for (int r = 0; r < 3; r++)
+        for (int c = 0; c < 4; c++) out12[4 * r + c] = colmajor16[c * 4 + r];
+}
+
+}  // namespace
+
+// Derives the per-substep constants from the parameter blocks with the reference's float
+// expressions (src/models/model.cpp:225-234; wcsph_with_boundary_model.slang:39-41, 322-323;
+// src/models/wcsph_with_boundary_model.cpp:84-89).
+void Model::refresh_params() {
+    StepParams& p = params;
+    const float r = sim.smooth_radius;
+    const float pi_f = 3.14159265358979323846f;
+    p.n = n;
+    p.mod_magic = n >= 1 ? (UINT64_MAX / (uint64_t)n + 1ull) : 0ull;
+    p.h = r;
+    p.h2 = r * r;
+    p.inv_h = 1.0f / r;
+    p.cubic = 8.0f / (pi_f * (float)std::pow(r, 3));
+    const float grad_scale = 48.0f / (pi_f * (float)std::pow(r, 4));
+    p.grad_over_h = grad_scale / r;
+    p.mass = sph.target_density * (0.8f * powf(r, 3.0f) / 8.0f);
+    p.rho0 = sph.target_density;
+    p.stiffness = wcsph.stiffness;
+    p.expoent = wcsph.expoent;
+    p.visc_scale = 2.0f * (3.0f + 2.0f) * wcsph.viscosity_strenght;
+    p.visc_eps = 0.01f * p.h2;
+    p.wall_k = wcsph.wall_stiffness;
+    p.dt = sph.time_scale * sph.fixed_dt / (float)sph.iterations;
+    p.gx = sim.gravity[0];
+    p.gy = sim.gravity[1];
+    p.gz = sim.gravity[2];
+    for (int a = 0; a < 3; a++) {
+        p.lo[a] = sph.bbox_pos[a];
+        p.hi[a] = sph.bbox_pos[a] + sph.bbox_size[a];
+    }
+    p.grad_eps = 0.1f * r;
+    p.bnd_eighth = 0.125f * r;
+    p.bnd_half = 0.5f * r;
+    p.n_objects = (uint32_t)objects.size();
+    for (size_t o = 0; o < objects.size() && o < (size_t)kMaxObjects; o++) {
+        DevObject& d = p.obj[o];
+        const vfs_boundary_object& b = objects[o].info;
+        to_rowmajor34(b.transform, d.T);
+        to_rowmajor34(b.rotation, d.R);
+        for (int a = 0; a < 3; a++) {
+            d.box_pos[a] = b.box_pos[a];
+            d.box_size[a] = b.box_size[a];
+            d.res[a] = b.resolution[a];
+        }
+        d.sdf = objects[o].d_sdf;
+        d.vm = objects[o].d_vm;
+    }
+    invalidate_graph();
+}
+
+void Model::invalidate_graph() {
+    if (graph_exec) cudaGraphExecDestroy(graph_exec);
+    graph_exec = nullptr;
+}
+
+int Model::alloc_sort_scratch() {
+    sc = make_sort_config(n, digit_bits, tile_items);
+    const size_t words = sort_scratch_words(sc);
+    if (words > scratch_words) {
+        if (scratch) cudaFree(scratch);
+        scratch = nullptr;
+        VFS_CUDA_TRY(cudaMalloc(&scratch, words * sizeof(uint32_t)));
+        scratch_words = words;
+    }
+    sort_scratch.ghist = scratch;
+    sort_scratch.counters = scratch + (size_t)sc.passes * sc.bins;
+    sort_scratch.status = sort_scratch.counters + sc.passes;
+    sort_scratch.err = err;
+    invalidate_graph();
+    return VFS_OK;
+}
+
+// Enqueues one substep (the body of WCSPHWithBoundaryModel::Step's loop,
+// src/models/wcsph_with_boundary_model.cpp:93-116). ExternalAccel needs no pass: the force
+// kernel starts its accumulator at g.
+int Model::enqueue_substep(cudaEvent_t* ev) {
+    cudaStream_t s = stream;
+    const int c = cur, o = 1 - cur;
+    if (ev) VFS_CUDA_TRY(cudaEventRecord(ev[0], s));
+    VFS_CUDA_TRY(cudaMemsetAsync(scratch, 0, sort_scratch_words(sc) * sizeof(uint32_t), s));
+    if (ev) VFS_CUDA_TRY(cudaEventRecord(ev[1], s));
+    VFS_CUDA_TRY(launch_keys(params, pos[c], keys, sc, sort_scratch.ghist, s));
+    if (ev) VFS_CUDA_TRY(cudaEventRecord(ev[2], s));
+    VFS_CUDA_TRY(launch_sort(n, sc, sort_scratch, keys, keys_alt, vals, vals_alt, &skeys, &sperm, s));
+    if (ev) VFS_CUDA_TRY(cudaEventRecord(ev[3], s));
+    VFS_CUDA_TRY(launch_cells_reorder(n, skeys, sperm, cell_scan, pos[c], vel[c], pos[o], vel[o], s));
+    if (ev) VFS_CUDA_TRY(cudaEventRecord(ev[4], s));
+    VFS_CUDA_TRY(launch_density(params, pos[o], cell_scan, aux, bnd, s));
+    if (ev) VFS_CUDA_TRY(cudaEventRecord(ev[5], s));
+    VFS_CUDA_TRY(launch_force(params, pos[o], vel[o], aux, bnd, cell_scan, pos[c], vel[c],
+                              record ? acc : nullptr, s));
+    if (ev) VFS_CUDA_TRY(cudaEventRecord(ev[6], s));
+    return VFS_OK;
+}
+
+int Model::run_substeps(int count) {
+    if (count < 0) return fail(VFS_ERR_INVALID_ARGUMENT, "substep count must be >= 0");
+    if (n == 0 || count == 0) return VFS_OK;
+    if (!use_graph) {
+        for (int i = 0; i < count; i++) {
+            const int rc = enqueue_substep(nullptr);
+            if (rc) return rc;
+        }
+        stepped = true;
+        return VFS_OK;
+    }
+    if (!graph_exec) {
+        cudaGraph_t g = nullptr;
+        VFS_CUDA_TRY(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+        const int rc = enqueue_substep(nullptr);
+        cudaError_t e = cudaStreamEndCapture(stream, &g);
+        if (rc) {
+            if (g) cudaGraphDestroy(g);
+            return rc;
+        }
+        if (e != cudaSuccess) return fail(VFS_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+        e = cudaGraphInstantiate(&graph_exec, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) {
+            graph_exec = nullptr;
+            return fail(VFS_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+        }
+    }
+    for (int i = 0; i < count; i++) VFS_CUDA_TRY(cudaGraphLaunch(graph_exec, stream));
+    stepped = true;
+    return VFS_OK;
+}
+
+int Model::check_device() {
+    VFS_CUDA_TRY(cudaStreamSynchronize(stream));
+    uint32_t e = 0;
+    VFS_CUDA_TRY(cudaMemcpy(&e, err, sizeof(e), cudaMemcpyDeviceToHost));
+    if (e) return fail(VFS_ERR_DEVICE_CHECK, "device error word set: " + std::to_string(e) +
+                                                 (e & kErrLookbackTimeout ? " (look-back timeout)" : ""));
+    return VFS_OK;
+}
+
+Model::~Model() {
+    invalidate_graph();
+    cudaFree(pos[0]);
+    cudaFree(pos[1]);
+    cudaFree(vel[0]);
+    cudaFree(vel[1]);
+    cudaFree(keys);
+    cudaFree(keys_alt);
+    cudaFree(vals);
+    cudaFree(vals_alt);
+    cudaFree(cell_scan);
+    cudaFree(aux);
+    cudaFree(bnd);
+    cudaFree(acc);
+    cudaFree(stage);
+    cudaFree(scratch);
+    cudaFree(err);
+    for (auto& o : objects) {
+        cudaFree(o.d_sdf);
+        cudaFree(o.d_vm);
+    }
+    if (own_stream && stream) cudaStreamDestroy(stream);
+}
+
+int Model::init() {
+    const size_t N = n ? n : 1;
+    VFS_CUDA_TRY(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    own_stream = true;
+    for (int b = 0; b < 2; b++) {
+        VFS_CUDA_TRY(cudaMalloc(&pos[b], N * sizeof(float4)));
+        VFS_CUDA_TRY(cudaMalloc(&vel[b], N * sizeof(float4)));
+    }
+    VFS_CUDA_TRY(cudaMalloc(&keys, N * 4));
+    VFS_CUDA_TRY(cudaMalloc(&keys_alt, N * 4));
+    VFS_CUDA_TRY(cudaMalloc(&vals, N * 4));
+    VFS_CUDA_TRY(cudaMalloc(&vals_alt, N * 4));
+    VFS_CUDA_TRY(cudaMalloc(&cell_scan, (N + 1) * 4));
+    VFS_CUDA_TRY(cudaMalloc(&aux, N * sizeof(float4)));
+    VFS_CUDA_TRY(cudaMalloc(&bnd, N * sizeof(float4)));
+    VFS_CUDA_TRY(cudaMalloc(&acc, N * sizeof(float4)));
+    VFS_CUDA_TRY(cudaMalloc(&stage, N * 32));
+    VFS_CUDA_TRY(cudaMalloc(&err, 4));
+    VFS_CUDA_TRY(cudaMemset(err, 0, 4));
+    for (int b = 0; b < 2; b++) {
+        VFS_CUDA_TRY(cudaMemset(pos[b], 0, N * sizeof(float4)));
+        VFS_CUDA_TRY(cudaMemset(vel[b], 0, N * sizeof(float4)));
+    }
+    VFS_CUDA_TRY(cudaMemset(aux, 0, N * sizeof(float4)));
+    VFS_CUDA_TRY(cudaMemset(bnd, 0, N * sizeof(float4)));
+    VFS_CUDA_TRY(cudaMemset(acc, 0, N * sizeof(float4)));
+    VFS_CUDA_TRY(cudaMemset(keys, 0, N * 4));
+    VFS_CUDA_TRY(cudaMemset(cell_scan, 0, (N + 1) * 4));
+    skeys = keys;
+    sperm = vals;
+    int rc = alloc_sort_scratch();
+    if (rc) return rc;
+    // Initial ids: slot index.
+    std::vector<float4> init(N);
+    for (size_t i = 0; i < N; i++) {
+        uint32_t id = (uint32_t)i;
+        float f;
+        std::memcpy(&f, &id, 4);
+        init[i] = make_float4(0.f, 0.f, 0.f, f);
+    }
+    VFS_CUDA_TRY(cudaMemcpy(pos[cur], init.data(), N * sizeof(float4), cudaMemcpyHostToDevice));
+    refresh_params();
+    return VFS_OK;
+}
+
+int Model::set_state(const float* pos3, const float* vel3, uint32_t offset, int64_t count) {
+    if (offset > n) return fail(VFS_ERR_INVALID_ARGUMENT, "offset beyond particle count");
+    const uint64_t cnt = count < 0 ? (uint64_t)(n - offset) : (uint64_t)count;
+    if (offset + cnt > n) return fail(VFS_ERR_CAPACITY, "offset + count exceeds the model's particle count");
+    if (cnt == 0) return VFS_OK;
+    if (!pos3 || !vel3) return fail(VFS_ERR_INVALID_ARGUMENT, "pos and vel must not be NULL");
+    float* sp = stage;
+    float* sv = stage + 3 * (size_t)n;
+    VFS_CUDA_TRY(cudaMemcpyAsync(sp, pos3, cnt * 12, cudaMemcpyHostToDevice, stream));
+    VFS_CUDA_TRY(cudaMemcpyAsync(sv, vel3, cnt * 12, cudaMemcpyHostToDevice, stream));
+    k_expand_state<<<(unsigned)((cnt + 255) / 256), 256, 0, stream>>>(offset, (uint32_t)cnt, sp, sv,
+                                                                    pos[cur], vel[cur], aux);
+    VFS_CUDA_TRY(cudaGetLastError());
+    VFS_CUDA_TRY(cudaStreamSynchronize(stream));
+    return VFS_OK;
+}
+
+int Model::get_state(float* pos3, float* vel3, float* dens, uint32_t* ids) {
+    if (n == 0) return VFS_OK;
+    float* sp = stage;
+    float* sv = stage + 3 * (size_t)n;
+    float* sd = stage + 6 * (size_t)n;
+    uint32_t* si = reinterpret_cast<uint32_t*>(stage + 7 * (size_t)n);
+    k_compact_state<<<(n + 255) / 256, 256, 0, stream>>>(n, pos[cur], vel[cur], aux, sp, sv, sd, si);
+    VFS_CUDA_TRY(cudaGetLastError());
+    if (pos3) VFS_CUDA_TRY(cudaMemcpyAsync(pos3, sp, (size_t)n * 12, cudaMemcpyDeviceToHost, stream));
+    if (vel3) VFS_CUDA_TRY(cudaMemcpyAsync(vel3, sv, (size_t)n * 12, cudaMemcpyDeviceToHost, stream));
+    if (dens) VFS_CUDA_TRY(cudaMemcpyAsync(dens, sd, (size_t)n * 4, cudaMemcpyDeviceToHost, stream));
+    if (ids) VFS_CUDA_TRY(cudaMemcpyAsync(ids, si, (size_t)n * 4, cudaMemcpyDeviceToHost, stream));
+    return check_device();
+}
+
+int Model::add_object(const vfs_boundary_object& src, const float* d_sdf_in, const float* d_vm_in) {
+    if (objects.size() >= (size_t)kMaxObjects)
+        return fail(VFS_ERR_CAPACITY, "at most " + std::to_string(kMaxObjects) + " boundary objects");
+    for (int a = 0; a < 3; a++)
+        if (src.resolution[a] < 2) return fail(VFS_ERR_INVALID_ARGUMENT, "grid resolution must be >= 2 per axis");
+    ObjectStore o;
+    o.info = src;
+    o.info.sdf_grid = nullptr;
+    o.info.volume_map_grid = nullptr;
+    const size_t cnt = (size_t)src.resolution[0] * src.resolution[1] * src.resolution[2];
+    VFS_CUDA_TRY(cudaMalloc(&o.d_sdf, cnt * 4));
+    VFS_CUDA_TRY(cudaMalloc(&o.d_vm, cnt * 4));
+    if (d_sdf_in) {
+        VFS_CUDA_TRY(cudaMemcpyAsync(o.d_sdf, d_sdf_in, cnt * 4, cudaMemcpyDeviceToDevice, stream));
+        VFS_CUDA_TRY(cudaMemcpyAsync(o.d_vm, d_vm_in, cnt * 4, cudaMemcpyDeviceToDevice, stream));
+    } else {
+        if (!src.sdf_grid || !src.volume_map_grid) {
+            cudaFree(o.d_sdf);
+            cudaFree(o.d_vm);
+            return fail(VFS_ERR_INVALID_ARGUMENT, "sdf_grid and volume_map_grid must not be NULL");
+        }
+        VFS_CUDA_TRY(cudaMemcpyAsync(o.d_sdf, src.sdf_grid, cnt * 4, cudaMemcpyHostToDevice, stream));
+        VFS_CUDA_TRY(cudaMemcpyAsync(o.d_vm, src.volume_map_grid, cnt * 4, cudaMemcpyHostToDevice, stream));
+    }
+    VFS_CUDA_TRY(cudaStreamSynchronize(stream));
+    objects.push_back(o);
+    refresh_params();
+    return VFS_OK;
+}
+
+int Model::add_analytic(const vfs_analytic_object& a) {
+    if (a.shape < 0 || a.shape > 2) return fail(VFS_ERR_INVALID_ARGUMENT, "unknown analytic shape");
+    for (int k = 0; k < 3; k++)
+        if (a.resolution[k] < 2) return fail(VFS_ERR_INVALID_ARGUMENT, "grid resolution must be >= 2 per axis");
+    const float h = sim.smooth_radius;
+    // Object matrix: translate * rotate * scale (gfx::Transform::Matrix, src/gfx/transform.cpp:33-45).
+    M4 T = m4_identity();
+    T.a[12] = a.position[0];
+    T.a[13] = a.position[1];
+    T.a[14] = a.position[2];
+    const M4 R = m4_rotation(a.rotation_angle_deg, a.rotation_axis);
+    M4 S = m4_identity();
+    for (int k = 0; k < 3; k++) S.a[k * 5] = (a.scale[k] == 0.0f) ? 1.0 : (double)a.scale[k];
+    const M4 W = m4_mul(m4_mul(T, R), S);
+    M4 Wi;
+    if (!m4_inverse(W, Wi)) return fail(VFS_ERR_INVALID_ARGUMENT, "object transform is singular");
+    vfs_boundary_object info{};
+    for (int k = 0; k < 16; k++) {
+        info.transform[k] = (float)Wi.a[k];
+        info.rotation[k] = (float)R.a[k];
+    }
+    // MeshSDF::Build box: shape AABB grown by tolerance (0) + margin (8h), in float
+    // (src/util/mesh_sdf.cpp:69-86, src/scenes/generic_scene.cpp:101).
+    const float margin = (float)(8.0 * (double)h);
+    float lo[3], hi[3];
+    for (int k = 0; k < 3; k++) {
+        const double e = a.shape == 0 ? a.params[0] : a.params[k];
+        lo[k] = (float)-e;
+        hi[k] = (float)e;
+        info.box_size[k] = (hi[k] - lo[k]) + 2.0f * margin;
+        info.box_pos[k] = lo[k] - margin;
+        info.resolution[k] = a.resolution[k];
+    }
+    VolumeMapParams vp{};
+    vp.shape = a.shape;
+    for (int k = 0; k < 3; k++) vp.prm[k] = a.params[k];
+    vp.h = h;
+    for (int k = 0; k < 3; k++) {
+        vp.res[k] = a.resolution[k];
+        vp.dmin[k] = info.box_pos[k];
+        const float dmax = info.box_pos[k] + info.box_size[k];
+        vp.step[k] = (double)((dmax - vp.dmin[k]) / (float)(a.resolution[k] - 1u));
+    }
+    vp.qn = 16;
+    gauss_legendre_nodes(vp.qn, vp.gx, vp.gw);
+    vp.c0 = 0.5 * (double)(h - (-h));
+    vp.c1 = 0.5 * (double)(h + (-h));
+    const double hd = (double)h;
+    vp.w_factor = 8.0 / (pi_d() * hd * hd * hd);
+    const size_t cnt = (size_t)a.resolution[0] * a.resolution[1] * a.resolution[2];
+    float *d_sdf = nullptr, *d_vm = nullptr;
+    VFS_CUDA_TRY(cudaMalloc(&d_sdf, cnt * 4));
+    VFS_CUDA_TRY(cudaMalloc(&d_vm, cnt * 4));
+    cudaError_t e = launch_volume_map(vp, d_sdf, d_vm, stream);
+    if (e != cudaSuccess) {
+        cudaFree(d_sdf);
+        cudaFree(d_vm);
+        return fail(VFS_ERR_CUDA, std::string("volume map: ") + cudaGetErrorString(e));
+    }
+    const int rc = add_object(info, d_sdf, d_vm);
+    cudaFree(d_sdf);
+    cudaFree(d_vm);
+    return rc;
+}
+
+}  // namespace vfs
+
+using vfs::fail;
+using vfs::Model;
+
+extern "C" {
+
+struct vfs_model {
+    Model m;
+};
+
+}  // extern "C"
+
+vfs::Model* vfs_model_impl(vfs_model* h) { return h ? &h->m : nullptr; }
+
+extern "C" {
+
+const char* vfs_last_error(void) { return vfs::g_last_error.c_str(); }
+const char* vfs_version(void) { return "vkfluidsim_gb300 0.1 (sm_103a)"; }
+
+int vfs_device_count(void) {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return n;
+}
+
+static int validate(const vfs_sim_params* sim, const vfs_sph_params* sph, const vfs_wcsph_params* wc) {
+    if (sim && !(sim->smooth_radius > 0.0f)) return fail(VFS_ERR_INVALID_ARGUMENT, "smooth_radius must be > 0");
+    if (sph && sph->iterations < 1) return fail(VFS_ERR_INVALID_ARGUMENT, "iterations must be >= 1");
+    if (sph && !(sph->target_density > 0.0f)) return fail(VFS_ERR_INVALID_ARGUMENT, "target_density must be > 0");
+    (void)wc;
+    return VFS_OK;
+}
+
+int vfs_model_create(const vfs_sim_params* sim, const vfs_sph_params* sph,
+                     const vfs_wcsph_params* wcsph, vfs_model** out) {
+    try {
+        if (!sim || !sph || !wcsph || !out) return fail(VFS_ERR_INVALID_ARGUMENT, "NULL argument");
+        *out = nullptr;
+        int rc = validate(sim, sph, wcsph);
+        if (rc) return rc;
+        if (sph->n_particles < 0 || (uint64_t)sph->n_particles > vfs::kMaxParticles)
+            return fail(VFS_ERR_CAPACITY, "n_particles must be in [0, 2^30]");
+        vfs_model* h = new vfs_model();
+        h->m.sim = *sim;
+        h->m.sph = *sph;
+        h->m.wcsph = *wcsph;
+        h->m.n = (uint32_t)sph->n_particles;
+        rc = h->m.init();
+        if (rc) {
+            delete h;
+            return rc;
+        }
+        *out = h;
+        return VFS_OK;
+    } catch (const std::exception& e) {
+        return fail(VFS_ERR_OUT_OF_MEMORY, e.what());
+    }
+}
+
+int vfs_model_destroy(vfs_model* m) {
+    delete m;
+    return VFS_OK;
+}
+
+int vfs_model_set_stream(vfs_model* h, void* stream) {
+    if (!h) return fail(VFS_ERR_INVALID_ARGUMENT, "NULL model");
+    Model& m = h->m;
+    cudaStreamSynchronize(m.stream);
+    if (m.own_stream && m.stream) cudaStreamDestroy(m.stream);
+    m.own_stream = false;
+    m.stream = nullptr;
+    if (stream) {
+        m.stream = (cudaStream_t)stream;
+    } else {
+        VFS_CUDA_TRY(cudaStreamCreateWithFlags(&m.stream, cudaStreamNonBlocking));
+        m.own_stream = true;
+    }
+    m.invalidate_graph();
+    return VFS_OK;
+}
+
+int vfs_model_set_parameters(vfs_model* h, const vfs_sim_params* sim, const vfs_sph_params* sph,
+                             const vfs_wcsph_params* wc) {
+    if (!h) return fail(VFS_ERR_INVALID_ARGUMENT, "NULL model");
+    int rc = validate(sim, sph, wc);
+    if (rc) return rc;
+    Model& m = h->m;
+    if (sim) m.sim = *sim;
+    if (sph) {
+        const int32_t n = m.sph.n_particles;
+        m.sph = *sph;
+        m.sph.n_particles = n;
+    }
+    if (wc) m.wcsph = *wc;
+    m.refresh_params();
+    return VFS_OK;
+}
+
+int vfs_model_get_parameters(const vfs_model* h, vfs_sim_params* sim, vfs_sph_params* sph,
+                             vfs_wcsph_params* wc) {
+    if (!h) return fail(VFS_ERR_INVALID_ARGUMENT, "NULL model");
+    if (sim) *sim = h->m.sim;
+    if (sph) *sph = h->m.sph;
+    if (wc) *wc = h->m.wcsph;
+    return VFS_OK;
+}
+
+uint32_t vfs_model_num_particles(const vfs_model* h) { return h ? h->m.n : 0u; }
+
+int vfs_model_add_boundary_object(vfs_model* h, const vfs_boundary_object* obj) {
+    if (!h || !obj) return fail(VFS_ERR_INVALID_ARGUMENT, "NULL argument");
+    return h->m.add_object(*obj, nullptr, nullptr);
+}
+
+int vfs_model_add_analytic_object(vfs_model* h, const vfs_analytic_object* obj) {
+    if (!h || !obj) return fail(VFS_ERR_INVALID_ARGUMENT, "NULL argument");
+    return h->m.add_analytic(*obj);
+}
+
+uint32_t vfs_model_num_boundary_objects(const vfs_model* h) {
+    return h ? (uint32_t)h->m.objects.size() : 0u;
+}
+
+int vfs_model_get_boundary_object(const vfs_model* h, uint32_t idx, vfs_boundary_object* info,
+                                  float* sdf_out, float* vm_out) {
+    if (!h) return fail(VFS_ERR_INVALID_ARGUMENT, "NULL model");
+    const Model& m = h->m;
+    if (idx >= m.objects.size()) return fail(VFS_ERR_INVALID_ARGUMENT, "object index out of range");
+    const vfs::ObjectStore& o = m.objects[idx];
+    if (info) *info = o.info;
+    const size_t cnt = (size_t)o.info.resolution[0] * o.info.resolution[1] * o.info.resolution[2];
+    if (sdf_out) VFS_CUDA_TRY(cudaMemcpy(sdf_out, o.d_sdf, cnt * 4, cudaMemcpyDeviceToHost));
+    if (vm_out) VFS_CUDA_TRY(cudaMemcpy(vm_out, o.d_vm, cnt * 4, cudaMemcpyDeviceToHost));
+    return VFS_OK;
+}
+
+int vfs_model_set_particle_state(vfs_model* h, const float* pos, const float* vel,
+                                 uint32_t offset, int64_t count) {
+    if (!h) return fail(VFS_ERR_INVALID_ARGUMENT, "NULL model");
+    return h->m.set_state(pos, vel, offset, count);
+}
+
+int vfs_model_copy_data_buffers(vfs_model* h, float* pos, float* vel, float* dens, float* acc) {
+    if (!h) return fail(VFS_ERR_INVALID_ARGUMENT, "NULL model");
+    Model& m = h->m;
+    int rc = m.get_state(pos, vel, dens, nullptr);
+    if (rc) return rc;
+    if (acc && m.n) {
+        std::vector<float4> a(m.n);
+        VFS_CUDA_TRY(cudaMemcpy(a.data(), m.acc, (size_t)m.n * sizeof(float4), cudaMemcpyDeviceToHost));
+        for (uint32_t i = 0; i < m.n; i++) {
+            acc[3 * i] = a[i].x;
+            acc[3 * i + 1] = a[i].y;
+            acc[3 * i + 2] = a[i].z;
+        }
+    }
+    return VFS_OK;
+}
+
+int vfs_model_get_ids(vfs_model* h, uint32_t* ids) {
+    if (!h || !ids) return fail(VFS_ERR_INVALID_ARGUMENT, "NULL argument");
+    return h->m.get_state(nullptr, nullptr, nullptr, ids);
+}
+
+int vfs_model_get_neighbor_arrays(vfs_model* h, uint32_t* keys, uint32_t* sorted_indices,
+                                  uint32_t* offsets) {
+    if (!h) return fail(VFS_ERR_INVALID_ARGUMENT, "NULL model");
+    Model& m = h->m;
+    if (!m.stepped) return fail(VFS_ERR_NOT_READY, "no substep has run yet");
+    if (m.n == 0) return VFS_OK;
+    uint32_t* off = reinterpret_cast<uint32_t*>(m.stage);
+    VFS_CUDA_TRY(vfs::launch_offsets(m.n, m.cell_scan, off, m.stream));
+    if (keys) VFS_CUDA_TRY(cudaMemcpyAsync(keys, m.skeys, (size_t)m.n * 4, cudaMemcpyDeviceToHost, m.stream));
+    if (sorted_indices)
+        VFS_CUDA_TRY(cudaMemcpyAsync(sorted_indices, m.sperm, (size_t)m.n * 4, cudaMemcpyDeviceToHost, m.stream));
+    if (offsets) VFS_CUDA_TRY(cudaMemcpyAsync(offsets, off, (size_t)m.n * 4, cudaMemcpyDeviceToHost, m.stream));
+    return m.check_device();
+}
+
+int vfs_model_get_boundary_fields(vfs_model* h, float* bdens, float* bgrad) {
+    if (!h) return fail(VFS_ERR_INVALID_ARGUMENT, "NULL model");
+    Model& m = h->m;
+    if (m.n == 0) return VFS_OK;
+    int rc = m.check_device();
+    if (rc) return rc;
+    std::vector<float4> b(m.n);
+    VFS_CUDA_TRY(cudaMemcpy(b.data(), m.bnd, (size_t)m.n * sizeof(float4), cudaMemcpyDeviceToHost));
+    for (uint32_t i = 0; i < m.n; i++) {
+        if (bdens) bdens[i] = b[i].w;
+        if (bgrad) {
+            bgrad[3 * i] = b[i].x;
+            bgrad[3 * i + 1] = b[i].y;
+            bgrad[3 * i + 2] = b[i].z;
+        }
+    }
+    return VFS_OK;
+}
+
+int vfs_model_record_fields(vfs_model* h, int32_t enable) {
+    if (!h) return fail(VFS_ERR_INVALID_ARGUMENT, "NULL model");
+    h->m.record = enable != 0;
+    h->m.invalidate_graph();
+    return VFS_OK;
+}
+
+int vfs_model_step(vfs_model* h) {
+    if (!h) return fail(VFS_ERR_INVALID_ARGUMENT, "NULL model");
+    return h->m.run_substeps(h->m.sph.iterations);
+}
+
+int vfs_model_substeps(vfs_model* h, int32_t count) {
+    if (!h) return fail(VFS_ERR_INVALID_ARGUMENT, "NULL model");
+    return h->m.run_substeps(count);
+}
+
+int vfs_model_use_graph(vfs_model* h, int32_t enable) {
+    if (!h) return fail(VFS_ERR_INVALID_ARGUMENT, "NULL model");
+    h->m.use_graph = enable != 0;
+    h->m.invalidate_graph();
+    return VFS_OK;
+}
+
+int vfs_model_synchronize(vfs_model* h) {
+    if (!h) return fail(VFS_ERR_INVALID_ARGUMENT, "NULL model");
+    return h->m.check_device();
+}
+
+int vfs_model_profile_substeps(vfs_model* h, int32_t count, float* phase_ms) {
+    if (!h || !phase_ms || count < 1) return fail(VFS_ERR_INVALID_ARGUMENT, "bad argument");
+    Model& m = h->m;
+    for (int k = 0; k < 6; k++) phase_ms[k] = 0.0f;
+    if (m.n == 0) return VFS_OK;
+    cudaEvent_t ev[7];
+    for (int k = 0; k < 7; k++) VFS_CUDA_TRY(cudaEventCreate(&ev[k]));
+    // Phase order of the event pairs: clear, keys, sort, cells+reorder, density, force.
+    double acc_ms[6] = {0, 0, 0, 0, 0, 0};
+    int rc = VFS_OK;
+    for (int it = 0; it < count && rc == VFS_OK; it++) {
+        rc = m.enqueue_substep(ev);
+        if (rc) break;
+        cudaError_t e = cudaEventSynchronize(ev[6]);
+        if (e != cudaSuccess) {
+            rc = fail(VFS_ERR_CUDA, cudaGetErrorString(e));
+            break;
+        }
+        for (int k = 0; k < 6; k++) {
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, ev[k], ev[k + 1]);
+            acc_ms[k] += ms;
+        }
+    }
+    for (int k = 0; k < 7; k++) cudaEventDestroy(ev[k]);
+    m.stepped = true;
+    if (rc) return rc;
+    // Reported order: keys, sort, cells+reorder, density, force, clear.
+    phase_ms[0] = (float)(acc_ms[1] / count);
+    phase_ms[1] = (float)(acc_ms[2] / count);
+    phase_ms[2] = (float)(acc_ms[3] / count);
+    phase_ms[3] = (float)(acc_ms[4] / count);
+    phase_ms[4] = (float)(acc_ms[5] / count);
+    phase_ms[5] = (float)(acc_ms[0] / count);
+    return m.check_device();
+}
+
+int vfs_model_set_sort_config(vfs_model* h, int32_t digit_bits, int32_t tile_items) {
+    if (!h) return fail(VFS_ERR_INVALID_ARGUMENT, "NULL model");
+    if (digit_bits < 4 || digit_bits > 8) return fail(VFS_ERR_INVALID_ARGUMENT, "digit_bits must be in [4, 8]");
+    if (tile_items != 8 && tile_items != 12 && tile_items != 16)
+        return fail(VFS_ERR_INVALID_ARGUMENT, "tile_items must be 8, 12 or 16");
+    Model& m = h->m;
+    VFS_CUDA_TRY(cudaStreamSynchronize(m.stream));
+    m.digit_bits = digit_bits;
+    m.tile_items = tile_items;
+    return m.alloc_sort_scratch();
+}
+
+int vfs_model_get_sort_config(const vfs_model* h, int32_t* digit_bits, int32_t* tile_items,
+                              int32_t* passes) {
+    if (!h) return fail(VFS_ERR_INVALID_ARGUMENT, "NULL model");
+    if (digit_bits) *digit_bits = h->m.sc.digit_bits;
+    if (tile_items) *tile_items = h->m.sc.tile / 256;
+    if (passes) *passes = h->m.sc.passes;
+    return VFS_OK;
+}
+
+int vfs_model_device_state(vfs_model* h, void** pos4, void** vel4) {
+    if (!h) return fail(VFS_ERR_INVALID_ARGUMENT, "NULL model");
+    if (pos4) *pos4 = h->m.pos[h->m.cur];
+    if (vel4) *vel4 = h->m.vel[h->m.cur];
+    return VFS_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,97 @@
+// Internal structures shared by the host runtime and the sm_103a kernels of the WCSPH step.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace vfs {
+
+constexpr int kMaxObjects = 8;      // boundary objects per model (kernel-parameter resident)
+constexpr int kMaxSortPasses = 4;   // 32-bit keys at >= 8-bit digits
+constexpr int kMaxSortBins = 256;   // digit width <= 8 bits
+constexpr uint32_t kFlagAggregate = 1u << 30;
+constexpr uint32_t kFlagPrefix = 2u << 30;
+constexpr uint32_t kCountMask = (1u << 30) - 1u;
+constexpr uint32_t kMaxParticles = 1u << 30;
+
+// Error bits of the per-model device error word.
+constexpr uint32_t kErrLookbackTimeout = 1u;
+
+// One volume-map boundary object as the kernels read it
+// (WCSPHWithBoundaryModel::BoundaryObjectInfo, src/models/wcsph_with_boundary_model.h:16-24):
+// the glm column-major matrices are stored row-major 3x4 (the fourth row of both is (0,0,0,1)).
+struct DevObject {
+    float T[12];  // world -> object-local affine (inverse of the object transform)
+    float R[12];  // rotation applied to the local normal, with w = 1 as the shader does
+    float box_pos[3];
+    float box_size[3];
+    uint32_t res[3];
+    const float* sdf;
+    const float* vm;
+};
+
+// Per-substep constants. Derived on the host once, from the same float expressions the
+// reference host and shaders use (src/models/model.cpp:225-234, wcsph_with_boundary_model.slang:39-41).
+struct StepParams {
+    uint32_t n;
+    uint32_t n_objects;
+    uint64_t mod_magic;  // ceil(2^64 / n): key = hash % n by multiply-high
+    float h, h2, inv_h;
+    float cubic;        // 8 / (pi h^3)
+    float grad_over_h;  // 48 / (pi h^4) / h (the shader's extra 1/h)
+    float mass;         // rho0 * 0.8 h^3 / 8
+    float rho0, stiffness, expoent;
+    float visc_scale;   // 2 (d + 2) nu with d = 3
+    float visc_eps;     // 0.01 h^2
+    float wall_k, dt;
+    float gx, gy, gz;
+    float lo[3], hi[3];
+    float grad_eps;     // 0.1 h (GradientVector)
+    float bnd_eighth;   // 0.125 h
+    float bnd_half;     // 0.5 h
+    DevObject obj[kMaxObjects];
+};
+
+// Scratch of one onesweep sort: global digit histograms, tile counters, look-back status words.
+struct SortScratch {
+    uint32_t* ghist;     // [passes][bins]
+    uint32_t* counters;  // [passes]
+    uint32_t* status;    // [passes][tiles][bins]
+    uint32_t* err;       // device error word
+};
+
+struct SortConfig {
+    int digit_bits;  // 4..8
+    int passes;
+    int bins;
+    int tile;        // elements per onesweep tile
+    uint32_t tiles;
+};
+
+// ---- launch wrappers (vfs_kernels.cu) ----
+SortConfig make_sort_config(uint32_t n, int digit_bits, int tile_items);
+size_t sort_scratch_words(const SortConfig& c);
+
+// keys[i] = HashCell3D(floor(pos[i] / h)) % n and the per-pass digit histograms.
+cudaError_t launch_keys(const StepParams& p, const float4* pos, uint32_t* keys,
+                        const SortConfig& sc, uint32_t* ghist, cudaStream_t s);
+// Stable LSD onesweep over sc.passes digits; returns the buffers holding sorted keys / perm.
+cudaError_t launch_sort(uint32_t n, const SortConfig& sc, const SortScratch& scratch,
+                        uint32_t* keys, uint32_t* keys_alt, uint32_t* vals, uint32_t* vals_alt,
+                        uint32_t** sorted_keys, uint32_t** sorted_perm, cudaStream_t s);
+// cell_scan[k] = first sorted index with key >= k (k in [0, n]); gathers pos/vel by perm.
+cudaError_t launch_cells_reorder(uint32_t n, const uint32_t* skeys, const uint32_t* perm,
+                                 uint32_t* cell_scan, const float4* pos_in, const float4* vel_in,
+                                 float4* pos_out, float4* vel_out, cudaStream_t s);
+// Boundary volume + density + EOS epilogue.
+cudaError_t launch_density(const StepParams& p, const float4* pos, const uint32_t* cell_scan,
+                           float4* aux, float4* bnd, cudaStream_t s);
+// Pressure + viscosity + wall + symplectic Euler.
+cudaError_t launch_force(const StepParams& p, const float4* pos, const float4* vel,
+                         const float4* aux, const float4* bnd, const uint32_t* cell_scan,
+                         float4* pos_out, float4* vel_out, float4* acc_out, cudaStream_t s);
+// spatial_offsets[k] = cell start or n for empty keys (reference layout).
+cudaError_t launch_offsets(uint32_t n, const uint32_t* cell_scan, uint32_t* offsets,
+                           cudaStream_t s);
+
+}  // namespace vfs

@@ -1,0 +1,672 @@
+// sm_103a kernels of one WCSPH-with-boundary substep (VkFluidSim's
+// WCSPHWithBoundaryModel::Step, src/models/wcsph_with_boundary_model.cpp:81-117):
+//
+//   k_keys            key[i] = HashCell3D(floor(x_i / h)) % N  + per-pass digit histograms
+//   k_onesweep        stable LSD radix pass of (key, index) with decoupled look-back
+//   k_cells_reorder   cell_scan[] (lower bound of every key) + gather of x, v (and ids in x.w)
+//   k_density         volume-map boundary terms + density + Tait EOS epilogue
+//   k_force           pressure + viscosity + wall penalty + symplectic Euler
+//
+// Data layout: particle state is float4 SoA (x,y,z,id-bits) and (vx,vy,vz,0) in sorted order;
+// per-particle density products aux = (p/rho^2, m/max(rho,1e-6), rho, p/rho0^2); boundary
+// bnd = (grad Psi_b, Psi_b). All arrays are 16-byte aligned and read with 128-bit loads.
+//
+// The neighbour loops visit exactly the reference's candidate multiset in the reference's order:
+// for each (dy, dz) the keys of cells (cx-1..cx+1) are usually consecutive (HashCell3D is
+// x-linear inside a 50-cell block), and consecutive keys' buckets are adjacent in the sorted
+// array, so the three buckets are one contiguous range [scan[kA], scan[kA+3]). When the three
+// keys are not consecutive, each bucket is walked on its own. Duplicate keys among the 27 are
+// walked as often as they occur, like wcsph_with_boundary_model.slang:166-190.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "vfs_internal.h"
+
+namespace vfs {
+namespace {
+
+// ---------------------------------------------------------------- hashing
+
+// HashCell3D, assets/shaders/simulation/spatial_hash/spatial_hash_3d.slang:20-28.
+__device__ __forceinline__ uint32_t hash_cell(uint32_t cx, uint32_t cy, uint32_t cz) {
+    const uint32_t ux = cx + 25u, uy = cy + 25u, uz = cz + 25u;
+    const uint32_t lx = ux % 50u, ly = uy % 50u, lz = uz % 50u;
+    const uint32_t bx = ux / 50u, by = uy / 50u, bz = uz / 50u;
+    const uint32_t block_hash = bx * 15823u + by * 9737333u + bz * 440817757u;
+    return lx + 50u * (ly + 50u * lz) + block_hash;
+}
+
+// KeyFromHash (spatial_hash_3d.slang:30-32): hash % n, computed as the high word of
+// (magic * hash mod 2^64) * n with magic = ceil(2^64 / n) (exact for 32-bit operands).
+__device__ __forceinline__ uint32_t key_mod(uint32_t hash, uint64_t magic, uint32_t n) {
+    const uint64_t low = magic * (uint64_t)hash;
+    return (uint32_t)__umul64hi(low, (uint64_t)n);
+}
+
+// GetCell3D (spatial_hash_3d.slang:16-18): IEEE division, floor, saturating conversion.
+__device__ __forceinline__ uint32_t cell_coord(float x, float h) {
+    return (uint32_t)__float2int_rz(floorf(__fdiv_rn(x, h)));
+}
+
+// ---------------------------------------------------------------- SPH kernel
+
+// CubicSpline (kernels_3d.slang:62-76) at q = r / h.
+__device__ __forceinline__ float cubic_w(float q, float sigma) {
+    if (q <= 1.0f) {
+        if (q > 0.5f) {
+            const float t = 1.0f - q;
+            return sigma * 2.0f * (t * t * t);
+        }
+        const float q2 = q * q;
+        const float q3 = q2 * q;
+        return sigma * (6.0f * q3 - 6.0f * q2 + 1.0f);
+    }
+    return 0.0f;
+}
+
+// GradCubicSpline (kernels_3d.slang:78-91); sigma already carries the extra 1/h.
+__device__ __forceinline__ float cubic_dw(float r, float q, float sigma) {
+    if ((r > 1e-9f) && (q <= 1.0f)) {
+        if (q > 0.5f) {
+            const float t = 1.0f - q;
+            return -sigma * (t * t);
+        }
+        return sigma * q * (3.0f * q - 2.0f);
+    }
+    return 0.0f;
+}
+
+// ---------------------------------------------------------------- volume-map sampling
+// Written with round-to-nearest intrinsics, which the compiler never fuses, so the thresholds
+// of CalculateBoundaryVolume (inside-box, 0 <= dist < h, volume > 0) evaluate bit-identically
+// to an unfused IEEE restatement.
+
+__device__ __forceinline__ float fm(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float fa(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float fsb(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float fdv(float a, float b) { return __fdiv_rn(a, b); }
+
+// One axis of SampleGrid with the cell index clamped to [0, n-2] (linear extrapolation outside;
+// the reference reads out of bounds there, wcsph_with_boundary_model.slang:51-66).
+__device__ __forceinline__ void grid_axis(uint32_t n, float u, uint32_t& cell, float& chi) {
+    const float x = fm(fsb((float)n, 1.0f), u);
+    float f = floorf(x);
+    const float hi = (float)(n - 2u);
+    if (!(f >= 0.0f)) f = 0.0f;
+    if (f > hi) f = hi;
+    cell = (uint32_t)f;
+    chi = fsb(fm(2.0f, fsb(x, f)), 1.0f);
+}
+
+// SampleGrid, wcsph_with_boundary_model.slang:51-66.
+__device__ __forceinline__ float sample_grid(const float* __restrict__ g, const uint32_t* n,
+                                             float u, float v, float w) {
+    uint32_t cx, cy, cz;
+    float ax, ay, az;
+    grid_axis(n[0], u, cx, ax);
+    grid_axis(n[1], v, cy, ay);
+    grid_axis(n[2], w, cz, az);
+    const size_t sx = 1, sy = n[0], sz = (size_t)n[0] * n[1];
+    const size_t b = cx + sy * cy + sz * cz;
+    // Corner order of the shader's offsets[8]: (0,0,0) (0,1,0) (0,0,1) (0,1,1) (1,0,0) ...
+    float val = 0.0f;
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+        const int ox = i >> 2, oy = i & 1, oz = (i >> 1) & 1;
+        const float fx = fa(1.0f, fm(ox ? 1.0f : -1.0f, ax));
+        const float fy = fa(1.0f, fm(oy ? 1.0f : -1.0f, ay));
+        const float fz = fa(1.0f, fm(oz ? 1.0f : -1.0f, az));
+        const float gval = __ldg(g + b + ox * sx + oy * sy + oz * sz);
+        val = fa(val, fm(gval, fm(fm(fx, fy), fz)));
+    }
+    return fdv(val, 8.0f);
+}
+
+__device__ __forceinline__ void to_uvw(const DevObject& o, float x, float y, float z, float& u,
+                                       float& v, float& w) {
+    u = fdv(fsb(x, o.box_pos[0]), o.box_size[0]);
+    v = fdv(fsb(y, o.box_pos[1]), o.box_size[1]);
+    w = fdv(fsb(z, o.box_pos[2]), o.box_size[2]);
+}
+
+// Row r of a row-major 3x4 matrix applied to (x, y, z, 1), summed left to right.
+__device__ __forceinline__ float mat_row(const float* M, int r, float x, float y, float z) {
+    return fa(fa(fa(fm(M[4 * r], x), fm(M[4 * r + 1], y)), fm(M[4 * r + 2], z)), M[4 * r + 3]);
+}
+
+// CalculateBoundaryVolume for one particle (wcsph_with_boundary_model.slang:102-151).
+__device__ __forceinline__ void boundary_terms(const StepParams& p, float px, float py, float pz,
+                                               float& bd, float& bgx, float& bgy, float& bgz) {
+    bd = 0.0f;
+    bgx = bgy = bgz = 0.0f;
+    for (uint32_t oi = 0; oi < p.n_objects; oi++) {
+        const DevObject& o = p.obj[oi];
+        const float lx = mat_row(o.T, 0, px, py, pz);
+        const float ly = mat_row(o.T, 1, px, py, pz);
+        const float lz = mat_row(o.T, 2, px, py, pz);
+        const bool outside = lx < o.box_pos[0] || ly < o.box_pos[1] || lz < o.box_pos[2] ||
+                             lx > fa(o.box_pos[0], o.box_size[0]) ||
+                             ly > fa(o.box_pos[1], o.box_size[1]) ||
+                             lz > fa(o.box_pos[2], o.box_size[2]);
+        if (outside) continue;
+        float u, v, w;
+        to_uvw(o, lx, ly, lz, u, v, w);
+        const float dist = sample_grid(o.sdf, o.res, u, v, w);
+        if (!(dist >= 0.0f && dist < p.h)) continue;
+        const float volume = sample_grid(o.vm, o.res, u, v, w);
+        if (!(volume > 0.0f)) continue;
+        // GradientVector (slang:68-85): central differences of the SDF at +-0.1 h.
+        const float e = p.grad_eps;
+        float gx, gy, gz;
+        {
+            float a0, a1, a2;
+            to_uvw(o, fa(lx, e), ly, lz, a0, a1, a2);
+            const float v1x = sample_grid(o.sdf, o.res, a0, a1, a2);
+            to_uvw(o, fsb(lx, e), ly, lz, a0, a1, a2);
+            const float v0x = sample_grid(o.sdf, o.res, a0, a1, a2);
+            to_uvw(o, lx, fa(ly, e), lz, a0, a1, a2);
+            const float v1y = sample_grid(o.sdf, o.res, a0, a1, a2);
+            to_uvw(o, lx, fsb(ly, e), lz, a0, a1, a2);
+            const float v0y = sample_grid(o.sdf, o.res, a0, a1, a2);
+            to_uvw(o, lx, ly, fa(lz, e), a0, a1, a2);
+            const float v1z = sample_grid(o.sdf, o.res, a0, a1, a2);
+            to_uvw(o, lx, ly, fsb(lz, e), a0, a1, a2);
+            const float v0z = sample_grid(o.sdf, o.res, a0, a1, a2);
+            const float den = fm(2.0f, e);
+            gx = fdv(fsb(v1x, v0x), den);
+            gy = fdv(fsb(v1y, v0y), den);
+            gz = fdv(fsb(v1z, v0z), den);
+        }
+        const float modn = __fsqrt_rn(fa(fa(fm(gx, gx), fm(gy, gy)), fm(gz, gz)));
+        if (!(modn > 1e-9f)) continue;
+        float nx = mat_row(o.R, 0, gx, gy, gz);
+        float ny = mat_row(o.R, 1, gx, gy, gz);
+        float nz = mat_row(o.R, 2, gx, gy, gz);
+        nx = fdv(nx, modn);
+        ny = fdv(ny, modn);
+        nz = fdv(nz, modn);
+        const float d = fmaxf(fa(dist, p.bnd_eighth), p.bnd_half);
+        const float xbx = fsb(px, fm(d, nx)), xby = fsb(py, fm(d, ny)), xbz = fsb(pz, fm(d, nz));
+        const float xx = fsb(px, xbx), xy = fsb(py, xby), xz = fsb(pz, xbz);
+        const float r = __fsqrt_rn(fa(fa(fm(xx, xx), fm(xy, xy)), fm(xz, xz)));
+        float ux = 0.0f, uy = 0.0f, uz = 0.0f;
+        if (r > 0.0f) {
+            ux = fdv(xx, r);
+            uy = fdv(xy, r);
+            uz = fdv(xz, r);
+        }
+        const float q = fdv(r, p.h);
+        bd = fa(bd, fm(volume, cubic_w(q, p.cubic)));
+        const float s = fm(volume, cubic_dw(r, q, p.grad_over_h));
+        bgx = fa(bgx, fm(s, ux));
+        bgy = fa(bgy, fm(s, uy));
+        bgz = fa(bgz, fm(s, uz));
+    }
+}
+
+// ---------------------------------------------------------------- neighbour ranges
+
+struct Ranges {
+    uint32_t b0, e0, b1, e1, b2, e2;
+};
+
+// Sorted-index ranges of the three x-neighbour buckets of row (dy, dz), in the order the
+// reference visits them (offsets_3d: x fastest).
+__device__ __forceinline__ Ranges row_ranges(const StepParams& p,
+                                             const uint32_t* __restrict__ scan, uint32_t cx,
+                                             uint32_t cy, uint32_t cz) {
+    const uint32_t kA = key_mod(hash_cell(cx - 1u, cy, cz), p.mod_magic, p.n);
+    const uint32_t kB = key_mod(hash_cell(cx, cy, cz), p.mod_magic, p.n);
+    const uint32_t kC = key_mod(hash_cell(cx + 1u, cy, cz), p.mod_magic, p.n);
+    Ranges r;
+    r.b0 = __ldg(scan + kA);
+    if (kB == kA + 1u && kC == kA + 2u) {
+        r.e0 = __ldg(scan + kA + 3u);
+        r.b1 = r.e1 = r.b2 = r.e2 = 0u;
+    } else {
+        r.e0 = __ldg(scan + kA + 1u);
+        r.b1 = __ldg(scan + kB);
+        r.e1 = __ldg(scan + kB + 1u);
+        r.b2 = __ldg(scan + kC);
+        r.e2 = __ldg(scan + kC + 1u);
+    }
+    return r;
+}
+
+// ---------------------------------------------------------------- kernels
+
+__global__ void __launch_bounds__(256) k_keys(StepParams p, const float4* __restrict__ pos,
+                                              uint32_t* __restrict__ keys, int passes,
+                                              int digit_bits, uint32_t* __restrict__ ghist) {
+    __shared__ uint32_t s_h[kMaxSortPasses * kMaxSortBins];
+    const int bins = 1 << digit_bits;
+    const uint32_t mask = (uint32_t)bins - 1u;
+    for (int e = threadIdx.x; e < passes * bins; e += blockDim.x) s_h[e] = 0u;
+    __syncthreads();
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < p.n;
+         i += gridDim.x * blockDim.x) {
+        const float4 x = pos[i];
+        const uint32_t key = key_mod(
+            hash_cell(cell_coord(x.x, p.h), cell_coord(x.y, p.h), cell_coord(x.z, p.h)),
+            p.mod_magic, p.n);
+        keys[i] = key;
+        for (int ps = 0; ps < passes; ps++)
+            atomicAdd(&s_h[ps * bins + ((key >> (ps * digit_bits)) & mask)], 1u);
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < passes * bins; e += blockDim.x)
+        if (s_h[e]) atomicAdd(&ghist[e], s_h[e]);
+}
+
+__device__ __forceinline__ uint32_t ld_volatile(const uint32_t* p) {
+    return *(const volatile uint32_t*)p;
+}
+__device__ __forceinline__ void st_volatile(uint32_t* p, uint32_t v) { *(volatile uint32_t*)p = v; }
+
+// Exclusive scan over a 256-thread block; returns the exclusive prefix and writes the total.
+__device__ __forceinline__ uint32_t block_excl_scan256(uint32_t v, uint32_t* s_warp) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t incl = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += t;
+    }
+    if (lane == 31) s_warp[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t w = lane < 8 ? s_warp[lane] : 0u;
+        uint32_t wi = w;
+#pragma unroll
+        for (int o = 1; o < 8; o <<= 1) {
+            const uint32_t t = __shfl_up_sync(0xffffffffu, wi, o);
+            if (lane >= o) wi += t;
+        }
+        if (lane < 8) s_warp[8 + lane] = wi - w;
+    }
+    __syncthreads();
+    const uint32_t r = s_warp[8 + warp] + incl - v;
+    __syncthreads();
+    return r;
+}
+
+constexpr uint32_t kLookbackSpinLimit = 1u << 20;
+
+// One stable LSD radix pass (onesweep: Adinets & Merrill 2022). Tiles are claimed in launch
+// order through an atomic counter, so every predecessor of a tile is already resident and the
+// bounded look-back always terminates; a timeout sets an error bit instead of hanging.
+template <int BLOCK, int ITEMS>
+__global__ void __launch_bounds__(BLOCK)
+    k_onesweep(const uint32_t* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
+               uint32_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out, uint32_t n,
+               int shift, int bins, const uint32_t* __restrict__ ghist,
+               uint32_t* __restrict__ counter, uint32_t* __restrict__ status,
+               uint32_t* __restrict__ err) {
+    static_assert(BLOCK == 256, "block scan assumes 256 threads");
+    constexpr int WARPS = BLOCK / 32;
+    constexpr int TILE = BLOCK * ITEMS;
+    __shared__ uint32_t s_whist[WARPS][kMaxSortBins];
+    __shared__ uint32_t s_dstart[kMaxSortBins];
+    __shared__ uint32_t s_gofs[kMaxSortBins];
+    __shared__ uint32_t s_keys[TILE];
+    __shared__ uint32_t s_vals[TILE];
+    __shared__ uint32_t s_scan[16];
+    __shared__ uint32_t s_tile;
+
+    const int tid = threadIdx.x;
+    const int lane = tid & 31, warp = tid >> 5;
+    const uint32_t mask = (uint32_t)bins - 1u;
+    if (tid == 0) s_tile = atomicAdd(counter, 1u);
+    for (int e = tid; e < WARPS * kMaxSortBins; e += BLOCK) (&s_whist[0][0])[e] = 0u;
+    // Global exclusive digit offsets of this pass.
+    const uint32_t gcount = tid < bins ? __ldg(ghist + tid) : 0u;
+    const uint32_t gbase = block_excl_scan256(gcount, s_scan);  // contains __syncthreads
+    const uint32_t tile = s_tile;
+    const uint32_t base = tile * (uint32_t)TILE + (uint32_t)warp * ITEMS * 32u;
+    const uint32_t lt_mask = (1u << lane) - 1u;
+
+    uint32_t k[ITEMS], v[ITEMS], r[ITEMS];
+#pragma unroll
+    for (int it = 0; it < ITEMS; it++) {
+        const uint32_t idx = base + it * 32u + lane;
+        const bool valid = idx < n;
+        k[it] = valid ? keys_in[idx] : 0u;
+        v[it] = valid ? (vals_in ? vals_in[idx] : idx) : 0u;
+    }
+#pragma unroll
+    for (int it = 0; it < ITEMS; it++) {
+        const uint32_t idx = base + it * 32u + lane;
+        const bool valid = idx < n;
+        const uint32_t d = valid ? ((k[it] >> shift) & mask) : (uint32_t)bins;
+        const uint32_t peers = __match_any_sync(0xffffffffu, d);
+        const uint32_t pre = __popc(peers & lt_mask);
+        uint32_t prev = 0u;
+        if (valid) prev = s_whist[warp][d];
+        __syncwarp();
+        if (valid && pre == 0u) s_whist[warp][d] = prev + __popc(peers);
+        __syncwarp();
+        r[it] = prev + pre;
+    }
+    __syncthreads();
+    uint32_t cnt = 0u;
+    if (tid < bins) {
+        uint32_t run = 0u;
+#pragma unroll
+        for (int w = 0; w < WARPS; w++) {
+            const uint32_t c = s_whist[w][tid];
+            s_whist[w][tid] = run;
+            run += c;
+        }
+        cnt = run;
+    }
+    const uint32_t dstart = block_excl_scan256(cnt, s_scan);
+    if (tid < bins) {
+        s_dstart[tid] = dstart;
+        uint32_t* st = status + (size_t)tile * bins + tid;
+        uint32_t excl = 0u;
+        if (tile == 0u) {
+            st_volatile(st, kFlagPrefix | cnt);
+        } else {
+            st_volatile(st, kFlagAggregate | cnt);
+            uint32_t t = tile - 1u;
+            uint32_t spins = 0u;
+            while (true) {
+                const uint32_t s = ld_volatile(status + (size_t)t * bins + tid);
+                const uint32_t flag = s & ~kCountMask;
+                if (flag == 0u) {
+                    if (++spins > kLookbackSpinLimit) {
+                        atomicOr(err, kErrLookbackTimeout);
+                        break;
+                    }
+                    __nanosleep(32);
+                    continue;
+                }
+                excl += s & kCountMask;
+                if (flag == kFlagPrefix || t == 0u) break;
+                t--;
+            }
+            st_volatile(st, kFlagPrefix | ((excl + cnt) & kCountMask));
+        }
+        s_gofs[tid] = gbase + excl;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int it = 0; it < ITEMS; it++) {
+        const uint32_t idx = base + it * 32u + lane;
+        if (idx < n) {
+            const uint32_t d = (k[it] >> shift) & mask;
+            const uint32_t lpos = s_dstart[d] + s_whist[warp][d] + r[it];
+            s_keys[lpos] = k[it];
+            s_vals[lpos] = v[it];
+        }
+    }
+    __syncthreads();
+    const uint32_t tile_base = tile * (uint32_t)TILE;
+    const uint32_t tile_n = min((uint32_t)TILE, n - tile_base);
+    for (uint32_t i = tid; i < tile_n; i += BLOCK) {
+        const uint32_t kk = s_keys[i];
+        const uint32_t d = (kk >> shift) & mask;
+        const uint32_t g = s_gofs[d] + (i - s_dstart[d]);
+        if (g < n) {  // always true unless a look-back timed out (error word set)
+            keys_out[g] = kk;
+            vals_out[g] = s_vals[i];
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256)
+    k_cells_reorder(uint32_t n, const uint32_t* __restrict__ skeys,
+                    const uint32_t* __restrict__ perm, uint32_t* __restrict__ scan,
+                    const float4* __restrict__ pos_in, const float4* __restrict__ vel_in,
+                    float4* __restrict__ pos_out, float4* __restrict__ vel_out) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    // Keys and permutation entries are < n by construction; the clamps only keep accesses in
+    // bounds after a reported sort failure.
+    const uint32_t k = min(skeys[i], n - 1u);
+    const uint32_t c0 = i == 0u ? 0u : min(skeys[i - 1], n - 1u) + 1u;
+    for (uint32_t c = c0; c <= k; c++) scan[c] = i;
+    if (i == n - 1u)
+        for (uint32_t c = k + 1u; c <= n; c++) scan[c] = n;
+    uint32_t src = perm[i];
+    if (src >= n) src = i;
+    pos_out[i] = __ldg(pos_in + src);
+    vel_out[i] = __ldg(vel_in + src);
+}
+
+__global__ void __launch_bounds__(256)
+    k_offsets(uint32_t n, const uint32_t* __restrict__ scan, uint32_t* __restrict__ offsets) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const uint32_t a = scan[k], b = scan[k + 1];
+    offsets[k] = b > a ? a : n;
+}
+
+// CalculateBoundaryVolume + CalculateDensities + the per-particle part of PressureFromDensityEOS
+// (wcsph_with_boundary_model.slang:102-203).
+__global__ void __launch_bounds__(128)
+    k_density(StepParams p, const float4* __restrict__ pos, const uint32_t* __restrict__ scan,
+              float4* __restrict__ aux, float4* __restrict__ bnd) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= p.n) return;
+    const float4 xi = __ldg(pos + i);
+    float bd, bgx, bgy, bgz;
+    boundary_terms(p, xi.x, xi.y, xi.z, bd, bgx, bgy, bgz);
+
+    const uint32_t cx = cell_coord(xi.x, p.h), cy = cell_coord(xi.y, p.h),
+                   cz = cell_coord(xi.z, p.h);
+    float rho = 0.0f;
+#pragma unroll 1
+    for (int t = 0; t < 9; t++) {
+        const uint32_t dy = (uint32_t)(t % 3) - 1u, dz = (uint32_t)(t / 3) - 1u;
+        const Ranges rg = row_ranges(p, scan, cx, cy + dy, cz + dz);
+#pragma unroll 1
+        for (int seg = 0; seg < 3; seg++) {
+            const uint32_t b = seg == 0 ? rg.b0 : (seg == 1 ? rg.b1 : rg.b2);
+            const uint32_t e = seg == 0 ? rg.e0 : (seg == 1 ? rg.e1 : rg.e2);
+            for (uint32_t j = b; j < e; j++) {
+                const float4 xj = __ldg(pos + j);
+                const float dx = xj.x - xi.x, dyy = xj.y - xi.y, dzz = xj.z - xi.z;
+                const float r2 = dx * dx + dyy * dyy + dzz * dzz;
+                if (r2 > p.h2) continue;
+                const float r = sqrtf(r2);
+                rho += p.mass * cubic_w(r * p.inv_h, p.cubic);
+            }
+        }
+    }
+    rho += p.rho0 * bd;
+    const float pr = p.stiffness * (powf(fmaxf(rho, p.rho0) / p.rho0, p.expoent) - 1.0f);
+    const float pd = rho > 0.0f ? pr / (rho * rho) : 0.0f;
+    const float mr = p.mass / fmaxf(rho, 1e-6f);
+    const float pb = rho > 0.0f ? pr / (p.rho0 * p.rho0) : 0.0f;
+    aux[i] = make_float4(pd, mr, rho, pb);
+    bnd[i] = make_float4(bgx, bgy, bgz, bd);
+}
+
+// CalculatePressureAccel + CalculateViscousAccel + UpdatePositions
+// (wcsph_with_boundary_model.slang:205-360), fused: both sums are accumulated separately in the
+// reference's visiting order, then a = ((g - P) + V) + wall, v += a dt, x += v dt.
+__global__ void __launch_bounds__(128)
+    k_force(StepParams p, const float4* __restrict__ pos, const float4* __restrict__ vel,
+            const float4* __restrict__ aux, const float4* __restrict__ bnd,
+            const uint32_t* __restrict__ scan, float4* __restrict__ pos_out,
+            float4* __restrict__ vel_out, float4* __restrict__ acc_out) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= p.n) return;
+    const float4 xi = __ldg(pos + i);
+    const float4 vi = __ldg(vel + i);
+    const float4 ai = __ldg(aux + i);
+    const float2* __restrict__ aux2 = reinterpret_cast<const float2*>(aux);
+    const float pdi = ai.x;
+
+    const uint32_t cx = cell_coord(xi.x, p.h), cy = cell_coord(xi.y, p.h),
+                   cz = cell_coord(xi.z, p.h);
+    float Px = 0.0f, Py = 0.0f, Pz = 0.0f;
+    float Vx = 0.0f, Vy = 0.0f, Vz = 0.0f;
+#pragma unroll 1
+    for (int t = 0; t < 9; t++) {
+        const uint32_t dy = (uint32_t)(t % 3) - 1u, dz = (uint32_t)(t / 3) - 1u;
+        const Ranges rg = row_ranges(p, scan, cx, cy + dy, cz + dz);
+#pragma unroll 1
+        for (int seg = 0; seg < 3; seg++) {
+            const uint32_t b = seg == 0 ? rg.b0 : (seg == 1 ? rg.b1 : rg.b2);
+            const uint32_t e = seg == 0 ? rg.e0 : (seg == 1 ? rg.e1 : rg.e2);
+            for (uint32_t j = b; j < e; j++) {
+                if (j == i) continue;
+                const float4 xj = __ldg(pos + j);
+                const float xx = xi.x - xj.x, xy = xi.y - xj.y, xz = xi.z - xj.z;
+                const float r2 = xx * xx + xy * xy + xz * xz;
+                if (r2 > p.h2) continue;
+                const float2 aj = __ldg(aux2 + 2 * (size_t)j);
+                const float4 vj = __ldg(vel + j);
+                const float r = sqrtf(r2);
+                float nx = 0.0f, ny = 1.0f, nz = 0.0f;
+                if (r > 0.0f) {
+                    const float ir = 1.0f / r;
+                    nx = xx * ir;
+                    ny = xy * ir;
+                    nz = xz * ir;
+                }
+                const float gw = cubic_dw(r, r * p.inv_h, p.grad_over_h);
+                const float s = (p.mass * (pdi + aj.x)) * gw;
+                Px += s * nx;
+                Py += s * ny;
+                Pz += s * nz;
+                const float dv = (vi.x - vj.x) * xx + (vi.y - vj.y) * xy + (vi.z - vj.z) * xz;
+                const float tv = aj.y * dv;
+                const float iden = 1.0f / (r2 + p.visc_eps);
+                Vx += (tv * (nx * gw)) * iden;
+                Vy += (tv * (ny * gw)) * iden;
+                Vz += (tv * (nz * gw)) * iden;
+            }
+        }
+    }
+    const float4 bi = __ldg(bnd + i);
+    const float sb = (pdi + ai.w) * p.rho0;
+    Px += sb * bi.x;
+    Py += sb * bi.y;
+    Pz += sb * bi.z;
+
+    float ax = p.gx + -Px, ay = p.gy + -Py, az = p.gz + -Pz;
+    ax += p.visc_scale * Vx;
+    ay += p.visc_scale * Vy;
+    az += p.visc_scale * Vz;
+    // WallAcceleration, wcsph_with_boundary_model.slang:336-347.
+    const float dx = fminf(xi.x - p.lo[0], 0.0f) - fminf(p.hi[0] - xi.x, 0.0f);
+    const float dyw = fminf(xi.y - p.lo[1], 0.0f) - fminf(p.hi[1] - xi.y, 0.0f);
+    const float dzw = fminf(xi.z - p.lo[2], 0.0f) - fminf(p.hi[2] - xi.z, 0.0f);
+    if (fabsf(dx) > 1e-9f || fabsf(dyw) > 1e-9f || fabsf(dzw) > 1e-9f) {
+        ax += -p.wall_k * dx;
+        ay += -p.wall_k * dyw;
+        az += -p.wall_k * dzw;
+    }
+    if (acc_out) acc_out[i] = make_float4(ax, ay, az, 0.0f);
+    const float nvx = vi.x + ax * p.dt, nvy = vi.y + ay * p.dt, nvz = vi.z + az * p.dt;
+    vel_out[i] = make_float4(nvx, nvy, nvz, 0.0f);
+    pos_out[i] = make_float4(xi.x + nvx * p.dt, xi.y + nvy * p.dt, xi.z + nvz * p.dt, xi.w);
+}
+
+constexpr int kSortBlock = 256;
+
+template <int ITEMS>
+cudaError_t launch_onesweep_t(uint32_t n, const SortConfig& sc, const SortScratch& scr, int pass,
+                              const uint32_t* kin, const uint32_t* vin, uint32_t* kout,
+                              uint32_t* vout, cudaStream_t s) {
+    k_onesweep<kSortBlock, ITEMS><<<sc.tiles, kSortBlock, 0, s>>>(
+        kin, vin, kout, vout, n, pass * sc.digit_bits, sc.bins, scr.ghist + pass * sc.bins,
+        scr.counters + pass, scr.status + (size_t)pass * sc.tiles * sc.bins, scr.err);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+SortConfig make_sort_config(uint32_t n, int digit_bits, int tile_items) {
+    SortConfig c{};
+    if (digit_bits < 4) digit_bits = 4;
+    if (digit_bits > 8) digit_bits = 8;
+    if (tile_items != 8 && tile_items != 12 && tile_items != 16) tile_items = 16;
+    int bits = 1;
+    while (bits < 32 && (((uint64_t)1 << bits) < (uint64_t)n)) bits++;  // keys <= n - 1
+    while ((bits + digit_bits - 1) / digit_bits > kMaxSortPasses) digit_bits++;  // <= 8 covers 32 bits
+    c.digit_bits = digit_bits;
+    c.passes = (bits + digit_bits - 1) / digit_bits;
+    c.bins = 1 << digit_bits;
+    c.tile = kSortBlock * tile_items;
+    c.tiles = (uint32_t)(((uint64_t)n + c.tile - 1) / c.tile);
+    if (c.tiles == 0) c.tiles = 1;
+    return c;
+}
+
+size_t sort_scratch_words(const SortConfig& c) {
+    return (size_t)c.passes * c.bins + (size_t)c.passes + (size_t)c.passes * c.tiles * c.bins;
+}
+
+cudaError_t launch_keys(const StepParams& p, const float4* pos, uint32_t* keys,
+                        const SortConfig& sc, uint32_t* ghist, cudaStream_t s) {
+    if (p.n == 0) return cudaSuccess;
+    uint32_t blocks = (p.n + 255u) / 256u;
+    if (blocks > 152u * 8u) blocks = 152u * 8u;
+    k_keys<<<blocks, 256, 0, s>>>(p, pos, keys, sc.passes, sc.digit_bits, ghist);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sort(uint32_t n, const SortConfig& sc, const SortScratch& scr, uint32_t* keys,
+                        uint32_t* keys_alt, uint32_t* vals, uint32_t* vals_alt,
+                        uint32_t** sorted_keys, uint32_t** sorted_perm, cudaStream_t s) {
+    const uint32_t* kin = keys;
+    const uint32_t* vin = nullptr;  // pass 0 ranks (key, index)
+    uint32_t* kout = keys_alt;
+    uint32_t* vout = vals_alt;
+    for (int pass = 0; pass < sc.passes; pass++) {
+        cudaError_t e;
+        const int items = sc.tile / kSortBlock;
+        if (items == 8)
+            e = launch_onesweep_t<8>(n, sc, scr, pass, kin, vin, kout, vout, s);
+        else if (items == 12)
+            e = launch_onesweep_t<12>(n, sc, scr, pass, kin, vin, kout, vout, s);
+        else
+            e = launch_onesweep_t<16>(n, sc, scr, pass, kin, vin, kout, vout, s);
+        if (e != cudaSuccess) return e;
+        kin = kout;
+        vin = vout;
+        kout = (kout == keys_alt) ? keys : keys_alt;
+        vout = (vout == vals_alt) ? vals : vals_alt;
+    }
+    *sorted_keys = const_cast<uint32_t*>(kin);
+    *sorted_perm = const_cast<uint32_t*>(vin);
+    return cudaSuccess;
+}
+
+cudaError_t launch_cells_reorder(uint32_t n, const uint32_t* skeys, const uint32_t* perm,
+                                 uint32_t* cell_scan, const float4* pos_in, const float4* vel_in,
+                                 float4* pos_out, float4* vel_out, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    k_cells_reorder<<<(n + 255u) / 256u, 256, 0, s>>>(n, skeys, perm, cell_scan, pos_in, vel_in,
+                                                      pos_out, vel_out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_density(const StepParams& p, const float4* pos, const uint32_t* cell_scan,
+                           float4* aux, float4* bnd, cudaStream_t s) {
+    if (p.n == 0) return cudaSuccess;
+    k_density<<<(p.n + 127u) / 128u, 128, 0, s>>>(p, pos, cell_scan, aux, bnd);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_force(const StepParams& p, const float4* pos, const float4* vel,
+                         const float4* aux, const float4* bnd, const uint32_t* cell_scan,
+                         float4* pos_out, float4* vel_out, float4* acc_out, cudaStream_t s) {
+    if (p.n == 0) return cudaSuccess;
+    k_force<<<(p.n + 127u) / 128u, 128, 0, s>>>(p, pos, vel, aux, bnd, cell_scan, pos_out, vel_out,
+                                                acc_out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_offsets(uint32_t n, const uint32_t* cell_scan, uint32_t* offsets,
+                           cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    k_offsets<<<(n + 255u) / 256u, 256, 0, s>>>(n, cell_scan, offsets);
+    return cudaGetLastError();
+}
+
+}  // namespace vfs

@@ -1,0 +1,26 @@
+// GPU SDF + volume-map generation for analytic boundary shapes.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace vfs {
+
+constexpr int kMaxQuadrature = 32;
+
+struct VolumeMapParams {
+    int shape;          // 0 sphere, 1 solid box, 2 container
+    double prm[3];      // radius or half extents
+    float h;            // support radius
+    uint32_t res[3];
+    float dmin[3];      // grid origin (float, like the reference's AABB)
+    double step[3];     // grid step, computed in float then widened
+    int qn;             // Gauss-Legendre points per axis
+    double gx[kMaxQuadrature], gw[kMaxQuadrature];
+    double c0, c1;      // integration-domain half width and centre
+    double w_factor;    // 8 / (pi h^3) in double
+};
+
+cudaError_t launch_volume_map(const VolumeMapParams& p, float* sdf, float* vm, cudaStream_t s);
+
+}  // namespace vfs

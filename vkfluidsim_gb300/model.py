@@ -1,0 +1,322 @@
+"""Python mirror of VkFluidSim's model / scene interface over the C ABI.
+
+Names follow the reference: ``SimulationParameters`` (src/simulation.h:10-13),
+``SPHModel.Parameters`` (src/models/model.h:14-21), ``WCSPHWithBoundaryModel.Parameters``
+(src/models/wcsph_with_boundary_model.h:26-33), ``set_particle_state`` / ``set_particles_in_box``
+/ ``copy_data_buffers`` (src/models/model.h:68-84), ``step`` (wcsph_with_boundary_model.cpp:81-117)
+and ``load_scene`` (src/util/scene_loader.h:8). Arrays are numpy; every call goes through
+``libvfs_cuda.so`` and raises ``VfsError`` with the library's message on a non-zero status.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+from typing import Optional, Sequence
+
+import numpy as np
+
+from . import _abi
+from ._abi import check, load_library
+
+__all__ = [
+    "SimulationParameters", "SPHParameters", "WCSPHParameters", "WCSPHWithBoundaryModel",
+    "AnalyticObject", "load_scene", "generate_lattice", "generate_uniform_blob",
+    "generate_fourier_velocity",
+]
+
+
+def _fp(a: Optional[np.ndarray]):
+    return None if a is None else a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+def _up(a: Optional[np.ndarray]):
+    return None if a is None else a.ctypes.data_as(C.POINTER(C.c_uint32))
+
+
+def _f32(a, shape=None) -> np.ndarray:
+    out = np.ascontiguousarray(np.asarray(a, dtype=np.float32))
+    if shape is not None:
+        out = out.reshape(shape)
+    return out
+
+
+@dataclass
+class SimulationParameters:
+    gravity: Sequence[float] = (0.0, -9.81, 0.0)
+    smooth_radius: float = 0.2
+
+    def to_c(self):
+        return _abi.SimParams((C.c_float * 3)(*self.gravity), self.smooth_radius)
+
+
+@dataclass
+class SPHParameters:
+    time_scale: float = 1.0
+    iterations: int = 3
+    n_particles: int = 8192
+    fixed_dt: float = 1.0 / 60.0
+    target_density: float = 100.0
+    bbox_size: Sequence[float] = (10.0, 10.0, 10.0)
+    bbox_pos: Sequence[float] = (0.0, 0.0, 0.0)
+
+    def to_c(self):
+        return _abi.SphParams(self.time_scale, self.iterations, self.n_particles, self.fixed_dt,
+                              self.target_density, (C.c_float * 3)(*self.bbox_size),
+                              (C.c_float * 3)(*self.bbox_pos))
+
+
+@dataclass
+class WCSPHParameters:
+    wall_stiffness: float = 1e4
+    stiffness: float = 1000.0
+    expoent: float = 7.0
+    viscosity_strenght: float = 0.01
+
+    def to_c(self):
+        return _abi.WcsphParams(self.wall_stiffness, self.stiffness, self.expoent,
+                                self.viscosity_strenght)
+
+
+@dataclass
+class AnalyticObject:
+    """Boundary shape whose SDF and volume map are generated on the GPU."""
+    shape: int
+    params: Sequence[float]
+    position: Sequence[float] = (0.0, 0.0, 0.0)
+    rotation_angle_deg: float = 0.0
+    rotation_axis: Sequence[float] = (0.0, 1.0, 0.0)
+    scale: Sequence[float] = (1.0, 1.0, 1.0)
+    resolution: Sequence[int] = (64, 64, 64)
+
+    def to_c(self):
+        prm = list(self.params) + [0.0] * (3 - len(self.params))
+        return _abi.AnalyticObject(self.shape, (C.c_double * 3)(*prm),
+                                   (C.c_float * 3)(*self.position), self.rotation_angle_deg,
+                                   (C.c_float * 3)(*self.rotation_axis),
+                                   (C.c_float * 3)(*self.scale),
+                                   (C.c_uint32 * 3)(*self.resolution))
+
+
+@dataclass
+class BoundaryObjectInfo:
+    transform: np.ndarray
+    rotation: np.ndarray
+    box_size: np.ndarray
+    box_pos: np.ndarray
+    resolution: tuple
+    sdf: np.ndarray = field(repr=False)
+    volume_map: np.ndarray = field(repr=False)
+
+
+class WCSPHWithBoundaryModel:
+    """A WCSPH-with-boundary model on the GPU (one handle of libvfs_cuda)."""
+
+    def __init__(self, sim: SimulationParameters, sph: SPHParameters, wcsph: WCSPHParameters,
+                 _handle: Optional[int] = None):
+        self._lib = load_library()
+        if _handle is not None:
+            self._h = C.c_void_p(_handle)
+        else:
+            h = C.c_void_p()
+            check(self._lib.vfs_model_create(C.byref(sim.to_c()), C.byref(sph.to_c()),
+                                             C.byref(wcsph.to_c()), C.byref(h)))
+            self._h = h
+
+    # -- lifecycle
+    def clear(self) -> None:
+        if getattr(self, "_h", None) and self._h.value:
+            self._lib.vfs_model_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.clear()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.clear()
+
+    @property
+    def n_particles(self) -> int:
+        return int(self._lib.vfs_model_num_particles(self._h))
+
+    def get_parameters(self):
+        s, p, w = _abi.SimParams(), _abi.SphParams(), _abi.WcsphParams()
+        check(self._lib.vfs_model_get_parameters(self._h, C.byref(s), C.byref(p), C.byref(w)))
+        return (SimulationParameters(tuple(s.gravity), s.smooth_radius),
+                SPHParameters(p.time_scale, p.iterations, p.n_particles, p.fixed_dt,
+                              p.target_density, tuple(p.bbox_size), tuple(p.bbox_pos)),
+                WCSPHParameters(w.wall_stiffness, w.stiffness, w.expoent, w.viscosity_strenght))
+
+    def set_parameters(self, sim=None, sph=None, wcsph=None) -> None:
+        a = C.byref(sim.to_c()) if sim else None
+        b = C.byref(sph.to_c()) if sph else None
+        c = C.byref(wcsph.to_c()) if wcsph else None
+        check(self._lib.vfs_model_set_parameters(self._h, a, b, c))
+
+    def set_stream(self, stream_handle: int) -> None:
+        check(self._lib.vfs_model_set_stream(self._h, C.c_void_p(stream_handle)))
+
+    # -- boundary objects
+    def add_boundary_object(self, transform, rotation, box_size, box_pos, resolution, sdf,
+                            volume_map) -> None:
+        sdf = _f32(sdf).ravel()
+        vm = _f32(volume_map).ravel()
+        o = _abi.BoundaryObject()
+        o.transform[:] = [float(x) for x in np.asarray(transform, np.float32).ravel()]
+        o.rotation[:] = [float(x) for x in np.asarray(rotation, np.float32).ravel()]
+        o.box_size[:] = list(map(float, box_size))
+        o.box_pos[:] = list(map(float, box_pos))
+        o.resolution[:] = list(map(int, resolution))
+        o.sdf_grid = _fp(sdf)
+        o.volume_map_grid = _fp(vm)
+        check(self._lib.vfs_model_add_boundary_object(self._h, C.byref(o)))
+
+    def add_analytic_object(self, obj: AnalyticObject) -> None:
+        check(self._lib.vfs_model_add_analytic_object(self._h, C.byref(obj.to_c())))
+
+    @property
+    def n_boundary_objects(self) -> int:
+        return int(self._lib.vfs_model_num_boundary_objects(self._h))
+
+    def get_boundary_object(self, idx: int) -> BoundaryObjectInfo:
+        info = _abi.BoundaryObject()
+        check(self._lib.vfs_model_get_boundary_object(self._h, idx, C.byref(info), None, None))
+        res = tuple(int(x) for x in info.resolution)
+        cnt = res[0] * res[1] * res[2]
+        sdf = np.empty(cnt, np.float32)
+        vm = np.empty(cnt, np.float32)
+        check(self._lib.vfs_model_get_boundary_object(self._h, idx, None, _fp(sdf), _fp(vm)))
+        return BoundaryObjectInfo(np.array(info.transform[:], np.float32),
+                                  np.array(info.rotation[:], np.float32),
+                                  np.array(info.box_size[:], np.float32),
+                                  np.array(info.box_pos[:], np.float32), res, sdf, vm)
+
+    # -- state
+    def set_particle_state(self, pos, vel, offset: int = 0, count: int = -1) -> None:
+        pos = _f32(pos, (-1, 3))
+        vel = _f32(vel, (-1, 3))
+        if count < 0:
+            count = pos.shape[0]
+        if pos.shape[0] < count or vel.shape[0] < count:
+            raise ValueError("pos/vel hold fewer rows than count")
+        check(self._lib.vfs_model_set_particle_state(self._h, _fp(pos), _fp(vel), offset, count))
+
+    def set_particles_in_box(self, box_size, box_pos, offset: int = 0, count: int = -1,
+                             mode: int = 0, seed: int = 0) -> None:
+        bs = _f32(box_size, (3,))
+        bp = _f32(box_pos, (3,))
+        check(self._lib.vfs_model_set_particles_in_box(self._h, _fp(bs), _fp(bp), offset, count,
+                                                       mode, seed))
+
+    def copy_data_buffers(self, with_acc: bool = False) -> dict:
+        n = self.n_particles
+        pos = np.empty((n, 3), np.float32)
+        vel = np.empty((n, 3), np.float32)
+        dens = np.empty(n, np.float32)
+        acc = np.empty((n, 3), np.float32) if with_acc else None
+        check(self._lib.vfs_model_copy_data_buffers(self._h, _fp(pos), _fp(vel), _fp(dens),
+                                                    _fp(acc)))
+        out = {"positions": pos, "velocities": vel, "densities": dens}
+        if with_acc:
+            out["accelerations"] = acc
+        return out
+
+    def get_ids(self) -> np.ndarray:
+        ids = np.empty(self.n_particles, np.uint32)
+        check(self._lib.vfs_model_get_ids(self._h, _up(ids)))
+        return ids
+
+    def get_neighbor_arrays(self):
+        n = self.n_particles
+        keys = np.empty(n, np.uint32)
+        perm = np.empty(n, np.uint32)
+        offs = np.empty(n, np.uint32)
+        check(self._lib.vfs_model_get_neighbor_arrays(self._h, _up(keys), _up(perm), _up(offs)))
+        return keys, perm, offs
+
+    def get_boundary_fields(self):
+        n = self.n_particles
+        bd = np.empty(n, np.float32)
+        bg = np.empty((n, 3), np.float32)
+        check(self._lib.vfs_model_get_boundary_fields(self._h, _fp(bd), _fp(bg)))
+        return bd, bg
+
+    def record_fields(self, enable: bool = True) -> None:
+        check(self._lib.vfs_model_record_fields(self._h, int(enable)))
+
+    # -- stepping
+    def step(self) -> None:
+        check(self._lib.vfs_model_step(self._h))
+
+    def substeps(self, count: int) -> None:
+        check(self._lib.vfs_model_substeps(self._h, count))
+
+    def use_graph(self, enable: bool) -> None:
+        check(self._lib.vfs_model_use_graph(self._h, int(enable)))
+
+    def synchronize(self) -> None:
+        check(self._lib.vfs_model_synchronize(self._h))
+
+    PHASES = ("keys", "sort", "cells_reorder", "density", "force", "clear")
+
+    def profile_substeps(self, count: int) -> dict:
+        ms = (C.c_float * 6)()
+        check(self._lib.vfs_model_profile_substeps(self._h, count, ms))
+        return dict(zip(self.PHASES, (float(x) for x in ms)))
+
+    def set_sort_config(self, digit_bits: int, tile_items: int) -> None:
+        check(self._lib.vfs_model_set_sort_config(self._h, digit_bits, tile_items))
+
+    def get_sort_config(self):
+        d, t, p = C.c_int32(), C.c_int32(), C.c_int32()
+        check(self._lib.vfs_model_get_sort_config(self._h, C.byref(d), C.byref(t), C.byref(p)))
+        return d.value, t.value, p.value
+
+    def device_state(self):
+        p, v = C.c_void_p(), C.c_void_p()
+        check(self._lib.vfs_model_device_state(self._h, C.byref(p), C.byref(v)))
+        return p.value, v.value
+
+    # -- scene
+    def reset(self) -> None:
+        check(self._lib.vfs_scene_reset(self._h))
+
+
+def load_scene(json_path: str, resources_dir: str = "") -> WCSPHWithBoundaryModel:
+    """LoadScene + GenericScene::Init/Reset (src/util/scene_loader.cpp:113-140)."""
+    lib = load_library()
+    h = C.c_void_p()
+    check(lib.vfs_scene_load(str(json_path).encode(), str(resources_dir).encode(), C.byref(h)))
+    return WCSPHWithBoundaryModel(None, None, None, _handle=h.value)
+
+
+def generate_lattice(dims, origin, spacing: float, jitter: float, seed: int) -> np.ndarray:
+    lib = load_library()
+    d = np.asarray(dims, np.uint32)
+    o = _f32(origin, (3,))
+    out = np.empty((int(np.prod(d.astype(np.uint64))), 3), np.float32)
+    check(lib.vfs_generate_lattice(_up(d), _fp(o), spacing, jitter, seed, _fp(out)))
+    return out
+
+
+def generate_uniform_blob(n_uniform: int, lo, hi, n_blob: int, center, sigma: float,
+                          seed: int) -> np.ndarray:
+    lib = load_library()
+    out = np.empty((n_uniform + n_blob, 3), np.float32)
+    check(lib.vfs_generate_uniform_blob(n_uniform, _fp(_f32(lo, (3,))), _fp(_f32(hi, (3,))),
+                                        n_blob, _fp(_f32(center, (3,))), sigma, seed, _fp(out)))
+    return out
+
+
+def generate_fourier_velocity(pos, modes: int, amplitude: float, seed: int) -> np.ndarray:
+    lib = load_library()
+    pos = _f32(pos, (-1, 3))
+    out = np.empty_like(pos)
+    check(lib.vfs_generate_fourier_velocity(pos.shape[0], _fp(pos), modes, amplitude, seed,
+                                            _fp(out)))
+    return out

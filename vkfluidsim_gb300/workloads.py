@@ -1,0 +1,116 @@
+"""Seeded synthetic scenes with the shapes of the benchmark configurations.
+
+Each workload is a parameter set, a list of analytic boundary objects and an initial state; the
+same description builds the GPU model and (in tests) the CPU oracle.
+
+* ``dam_break_32k``  — 32^3 jittered lattice (spacing 0.02, jitter +-0.1 spacing) in the corner of
+  a 1 m box, h = 0.04, rho0 = 1000, k = 50, gamma = 7, nu = 0.01, g = -9.81 z, dt = 2e-4, box walls
+  as a 64^3 container volume map.
+* ``obstacle_1m``    — 1,048,576 particles: a 128 x 128 x 64 lattice at spacing 0.0075 (h = 0.015)
+  in a 2 x 1 x 1 m box holding a sphere of radius 0.2 (128^3 volume map), dt = 1e-4. (128^3
+  particles at spacing 0.01 cannot give 1,048,576 particles nor fit the box, so the particle
+  count is kept and the lattice is resized.)
+* ``stress_4m``      — 4,194,304 uniform particles in 4 x 2 x 2 m plus 419,430 in a Gaussian blob
+  (sigma = 0.1 m), h = 0.02, container volume map 128^3.
+* ``dam_break_64k``  — 65,536 particles (64 x 32 x 32 lattice, spacing 0.015, h = 0.03) in a 1 m
+  box, dt = 2e-4: the differentiable-rollout scene.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field, replace
+from typing import List
+
+import numpy as np
+
+from ._abi import SHAPE_CONTAINER, SHAPE_SPHERE
+from .model import (AnalyticObject, SimulationParameters, SPHParameters, WCSPHParameters,
+                    WCSPHWithBoundaryModel, generate_lattice, generate_uniform_blob)
+
+
+@dataclass
+class Workload:
+    name: str
+    sim: SimulationParameters
+    sph: SPHParameters
+    wcsph: WCSPHParameters
+    objects: List[AnalyticObject]
+    pos: np.ndarray
+    vel: np.ndarray
+    steps: int = 1
+    notes: dict = field(default_factory=dict)
+
+    @property
+    def n(self) -> int:
+        return int(self.pos.shape[0])
+
+
+def _container(lo, hi, res) -> AnalyticObject:
+    lo = np.asarray(lo, np.float64)
+    hi = np.asarray(hi, np.float64)
+    c = 0.5 * (lo + hi)
+    he = 0.5 * (hi - lo)
+    return AnalyticObject(SHAPE_CONTAINER, tuple(he), position=tuple(float(x) for x in c),
+                          resolution=tuple(res))
+
+
+def dam_break(dims=(32, 32, 32), spacing=0.02, box=(1.0, 1.0, 1.0), map_res=64, dt=2e-4,
+              stiffness=50.0, viscosity=0.01, seed=0, jitter=0.1, steps=200,
+              name="dam_break") -> Workload:
+    h = 2.0 * spacing
+    pos = generate_lattice(dims, (0.0, 0.0, 0.0), spacing, jitter, seed)
+    n = pos.shape[0]
+    sim = SimulationParameters((0.0, 0.0, -9.81), h)
+    sph = SPHParameters(1.0, 1, n, dt, 1000.0, box, (0.0, 0.0, 0.0))
+    wc = WCSPHParameters(1e4, stiffness, 7.0, viscosity)
+    objs = [_container((0, 0, 0), box, (map_res,) * 3)] if map_res else []
+    return Workload(name, sim, sph, wc, objs, pos, np.zeros_like(pos), steps)
+
+
+def dam_break_32k(**kw) -> Workload:
+    return dam_break(name="dam_break_32k", **kw)
+
+
+def obstacle_1m(map_res=128, seed=1, steps=1000) -> Workload:
+    spacing = 0.0075
+    h = 2.0 * spacing
+    pos = generate_lattice((128, 128, 64), (0.0, 0.0, 0.0), spacing, 0.1, seed)
+    n = pos.shape[0]
+    sim = SimulationParameters((0.0, 0.0, -9.81), h)
+    sph = SPHParameters(1.0, 1, n, 1e-4, 1000.0, (2.0, 1.0, 1.0), (0.0, 0.0, 0.0))
+    wc = WCSPHParameters(1e4, 50.0, 7.0, 0.01)
+    sphere = AnalyticObject(SHAPE_SPHERE, (0.2,), position=(1.4, 0.5, 0.2),
+                            resolution=(map_res,) * 3)
+    return Workload("obstacle_1m", sim, sph, wc, [sphere], pos, np.zeros_like(pos), steps)
+
+
+def stress_4m(n_uniform=4_194_304, n_blob=419_430, map_res=128, seed=2, steps=100) -> Workload:
+    box = (4.0, 2.0, 2.0)
+    pos = generate_uniform_blob(n_uniform, (0, 0, 0), box, n_blob, (2.0, 1.0, 1.0), 0.1, seed)
+    n = pos.shape[0]
+    sim = SimulationParameters((0.0, 0.0, -9.81), 0.02)
+    sph = SPHParameters(1.0, 1, n, 1e-4, 1000.0, box, (0.0, 0.0, 0.0))
+    wc = WCSPHParameters(1e4, 50.0, 7.0, 0.01)
+    objs = [_container((0, 0, 0), box, (map_res,) * 3)] if map_res else []
+    return Workload("stress_4m", sim, sph, wc, objs, pos, np.zeros_like(pos), steps)
+
+
+def dam_break_64k(map_res=64, seed=4, steps=300) -> Workload:
+    return dam_break(dims=(64, 32, 32), spacing=0.015, map_res=map_res, dt=2e-4, stiffness=50.0,
+                     viscosity=0.01, seed=seed, steps=steps, name="dam_break_64k")
+
+
+def build_model(w: Workload) -> WCSPHWithBoundaryModel:
+    """Creates the GPU model of a workload: parameters, boundary objects, initial state."""
+    m = WCSPHWithBoundaryModel(w.sim, replace(w.sph, n_particles=w.n), w.wcsph)
+    for o in w.objects:
+        m.add_analytic_object(o)
+    m.set_particle_state(w.pos, w.vel)
+    return m
+
+
+WORKLOADS = {
+    "dam_break_32k": dam_break_32k,
+    "obstacle_1m": obstacle_1m,
+    "stress_4m": stress_4m,
+    "dam_break_64k": dam_break_64k,
+}
