@@ -211,15 +211,24 @@ struct Ranges {
 };
 
 // Sorted-index ranges of the three x-neighbour buckets of row (dy, dz), in the order the
-// reference visits them (offsets_3d: x fastest).
+// reference visits them (offsets_3d: x fastest). When cells cx-1..cx+1 lie in one 50-cell hash
+// block their hashes are hA, hA+1, hA+2, so one hash and one modulo give all three keys, and the
+// keys are consecutive unless kA + 2 wraps past n.
 __device__ __forceinline__ Ranges row_ranges(const StepParams& p,
                                              const uint32_t* __restrict__ scan, uint32_t cx,
                                              uint32_t cy, uint32_t cz) {
-    const uint32_t kA = key_mod(hash_cell(cx - 1u, cy, cz), p.mod_magic, p.n);
-    const uint32_t kB = key_mod(hash_cell(cx, cy, cz), p.mod_magic, p.n);
-    const uint32_t kC = key_mod(hash_cell(cx + 1u, cy, cz), p.mod_magic, p.n);
+    const uint32_t hA = hash_cell(cx - 1u, cy, cz);
+    const uint32_t kA = key_mod(hA, p.mod_magic, p.n);
     Ranges r;
     r.b0 = __ldg(scan + kA);
+    const bool same_block = ((cx - 1u + 25u) % 50u) <= 47u && hA <= 0xFFFFFFFDu;
+    if (same_block && kA + 2u < p.n) {
+        r.e0 = __ldg(scan + kA + 3u);
+        r.b1 = r.e1 = r.b2 = r.e2 = 0u;
+        return r;
+    }
+    const uint32_t kB = key_mod(hash_cell(cx, cy, cz), p.mod_magic, p.n);
+    const uint32_t kC = key_mod(hash_cell(cx + 1u, cy, cz), p.mod_magic, p.n);
     if (kB == kA + 1u && kC == kA + 2u) {
         r.e0 = __ldg(scan + kA + 3u);
         r.b1 = r.e1 = r.b2 = r.e2 = 0u;
@@ -414,24 +423,60 @@ __global__ void __launch_bounds__(BLOCK)
     }
 }
 
-__global__ void __launch_bounds__(256)
+// First index in sorted keys[0, n) whose key is >= c (n when none).
+__device__ __forceinline__ uint32_t lower_bound_keys(const uint32_t* __restrict__ keys, uint32_t n,
+                                                    uint32_t c) {
+    uint32_t lo = 0u, hi = n;
+    while (lo < hi) {
+        const uint32_t mid = lo + ((hi - lo) >> 1);
+        if (keys[mid] < c)
+            lo = mid + 1u;
+        else
+            hi = mid;
+    }
+    return lo;
+}
+
+constexpr uint32_t kCellBlock = 256;
+
+// Block b owns keys [256 b, 256 b + 256) of cell_scan (n + 1 entries: cell_scan[k] is the first
+// sorted index with key >= k, so bucket k is [cell_scan[k], cell_scan[k + 1])) and gathers the
+// particles with sorted indices in the same range. Two binary searches bound the block's slice
+// of the sorted keys; each element of the slice writes the entries between its predecessor's key
+// and its own, which never leave the block's range, so no thread loops over more than 256
+// entries however the keys cluster.
+__global__ void __launch_bounds__(kCellBlock)
     k_cells_reorder(uint32_t n, const uint32_t* __restrict__ skeys,
                     const uint32_t* __restrict__ perm, uint32_t* __restrict__ scan,
                     const float4* __restrict__ pos_in, const float4* __restrict__ vel_in,
                     float4* __restrict__ pos_out, float4* __restrict__ vel_out) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    // Keys and permutation entries are < n by construction; the clamps only keep accesses in
-    // bounds after a reported sort failure.
-    const uint32_t k = min(skeys[i], n - 1u);
-    const uint32_t c0 = i == 0u ? 0u : min(skeys[i - 1], n - 1u) + 1u;
-    for (uint32_t c = c0; c <= k; c++) scan[c] = i;
-    if (i == n - 1u)
-        for (uint32_t c = k + 1u; c <= n; c++) scan[c] = n;
-    uint32_t src = perm[i];
-    if (src >= n) src = i;
-    pos_out[i] = __ldg(pos_in + src);
-    vel_out[i] = __ldg(vel_in + src);
+    __shared__ uint32_t s_lo, s_hi;
+    const uint32_t c0 = blockIdx.x * kCellBlock;
+    const uint32_t c1 = min(c0 + kCellBlock, n + 1u);
+    const uint32_t tid = threadIdx.x;
+    if (tid == 0) s_lo = lower_bound_keys(skeys, n, c0);
+    if (tid == 32) s_hi = lower_bound_keys(skeys, n, c1);
+    const uint32_t i = c0 + tid;
+    if (i < n) {
+        uint32_t src = perm[i];
+        if (src >= n) src = i;  // only after a reported sort failure
+        pos_out[i] = __ldg(pos_in + src);
+        vel_out[i] = __ldg(vel_in + src);
+    }
+    __syncthreads();
+    const uint32_t lo = s_lo, hi = max(s_lo, s_hi);
+    if (lo == hi) {
+        for (uint32_t c = c0 + tid; c < c1; c += kCellBlock) scan[c] = lo;
+        return;
+    }
+    // The clamps keep writes inside [c0, c1) even if the keys were not sorted.
+    for (uint32_t j = lo + tid; j < hi; j += kCellBlock) {
+        const uint32_t k = min(skeys[j], c1 - 1u);
+        const uint32_t start = j == lo ? c0 : max(skeys[j - 1] + 1u, c0);
+        for (uint32_t c = start; c <= k; c++) scan[c] = j;
+    }
+    const uint32_t last = max(min(skeys[hi - 1u], c1 - 1u) + 1u, c0);
+    for (uint32_t c = last + tid; c < c1; c += kCellBlock) scan[c] = hi;
 }
 
 __global__ void __launch_bounds__(256)
@@ -442,8 +487,20 @@ __global__ void __launch_bounds__(256)
     offsets[k] = b > a ? a : n;
 }
 
+// Density contribution of one candidate (CalculateDensities inner loop, slang:180-188).
+__device__ __forceinline__ void density_term(const StepParams& p, const float4& xi, const float4& xj,
+                                             float& rho) {
+    const float dx = xj.x - xi.x, dy = xj.y - xi.y, dz = xj.z - xi.z;
+    const float r2 = dx * dx + dy * dy + dz * dz;
+    if (r2 <= p.h2) {
+        const float r = sqrtf(r2);
+        rho += p.mass * cubic_w(r * p.inv_h, p.cubic);
+    }
+}
+
 // CalculateBoundaryVolume + CalculateDensities + the per-particle part of PressureFromDensityEOS
-// (wcsph_with_boundary_model.slang:102-203).
+// (wcsph_with_boundary_model.slang:102-203). Candidates are fetched four at a time so several
+// 128-bit loads are in flight per thread; they are accumulated in the reference's order.
 __global__ void __launch_bounds__(128)
     k_density(StepParams p, const float4* __restrict__ pos, const uint32_t* __restrict__ scan,
               float4* __restrict__ aux, float4* __restrict__ bnd) {
@@ -464,14 +521,18 @@ __global__ void __launch_bounds__(128)
         for (int seg = 0; seg < 3; seg++) {
             const uint32_t b = seg == 0 ? rg.b0 : (seg == 1 ? rg.b1 : rg.b2);
             const uint32_t e = seg == 0 ? rg.e0 : (seg == 1 ? rg.e1 : rg.e2);
-            for (uint32_t j = b; j < e; j++) {
-                const float4 xj = __ldg(pos + j);
-                const float dx = xj.x - xi.x, dyy = xj.y - xi.y, dzz = xj.z - xi.z;
-                const float r2 = dx * dx + dyy * dyy + dzz * dzz;
-                if (r2 > p.h2) continue;
-                const float r = sqrtf(r2);
-                rho += p.mass * cubic_w(r * p.inv_h, p.cubic);
+            uint32_t j = b;
+#pragma unroll 1
+            for (; j + 4u <= e; j += 4u) {
+                const float4 q0 = __ldg(pos + j), q1 = __ldg(pos + j + 1u);
+                const float4 q2 = __ldg(pos + j + 2u), q3 = __ldg(pos + j + 3u);
+                density_term(p, xi, q0, rho);
+                density_term(p, xi, q1, rho);
+                density_term(p, xi, q2, rho);
+                density_term(p, xi, q3, rho);
             }
+#pragma unroll 1
+            for (; j < e; j++) density_term(p, xi, __ldg(pos + j), rho);
         }
     }
     rho += p.rho0 * bd;
@@ -483,9 +544,40 @@ __global__ void __launch_bounds__(128)
     bnd[i] = make_float4(bgx, bgy, bgz, bd);
 }
 
+struct ForceAcc {
+    float Px, Py, Pz, Vx, Vy, Vz;
+};
+
+// Pressure and viscosity contributions of one in-range neighbour (PressureAccel slang:234-249,
+// ViscousAccel slang:301-318); both sums keep the reference's visiting order.
+__device__ __forceinline__ void force_term(const StepParams& p, const float4& xi, const float4& vi,
+                                           float pdi, float xx, float xy, float xz, float r2,
+                                           const float2& aj, const float4& vj, ForceAcc& f) {
+    const float r = sqrtf(r2);
+    float nx = 0.0f, ny = 1.0f, nz = 0.0f;
+    if (r > 0.0f) {
+        const float ir = 1.0f / r;
+        nx = xx * ir;
+        ny = xy * ir;
+        nz = xz * ir;
+    }
+    const float gw = cubic_dw(r, r * p.inv_h, p.grad_over_h);
+    const float s = (p.mass * (pdi + aj.x)) * gw;
+    f.Px += s * nx;
+    f.Py += s * ny;
+    f.Pz += s * nz;
+    const float dv = (vi.x - vj.x) * xx + (vi.y - vj.y) * xy + (vi.z - vj.z) * xz;
+    const float tv = aj.y * dv;
+    const float iden = 1.0f / (r2 + p.visc_eps);
+    f.Vx += (tv * (nx * gw)) * iden;
+    f.Vy += (tv * (ny * gw)) * iden;
+    f.Vz += (tv * (nz * gw)) * iden;
+}
+
 // CalculatePressureAccel + CalculateViscousAccel + UpdatePositions
 // (wcsph_with_boundary_model.slang:205-360), fused: both sums are accumulated separately in the
-// reference's visiting order, then a = ((g - P) + V) + wall, v += a dt, x += v dt.
+// reference's visiting order, then a = ((g - P) + V) + wall, v += a dt, x += v dt. Positions of
+// four candidates are fetched together; velocity and density products only for those in range.
 __global__ void __launch_bounds__(128)
     k_force(StepParams p, const float4* __restrict__ pos, const float4* __restrict__ vel,
             const float4* __restrict__ aux, const float4* __restrict__ bnd,
@@ -501,8 +593,7 @@ __global__ void __launch_bounds__(128)
 
     const uint32_t cx = cell_coord(xi.x, p.h), cy = cell_coord(xi.y, p.h),
                    cz = cell_coord(xi.z, p.h);
-    float Px = 0.0f, Py = 0.0f, Pz = 0.0f;
-    float Vx = 0.0f, Vy = 0.0f, Vz = 0.0f;
+    ForceAcc f{0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
 #pragma unroll 1
     for (int t = 0; t < 9; t++) {
         const uint32_t dy = (uint32_t)(t % 3) - 1u, dz = (uint32_t)(t / 3) - 1u;
@@ -511,46 +602,50 @@ __global__ void __launch_bounds__(128)
         for (int seg = 0; seg < 3; seg++) {
             const uint32_t b = seg == 0 ? rg.b0 : (seg == 1 ? rg.b1 : rg.b2);
             const uint32_t e = seg == 0 ? rg.e0 : (seg == 1 ? rg.e1 : rg.e2);
-            for (uint32_t j = b; j < e; j++) {
-                if (j == i) continue;
-                const float4 xj = __ldg(pos + j);
-                const float xx = xi.x - xj.x, xy = xi.y - xj.y, xz = xi.z - xj.z;
-                const float r2 = xx * xx + xy * xy + xz * xz;
-                if (r2 > p.h2) continue;
-                const float2 aj = __ldg(aux2 + 2 * (size_t)j);
-                const float4 vj = __ldg(vel + j);
-                const float r = sqrtf(r2);
-                float nx = 0.0f, ny = 1.0f, nz = 0.0f;
-                if (r > 0.0f) {
-                    const float ir = 1.0f / r;
-                    nx = xx * ir;
-                    ny = xy * ir;
-                    nz = xz * ir;
+#pragma unroll 1
+            for (uint32_t j = b; j < e; j += 4u) {
+                float4 q[4];
+                float r2[4];
+                bool in[4];
+#pragma unroll
+                for (int u = 0; u < 4; u++) {
+                    const uint32_t jj = j + u;
+                    q[u] = jj < e ? __ldg(pos + jj) : make_float4(0.f, 0.f, 0.f, 0.f);
                 }
-                const float gw = cubic_dw(r, r * p.inv_h, p.grad_over_h);
-                const float s = (p.mass * (pdi + aj.x)) * gw;
-                Px += s * nx;
-                Py += s * ny;
-                Pz += s * nz;
-                const float dv = (vi.x - vj.x) * xx + (vi.y - vj.y) * xy + (vi.z - vj.z) * xz;
-                const float tv = aj.y * dv;
-                const float iden = 1.0f / (r2 + p.visc_eps);
-                Vx += (tv * (nx * gw)) * iden;
-                Vy += (tv * (ny * gw)) * iden;
-                Vz += (tv * (nz * gw)) * iden;
+#pragma unroll
+                for (int u = 0; u < 4; u++) {
+                    const uint32_t jj = j + u;
+                    q[u].x = xi.x - q[u].x;
+                    q[u].y = xi.y - q[u].y;
+                    q[u].z = xi.z - q[u].z;
+                    r2[u] = q[u].x * q[u].x + q[u].y * q[u].y + q[u].z * q[u].z;
+                    in[u] = jj < e && jj != i && r2[u] <= p.h2;
+                }
+                float2 a[4];
+                float4 v[4];
+#pragma unroll
+                for (int u = 0; u < 4; u++) {
+                    if (in[u]) {
+                        a[u] = __ldg(aux2 + 2 * (size_t)(j + u));
+                        v[u] = __ldg(vel + j + u);
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < 4; u++)
+                    if (in[u]) force_term(p, xi, vi, pdi, q[u].x, q[u].y, q[u].z, r2[u], a[u], v[u], f);
             }
         }
     }
     const float4 bi = __ldg(bnd + i);
     const float sb = (pdi + ai.w) * p.rho0;
-    Px += sb * bi.x;
-    Py += sb * bi.y;
-    Pz += sb * bi.z;
+    f.Px += sb * bi.x;
+    f.Py += sb * bi.y;
+    f.Pz += sb * bi.z;
 
-    float ax = p.gx + -Px, ay = p.gy + -Py, az = p.gz + -Pz;
-    ax += p.visc_scale * Vx;
-    ay += p.visc_scale * Vy;
-    az += p.visc_scale * Vz;
+    float ax = p.gx + -f.Px, ay = p.gy + -f.Py, az = p.gz + -f.Pz;
+    ax += p.visc_scale * f.Vx;
+    ay += p.visc_scale * f.Vy;
+    az += p.visc_scale * f.Vz;
     // WallAcceleration, wcsph_with_boundary_model.slang:336-347.
     const float dx = fminf(xi.x - p.lo[0], 0.0f) - fminf(p.hi[0] - xi.x, 0.0f);
     const float dyw = fminf(xi.y - p.lo[1], 0.0f) - fminf(p.hi[1] - xi.y, 0.0f);
@@ -641,8 +736,8 @@ cudaError_t launch_cells_reorder(uint32_t n, const uint32_t* skeys, const uint32
                                  uint32_t* cell_scan, const float4* pos_in, const float4* vel_in,
                                  float4* pos_out, float4* vel_out, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
-    k_cells_reorder<<<(n + 255u) / 256u, 256, 0, s>>>(n, skeys, perm, cell_scan, pos_in, vel_in,
-                                                      pos_out, vel_out);
+    k_cells_reorder<<<(n + kCellBlock) / kCellBlock, kCellBlock, 0, s>>>(
+        n, skeys, perm, cell_scan, pos_in, vel_in, pos_out, vel_out);
     return cudaGetLastError();
 }
 
