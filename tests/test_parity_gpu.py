@@ -266,3 +266,16 @@ def test_partial_state_update_and_profile():
     m.synchronize()
     with pytest.raises(vfs.VfsError):
         m.set_particle_state(newp, newp, offset=w.n - 10, count=100)
+
+
+def test_dense_cluster_overflows_the_neighbour_list():
+    """A tight Gaussian cluster gives hundreds of neighbours per particle, more than the
+    neighbour-list capacity: the force pass must fall back to its own candidate walk."""
+    w = W.stress_4m(n_uniform=20000, n_blob=4000, map_res=0)
+    blob = vfs.generate_uniform_blob(0, (0, 0, 0), (1, 1, 1), 4000, (2.0, 1.0, 1.0), 0.008, 77)
+    w.pos[20000:] = blob
+    m = W.build_model(w)
+    o = oracle_for(w, m)
+    compare_step(m, o, "dense_cluster")
+    g = m.copy_data_buffers()
+    assert g["densities"].max() > 50 * np.median(g["densities"])

@@ -203,6 +203,7 @@ void Model::refresh_params() {
     p.grad_eps = 0.1f * r;
     p.bnd_eighth = 0.125f * r;
     p.bnd_half = 0.5f * r;
+    p.nbr_cap = kNbrCap;
     p.n_objects = (uint32_t)objects.size();
     for (size_t o = 0; o < objects.size() && o < (size_t)kMaxObjects; o++) {
         DevObject& d = p.obj[o];
@@ -257,10 +258,10 @@ int Model::enqueue_substep(cudaEvent_t* ev) {
     if (ev) VFS_CUDA_TRY(cudaEventRecord(ev[3], s));
     VFS_CUDA_TRY(launch_cells_reorder(n, skeys, sperm, cell_scan, pos[c], vel[c], pos[o], vel[o], s));
     if (ev) VFS_CUDA_TRY(cudaEventRecord(ev[4], s));
-    VFS_CUDA_TRY(launch_density(params, pos[o], cell_scan, aux, bnd, s));
+    VFS_CUDA_TRY(launch_density(params, pos[o], cell_scan, aux, bnd, nbr, nbr_count, s));
     if (ev) VFS_CUDA_TRY(cudaEventRecord(ev[5], s));
-    VFS_CUDA_TRY(launch_force(params, pos[o], vel[o], aux, bnd, cell_scan, pos[c], vel[c],
-                              record ? acc : nullptr, s));
+    VFS_CUDA_TRY(launch_force(params, pos[o], vel[o], aux, bnd, cell_scan, nbr, nbr_count, pos[c],
+                              vel[c], record ? acc : nullptr, s));
     if (ev) VFS_CUDA_TRY(cudaEventRecord(ev[6], s));
     return VFS_OK;
 }
@@ -322,6 +323,8 @@ Model::~Model() {
     cudaFree(bnd);
     cudaFree(acc);
     cudaFree(stage);
+    cudaFree(nbr);
+    cudaFree(nbr_count);
     cudaFree(scratch);
     cudaFree(err);
     for (auto& o : objects) {
@@ -348,6 +351,8 @@ int Model::init() {
     VFS_CUDA_TRY(cudaMalloc(&bnd, N * sizeof(float4)));
     VFS_CUDA_TRY(cudaMalloc(&acc, N * sizeof(float4)));
     VFS_CUDA_TRY(cudaMalloc(&stage, N * 32));
+    VFS_CUDA_TRY(cudaMalloc(&nbr, N * kNbrCap * sizeof(uint32_t)));
+    VFS_CUDA_TRY(cudaMalloc(&nbr_count, N * sizeof(uint32_t)));
     VFS_CUDA_TRY(cudaMalloc(&err, 4));
     VFS_CUDA_TRY(cudaMemset(err, 0, 4));
     for (int b = 0; b < 2; b++) {

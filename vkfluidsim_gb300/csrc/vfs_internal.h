@@ -13,6 +13,7 @@ constexpr uint32_t kFlagAggregate = 1u << 30;
 constexpr uint32_t kFlagPrefix = 2u << 30;
 constexpr uint32_t kCountMask = (1u << 30) - 1u;
 constexpr uint32_t kMaxParticles = 1u << 30;
+constexpr uint32_t kNbrCap = 64;  // neighbour-list slots per particle (overflow falls back)
 
 // Error bits of the per-model device error word.
 constexpr uint32_t kErrLookbackTimeout = 1u;
@@ -49,6 +50,7 @@ struct StepParams {
     float grad_eps;     // 0.1 h (GradientVector)
     float bnd_eighth;   // 0.125 h
     float bnd_half;     // 0.5 h
+    uint32_t nbr_cap;   // neighbour-list slots per particle
     DevObject obj[kMaxObjects];
 };
 
@@ -83,13 +85,15 @@ cudaError_t launch_sort(uint32_t n, const SortConfig& sc, const SortScratch& scr
 cudaError_t launch_cells_reorder(uint32_t n, const uint32_t* skeys, const uint32_t* perm,
                                  uint32_t* cell_scan, const float4* pos_in, const float4* vel_in,
                                  float4* pos_out, float4* vel_out, cudaStream_t s);
-// Boundary volume + density + EOS epilogue.
+// Boundary volume + density + EOS epilogue; writes each particle's neighbour list.
 cudaError_t launch_density(const StepParams& p, const float4* pos, const uint32_t* cell_scan,
-                           float4* aux, float4* bnd, cudaStream_t s);
-// Pressure + viscosity + wall + symplectic Euler.
+                           float4* aux, float4* bnd, uint32_t* nbr, uint32_t* nbr_count,
+                           cudaStream_t s);
+// Pressure + viscosity + wall + symplectic Euler over the density pass's neighbour lists.
 cudaError_t launch_force(const StepParams& p, const float4* pos, const float4* vel,
                          const float4* aux, const float4* bnd, const uint32_t* cell_scan,
-                         float4* pos_out, float4* vel_out, float4* acc_out, cudaStream_t s);
+                         const uint32_t* nbr, const uint32_t* nbr_count, float4* pos_out,
+                         float4* vel_out, float4* acc_out, cudaStream_t s);
 // spatial_offsets[k] = cell start or n for empty keys (reference layout).
 cudaError_t launch_offsets(uint32_t n, const uint32_t* cell_scan, uint32_t* offsets,
                            cudaStream_t s);

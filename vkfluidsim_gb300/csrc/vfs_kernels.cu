@@ -487,32 +487,28 @@ __global__ void __launch_bounds__(256)
     offsets[k] = b > a ? a : n;
 }
 
-// Density contribution of one candidate (CalculateDensities inner loop, slang:180-188).
-__device__ __forceinline__ void density_term(const StepParams& p, const float4& xi, const float4& xj,
-                                             float& rho) {
-    const float dx = xj.x - xi.x, dy = xj.y - xi.y, dz = xj.z - xi.z;
-    const float r2 = dx * dx + dy * dy + dz * dz;
-    if (r2 <= p.h2) {
-        const float r = sqrtf(r2);
-        rho += p.mass * cubic_w(r * p.inv_h, p.cubic);
-    }
-}
+// ---------------------------------------------------------------- neighbour passes
+// Two phases per particle. Phase A walks every candidate of the 27 buckets with a cheap,
+// branch-free distance test and appends the in-range ones to a per-thread list in shared memory
+// (slot-major, so a warp's lanes hit consecutive banks). Phase B runs the kernel math over the
+// compacted list. Without the split a warp pays the in-range path for almost every candidate
+// (only ~15% of candidates are within h, but one of 32 lanes nearly always is). The list keeps
+// candidate order, so the sums are accumulated in the reference's visiting order. A list that
+// fills up (dense regions) is drained early and refilled.
 
-// CalculateBoundaryVolume + CalculateDensities + the per-particle part of PressureFromDensityEOS
-// (wcsph_with_boundary_model.slang:102-203). Candidates are fetched four at a time so several
-// 128-bit loads are in flight per thread; they are accumulated in the reference's order.
-__global__ void __launch_bounds__(128)
-    k_density(StepParams p, const float4* __restrict__ pos, const uint32_t* __restrict__ scan,
-              float4* __restrict__ aux, float4* __restrict__ bnd) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= p.n) return;
-    const float4 xi = __ldg(pos + i);
-    float bd, bgx, bgy, bgz;
-    boundary_terms(p, xi.x, xi.y, xi.z, bd, bgx, bgy, bgz);
+constexpr int kNbrBlock = 128;
+constexpr int kListCap = 48;
+constexpr int kDrainAt = kListCap - 4;  // a batch of four never overflows the list
 
-    const uint32_t cx = cell_coord(xi.x, p.h), cy = cell_coord(xi.y, p.h),
-                   cz = cell_coord(xi.z, p.h);
-    float rho = 0.0f;
+// Walks the candidates of the 27 neighbour buckets of cell (cx, cy, cz) and calls
+// visit(j, q) for each, with q = pos[j]; four positions are fetched per iteration and
+// batch_end() runs after each group of four (where a full list is drained).
+template <typename Visit, typename BatchEnd>
+__device__ __forceinline__ void for_each_candidate(const StepParams& p,
+                                                   const uint32_t* __restrict__ scan,
+                                                   const float4* __restrict__ pos, uint32_t cx,
+                                                   uint32_t cy, uint32_t cz, Visit&& visit,
+                                                   BatchEnd&& batch_end) {
 #pragma unroll 1
     for (int t = 0; t < 9; t++) {
         const uint32_t dy = (uint32_t)(t % 3) - 1u, dz = (uint32_t)(t / 3) - 1u;
@@ -521,20 +517,71 @@ __global__ void __launch_bounds__(128)
         for (int seg = 0; seg < 3; seg++) {
             const uint32_t b = seg == 0 ? rg.b0 : (seg == 1 ? rg.b1 : rg.b2);
             const uint32_t e = seg == 0 ? rg.e0 : (seg == 1 ? rg.e1 : rg.e2);
-            uint32_t j = b;
 #pragma unroll 1
-            for (; j + 4u <= e; j += 4u) {
-                const float4 q0 = __ldg(pos + j), q1 = __ldg(pos + j + 1u);
-                const float4 q2 = __ldg(pos + j + 2u), q3 = __ldg(pos + j + 3u);
-                density_term(p, xi, q0, rho);
-                density_term(p, xi, q1, rho);
-                density_term(p, xi, q2, rho);
-                density_term(p, xi, q3, rho);
+            for (uint32_t j = b; j < e; j += 4u) {
+                float4 q[4];
+#pragma unroll
+                for (int u = 0; u < 4; u++)
+                    q[u] = (j + u < e) ? __ldg(pos + j + u) : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+                for (int u = 0; u < 4; u++)
+                    if (j + u < e) visit(j + u, q[u]);
+                batch_end();
             }
-#pragma unroll 1
-            for (; j < e; j++) density_term(p, xi, __ldg(pos + j), rho);
         }
     }
+}
+
+// CalculateBoundaryVolume + CalculateDensities + the per-particle part of PressureFromDensityEOS
+// (wcsph_with_boundary_model.slang:102-203). Besides the density products it writes particle i's
+// neighbour list: every in-range j except i itself, in visiting order, slot-major
+// (nbr[s * n + i], so a warp's lanes store and later load consecutive words), and its length in
+// nbr_count[i] (a length above nbr_cap means the list overflowed and was truncated). Positions
+// do not change before the force pass, so that list is exactly the force pass's neighbour set.
+__global__ void __launch_bounds__(kNbrBlock, 6)
+    k_density(StepParams p, const float4* __restrict__ pos, const uint32_t* __restrict__ scan,
+              float4* __restrict__ aux, float4* __restrict__ bnd, uint32_t* __restrict__ nbr,
+              uint32_t* __restrict__ nbr_count) {
+    __shared__ uint32_t s_j[kListCap * kNbrBlock];
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= p.n) return;
+    const int tid = threadIdx.x;
+    const float4 xi = __ldg(pos + i);
+    float bd, bgx, bgy, bgz;
+    boundary_terms(p, xi.x, xi.y, xi.z, bd, bgx, bgy, bgz);
+
+    const uint32_t cx = cell_coord(xi.x, p.h), cy = cell_coord(xi.y, p.h),
+                   cz = cell_coord(xi.z, p.h);
+    float rho = 0.0f;
+    int cnt = 0;
+    uint32_t listed = 0;
+    auto drain = [&]() {
+#pragma unroll 2
+        for (int k = 0; k < cnt; k++) {
+            const uint32_t j = s_j[k * kNbrBlock + tid];
+            const float4 xj = __ldg(pos + j);
+            const float dx = xj.x - xi.x, dy = xj.y - xi.y, dz = xj.z - xi.z;
+            const float r = sqrtf(dx * dx + dy * dy + dz * dz);
+            rho += p.mass * cubic_w(r * p.inv_h, p.cubic);
+            if (j != i) {
+                if (listed < p.nbr_cap) nbr[(size_t)listed * p.n + i] = j;
+                listed++;
+            }
+        }
+        cnt = 0;
+    };
+    for_each_candidate(p, scan, pos, cx, cy, cz, [&](uint32_t j, const float4& xj) {
+        const float dx = xj.x - xi.x, dy = xj.y - xi.y, dz = xj.z - xi.z;
+        const float r2 = dx * dx + dy * dy + dz * dz;
+        if (r2 <= p.h2) {
+            s_j[cnt * kNbrBlock + tid] = j;
+            cnt++;
+        }
+    }, [&]() {
+        if (cnt > kDrainAt) drain();
+    });
+    drain();
+    nbr_count[i] = listed;
     rho += p.rho0 * bd;
     const float pr = p.stiffness * (powf(fmaxf(rho, p.rho0) / p.rho0, p.expoent) - 1.0f);
     const float pd = rho > 0.0f ? pr / (rho * rho) : 0.0f;
@@ -549,10 +596,12 @@ struct ForceAcc {
 };
 
 // Pressure and viscosity contributions of one in-range neighbour (PressureAccel slang:234-249,
-// ViscousAccel slang:301-318); both sums keep the reference's visiting order.
+// ViscousAccel slang:301-318).
 __device__ __forceinline__ void force_term(const StepParams& p, const float4& xi, const float4& vi,
-                                           float pdi, float xx, float xy, float xz, float r2,
-                                           const float2& aj, const float4& vj, ForceAcc& f) {
+                                           float pdi, const float4& xj, const float2& aj,
+                                           const float4& vj, ForceAcc& f) {
+    const float xx = xi.x - xj.x, xy = xi.y - xj.y, xz = xi.z - xj.z;
+    const float r2 = xx * xx + xy * xy + xz * xz;
     const float r = sqrtf(r2);
     float nx = 0.0f, ny = 1.0f, nz = 0.0f;
     if (r > 0.0f) {
@@ -574,67 +623,87 @@ __device__ __forceinline__ void force_term(const StepParams& p, const float4& xi
     f.Vz += (tv * (nz * gw)) * iden;
 }
 
+// Phase B of the force pass over the first cnt listed neighbours.
+__device__ __forceinline__ void force_drain(const StepParams& p, const float4* __restrict__ pos,
+                                            const float4* __restrict__ vel,
+                                            const float2* __restrict__ aux2,
+                                            const uint32_t* s_j, int tid, int cnt,
+                                            const float4& xi, const float4& vi, float pdi,
+                                            ForceAcc& f) {
+    int k = 0;
+#pragma unroll 1
+    for (; k + 2 <= cnt; k += 2) {
+        const uint32_t j0 = s_j[k * kNbrBlock + tid], j1 = s_j[(k + 1) * kNbrBlock + tid];
+        const float4 x0 = __ldg(pos + j0), x1 = __ldg(pos + j1);
+        const float4 v0 = __ldg(vel + j0), v1 = __ldg(vel + j1);
+        const float2 a0 = __ldg(aux2 + 2 * (size_t)j0), a1 = __ldg(aux2 + 2 * (size_t)j1);
+        force_term(p, xi, vi, pdi, x0, a0, v0, f);
+        force_term(p, xi, vi, pdi, x1, a1, v1, f);
+    }
+    if (k < cnt) {
+        const uint32_t j0 = s_j[k * kNbrBlock + tid];
+        force_term(p, xi, vi, pdi, __ldg(pos + j0), __ldg(aux2 + 2 * (size_t)j0),
+                   __ldg(vel + j0), f);
+    }
+}
+
 // CalculatePressureAccel + CalculateViscousAccel + UpdatePositions
 // (wcsph_with_boundary_model.slang:205-360), fused: both sums are accumulated separately in the
-// reference's visiting order, then a = ((g - P) + V) + wall, v += a dt, x += v dt. Positions of
-// four candidates are fetched together; velocity and density products only for those in range.
-__global__ void __launch_bounds__(128)
+// reference's visiting order, then a = ((g - P) + V) + wall, v += a dt, x += v dt.
+__global__ void __launch_bounds__(kNbrBlock, 6)
     k_force(StepParams p, const float4* __restrict__ pos, const float4* __restrict__ vel,
             const float4* __restrict__ aux, const float4* __restrict__ bnd,
-            const uint32_t* __restrict__ scan, float4* __restrict__ pos_out,
+            const uint32_t* __restrict__ scan, const uint32_t* __restrict__ nbr,
+            const uint32_t* __restrict__ nbr_count, float4* __restrict__ pos_out,
             float4* __restrict__ vel_out, float4* __restrict__ acc_out) {
+    __shared__ uint32_t s_j[kListCap * kNbrBlock];
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.n) return;
+    const int tid = threadIdx.x;
     const float4 xi = __ldg(pos + i);
     const float4 vi = __ldg(vel + i);
     const float4 ai = __ldg(aux + i);
     const float2* __restrict__ aux2 = reinterpret_cast<const float2*>(aux);
     const float pdi = ai.x;
 
-    const uint32_t cx = cell_coord(xi.x, p.h), cy = cell_coord(xi.y, p.h),
-                   cz = cell_coord(xi.z, p.h);
     ForceAcc f{0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+    const uint32_t listed = nbr_count[i];
+    if (listed <= p.nbr_cap) {
+        // The density pass's list: the in-range neighbours in the reference's visiting order.
+        uint32_t k = 0;
 #pragma unroll 1
-    for (int t = 0; t < 9; t++) {
-        const uint32_t dy = (uint32_t)(t % 3) - 1u, dz = (uint32_t)(t / 3) - 1u;
-        const Ranges rg = row_ranges(p, scan, cx, cy + dy, cz + dz);
-#pragma unroll 1
-        for (int seg = 0; seg < 3; seg++) {
-            const uint32_t b = seg == 0 ? rg.b0 : (seg == 1 ? rg.b1 : rg.b2);
-            const uint32_t e = seg == 0 ? rg.e0 : (seg == 1 ? rg.e1 : rg.e2);
-#pragma unroll 1
-            for (uint32_t j = b; j < e; j += 4u) {
-                float4 q[4];
-                float r2[4];
-                bool in[4];
-#pragma unroll
-                for (int u = 0; u < 4; u++) {
-                    const uint32_t jj = j + u;
-                    q[u] = jj < e ? __ldg(pos + jj) : make_float4(0.f, 0.f, 0.f, 0.f);
-                }
-#pragma unroll
-                for (int u = 0; u < 4; u++) {
-                    const uint32_t jj = j + u;
-                    q[u].x = xi.x - q[u].x;
-                    q[u].y = xi.y - q[u].y;
-                    q[u].z = xi.z - q[u].z;
-                    r2[u] = q[u].x * q[u].x + q[u].y * q[u].y + q[u].z * q[u].z;
-                    in[u] = jj < e && jj != i && r2[u] <= p.h2;
-                }
-                float2 a[4];
-                float4 v[4];
-#pragma unroll
-                for (int u = 0; u < 4; u++) {
-                    if (in[u]) {
-                        a[u] = __ldg(aux2 + 2 * (size_t)(j + u));
-                        v[u] = __ldg(vel + j + u);
-                    }
-                }
-#pragma unroll
-                for (int u = 0; u < 4; u++)
-                    if (in[u]) force_term(p, xi, vi, pdi, q[u].x, q[u].y, q[u].z, r2[u], a[u], v[u], f);
-            }
+        for (; k + 2u <= listed; k += 2u) {
+            const uint32_t j0 = nbr[(size_t)k * p.n + i], j1 = nbr[(size_t)(k + 1u) * p.n + i];
+            const float4 x0 = __ldg(pos + j0), x1 = __ldg(pos + j1);
+            const float4 v0 = __ldg(vel + j0), v1 = __ldg(vel + j1);
+            const float2 a0 = __ldg(aux2 + 2 * (size_t)j0), a1 = __ldg(aux2 + 2 * (size_t)j1);
+            force_term(p, xi, vi, pdi, x0, a0, v0, f);
+            force_term(p, xi, vi, pdi, x1, a1, v1, f);
         }
+        if (k < listed) {
+            const uint32_t j0 = nbr[(size_t)k * p.n + i];
+            force_term(p, xi, vi, pdi, __ldg(pos + j0), __ldg(aux2 + 2 * (size_t)j0),
+                       __ldg(vel + j0), f);
+        }
+    } else {
+        // Overflowed list (very dense neighbourhood): walk the candidates again.
+        const uint32_t cx = cell_coord(xi.x, p.h), cy = cell_coord(xi.y, p.h),
+                       cz = cell_coord(xi.z, p.h);
+        int cnt = 0;
+        for_each_candidate(p, scan, pos, cx, cy, cz, [&](uint32_t j, const float4& xj) {
+            const float xx = xi.x - xj.x, xy = xi.y - xj.y, xz = xi.z - xj.z;
+            const float r2 = xx * xx + xy * xy + xz * xz;
+            if (r2 <= p.h2 && j != i) {
+                s_j[cnt * kNbrBlock + tid] = j;
+                cnt++;
+            }
+        }, [&]() {
+            if (cnt > kDrainAt) {
+                force_drain(p, pos, vel, aux2, s_j, tid, cnt, xi, vi, pdi, f);
+                cnt = 0;
+            }
+        });
+        force_drain(p, pos, vel, aux2, s_j, tid, cnt, xi, vi, pdi, f);
     }
     const float4 bi = __ldg(bnd + i);
     const float sb = (pdi + ai.w) * p.rho0;
@@ -742,18 +811,21 @@ cudaError_t launch_cells_reorder(uint32_t n, const uint32_t* skeys, const uint32
 }
 
 cudaError_t launch_density(const StepParams& p, const float4* pos, const uint32_t* cell_scan,
-                           float4* aux, float4* bnd, cudaStream_t s) {
+                           float4* aux, float4* bnd, uint32_t* nbr, uint32_t* nbr_count,
+                           cudaStream_t s) {
     if (p.n == 0) return cudaSuccess;
-    k_density<<<(p.n + 127u) / 128u, 128, 0, s>>>(p, pos, cell_scan, aux, bnd);
+    k_density<<<(p.n + kNbrBlock - 1) / kNbrBlock, kNbrBlock, 0, s>>>(p, pos, cell_scan, aux, bnd,
+                                                                      nbr, nbr_count);
     return cudaGetLastError();
 }
 
 cudaError_t launch_force(const StepParams& p, const float4* pos, const float4* vel,
                          const float4* aux, const float4* bnd, const uint32_t* cell_scan,
-                         float4* pos_out, float4* vel_out, float4* acc_out, cudaStream_t s) {
+                         const uint32_t* nbr, const uint32_t* nbr_count, float4* pos_out,
+                         float4* vel_out, float4* acc_out, cudaStream_t s) {
     if (p.n == 0) return cudaSuccess;
-    k_force<<<(p.n + 127u) / 128u, 128, 0, s>>>(p, pos, vel, aux, bnd, cell_scan, pos_out, vel_out,
-                                                acc_out);
+    k_force<<<(p.n + kNbrBlock - 1) / kNbrBlock, kNbrBlock, 0, s>>>(
+        p, pos, vel, aux, bnd, cell_scan, nbr, nbr_count, pos_out, vel_out, acc_out);
     return cudaGetLastError();
 }
 

@@ -47,6 +47,8 @@ struct Model {
     float4* aux = nullptr;
     float4* bnd = nullptr;
     float4* acc = nullptr;
+    uint32_t* nbr = nullptr;        // kNbrCap slot-major neighbour lists
+    uint32_t* nbr_count = nullptr;  // list length per particle
     float* stage = nullptr;  // 32 bytes per particle of host-transfer staging
     uint32_t* scratch = nullptr;
     size_t scratch_words = 0;
