@@ -279,3 +279,17 @@ def test_dense_cluster_overflows_the_neighbour_list():
     compare_step(m, o, "dense_cluster")
     g = m.copy_data_buffers()
     assert g["densities"].max() > 50 * np.median(g["densities"])
+
+
+def test_negative_cells_and_hash_block_boundaries():
+    """Particles spanning cells -31..31 cross the uint wrap of cell + 25 (cells -26/-25) and the
+    50-cell hash-block boundaries, where the candidate walk must not skip any bucket."""
+    w = W.stress_4m(n_uniform=30000, n_blob=0, map_res=0)
+    rng = np.random.default_rng(5)
+    w.pos = ((rng.random((30000, 3)) - 0.5) * 1.25).astype(np.float32)
+    w.sph = replace(w.sph, bbox_size=(2.0, 2.0, 2.0), bbox_pos=(-1.0, -1.0, -1.0))
+    w.vel = ((rng.random((30000, 3)) - 0.5) * 0.2).astype(np.float32)
+    m = W.build_model(w)
+    o = oracle_for(w, m)
+    for _ in range(2):
+        compare_step(m, o, "negative_cells")

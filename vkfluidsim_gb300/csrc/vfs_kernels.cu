@@ -206,42 +206,6 @@ __device__ __forceinline__ void boundary_terms(const StepParams& p, float px, fl
 
 // ---------------------------------------------------------------- neighbour ranges
 
-struct Ranges {
-    uint32_t b0, e0, b1, e1, b2, e2;
-};
-
-// Sorted-index ranges of the three x-neighbour buckets of row (dy, dz), in the order the
-// reference visits them (offsets_3d: x fastest). When cells cx-1..cx+1 lie in one 50-cell hash
-// block their hashes are hA, hA+1, hA+2, so one hash and one modulo give all three keys, and the
-// keys are consecutive unless kA + 2 wraps past n.
-__device__ __forceinline__ Ranges row_ranges(const StepParams& p,
-                                             const uint32_t* __restrict__ scan, uint32_t cx,
-                                             uint32_t cy, uint32_t cz) {
-    const uint32_t hA = hash_cell(cx - 1u, cy, cz);
-    const uint32_t kA = key_mod(hA, p.mod_magic, p.n);
-    Ranges r;
-    r.b0 = __ldg(scan + kA);
-    const bool same_block = ((cx - 1u + 25u) % 50u) <= 47u && hA <= 0xFFFFFFFDu;
-    if (same_block && kA + 2u < p.n) {
-        r.e0 = __ldg(scan + kA + 3u);
-        r.b1 = r.e1 = r.b2 = r.e2 = 0u;
-        return r;
-    }
-    const uint32_t kB = key_mod(hash_cell(cx, cy, cz), p.mod_magic, p.n);
-    const uint32_t kC = key_mod(hash_cell(cx + 1u, cy, cz), p.mod_magic, p.n);
-    if (kB == kA + 1u && kC == kA + 2u) {
-        r.e0 = __ldg(scan + kA + 3u);
-        r.b1 = r.e1 = r.b2 = r.e2 = 0u;
-    } else {
-        r.e0 = __ldg(scan + kA + 1u);
-        r.b1 = __ldg(scan + kB);
-        r.e1 = __ldg(scan + kB + 1u);
-        r.b2 = __ldg(scan + kC);
-        r.e2 = __ldg(scan + kC + 1u);
-    }
-    return r;
-}
-
 // ---------------------------------------------------------------- kernels
 
 __global__ void __launch_bounds__(256) k_keys(StepParams p, const float4* __restrict__ pos,
@@ -500,34 +464,87 @@ constexpr int kNbrBlock = 128;
 constexpr int kListCap = 48;
 constexpr int kDrainAt = kListCap - 4;  // a batch of four never overflows the list
 
-// Walks the candidates of the 27 neighbour buckets of cell (cx, cy, cz) and calls
-// visit(j, q) for each, with q = pos[j]; four positions are fetched per iteration and
-// batch_end() runs after each group of four (where a full list is drained).
+// Squared distance, in units of h^2, from a particle at fraction f of its cell (along one axis)
+// to the neighbour cell at offset d in {-1, 0, +1} along that axis.
+__device__ __forceinline__ float face_dist2(uint32_t d, float f) {
+    const float l = d == 0xFFFFFFFFu ? f : (d == 1u ? 1.0f - f : 0.0f);
+    const float c = fmaxf(l, 0.0f);
+    return c * c;
+}
+
+// Cells whose box lies farther than h from the particle hold no in-range candidate and are
+// skipped, which cannot change any sum as long as no other of the 27 neighbour cells shares
+// their key (a shared key would be walked once more by the reference). The 27 keys are distinct
+// when the 3x3x3 block of cells lies inside one 50^3 hash block and its hashes do not wrap past
+// 2^32 (they are then hmin + d with distinct d in [0, 5102]) and n > 5102; elsewhere nothing is
+// skipped. The 2e-3 margin keeps the float cell fractions conservative.
+constexpr float kPruneLimit = 1.002f;
+
+// Walks the candidates of the 27 neighbour buckets of cell (cx, cy, cz) in the reference's order
+// and calls visit(j, q) for each, with q = pos[j]; four positions are fetched per iteration and
+// batch_end() runs after each group of at most four (where a full list is drained).
 template <typename Visit, typename BatchEnd>
 __device__ __forceinline__ void for_each_candidate(const StepParams& p,
                                                    const uint32_t* __restrict__ scan,
-                                                   const float4* __restrict__ pos, uint32_t cx,
-                                                   uint32_t cy, uint32_t cz, Visit&& visit,
+                                                   const float4* __restrict__ pos,
+                                                   const float4& xi, uint32_t cx, uint32_t cy,
+                                                   uint32_t cz, Visit&& visit,
                                                    BatchEnd&& batch_end) {
+    const uint32_t h_lo = hash_cell(cx - 1u, cy - 1u, cz - 1u);
+    const uint32_t h_hi = hash_cell(cx + 1u, cy + 1u, cz + 1u);
+    const bool interior = p.n > 5102u && (cx + 24u) / 50u == (cx + 26u) / 50u &&
+                          (cy + 24u) / 50u == (cy + 26u) / 50u &&
+                          (cz + 24u) / 50u == (cz + 26u) / 50u && h_hi >= h_lo;
+    const float lim = interior ? kPruneLimit : 1e30f;
+    const float fx = fmaf(-(float)(int)cx, p.h, xi.x) * p.inv_h;
+    const float fy = fmaf(-(float)(int)cy, p.h, xi.y) * p.inv_h;
+    const float fz = fmaf(-(float)(int)cz, p.h, xi.z) * p.inv_h;
+    const float dxl = face_dist2(0xFFFFFFFFu, fx), dxr = face_dist2(1u, fx);
 #pragma unroll 1
     for (int t = 0; t < 9; t++) {
         const uint32_t dy = (uint32_t)(t % 3) - 1u, dz = (uint32_t)(t / 3) - 1u;
-        const Ranges rg = row_ranges(p, scan, cx, cy + dy, cz + dz);
+        const float dyz = face_dist2(dy, fy) + face_dist2(dz, fz);
+        if (dyz > lim) continue;
+        const bool skip_l = dyz + dxl > lim, skip_r = dyz + dxr > lim;
+        const uint32_t ry = cy + dy, rz = cz + dz;
+        const uint32_t hA = hash_cell(cx - 1u, ry, rz);
+        const uint32_t kA = key_mod(hA, p.mod_magic, p.n);
+        uint32_t b0, e0, b1 = 0u, e1 = 0u, b2 = 0u, e2 = 0u;
+        const bool same_block = ((cx - 1u + 25u) % 50u) <= 47u && hA <= 0xFFFFFFFDu;
+        if (same_block && kA + 2u < p.n) {
+            // Buckets kA, kA+1, kA+2 are adjacent: one range, trimmed at either end.
+            b0 = __ldg(scan + kA + (skip_l ? 1u : 0u));
+            e0 = __ldg(scan + kA + (skip_r ? 2u : 3u));
+        } else {
+            const uint32_t kB = key_mod(hash_cell(cx, ry, rz), p.mod_magic, p.n);
+            const uint32_t kC = key_mod(hash_cell(cx + 1u, ry, rz), p.mod_magic, p.n);
+            b0 = __ldg(scan + kA);
+            e0 = skip_l ? b0 : __ldg(scan + kA + 1u);
+            b1 = __ldg(scan + kB);
+            e1 = __ldg(scan + kB + 1u);
+            if (!skip_r) {
+                b2 = __ldg(scan + kC);
+                e2 = __ldg(scan + kC + 1u);
+            }
+        }
 #pragma unroll 1
         for (int seg = 0; seg < 3; seg++) {
-            const uint32_t b = seg == 0 ? rg.b0 : (seg == 1 ? rg.b1 : rg.b2);
-            const uint32_t e = seg == 0 ? rg.e0 : (seg == 1 ? rg.e1 : rg.e2);
+            const uint32_t b = seg == 0 ? b0 : (seg == 1 ? b1 : b2);
+            const uint32_t e = seg == 0 ? e0 : (seg == 1 ? e1 : e2);
+            uint32_t j = b;
 #pragma unroll 1
-            for (uint32_t j = b; j < e; j += 4u) {
-                float4 q[4];
-#pragma unroll
-                for (int u = 0; u < 4; u++)
-                    q[u] = (j + u < e) ? __ldg(pos + j + u) : make_float4(0.f, 0.f, 0.f, 0.f);
-#pragma unroll
-                for (int u = 0; u < 4; u++)
-                    if (j + u < e) visit(j + u, q[u]);
+            for (; j + 4u <= e; j += 4u) {
+                const float4 q0 = __ldg(pos + j), q1 = __ldg(pos + j + 1u);
+                const float4 q2 = __ldg(pos + j + 2u), q3 = __ldg(pos + j + 3u);
+                visit(j, q0);
+                visit(j + 1u, q1);
+                visit(j + 2u, q2);
+                visit(j + 3u, q3);
                 batch_end();
             }
+#pragma unroll 1
+            for (; j < e; j++) visit(j, __ldg(pos + j));
+            batch_end();
         }
     }
 }
@@ -547,9 +564,6 @@ __global__ void __launch_bounds__(kNbrBlock, 6)
     if (i >= p.n) return;
     const int tid = threadIdx.x;
     const float4 xi = __ldg(pos + i);
-    float bd, bgx, bgy, bgz;
-    boundary_terms(p, xi.x, xi.y, xi.z, bd, bgx, bgy, bgz);
-
     const uint32_t cx = cell_coord(xi.x, p.h), cy = cell_coord(xi.y, p.h),
                    cz = cell_coord(xi.z, p.h);
     float rho = 0.0f;
@@ -561,7 +575,8 @@ __global__ void __launch_bounds__(kNbrBlock, 6)
             const uint32_t j = s_j[k * kNbrBlock + tid];
             const float4 xj = __ldg(pos + j);
             const float dx = xj.x - xi.x, dy = xj.y - xi.y, dz = xj.z - xi.z;
-            const float r = sqrtf(dx * dx + dy * dy + dz * dz);
+            const float r2 = dx * dx + dy * dy + dz * dz;
+            const float r = r2 > 0.0f ? r2 * rsqrtf(r2) : 0.0f;
             rho += p.mass * cubic_w(r * p.inv_h, p.cubic);
             if (j != i) {
                 if (listed < p.nbr_cap) nbr[(size_t)listed * p.n + i] = j;
@@ -570,7 +585,7 @@ __global__ void __launch_bounds__(kNbrBlock, 6)
         }
         cnt = 0;
     };
-    for_each_candidate(p, scan, pos, cx, cy, cz, [&](uint32_t j, const float4& xj) {
+    for_each_candidate(p, scan, pos, xi, cx, cy, cz, [&](uint32_t j, const float4& xj) {
         const float dx = xj.x - xi.x, dy = xj.y - xi.y, dz = xj.z - xi.z;
         const float r2 = dx * dx + dy * dy + dz * dz;
         if (r2 <= p.h2) {
@@ -582,6 +597,8 @@ __global__ void __launch_bounds__(kNbrBlock, 6)
     });
     drain();
     nbr_count[i] = listed;
+    float bd, bgx, bgy, bgz;
+    boundary_terms(p, xi.x, xi.y, xi.z, bd, bgx, bgy, bgz);
     rho += p.rho0 * bd;
     const float pr = p.stiffness * (powf(fmaxf(rho, p.rho0) / p.rho0, p.expoent) - 1.0f);
     const float pd = rho > 0.0f ? pr / (rho * rho) : 0.0f;
@@ -602,14 +619,12 @@ __device__ __forceinline__ void force_term(const StepParams& p, const float4& xi
                                            const float4& vj, ForceAcc& f) {
     const float xx = xi.x - xj.x, xy = xi.y - xj.y, xz = xi.z - xj.z;
     const float r2 = xx * xx + xy * xy + xz * xz;
-    const float r = sqrtf(r2);
-    float nx = 0.0f, ny = 1.0f, nz = 0.0f;
-    if (r > 0.0f) {
-        const float ir = 1.0f / r;
-        nx = xx * ir;
-        ny = xy * ir;
-        nz = xz * ir;
-    }
+    const bool pos_r = r2 > 0.0f;
+    const float ir = pos_r ? rsqrtf(r2) : 0.0f;
+    const float r = r2 * ir;
+    const float nx = pos_r ? xx * ir : 0.0f;
+    const float ny = pos_r ? xy * ir : 1.0f;
+    const float nz = pos_r ? xz * ir : 0.0f;
     const float gw = cubic_dw(r, r * p.inv_h, p.grad_over_h);
     const float s = (p.mass * (pdi + aj.x)) * gw;
     f.Px += s * nx;
@@ -617,7 +632,7 @@ __device__ __forceinline__ void force_term(const StepParams& p, const float4& xi
     f.Pz += s * nz;
     const float dv = (vi.x - vj.x) * xx + (vi.y - vj.y) * xy + (vi.z - vj.z) * xz;
     const float tv = aj.y * dv;
-    const float iden = 1.0f / (r2 + p.visc_eps);
+    const float iden = __fdividef(1.0f, r2 + p.visc_eps);
     f.Vx += (tv * (nx * gw)) * iden;
     f.Vy += (tv * (ny * gw)) * iden;
     f.Vz += (tv * (nz * gw)) * iden;
@@ -690,7 +705,7 @@ __global__ void __launch_bounds__(kNbrBlock, 6)
         const uint32_t cx = cell_coord(xi.x, p.h), cy = cell_coord(xi.y, p.h),
                        cz = cell_coord(xi.z, p.h);
         int cnt = 0;
-        for_each_candidate(p, scan, pos, cx, cy, cz, [&](uint32_t j, const float4& xj) {
+        for_each_candidate(p, scan, pos, xi, cx, cy, cz, [&](uint32_t j, const float4& xj) {
             const float xx = xi.x - xj.x, xy = xi.y - xj.y, xz = xi.z - xj.z;
             const float r2 = xx * xx + xy * xy + xz * xz;
             if (r2 <= p.h2 && j != i) {
