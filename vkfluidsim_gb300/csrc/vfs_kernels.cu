@@ -510,7 +510,9 @@ __device__ __forceinline__ void for_each_candidate(const StepParams& p,
         const uint32_t hA = hash_cell(cx - 1u, ry, rz);
         const uint32_t kA = key_mod(hA, p.mod_magic, p.n);
         uint32_t b0, e0, b1 = 0u, e1 = 0u, b2 = 0u, e2 = 0u;
-        const bool same_block = ((cx - 1u + 25u) % 50u) <= 47u && hA <= 0xFFFFFFFDu;
+        // Cells cx-1..cx+1 share a hash block iff (cell + 25) / 50 agrees at both ends (this also
+        // covers the wrap of cell + 25 at 2^32 near cell -26).
+        const bool same_block = (cx + 24u) / 50u == (cx + 26u) / 50u && hA <= 0xFFFFFFFDu;
         if (same_block && kA + 2u < p.n) {
             // Buckets kA, kA+1, kA+2 are adjacent: one range, trimmed at either end.
             b0 = __ldg(scan + kA + (skip_l ? 1u : 0u));
