@@ -193,6 +193,22 @@ int vfs_scene_load(const char* json_path, const char* resources_dir, vfs_model**
  * model created by vfs_scene_load. */
 int vfs_scene_reset(vfs_model* m);
 
+/* ---- spatial-hash compute primitives on device buffers (enqueued on `stream`, a cudaStream_t
+ * passed as void*; NULL is the legacy default stream; no host synchronisation) ---- */
+
+/* GPUCountSort::Run (src/compute/sort.cpp:107-143, sort.slang:13-55): sorts the n (key, item)
+ * pairs in place by key, stably; items are first set to 0..n-1 (ClearCounts), so on return
+ * items[] is the sorting permutation and keys[] the sorted keys. Keys must be <= max_value.
+ * Temporary buffers come from the stream-ordered allocator. */
+int vfs_sort_pairs(uint32_t* items, uint32_t* keys, uint32_t n, uint32_t max_value, void* stream);
+/* SpatialOffset::Run with init (src/compute/sort.cpp:155-176, spatial_offsets.slang:10-31):
+ * offsets[k] = first index of key k in sorted_keys, or n when k is absent. */
+int vfs_spatial_offsets(const uint32_t* sorted_keys, uint32_t* offsets, uint32_t n, void* stream);
+/* BufferReorder::Reorder (src/compute/sort.cpp:206-219, reorder.slang:11-19) on packed float3:
+ * dst[i] = src[sorted_indices[i]]; src and dst must not alias (the reference copies back). */
+int vfs_reorder_float3(const uint32_t* sorted_indices, const float* src, float* dst, uint32_t n,
+                       void* stream);
+
 /* ---- seeded synthetic inputs (counter-based generator; identical on every host) ---- */
 
 /* Jittered lattice: positions origin + spacing * (i + 0.5, j + 0.5, k + 0.5) + U(-jitter,

@@ -117,6 +117,9 @@ SIGNATURES = {
     "vfs_model_device_state": (_I, [_P, C.POINTER(_P), C.POINTER(_P)]),
     "vfs_scene_load": (_I, [C.c_char_p, C.c_char_p, C.POINTER(_P)]),
     "vfs_scene_reset": (_I, [_P]),
+    "vfs_sort_pairs": (_I, [_P, _P, _U32, _U32, _P]),
+    "vfs_spatial_offsets": (_I, [_P, _P, _U32, _P]),
+    "vfs_reorder_float3": (_I, [_P, _P, _P, _U32, _P]),
     "vfs_generate_lattice": (_I, [_U, _F, C.c_float, C.c_float, C.c_uint64, _F]),
     "vfs_generate_uniform_blob": (_I, [C.c_uint64, _F, _F, C.c_uint64, _F, C.c_float, C.c_uint64, _F]),
     "vfs_generate_fourier_velocity": (_I, [C.c_uint64, _F, C.c_int32, C.c_float, C.c_uint64, _F]),

@@ -71,12 +71,18 @@ struct SortConfig {
 };
 
 // ---- launch wrappers (vfs_kernels.cu) ----
-SortConfig make_sort_config(uint32_t n, int digit_bits, int tile_items);
+// Number of bits needed to hold every key <= max_key (at least 1).
+int key_bits_for(uint32_t max_key);
+// key_bits <= 0: keys are spatial-hash keys, < n.
+SortConfig make_sort_config(uint32_t n, int digit_bits, int tile_items, int key_bits = 0);
 size_t sort_scratch_words(const SortConfig& c);
 
 // keys[i] = HashCell3D(floor(pos[i] / h)) % n and the per-pass digit histograms.
 cudaError_t launch_keys(const StepParams& p, const float4* pos, uint32_t* keys,
                         const SortConfig& sc, uint32_t* ghist, cudaStream_t s);
+// Per-pass digit histograms of caller-provided keys.
+cudaError_t launch_digit_hist(const uint32_t* keys, uint32_t n, const SortConfig& sc,
+                              uint32_t* ghist, cudaStream_t s);
 // Stable LSD onesweep over sc.passes digits; returns the buffers holding sorted keys / perm.
 cudaError_t launch_sort(uint32_t n, const SortConfig& sc, const SortScratch& scratch,
                         uint32_t* keys, uint32_t* keys_alt, uint32_t* vals, uint32_t* vals_alt,

@@ -231,6 +231,25 @@ __global__ void __launch_bounds__(256) k_keys(StepParams p, const float4* __rest
         if (s_h[e]) atomicAdd(&ghist[e], s_h[e]);
 }
 
+// Per-pass digit histograms of caller-provided keys (the histogram half of k_keys).
+__global__ void __launch_bounds__(256) k_digit_hist(const uint32_t* __restrict__ keys, uint32_t n,
+                                                    int passes, int digit_bits,
+                                                    uint32_t* __restrict__ ghist) {
+    __shared__ uint32_t s_h[kMaxSortPasses * kMaxSortBins];
+    const int bins = 1 << digit_bits;
+    const uint32_t mask = (uint32_t)bins - 1u;
+    for (int e = threadIdx.x; e < passes * bins; e += blockDim.x) s_h[e] = 0u;
+    __syncthreads();
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t key = keys[i];
+        for (int ps = 0; ps < passes; ps++)
+            atomicAdd(&s_h[ps * bins + ((key >> (ps * digit_bits)) & mask)], 1u);
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < passes * bins; e += blockDim.x)
+        if (s_h[e]) atomicAdd(&ghist[e], s_h[e]);
+}
+
 __device__ __forceinline__ uint32_t ld_volatile(const uint32_t* p) {
     return *(const volatile uint32_t*)p;
 }
@@ -761,13 +780,20 @@ cudaError_t launch_onesweep_t(uint32_t n, const SortConfig& sc, const SortScratc
 
 }  // namespace
 
-SortConfig make_sort_config(uint32_t n, int digit_bits, int tile_items) {
+int key_bits_for(uint32_t max_key) {
+    int bits = 1;
+    while (bits < 32 && (((uint64_t)1 << bits) <= (uint64_t)max_key)) bits++;
+    return bits;
+}
+
+SortConfig make_sort_config(uint32_t n, int digit_bits, int tile_items, int key_bits) {
     SortConfig c{};
     if (digit_bits < 4) digit_bits = 4;
     if (digit_bits > 8) digit_bits = 8;
     if (tile_items != 8 && tile_items != 12 && tile_items != 16) tile_items = 16;
-    int bits = 1;
-    while (bits < 32 && (((uint64_t)1 << bits) < (uint64_t)n)) bits++;  // keys <= n - 1
+    // Spatial-hash keys are < n.
+    const int bits = key_bits > 0 ? (key_bits > 32 ? 32 : key_bits)
+                                  : key_bits_for(n > 0 ? n - 1u : 0u);
     while ((bits + digit_bits - 1) / digit_bits > kMaxSortPasses) digit_bits++;  // <= 8 covers 32 bits
     c.digit_bits = digit_bits;
     c.passes = (bits + digit_bits - 1) / digit_bits;
@@ -788,6 +814,15 @@ cudaError_t launch_keys(const StepParams& p, const float4* pos, uint32_t* keys,
     uint32_t blocks = (p.n + 255u) / 256u;
     if (blocks > 152u * 8u) blocks = 152u * 8u;
     k_keys<<<blocks, 256, 0, s>>>(p, pos, keys, sc.passes, sc.digit_bits, ghist);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_digit_hist(const uint32_t* keys, uint32_t n, const SortConfig& sc,
+                              uint32_t* ghist, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    uint32_t blocks = (n + 255u) / 256u;
+    if (blocks > 152u * 8u) blocks = 152u * 8u;
+    k_digit_hist<<<blocks, 256, 0, s>>>(keys, n, sc.passes, sc.digit_bits, ghist);
     return cudaGetLastError();
 }
 

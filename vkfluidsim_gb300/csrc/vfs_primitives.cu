@@ -1,0 +1,120 @@
+// The reference's spatial-hash compute primitives as standalone C-ABI calls on device buffers:
+//   GPUCountSort::Run  (src/compute/sort.cpp:107-143)  -> vfs_sort_pairs
+//   SpatialOffset::Run (src/compute/sort.cpp:155-176)  -> vfs_spatial_offsets
+//   BufferReorder      (src/compute/sort.cpp:185-227)  -> vfs_reorder_float3
+// They run on the caller's stream and return without synchronising it.
+#include <cuda_runtime.h>
+
+#include <string>
+
+#include "vfs_cuda.h"
+#include "vfs_internal.h"
+#include "vfs_model.h"
+
+namespace vfs {
+namespace {
+
+#define VFS_PRIM_TRY(expr)                                                                   \
+    do {                                                                                     \
+        cudaError_t e_ = (expr);                                                             \
+        if (e_ != cudaSuccess)                                                               \
+            return ::vfs::fail(VFS_ERR_CUDA, std::string(#expr) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+// InitOffsets + CalculateOffsets, assets/shaders/simulation/spatial_hash/spatial_offsets.slang:10-31.
+__global__ void k_init_offsets(uint32_t* __restrict__ offsets, uint32_t n) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) offsets[i] = n;
+}
+
+__global__ void k_calc_offsets(const uint32_t* __restrict__ sorted_keys,
+                               uint32_t* __restrict__ offsets, uint32_t n) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t key = sorted_keys[i];
+    const uint32_t prev = i == 0u ? n : sorted_keys[i - 1];
+    if (key != prev && key < n) offsets[key] = i;
+}
+
+// Reorder, assets/shaders/simulation/spatial_hash/reorder.slang:11-19, on packed float3.
+__global__ void k_reorder_float3(const uint32_t* __restrict__ idx, const float* __restrict__ src,
+                                 float* __restrict__ dst, uint32_t n) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t s = idx[i];
+    if (s >= n) return;
+    dst[3 * (size_t)i] = src[3 * (size_t)s];
+    dst[3 * (size_t)i + 1] = src[3 * (size_t)s + 1];
+    dst[3 * (size_t)i + 2] = src[3 * (size_t)s + 2];
+}
+
+}  // namespace
+
+// Enqueues a stable sort of (keys, index) with caller-provided scratch: tmp_keys / tmp_items
+// (n words each) and `scratch` of sort_scratch_words(sc) words plus one error word.
+int enqueue_sort_pairs(uint32_t* items, uint32_t* keys, uint32_t n, const SortConfig& sc,
+                       uint32_t* tmp_keys, uint32_t* tmp_items, uint32_t* scratch,
+                       cudaStream_t s) {
+    SortScratch scr;
+    scr.ghist = scratch;
+    scr.counters = scratch + (size_t)sc.passes * sc.bins;
+    scr.status = scr.counters + sc.passes;
+    scr.err = scratch + sort_scratch_words(sc);
+    VFS_PRIM_TRY(cudaMemsetAsync(scratch, 0, (sort_scratch_words(sc) + 1) * sizeof(uint32_t), s));
+    VFS_PRIM_TRY(launch_digit_hist(keys, n, sc, scr.ghist, s));
+    uint32_t* sk = nullptr;
+    uint32_t* sp = nullptr;
+    VFS_PRIM_TRY(launch_sort(n, sc, scr, keys, tmp_keys, items, tmp_items, &sk, &sp, s));
+    if (sk != keys) VFS_PRIM_TRY(cudaMemcpyAsync(keys, sk, (size_t)n * 4, cudaMemcpyDeviceToDevice, s));
+    if (sp != items)
+        VFS_PRIM_TRY(cudaMemcpyAsync(items, sp, (size_t)n * 4, cudaMemcpyDeviceToDevice, s));
+    return VFS_OK;
+}
+
+}  // namespace vfs
+
+using vfs::fail;
+
+extern "C" {
+
+int vfs_sort_pairs(uint32_t* items, uint32_t* keys, uint32_t n, uint32_t max_value, void* stream) {
+    if (n == 0) return VFS_OK;
+    if (!items || !keys) return fail(VFS_ERR_INVALID_ARGUMENT, "items and keys must not be NULL");
+    if (n > vfs::kMaxParticles) return fail(VFS_ERR_CAPACITY, "n must be <= 2^30");
+    cudaStream_t s = (cudaStream_t)stream;
+    const vfs::SortConfig sc = vfs::make_sort_config(n, 8, 16, vfs::key_bits_for(max_value));
+    const size_t words = vfs::sort_scratch_words(sc) + 1;
+    uint32_t *tk = nullptr, *ti = nullptr, *scratch = nullptr;
+    VFS_PRIM_TRY(cudaMallocAsync(&tk, (size_t)n * 4, s));
+    VFS_PRIM_TRY(cudaMallocAsync(&ti, (size_t)n * 4, s));
+    VFS_PRIM_TRY(cudaMallocAsync(&scratch, words * 4, s));
+    const int rc = vfs::enqueue_sort_pairs(items, keys, n, sc, tk, ti, scratch, s);
+    cudaFreeAsync(tk, s);
+    cudaFreeAsync(ti, s);
+    cudaFreeAsync(scratch, s);
+    return rc;
+}
+
+int vfs_spatial_offsets(const uint32_t* sorted_keys, uint32_t* offsets, uint32_t n, void* stream) {
+    if (n == 0) return VFS_OK;
+    if (!sorted_keys || !offsets) return fail(VFS_ERR_INVALID_ARGUMENT, "NULL buffer");
+    cudaStream_t s = (cudaStream_t)stream;
+    const unsigned blocks = (n + 255u) / 256u;
+    vfs::k_init_offsets<<<blocks, 256, 0, s>>>(offsets, n);
+    vfs::k_calc_offsets<<<blocks, 256, 0, s>>>(sorted_keys, offsets, n);
+    VFS_PRIM_TRY(cudaGetLastError());
+    return VFS_OK;
+}
+
+int vfs_reorder_float3(const uint32_t* sorted_indices, const float* src, float* dst, uint32_t n,
+                       void* stream) {
+    if (n == 0) return VFS_OK;
+    if (!sorted_indices || !src || !dst || src == dst)
+        return fail(VFS_ERR_INVALID_ARGUMENT, "NULL or aliased buffer");
+    vfs::k_reorder_float3<<<(n + 255u) / 256u, 256, 0, (cudaStream_t)stream>>>(sorted_indices, src,
+                                                                             dst, n);
+    VFS_PRIM_TRY(cudaGetLastError());
+    return VFS_OK;
+}
+
+}  // extern "C"
