@@ -201,6 +201,18 @@ int vfs_scene_reset(vfs_model* m);
  * items[] is the sorting permutation and keys[] the sorted keys. Keys must be <= max_value.
  * Temporary buffers come from the stream-ordered allocator. */
 int vfs_sort_pairs(uint32_t* items, uint32_t* keys, uint32_t n, uint32_t max_value, void* stream);
+/* The same sort without any allocation, for callers that cannot allocate device memory: code in
+ * a frame loop or inside a host framework that owns the GPU memory budget, where a cudaMalloc
+ * could synchronise the device, fragment the host's pool or break a stream capture. This entry
+ * point has no counterpart in the reference. Its temporaries live in one fixed device array of
+ * 2.3 MB that every GPU loading the library holds until the process exits; n above
+ * VFS_SORT_NOALLOC_MAX_PAIRS is rejected with VFS_ERR_CAPACITY. The first call on each device
+ * looks up that array's device address (cudaGetSymbolAddress) and should come before any stream
+ * capture. All calls share the array, so calls whose work overlaps on the GPU (other streams,
+ * other threads) race; serialise them on one stream. */
+#define VFS_SORT_NOALLOC_MAX_PAIRS 262144u
+int vfs_sort_pairs_noalloc(uint32_t* items, uint32_t* keys, uint32_t n, uint32_t max_value,
+                           void* stream);
 /* SpatialOffset::Run with init (src/compute/sort.cpp:155-176, spatial_offsets.slang:10-31):
  * offsets[k] = first index of key k in sorted_keys, or n when k is absent. */
 int vfs_spatial_offsets(const uint32_t* sorted_keys, uint32_t* offsets, uint32_t n, void* stream);

@@ -100,6 +100,11 @@ cudaError_t launch_force(const StepParams& p, const float4* pos, const float4* v
                          const float4* aux, const float4* bnd, const uint32_t* cell_scan,
                          const uint32_t* nbr, const uint32_t* nbr_count, float4* pos_out,
                          float4* vel_out, float4* acc_out, cudaStream_t s);
+// Stable in-place sort of (keys, items) with caller-provided temporaries (n words each) and
+// sort scratch (sort_scratch_words(sc) + 1 words, zeroed here); items become the permutation.
+int enqueue_sort_pairs(uint32_t* items, uint32_t* keys, uint32_t n, const SortConfig& sc,
+                       uint32_t* tmp_keys, uint32_t* tmp_items, uint32_t* scratch,
+                       cudaStream_t s);
 // spatial_offsets[k] = cell start or n for empty keys (reference layout).
 cudaError_t launch_offsets(uint32_t n, const uint32_t* cell_scan, uint32_t* offsets,
                            cudaStream_t s);
