@@ -182,6 +182,42 @@ int vfs_model_get_sort_config(const vfs_model* m, int32_t* digit_bits, int32_t* 
 /* Device pointers of the current state: float4 (x, y, z, id bits) and (vx, vy, vz, 0). */
 int vfs_model_device_state(vfs_model* m, void** pos4, void** vel4);
 
+/* ---- batches: many independent scenes advanced by one launch per pass ----
+ * Each scene is a complete reference simulation (its own parameters, particle count N_s = its
+ * hash-table size, boundary objects). Scene s owns particles and keys [off_s, off_s + N_s): its
+ * keys are off_s + HashCell3D % N_s, so one stable sort of all keys yields every scene's own stable
+ * sort and results equal those of one vfs_model per scene. Scene arguments index [0, n_scenes);
+ * offsets, ids and neighbour arrays are scene-local. */
+typedef struct vfs_batch vfs_batch;
+int vfs_batch_create(int32_t n_scenes, const vfs_sim_params* sims, const vfs_sph_params* sphs,
+                     const vfs_wcsph_params* wcsphs, vfs_batch** out);
+int vfs_batch_destroy(vfs_batch* b);
+int32_t vfs_batch_num_scenes(const vfs_batch* b);
+uint32_t vfs_batch_num_particles(const vfs_batch* b, int32_t scene);
+int vfs_batch_set_stream(vfs_batch* b, void* stream);
+int vfs_batch_set_scene_parameters(vfs_batch* b, int32_t scene, const vfs_sim_params* sim,
+                                   const vfs_sph_params* sph, const vfs_wcsph_params* wcsph);
+int vfs_batch_add_boundary_object(vfs_batch* b, int32_t scene, const vfs_boundary_object* obj);
+int vfs_batch_add_analytic_object(vfs_batch* b, int32_t scene, const vfs_analytic_object* obj);
+int vfs_batch_get_boundary_object(const vfs_batch* b, int32_t scene, uint32_t idx,
+                                  vfs_boundary_object* info, float* sdf_out, float* vm_out);
+int vfs_batch_set_particle_state(vfs_batch* b, int32_t scene, const float* pos, const float* vel,
+                                 uint32_t offset, int64_t count);
+int vfs_batch_copy_data_buffers(vfs_batch* b, int32_t scene, float* pos, float* vel, float* dens,
+                                float* acc);
+int vfs_batch_get_ids(vfs_batch* b, int32_t scene, uint32_t* ids);
+int vfs_batch_get_neighbor_arrays(vfs_batch* b, int32_t scene, uint32_t* keys,
+                                  uint32_t* sorted_indices, uint32_t* offsets);
+int vfs_batch_get_boundary_fields(vfs_batch* b, int32_t scene, float* boundary_density,
+                                  float* boundary_gradient);
+int vfs_batch_record_fields(vfs_batch* b, int32_t enable);
+/* count substeps of every scene (each with its own dt). */
+int vfs_batch_substeps(vfs_batch* b, int32_t count);
+int vfs_batch_use_graph(vfs_batch* b, int32_t enable);
+int vfs_batch_synchronize(vfs_batch* b);
+int vfs_batch_profile_substeps(vfs_batch* b, int32_t count, float* phase_ms);
+int vfs_batch_set_sort_config(vfs_batch* b, int32_t digit_bits, int32_t tile_items);
+
 /* ---- scene: LoadScene / GenericScene (src/util/scene_loader.cpp:113-140,
  * src/scenes/generic_scene.cpp:10-57) ---- */
 

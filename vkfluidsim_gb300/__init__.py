@@ -4,13 +4,13 @@ The compute path is ``_lib/libvfs_cuda.so`` (built by ``vkfluidsim_gb300.build``
 only binds it. Importing works without a GPU; every model call needs the library and a device.
 """
 from ._abi import LIB_PATH, VfsError, load_library, SHAPE_SPHERE, SHAPE_BOX, SHAPE_CONTAINER
-from .model import (AnalyticObject, SimulationParameters, SPHParameters, WCSPHParameters,
+from .model import (AnalyticObject, Batch, SimulationParameters, SPHParameters, WCSPHParameters,
                     WCSPHWithBoundaryModel, generate_fourier_velocity, generate_lattice,
                     generate_uniform_blob, load_scene)
 
 __all__ = [
     "LIB_PATH", "VfsError", "load_library", "SHAPE_SPHERE", "SHAPE_BOX", "SHAPE_CONTAINER",
-    "AnalyticObject", "SimulationParameters", "SPHParameters", "WCSPHParameters",
+    "AnalyticObject", "Batch", "SimulationParameters", "SPHParameters", "WCSPHParameters",
     "WCSPHWithBoundaryModel", "generate_fourier_velocity", "generate_lattice",
     "generate_uniform_blob", "load_scene",
 ]

@@ -115,6 +115,26 @@ SIGNATURES = {
     "vfs_model_set_sort_config": (_I, [_P, C.c_int32, C.c_int32]),
     "vfs_model_get_sort_config": (_I, [_P, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
     "vfs_model_device_state": (_I, [_P, C.POINTER(_P), C.POINTER(_P)]),
+    "vfs_batch_create": (_I, [C.c_int32, C.POINTER(SimParams), C.POINTER(SphParams), C.POINTER(WcsphParams), C.POINTER(_P)]),
+    "vfs_batch_destroy": (_I, [_P]),
+    "vfs_batch_num_scenes": (C.c_int32, [_P]),
+    "vfs_batch_num_particles": (_U32, [_P, C.c_int32]),
+    "vfs_batch_set_stream": (_I, [_P, _P]),
+    "vfs_batch_set_scene_parameters": (_I, [_P, C.c_int32, C.POINTER(SimParams), C.POINTER(SphParams), C.POINTER(WcsphParams)]),
+    "vfs_batch_add_boundary_object": (_I, [_P, C.c_int32, C.POINTER(BoundaryObject)]),
+    "vfs_batch_add_analytic_object": (_I, [_P, C.c_int32, C.POINTER(AnalyticObject)]),
+    "vfs_batch_get_boundary_object": (_I, [_P, C.c_int32, _U32, C.POINTER(BoundaryObject), _F, _F]),
+    "vfs_batch_set_particle_state": (_I, [_P, C.c_int32, _F, _F, _U32, C.c_int64]),
+    "vfs_batch_copy_data_buffers": (_I, [_P, C.c_int32, _F, _F, _F, _F]),
+    "vfs_batch_get_ids": (_I, [_P, C.c_int32, _U]),
+    "vfs_batch_get_neighbor_arrays": (_I, [_P, C.c_int32, _U, _U, _U]),
+    "vfs_batch_get_boundary_fields": (_I, [_P, C.c_int32, _F, _F]),
+    "vfs_batch_record_fields": (_I, [_P, C.c_int32]),
+    "vfs_batch_substeps": (_I, [_P, C.c_int32]),
+    "vfs_batch_use_graph": (_I, [_P, C.c_int32]),
+    "vfs_batch_synchronize": (_I, [_P]),
+    "vfs_batch_profile_substeps": (_I, [_P, C.c_int32, _F]),
+    "vfs_batch_set_sort_config": (_I, [_P, C.c_int32, C.c_int32]),
     "vfs_scene_load": (_I, [C.c_char_p, C.c_char_p, C.POINTER(_P)]),
     "vfs_scene_reset": (_I, [_P]),
     "vfs_sort_pairs": (_I, [_P, _P, _U32, _U32, _P]),

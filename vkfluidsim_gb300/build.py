@@ -67,14 +67,16 @@ def build_product(verbose: bool = False) -> Path:
         obj = OBJ_DIR / (src.stem + ".o")
         objs.append(obj)
         if not _newer(obj, [src, *headers, __file__]):
-            jobs.append([nvcc, "-O3", "-std=c++17", *ARCH, "-lineinfo", "-Xcompiler", "-fPIC",
+            jobs.append([nvcc, "-O3", "-std=c++17", *ARCH, "-lineinfo", "-Xcompiler",
+                         "-fPIC,-ffp-contract=off",
                          "-Xptxas", "-v" if verbose else "-O3", f"-I{INCLUDE}", f"-I{CSRC}",
                          "-c", str(src), "-o", str(obj)])
     for src in cpp:
         obj = OBJ_DIR / (src.stem + ".o")
         objs.append(obj)
         if not _newer(obj, [src, *headers, __file__]):
-            jobs.append(["g++", "-O2", "-std=c++17", "-fPIC", f"-I{INCLUDE}", f"-I{CSRC}",
+            jobs.append(["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", f"-I{INCLUDE}",
+                         f"-I{CSRC}",
                          f"-I{cuda / 'include'}", "-c", str(src), "-o", str(obj)])
     logs = []
     if jobs:

@@ -8,6 +8,11 @@
 // graph and replayed. State ping-pongs between two float4 buffer pairs: the reorder writes the
 // sorted copy into the spare pair and the force pass writes the integrated state back into the
 // original pair, so the substep is graph-stable.
+//
+// One engine serves one scene (vfs_model) or many independent scenes (vfs_batch): scene s owns
+// particles and keys [off_s, off_s + n_s) with key = off_s + HashCell3D % n_s, so one stable sort
+// of all keys sorts every scene by its own keys, one cell-range array serves all scenes, and every
+// pass is one launch over all scenes.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -50,22 +55,39 @@ __global__ void k_expand_state(uint32_t offset, uint32_t count, const float* __r
     aux[d].z = 0.0f;  // SetParticleState zeroes the densities it covers (model.cpp:146)
 }
 
-__global__ void k_compact_state(uint32_t n, const float4* __restrict__ pos,
+// Packs particles [start, start + n) into float3 / float arrays; ids become scene-local.
+__global__ void k_compact_state(uint32_t n, uint32_t start, const float4* __restrict__ pos,
                                 const float4* __restrict__ vel, const float4* __restrict__ aux,
                                 float* __restrict__ pos3, float* __restrict__ vel3,
                                 float* __restrict__ dens, uint32_t* __restrict__ ids) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const float4 p = pos[i];
-    const float4 v = vel[i];
+    const float4 p = pos[start + i];
+    const float4 v = vel[start + i];
     pos3[3 * i] = p.x;
     pos3[3 * i + 1] = p.y;
     pos3[3 * i + 2] = p.z;
     vel3[3 * i] = v.x;
     vel3[3 * i + 1] = v.y;
     vel3[3 * i + 2] = v.z;
-    dens[i] = aux[i].z;
-    ids[i] = __float_as_uint(p.w);
+    dens[i] = aux[start + i].z;
+    ids[i] = __float_as_uint(p.w) - start;
+}
+
+// Scene id of every particle of a batched model.
+__global__ void k_fill_scene_of(const uint32_t* __restrict__ scene_off, uint32_t n_scenes,
+                                uint32_t total, uint16_t* __restrict__ scene_of) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= total) return;
+    uint32_t lo = 0, hi = n_scenes;  // last scene with scene_off[s] <= i
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (scene_off[mid] <= i)
+            lo = mid;
+        else
+            hi = mid;
+    }
+    scene_of[i] = (uint16_t)lo;
 }
 
 double pi_d() { return 3.14159265358979323846; }
@@ -170,55 +192,94 @@ void to_rowmajor34(const float* colmajor16, float* out12) {
 
 }  // namespace
 
-// Derives the per-substep constants from the parameter blocks with the reference's float
+// Derives one scene's per-substep constants from its parameter blocks with the reference's float
 // expressions (src/models/model.cpp:225-234; wcsph_with_boundary_model.slang:39-41, 322-323;
 // src/models/wcsph_with_boundary_model.cpp:84-89).
-void Model::refresh_params() {
-    StepParams& p = params;
-    const float r = sim.smooth_radius;
+static void derive_scene_params(const SceneHost& sh, SceneParams& p) {
+    const float r = sh.sim.smooth_radius;
     const float pi_f = 3.14159265358979323846f;
-    p.n = n;
-    p.mod_magic = n >= 1 ? (UINT64_MAX / (uint64_t)n + 1ull) : 0ull;
+    p.n = sh.n;
+    p.off = sh.off;
+    p.mod_magic = sh.n >= 1 ? (UINT64_MAX / (uint64_t)sh.n + 1ull) : 0ull;
     p.h = r;
     p.h2 = r * r;
     p.inv_h = 1.0f / r;
     p.cubic = 8.0f / (pi_f * (float)std::pow(r, 3));
     const float grad_scale = 48.0f / (pi_f * (float)std::pow(r, 4));
     p.grad_over_h = grad_scale / r;
-    p.mass = sph.target_density * (0.8f * powf(r, 3.0f) / 8.0f);
-    p.rho0 = sph.target_density;
-    p.stiffness = wcsph.stiffness;
-    p.expoent = wcsph.expoent;
-    p.visc_scale = 2.0f * (3.0f + 2.0f) * wcsph.viscosity_strenght;
+    p.mass = sh.sph.target_density * (0.8f * powf(r, 3.0f) / 8.0f);
+    p.rho0 = sh.sph.target_density;
+    p.stiffness = sh.wcsph.stiffness;
+    p.expoent = sh.wcsph.expoent;
+    p.visc_scale = 2.0f * (3.0f + 2.0f) * sh.wcsph.viscosity_strenght;
     p.visc_eps = 0.01f * p.h2;
-    p.wall_k = wcsph.wall_stiffness;
-    p.dt = sph.time_scale * sph.fixed_dt / (float)sph.iterations;
-    p.gx = sim.gravity[0];
-    p.gy = sim.gravity[1];
-    p.gz = sim.gravity[2];
+    p.wall_k = sh.wcsph.wall_stiffness;
+    p.dt = sh.sph.time_scale * sh.sph.fixed_dt / (float)sh.sph.iterations;
+    p.gx = sh.sim.gravity[0];
+    p.gy = sh.sim.gravity[1];
+    p.gz = sh.sim.gravity[2];
     for (int a = 0; a < 3; a++) {
-        p.lo[a] = sph.bbox_pos[a];
-        p.hi[a] = sph.bbox_pos[a] + sph.bbox_size[a];
+        p.lo[a] = sh.sph.bbox_pos[a];
+        p.hi[a] = sh.sph.bbox_pos[a] + sh.sph.bbox_size[a];
     }
     p.grad_eps = 0.1f * r;
     p.bnd_eighth = 0.125f * r;
     p.bnd_half = 0.5f * r;
     p.nbr_cap = kNbrCap;
-    p.n_objects = (uint32_t)objects.size();
-    for (size_t o = 0; o < objects.size() && o < (size_t)kMaxObjects; o++) {
-        DevObject& d = p.obj[o];
-        const vfs_boundary_object& b = objects[o].info;
-        to_rowmajor34(b.transform, d.T);
-        to_rowmajor34(b.rotation, d.R);
-        for (int a = 0; a < 3; a++) {
-            d.box_pos[a] = b.box_pos[a];
-            d.box_size[a] = b.box_size[a];
-            d.res[a] = b.resolution[a];
-        }
-        d.sdf = objects[o].d_sdf;
-        d.vm = objects[o].d_vm;
+    p.n_objects = (uint32_t)sh.objects.size();
+    p.objects = nullptr;
+}
+
+static void to_dev_object(const ObjectStore& o, DevObject& d) {
+    to_rowmajor34(o.info.transform, d.T);
+    to_rowmajor34(o.info.rotation, d.R);
+    for (int a = 0; a < 3; a++) {
+        d.box_pos[a] = o.info.box_pos[a];
+        d.box_size[a] = o.info.box_size[a];
+        d.res[a] = o.info.resolution[a];
     }
+    d.sdf = o.d_sdf;
+    d.vm = o.d_vm;
+}
+
+// Rebuilds every scene's constants, the device object table and (batched) the scene table.
+int Model::refresh_params() {
+    std::vector<DevObject> objs;
+    for (SceneHost& sh : scenes) {
+        derive_scene_params(sh, sh.params);
+        for (const ObjectStore& o : sh.objects) {
+            DevObject d{};
+            to_dev_object(o, d);
+            objs.push_back(d);
+        }
+    }
+    if (objs.size() > d_objects_cap) {
+        if (d_objects) cudaFree(d_objects);
+        d_objects = nullptr;
+        d_objects_cap = 0;
+        VFS_CUDA_TRY(cudaMalloc(&d_objects, objs.size() * sizeof(DevObject)));
+        d_objects_cap = objs.size();
+    }
+    if (!objs.empty())
+        VFS_CUDA_TRY(cudaMemcpy(d_objects, objs.data(), objs.size() * sizeof(DevObject),
+                                cudaMemcpyHostToDevice));
+    size_t base = 0;
+    std::vector<SceneParams> table;
+    for (SceneHost& sh : scenes) {
+        sh.params.objects = sh.params.n_objects ? d_objects + base : nullptr;
+        base += sh.params.n_objects;
+        table.push_back(sh.params);
+    }
+    if (scenes.size() > 1)
+        VFS_CUDA_TRY(cudaMemcpy(d_scenes, table.data(), table.size() * sizeof(SceneParams),
+                                cudaMemcpyHostToDevice));
+    launch.total = n;
+    launch.n_scenes = (uint32_t)scenes.size();
+    launch.scenes = d_scenes;
+    launch.scene_of = d_scene_of;
+    launch.one = scenes.empty() ? SceneParams{} : scenes[0].params;
     invalidate_graph();
+    return VFS_OK;
 }
 
 void Model::invalidate_graph() {
@@ -244,23 +305,23 @@ int Model::alloc_sort_scratch() {
 }
 
 // Enqueues one substep (the body of WCSPHWithBoundaryModel::Step's loop,
-// src/models/wcsph_with_boundary_model.cpp:93-116). ExternalAccel needs no pass: the force
-// kernel starts its accumulator at g.
+// src/models/wcsph_with_boundary_model.cpp:93-116) for every scene. ExternalAccel needs no pass:
+// the force kernel starts its accumulator at g.
 int Model::enqueue_substep(cudaEvent_t* ev) {
     cudaStream_t s = stream;
     const int c = cur, o = 1 - cur;
     if (ev) VFS_CUDA_TRY(cudaEventRecord(ev[0], s));
     VFS_CUDA_TRY(cudaMemsetAsync(scratch, 0, sort_scratch_words(sc) * sizeof(uint32_t), s));
     if (ev) VFS_CUDA_TRY(cudaEventRecord(ev[1], s));
-    VFS_CUDA_TRY(launch_keys(params, pos[c], keys, sc, sort_scratch.ghist, s));
+    VFS_CUDA_TRY(launch_keys(launch, pos[c], keys, sc, sort_scratch.ghist, s));
     if (ev) VFS_CUDA_TRY(cudaEventRecord(ev[2], s));
     VFS_CUDA_TRY(launch_sort(n, sc, sort_scratch, keys, keys_alt, vals, vals_alt, &skeys, &sperm, s));
     if (ev) VFS_CUDA_TRY(cudaEventRecord(ev[3], s));
     VFS_CUDA_TRY(launch_cells_reorder(n, skeys, sperm, cell_scan, pos[c], vel[c], pos[o], vel[o], s));
     if (ev) VFS_CUDA_TRY(cudaEventRecord(ev[4], s));
-    VFS_CUDA_TRY(launch_density(params, pos[o], cell_scan, aux, bnd, nbr, nbr_count, s));
+    VFS_CUDA_TRY(launch_density(launch, pos[o], cell_scan, aux, bnd, nbr, nbr_count, s));
     if (ev) VFS_CUDA_TRY(cudaEventRecord(ev[5], s));
-    VFS_CUDA_TRY(launch_force(params, pos[o], vel[o], aux, bnd, cell_scan, nbr, nbr_count, pos[c],
+    VFS_CUDA_TRY(launch_force(launch, pos[o], vel[o], aux, bnd, cell_scan, nbr, nbr_count, pos[c],
                               vel[c], record ? acc : nullptr, s));
     if (ev) VFS_CUDA_TRY(cudaEventRecord(ev[6], s));
     return VFS_OK;
@@ -327,14 +388,26 @@ Model::~Model() {
     cudaFree(nbr_count);
     cudaFree(scratch);
     cudaFree(err);
-    for (auto& o : objects) {
-        cudaFree(o.d_sdf);
-        cudaFree(o.d_vm);
-    }
+    cudaFree(d_scenes);
+    cudaFree(d_scene_of);
+    cudaFree(d_objects);
+    for (auto& sh : scenes)
+        for (auto& o : sh.objects) {
+            cudaFree(o.d_sdf);
+            cudaFree(o.d_vm);
+        }
     if (own_stream && stream) cudaStreamDestroy(stream);
 }
 
 int Model::init() {
+    uint64_t total = 0;
+    for (SceneHost& sh : scenes) {
+        sh.off = (uint32_t)total;
+        sh.n = (uint32_t)sh.sph.n_particles;
+        total += sh.n;
+    }
+    if (total > kMaxParticles) return fail(VFS_ERR_CAPACITY, "more than 2^30 particles in total");
+    n = (uint32_t)total;
     const size_t N = n ? n : 1;
     VFS_CUDA_TRY(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
     own_stream = true;
@@ -364,6 +437,20 @@ int Model::init() {
     VFS_CUDA_TRY(cudaMemset(acc, 0, N * sizeof(float4)));
     VFS_CUDA_TRY(cudaMemset(keys, 0, N * 4));
     VFS_CUDA_TRY(cudaMemset(cell_scan, 0, (N + 1) * 4));
+    if (scenes.size() > 1) {
+        VFS_CUDA_TRY(cudaMalloc(&d_scenes, scenes.size() * sizeof(SceneParams)));
+        VFS_CUDA_TRY(cudaMalloc(&d_scene_of, N * sizeof(uint16_t)));
+        std::vector<uint32_t> off(scenes.size() + 1);
+        for (size_t k = 0; k < scenes.size(); k++) off[k] = scenes[k].off;
+        off[scenes.size()] = n;
+        uint32_t* d_off = nullptr;
+        VFS_CUDA_TRY(cudaMalloc(&d_off, off.size() * 4));
+        VFS_CUDA_TRY(cudaMemcpy(d_off, off.data(), off.size() * 4, cudaMemcpyHostToDevice));
+        if (n) k_fill_scene_of<<<(n + 255) / 256, 256>>>(d_off, (uint32_t)scenes.size(), n, d_scene_of);
+        VFS_CUDA_TRY(cudaGetLastError());
+        VFS_CUDA_TRY(cudaDeviceSynchronize());
+        cudaFree(d_off);
+    }
     skeys = keys;
     sperm = vals;
     int rc = alloc_sort_scratch();
@@ -377,45 +464,123 @@ int Model::init() {
         init[i] = make_float4(0.f, 0.f, 0.f, f);
     }
     VFS_CUDA_TRY(cudaMemcpy(pos[cur], init.data(), N * sizeof(float4), cudaMemcpyHostToDevice));
-    refresh_params();
+    return refresh_params();
+}
+
+int create_model(const std::vector<SceneHost>& scenes, Model** out) {
+    *out = nullptr;
+    Model* m = new Model();
+    m->scenes = scenes;
+    const int rc = m->init();
+    if (rc) {
+        delete m;
+        return rc;
+    }
+    *out = m;
     return VFS_OK;
 }
 
-int Model::set_state(const float* pos3, const float* vel3, uint32_t offset, int64_t count) {
-    if (offset > n) return fail(VFS_ERR_INVALID_ARGUMENT, "offset beyond particle count");
-    const uint64_t cnt = count < 0 ? (uint64_t)(n - offset) : (uint64_t)count;
-    if (offset + cnt > n) return fail(VFS_ERR_CAPACITY, "offset + count exceeds the model's particle count");
+int Model::set_state(uint32_t scene, const float* pos3, const float* vel3, uint32_t offset,
+                     int64_t count) {
+    if (scene >= scenes.size()) return fail(VFS_ERR_INVALID_ARGUMENT, "scene index out of range");
+    const SceneHost& sh = scenes[scene];
+    if (offset > sh.n) return fail(VFS_ERR_INVALID_ARGUMENT, "offset beyond the scene's particle count");
+    const uint64_t cnt = count < 0 ? (uint64_t)(sh.n - offset) : (uint64_t)count;
+    if (offset + cnt > sh.n)
+        return fail(VFS_ERR_CAPACITY, "offset + count exceeds the scene's particle count");
     if (cnt == 0) return VFS_OK;
     if (!pos3 || !vel3) return fail(VFS_ERR_INVALID_ARGUMENT, "pos and vel must not be NULL");
     float* sp = stage;
     float* sv = stage + 3 * (size_t)n;
     VFS_CUDA_TRY(cudaMemcpyAsync(sp, pos3, cnt * 12, cudaMemcpyHostToDevice, stream));
     VFS_CUDA_TRY(cudaMemcpyAsync(sv, vel3, cnt * 12, cudaMemcpyHostToDevice, stream));
-    k_expand_state<<<(unsigned)((cnt + 255) / 256), 256, 0, stream>>>(offset, (uint32_t)cnt, sp, sv,
-                                                                    pos[cur], vel[cur], aux);
+    k_expand_state<<<(unsigned)((cnt + 255) / 256), 256, 0, stream>>>(
+        sh.off + offset, (uint32_t)cnt, sp, sv, pos[cur], vel[cur], aux);
     VFS_CUDA_TRY(cudaGetLastError());
     VFS_CUDA_TRY(cudaStreamSynchronize(stream));
     return VFS_OK;
 }
 
-int Model::get_state(float* pos3, float* vel3, float* dens, uint32_t* ids) {
-    if (n == 0) return VFS_OK;
+int Model::get_state(uint32_t scene, float* pos3, float* vel3, float* dens, uint32_t* ids) {
+    if (scene >= scenes.size()) return fail(VFS_ERR_INVALID_ARGUMENT, "scene index out of range");
+    const SceneHost& sh = scenes[scene];
+    if (sh.n == 0) return VFS_OK;
     float* sp = stage;
     float* sv = stage + 3 * (size_t)n;
     float* sd = stage + 6 * (size_t)n;
     uint32_t* si = reinterpret_cast<uint32_t*>(stage + 7 * (size_t)n);
-    k_compact_state<<<(n + 255) / 256, 256, 0, stream>>>(n, pos[cur], vel[cur], aux, sp, sv, sd, si);
+    k_compact_state<<<(sh.n + 255) / 256, 256, 0, stream>>>(sh.n, sh.off, pos[cur], vel[cur], aux,
+                                                           sp, sv, sd, si);
     VFS_CUDA_TRY(cudaGetLastError());
-    if (pos3) VFS_CUDA_TRY(cudaMemcpyAsync(pos3, sp, (size_t)n * 12, cudaMemcpyDeviceToHost, stream));
-    if (vel3) VFS_CUDA_TRY(cudaMemcpyAsync(vel3, sv, (size_t)n * 12, cudaMemcpyDeviceToHost, stream));
-    if (dens) VFS_CUDA_TRY(cudaMemcpyAsync(dens, sd, (size_t)n * 4, cudaMemcpyDeviceToHost, stream));
-    if (ids) VFS_CUDA_TRY(cudaMemcpyAsync(ids, si, (size_t)n * 4, cudaMemcpyDeviceToHost, stream));
+    if (pos3) VFS_CUDA_TRY(cudaMemcpyAsync(pos3, sp, (size_t)sh.n * 12, cudaMemcpyDeviceToHost, stream));
+    if (vel3) VFS_CUDA_TRY(cudaMemcpyAsync(vel3, sv, (size_t)sh.n * 12, cudaMemcpyDeviceToHost, stream));
+    if (dens) VFS_CUDA_TRY(cudaMemcpyAsync(dens, sd, (size_t)sh.n * 4, cudaMemcpyDeviceToHost, stream));
+    if (ids) VFS_CUDA_TRY(cudaMemcpyAsync(ids, si, (size_t)sh.n * 4, cudaMemcpyDeviceToHost, stream));
     return check_device();
 }
 
-int Model::add_object(const vfs_boundary_object& src, const float* d_sdf_in, const float* d_vm_in) {
-    if (objects.size() >= (size_t)kMaxObjects)
-        return fail(VFS_ERR_CAPACITY, "at most " + std::to_string(kMaxObjects) + " boundary objects");
+int Model::get_acc(uint32_t scene, float* acc3) {
+    if (scene >= scenes.size()) return fail(VFS_ERR_INVALID_ARGUMENT, "scene index out of range");
+    const SceneHost& sh = scenes[scene];
+    if (!acc3 || sh.n == 0) return VFS_OK;
+    int rc = check_device();
+    if (rc) return rc;
+    std::vector<float4> a(sh.n);
+    VFS_CUDA_TRY(cudaMemcpy(a.data(), acc + sh.off, (size_t)sh.n * sizeof(float4), cudaMemcpyDeviceToHost));
+    for (uint32_t i = 0; i < sh.n; i++) {
+        acc3[3 * i] = a[i].x;
+        acc3[3 * i + 1] = a[i].y;
+        acc3[3 * i + 2] = a[i].z;
+    }
+    return VFS_OK;
+}
+
+int Model::get_neighbors(uint32_t scene, uint32_t* keys_out, uint32_t* perm_out, uint32_t* offs_out) {
+    if (scene >= scenes.size()) return fail(VFS_ERR_INVALID_ARGUMENT, "scene index out of range");
+    if (!stepped) return fail(VFS_ERR_NOT_READY, "no substep has run yet");
+    const SceneHost& sh = scenes[scene];
+    if (sh.n == 0) return VFS_OK;
+    uint32_t* off = reinterpret_cast<uint32_t*>(stage);
+    VFS_CUDA_TRY(launch_offsets(sh.n, sh.off, cell_scan, off, stream));
+    if (keys_out)
+        VFS_CUDA_TRY(cudaMemcpyAsync(keys_out, skeys + sh.off, (size_t)sh.n * 4, cudaMemcpyDeviceToHost, stream));
+    if (perm_out)
+        VFS_CUDA_TRY(cudaMemcpyAsync(perm_out, sperm + sh.off, (size_t)sh.n * 4, cudaMemcpyDeviceToHost, stream));
+    if (offs_out) VFS_CUDA_TRY(cudaMemcpyAsync(offs_out, off, (size_t)sh.n * 4, cudaMemcpyDeviceToHost, stream));
+    const int rc = check_device();
+    if (rc) return rc;
+    for (uint32_t i = 0; i < sh.n; i++) {  // scene-local keys and indices
+        if (keys_out) keys_out[i] -= sh.off;
+        if (perm_out) perm_out[i] -= sh.off;
+    }
+    return VFS_OK;
+}
+
+int Model::get_boundary(uint32_t scene, float* bdens, float* bgrad) {
+    if (scene >= scenes.size()) return fail(VFS_ERR_INVALID_ARGUMENT, "scene index out of range");
+    const SceneHost& sh = scenes[scene];
+    if (sh.n == 0) return VFS_OK;
+    int rc = check_device();
+    if (rc) return rc;
+    std::vector<float4> b(sh.n);
+    VFS_CUDA_TRY(cudaMemcpy(b.data(), bnd + sh.off, (size_t)sh.n * sizeof(float4), cudaMemcpyDeviceToHost));
+    for (uint32_t i = 0; i < sh.n; i++) {
+        if (bdens) bdens[i] = b[i].w;
+        if (bgrad) {
+            bgrad[3 * i] = b[i].x;
+            bgrad[3 * i + 1] = b[i].y;
+            bgrad[3 * i + 2] = b[i].z;
+        }
+    }
+    return VFS_OK;
+}
+
+int Model::add_object(uint32_t scene, const vfs_boundary_object& src, const float* d_sdf_in,
+                      const float* d_vm_in) {
+    if (scene >= scenes.size()) return fail(VFS_ERR_INVALID_ARGUMENT, "scene index out of range");
+    SceneHost& sh = scenes[scene];
+    if (sh.objects.size() >= (size_t)kMaxObjects)
+        return fail(VFS_ERR_CAPACITY, "at most " + std::to_string(kMaxObjects) + " boundary objects per scene");
     for (int a = 0; a < 3; a++)
         if (src.resolution[a] < 2) return fail(VFS_ERR_INVALID_ARGUMENT, "grid resolution must be >= 2 per axis");
     ObjectStore o;
@@ -423,31 +588,24 @@ int Model::add_object(const vfs_boundary_object& src, const float* d_sdf_in, con
     o.info.sdf_grid = nullptr;
     o.info.volume_map_grid = nullptr;
     const size_t cnt = (size_t)src.resolution[0] * src.resolution[1] * src.resolution[2];
+    if (!d_sdf_in && (!src.sdf_grid || !src.volume_map_grid))
+        return fail(VFS_ERR_INVALID_ARGUMENT, "sdf_grid and volume_map_grid must not be NULL");
     VFS_CUDA_TRY(cudaMalloc(&o.d_sdf, cnt * 4));
     VFS_CUDA_TRY(cudaMalloc(&o.d_vm, cnt * 4));
-    if (d_sdf_in) {
-        VFS_CUDA_TRY(cudaMemcpyAsync(o.d_sdf, d_sdf_in, cnt * 4, cudaMemcpyDeviceToDevice, stream));
-        VFS_CUDA_TRY(cudaMemcpyAsync(o.d_vm, d_vm_in, cnt * 4, cudaMemcpyDeviceToDevice, stream));
-    } else {
-        if (!src.sdf_grid || !src.volume_map_grid) {
-            cudaFree(o.d_sdf);
-            cudaFree(o.d_vm);
-            return fail(VFS_ERR_INVALID_ARGUMENT, "sdf_grid and volume_map_grid must not be NULL");
-        }
-        VFS_CUDA_TRY(cudaMemcpyAsync(o.d_sdf, src.sdf_grid, cnt * 4, cudaMemcpyHostToDevice, stream));
-        VFS_CUDA_TRY(cudaMemcpyAsync(o.d_vm, src.volume_map_grid, cnt * 4, cudaMemcpyHostToDevice, stream));
-    }
+    const cudaMemcpyKind kind = d_sdf_in ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    VFS_CUDA_TRY(cudaMemcpyAsync(o.d_sdf, d_sdf_in ? d_sdf_in : src.sdf_grid, cnt * 4, kind, stream));
+    VFS_CUDA_TRY(cudaMemcpyAsync(o.d_vm, d_vm_in ? d_vm_in : src.volume_map_grid, cnt * 4, kind, stream));
     VFS_CUDA_TRY(cudaStreamSynchronize(stream));
-    objects.push_back(o);
-    refresh_params();
-    return VFS_OK;
+    sh.objects.push_back(o);
+    return refresh_params();
 }
 
-int Model::add_analytic(const vfs_analytic_object& a) {
+int Model::add_analytic(uint32_t scene, const vfs_analytic_object& a) {
+    if (scene >= scenes.size()) return fail(VFS_ERR_INVALID_ARGUMENT, "scene index out of range");
     if (a.shape < 0 || a.shape > 2) return fail(VFS_ERR_INVALID_ARGUMENT, "unknown analytic shape");
     for (int k = 0; k < 3; k++)
         if (a.resolution[k] < 2) return fail(VFS_ERR_INVALID_ARGUMENT, "grid resolution must be >= 2 per axis");
-    const float h = sim.smooth_radius;
+    const float h = scenes[scene].sim.smooth_radius;
     // Object matrix: translate * rotate * scale (gfx::Transform::Matrix, src/gfx/transform.cpp:33-45).
     M4 T = m4_identity();
     T.a[12] = a.position[0];
@@ -465,7 +623,7 @@ int Model::add_analytic(const vfs_analytic_object& a) {
         info.rotation[k] = (float)R.a[k];
     }
     // MeshSDF::Build box: shape AABB grown by tolerance (0) + margin (8h), in float
-    // (src/util/mesh_sdf.cpp:69-86, src/scenes/generic_scene.cpp:101).
+    // (src/util/mesh_sdf.cpp:69-86, src/scenes/generic_scene.cpp:100).
     const float margin = (float)(8.0 * (double)h);
     float lo[3], hi[3];
     for (int k = 0; k < 3; k++) {
@@ -492,6 +650,7 @@ int Model::add_analytic(const vfs_analytic_object& a) {
     vp.c1 = 0.5 * (double)(h + (-h));
     const double hd = (double)h;
     vp.w_factor = 8.0 / (pi_d() * hd * hd * hd);
+    vp.full_ball = volume_map_full_ball(vp);
     const size_t cnt = (size_t)a.resolution[0] * a.resolution[1] * a.resolution[2];
     float *d_sdf = nullptr, *d_vm = nullptr;
     VFS_CUDA_TRY(cudaMalloc(&d_sdf, cnt * 4));
@@ -502,251 +661,19 @@ int Model::add_analytic(const vfs_analytic_object& a) {
         cudaFree(d_vm);
         return fail(VFS_ERR_CUDA, std::string("volume map: ") + cudaGetErrorString(e));
     }
-    const int rc = add_object(info, d_sdf, d_vm);
+    const int rc = add_object(scene, info, d_sdf, d_vm);
     cudaFree(d_sdf);
     cudaFree(d_vm);
     return rc;
 }
 
-}  // namespace vfs
-
-using vfs::fail;
-using vfs::Model;
-
-extern "C" {
-
-struct vfs_model {
-    Model m;
-};
-
-}  // extern "C"
-
-vfs::Model* vfs_model_impl(vfs_model* h) { return h ? &h->m : nullptr; }
-
-extern "C" {
-
-const char* vfs_last_error(void) { return vfs::g_last_error.c_str(); }
-const char* vfs_version(void) { return "vkfluidsim_gb300 0.1 (sm_103a)"; }
-
-int vfs_device_count(void) {
-    int n = 0;
-    if (cudaGetDeviceCount(&n) != cudaSuccess) {
-        cudaGetLastError();
-        return 0;
-    }
-    return n;
-}
-
-static int validate(const vfs_sim_params* sim, const vfs_sph_params* sph, const vfs_wcsph_params* wc) {
-    if (sim && !(sim->smooth_radius > 0.0f)) return fail(VFS_ERR_INVALID_ARGUMENT, "smooth_radius must be > 0");
-    if (sph && sph->iterations < 1) return fail(VFS_ERR_INVALID_ARGUMENT, "iterations must be >= 1");
-    if (sph && !(sph->target_density > 0.0f)) return fail(VFS_ERR_INVALID_ARGUMENT, "target_density must be > 0");
-    (void)wc;
-    return VFS_OK;
-}
-
-int vfs_model_create(const vfs_sim_params* sim, const vfs_sph_params* sph,
-                     const vfs_wcsph_params* wcsph, vfs_model** out) {
-    try {
-        if (!sim || !sph || !wcsph || !out) return fail(VFS_ERR_INVALID_ARGUMENT, "NULL argument");
-        *out = nullptr;
-        int rc = validate(sim, sph, wcsph);
-        if (rc) return rc;
-        if (sph->n_particles < 0 || (uint64_t)sph->n_particles > vfs::kMaxParticles)
-            return fail(VFS_ERR_CAPACITY, "n_particles must be in [0, 2^30]");
-        vfs_model* h = new vfs_model();
-        h->m.sim = *sim;
-        h->m.sph = *sph;
-        h->m.wcsph = *wcsph;
-        h->m.n = (uint32_t)sph->n_particles;
-        rc = h->m.init();
-        if (rc) {
-            delete h;
-            return rc;
-        }
-        *out = h;
-        return VFS_OK;
-    } catch (const std::exception& e) {
-        return fail(VFS_ERR_OUT_OF_MEMORY, e.what());
-    }
-}
-
-int vfs_model_destroy(vfs_model* m) {
-    delete m;
-    return VFS_OK;
-}
-
-int vfs_model_set_stream(vfs_model* h, void* stream) {
-    if (!h) return fail(VFS_ERR_INVALID_ARGUMENT, "NULL model");
-    Model& m = h->m;
-    cudaStreamSynchronize(m.stream);
-    if (m.own_stream && m.stream) cudaStreamDestroy(m.stream);
-    m.own_stream = false;
-    m.stream = nullptr;
-    if (stream) {
-        m.stream = (cudaStream_t)stream;
-    } else {
-        VFS_CUDA_TRY(cudaStreamCreateWithFlags(&m.stream, cudaStreamNonBlocking));
-        m.own_stream = true;
-    }
-    m.invalidate_graph();
-    return VFS_OK;
-}
-
-int vfs_model_set_parameters(vfs_model* h, const vfs_sim_params* sim, const vfs_sph_params* sph,
-                             const vfs_wcsph_params* wc) {
-    if (!h) return fail(VFS_ERR_INVALID_ARGUMENT, "NULL model");
-    int rc = validate(sim, sph, wc);
-    if (rc) return rc;
-    Model& m = h->m;
-    if (sim) m.sim = *sim;
-    if (sph) {
-        const int32_t n = m.sph.n_particles;
-        m.sph = *sph;
-        m.sph.n_particles = n;
-    }
-    if (wc) m.wcsph = *wc;
-    m.refresh_params();
-    return VFS_OK;
-}
-
-int vfs_model_get_parameters(const vfs_model* h, vfs_sim_params* sim, vfs_sph_params* sph,
-                             vfs_wcsph_params* wc) {
-    if (!h) return fail(VFS_ERR_INVALID_ARGUMENT, "NULL model");
-    if (sim) *sim = h->m.sim;
-    if (sph) *sph = h->m.sph;
-    if (wc) *wc = h->m.wcsph;
-    return VFS_OK;
-}
-
-uint32_t vfs_model_num_particles(const vfs_model* h) { return h ? h->m.n : 0u; }
-
-int vfs_model_add_boundary_object(vfs_model* h, const vfs_boundary_object* obj) {
-    if (!h || !obj) return fail(VFS_ERR_INVALID_ARGUMENT, "NULL argument");
-    return h->m.add_object(*obj, nullptr, nullptr);
-}
-
-int vfs_model_add_analytic_object(vfs_model* h, const vfs_analytic_object* obj) {
-    if (!h || !obj) return fail(VFS_ERR_INVALID_ARGUMENT, "NULL argument");
-    return h->m.add_analytic(*obj);
-}
-
-uint32_t vfs_model_num_boundary_objects(const vfs_model* h) {
-    return h ? (uint32_t)h->m.objects.size() : 0u;
-}
-
-int vfs_model_get_boundary_object(const vfs_model* h, uint32_t idx, vfs_boundary_object* info,
-                                  float* sdf_out, float* vm_out) {
-    if (!h) return fail(VFS_ERR_INVALID_ARGUMENT, "NULL model");
-    const Model& m = h->m;
-    if (idx >= m.objects.size()) return fail(VFS_ERR_INVALID_ARGUMENT, "object index out of range");
-    const vfs::ObjectStore& o = m.objects[idx];
-    if (info) *info = o.info;
-    const size_t cnt = (size_t)o.info.resolution[0] * o.info.resolution[1] * o.info.resolution[2];
-    if (sdf_out) VFS_CUDA_TRY(cudaMemcpy(sdf_out, o.d_sdf, cnt * 4, cudaMemcpyDeviceToHost));
-    if (vm_out) VFS_CUDA_TRY(cudaMemcpy(vm_out, o.d_vm, cnt * 4, cudaMemcpyDeviceToHost));
-    return VFS_OK;
-}
-
-int vfs_model_set_particle_state(vfs_model* h, const float* pos, const float* vel,
-                                 uint32_t offset, int64_t count) {
-    if (!h) return fail(VFS_ERR_INVALID_ARGUMENT, "NULL model");
-    return h->m.set_state(pos, vel, offset, count);
-}
-
-int vfs_model_copy_data_buffers(vfs_model* h, float* pos, float* vel, float* dens, float* acc) {
-    if (!h) return fail(VFS_ERR_INVALID_ARGUMENT, "NULL model");
-    Model& m = h->m;
-    int rc = m.get_state(pos, vel, dens, nullptr);
-    if (rc) return rc;
-    if (acc && m.n) {
-        std::vector<float4> a(m.n);
-        VFS_CUDA_TRY(cudaMemcpy(a.data(), m.acc, (size_t)m.n * sizeof(float4), cudaMemcpyDeviceToHost));
-        for (uint32_t i = 0; i < m.n; i++) {
-            acc[3 * i] = a[i].x;
-            acc[3 * i + 1] = a[i].y;
-            acc[3 * i + 2] = a[i].z;
-        }
-    }
-    return VFS_OK;
-}
-
-int vfs_model_get_ids(vfs_model* h, uint32_t* ids) {
-    if (!h || !ids) return fail(VFS_ERR_INVALID_ARGUMENT, "NULL argument");
-    return h->m.get_state(nullptr, nullptr, nullptr, ids);
-}
-
-int vfs_model_get_neighbor_arrays(vfs_model* h, uint32_t* keys, uint32_t* sorted_indices,
-                                  uint32_t* offsets) {
-    if (!h) return fail(VFS_ERR_INVALID_ARGUMENT, "NULL model");
-    Model& m = h->m;
-    if (!m.stepped) return fail(VFS_ERR_NOT_READY, "no substep has run yet");
-    if (m.n == 0) return VFS_OK;
-    uint32_t* off = reinterpret_cast<uint32_t*>(m.stage);
-    VFS_CUDA_TRY(vfs::launch_offsets(m.n, m.cell_scan, off, m.stream));
-    if (keys) VFS_CUDA_TRY(cudaMemcpyAsync(keys, m.skeys, (size_t)m.n * 4, cudaMemcpyDeviceToHost, m.stream));
-    if (sorted_indices)
-        VFS_CUDA_TRY(cudaMemcpyAsync(sorted_indices, m.sperm, (size_t)m.n * 4, cudaMemcpyDeviceToHost, m.stream));
-    if (offsets) VFS_CUDA_TRY(cudaMemcpyAsync(offsets, off, (size_t)m.n * 4, cudaMemcpyDeviceToHost, m.stream));
-    return m.check_device();
-}
-
-int vfs_model_get_boundary_fields(vfs_model* h, float* bdens, float* bgrad) {
-    if (!h) return fail(VFS_ERR_INVALID_ARGUMENT, "NULL model");
-    Model& m = h->m;
-    if (m.n == 0) return VFS_OK;
-    int rc = m.check_device();
-    if (rc) return rc;
-    std::vector<float4> b(m.n);
-    VFS_CUDA_TRY(cudaMemcpy(b.data(), m.bnd, (size_t)m.n * sizeof(float4), cudaMemcpyDeviceToHost));
-    for (uint32_t i = 0; i < m.n; i++) {
-        if (bdens) bdens[i] = b[i].w;
-        if (bgrad) {
-            bgrad[3 * i] = b[i].x;
-            bgrad[3 * i + 1] = b[i].y;
-            bgrad[3 * i + 2] = b[i].z;
-        }
-    }
-    return VFS_OK;
-}
-
-int vfs_model_record_fields(vfs_model* h, int32_t enable) {
-    if (!h) return fail(VFS_ERR_INVALID_ARGUMENT, "NULL model");
-    h->m.record = enable != 0;
-    h->m.invalidate_graph();
-    return VFS_OK;
-}
-
-int vfs_model_step(vfs_model* h) {
-    if (!h) return fail(VFS_ERR_INVALID_ARGUMENT, "NULL model");
-    return h->m.run_substeps(h->m.sph.iterations);
-}
-
-int vfs_model_substeps(vfs_model* h, int32_t count) {
-    if (!h) return fail(VFS_ERR_INVALID_ARGUMENT, "NULL model");
-    return h->m.run_substeps(count);
-}
-
-int vfs_model_use_graph(vfs_model* h, int32_t enable) {
-    if (!h) return fail(VFS_ERR_INVALID_ARGUMENT, "NULL model");
-    h->m.use_graph = enable != 0;
-    h->m.invalidate_graph();
-    return VFS_OK;
-}
-
-int vfs_model_synchronize(vfs_model* h) {
-    if (!h) return fail(VFS_ERR_INVALID_ARGUMENT, "NULL model");
-    return h->m.check_device();
-}
-
-int vfs_model_profile_substeps(vfs_model* h, int32_t count, float* phase_ms) {
-    if (!h || !phase_ms || count < 1) return fail(VFS_ERR_INVALID_ARGUMENT, "bad argument");
-    Model& m = h->m;
+static int profile(Model& m, int32_t count, float* phase_ms) {
+    if (!phase_ms || count < 1) return fail(VFS_ERR_INVALID_ARGUMENT, "bad argument");
     for (int k = 0; k < 6; k++) phase_ms[k] = 0.0f;
     if (m.n == 0) return VFS_OK;
     cudaEvent_t ev[7];
     for (int k = 0; k < 7; k++) VFS_CUDA_TRY(cudaEventCreate(&ev[k]));
-    // Phase order of the event pairs: clear, keys, sort, cells+reorder, density, force.
+    // Event pairs in enqueue order: clear, keys, sort, cells+reorder, density, force.
     double acc_ms[6] = {0, 0, 0, 0, 0, 0};
     int rc = VFS_OK;
     for (int it = 0; it < count && rc == VFS_OK; it++) {
@@ -776,32 +703,405 @@ int vfs_model_profile_substeps(vfs_model* h, int32_t count, float* phase_ms) {
     return m.check_device();
 }
 
-int vfs_model_set_sort_config(vfs_model* h, int32_t digit_bits, int32_t tile_items) {
-    if (!h) return fail(VFS_ERR_INVALID_ARGUMENT, "NULL model");
+static int set_stream(Model& m, void* stream) {
+    cudaStreamSynchronize(m.stream);
+    if (m.own_stream && m.stream) cudaStreamDestroy(m.stream);
+    m.own_stream = false;
+    m.stream = nullptr;
+    if (stream) {
+        m.stream = (cudaStream_t)stream;
+    } else {
+        VFS_CUDA_TRY(cudaStreamCreateWithFlags(&m.stream, cudaStreamNonBlocking));
+        m.own_stream = true;
+    }
+    m.invalidate_graph();
+    return VFS_OK;
+}
+
+static int set_sort_config(Model& m, int32_t digit_bits, int32_t tile_items) {
     if (digit_bits < 4 || digit_bits > 8) return fail(VFS_ERR_INVALID_ARGUMENT, "digit_bits must be in [4, 8]");
     if (tile_items != 8 && tile_items != 12 && tile_items != 16)
         return fail(VFS_ERR_INVALID_ARGUMENT, "tile_items must be 8, 12 or 16");
-    Model& m = h->m;
     VFS_CUDA_TRY(cudaStreamSynchronize(m.stream));
     m.digit_bits = digit_bits;
     m.tile_items = tile_items;
     return m.alloc_sort_scratch();
 }
 
+static int validate(const vfs_sim_params* sim, const vfs_sph_params* sph) {
+    if (sim && !(sim->smooth_radius > 0.0f)) return fail(VFS_ERR_INVALID_ARGUMENT, "smooth_radius must be > 0");
+    if (sph && sph->iterations < 1) return fail(VFS_ERR_INVALID_ARGUMENT, "iterations must be >= 1");
+    if (sph && !(sph->target_density > 0.0f)) return fail(VFS_ERR_INVALID_ARGUMENT, "target_density must be > 0");
+    if (sph && (sph->n_particles < 0 || (uint64_t)sph->n_particles > kMaxParticles))
+        return fail(VFS_ERR_CAPACITY, "n_particles must be in [0, 2^30]");
+    return VFS_OK;
+}
+
+static int set_scene_parameters(Model& m, uint32_t scene, const vfs_sim_params* sim,
+                                const vfs_sph_params* sph, const vfs_wcsph_params* wc) {
+    if (scene >= m.scenes.size()) return fail(VFS_ERR_INVALID_ARGUMENT, "scene index out of range");
+    int rc = validate(sim, nullptr);
+    if (rc) return rc;
+    if (sph && sph->iterations < 1) return fail(VFS_ERR_INVALID_ARGUMENT, "iterations must be >= 1");
+    if (sph && !(sph->target_density > 0.0f)) return fail(VFS_ERR_INVALID_ARGUMENT, "target_density must be > 0");
+    SceneHost& sh = m.scenes[scene];
+    if (sim) sh.sim = *sim;
+    if (sph) {
+        const int32_t keep = sh.sph.n_particles;
+        sh.sph = *sph;
+        sh.sph.n_particles = keep;
+    }
+    if (wc) sh.wcsph = *wc;
+    VFS_CUDA_TRY(cudaStreamSynchronize(m.stream));
+    return m.refresh_params();
+}
+
+}  // namespace vfs
+
+using vfs::fail;
+using vfs::Model;
+
+extern "C" {
+
+struct vfs_model {
+    Model* m = nullptr;
+    ~vfs_model() { delete m; }
+};
+
+struct vfs_batch {
+    Model* m = nullptr;
+    ~vfs_batch() { delete m; }
+};
+
+}  // extern "C"
+
+vfs::Model* vfs_model_impl(vfs_model* h) { return h ? h->m : nullptr; }
+
+#define VFS_HANDLE(h)                                                    \
+    if (!(h) || !(h)->m) return fail(VFS_ERR_INVALID_ARGUMENT, "NULL handle"); \
+    Model& m = *(h)->m
+
+extern "C" {
+
+const char* vfs_last_error(void) { return vfs::g_last_error.c_str(); }
+const char* vfs_version(void) { return "vkfluidsim_gb300 0.2 (sm_103a)"; }
+
+int vfs_device_count(void) {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return n;
+}
+
+// ---------------------------------------------------------------- single-scene model
+
+int vfs_model_create(const vfs_sim_params* sim, const vfs_sph_params* sph,
+                     const vfs_wcsph_params* wcsph, vfs_model** out) {
+    try {
+        if (!sim || !sph || !wcsph || !out) return fail(VFS_ERR_INVALID_ARGUMENT, "NULL argument");
+        *out = nullptr;
+        int rc = vfs::validate(sim, sph);
+        if (rc) return rc;
+        std::vector<vfs::SceneHost> scenes(1);
+        scenes[0].sim = *sim;
+        scenes[0].sph = *sph;
+        scenes[0].wcsph = *wcsph;
+        vfs::Model* m = nullptr;
+        rc = vfs::create_model(scenes, &m);
+        if (rc) return rc;
+        vfs_model* h = new vfs_model();
+        h->m = m;
+        *out = h;
+        return VFS_OK;
+    } catch (const std::exception& e) {
+        return fail(VFS_ERR_OUT_OF_MEMORY, e.what());
+    }
+}
+
+int vfs_model_destroy(vfs_model* h) {
+    delete h;
+    return VFS_OK;
+}
+
+int vfs_model_set_stream(vfs_model* h, void* stream) {
+    VFS_HANDLE(h);
+    return vfs::set_stream(m, stream);
+}
+
+int vfs_model_set_parameters(vfs_model* h, const vfs_sim_params* sim, const vfs_sph_params* sph,
+                             const vfs_wcsph_params* wc) {
+    VFS_HANDLE(h);
+    return vfs::set_scene_parameters(m, 0, sim, sph, wc);
+}
+
+int vfs_model_get_parameters(const vfs_model* h, vfs_sim_params* sim, vfs_sph_params* sph,
+                             vfs_wcsph_params* wc) {
+    VFS_HANDLE(h);
+    if (sim) *sim = m.scenes[0].sim;
+    if (sph) *sph = m.scenes[0].sph;
+    if (wc) *wc = m.scenes[0].wcsph;
+    return VFS_OK;
+}
+
+uint32_t vfs_model_num_particles(const vfs_model* h) { return h && h->m ? h->m->n : 0u; }
+
+int vfs_model_add_boundary_object(vfs_model* h, const vfs_boundary_object* obj) {
+    VFS_HANDLE(h);
+    if (!obj) return fail(VFS_ERR_INVALID_ARGUMENT, "NULL object");
+    return m.add_object(0, *obj, nullptr, nullptr);
+}
+
+int vfs_model_add_analytic_object(vfs_model* h, const vfs_analytic_object* obj) {
+    VFS_HANDLE(h);
+    if (!obj) return fail(VFS_ERR_INVALID_ARGUMENT, "NULL object");
+    return m.add_analytic(0, *obj);
+}
+
+uint32_t vfs_model_num_boundary_objects(const vfs_model* h) {
+    return h && h->m ? (uint32_t)h->m->scenes[0].objects.size() : 0u;
+}
+
+static int get_object(const Model& m, uint32_t scene, uint32_t idx, vfs_boundary_object* info,
+                      float* sdf_out, float* vm_out) {
+    if (scene >= m.scenes.size()) return fail(VFS_ERR_INVALID_ARGUMENT, "scene index out of range");
+    const auto& objs = m.scenes[scene].objects;
+    if (idx >= objs.size()) return fail(VFS_ERR_INVALID_ARGUMENT, "object index out of range");
+    const vfs::ObjectStore& o = objs[idx];
+    if (info) *info = o.info;
+    const size_t cnt = (size_t)o.info.resolution[0] * o.info.resolution[1] * o.info.resolution[2];
+    if (sdf_out) VFS_CUDA_TRY(cudaMemcpy(sdf_out, o.d_sdf, cnt * 4, cudaMemcpyDeviceToHost));
+    if (vm_out) VFS_CUDA_TRY(cudaMemcpy(vm_out, o.d_vm, cnt * 4, cudaMemcpyDeviceToHost));
+    return VFS_OK;
+}
+
+int vfs_model_get_boundary_object(const vfs_model* h, uint32_t idx, vfs_boundary_object* info,
+                                  float* sdf_out, float* vm_out) {
+    VFS_HANDLE(h);
+    return get_object(m, 0, idx, info, sdf_out, vm_out);
+}
+
+int vfs_model_set_particle_state(vfs_model* h, const float* pos, const float* vel,
+                                 uint32_t offset, int64_t count) {
+    VFS_HANDLE(h);
+    return m.set_state(0, pos, vel, offset, count);
+}
+
+int vfs_model_copy_data_buffers(vfs_model* h, float* pos, float* vel, float* dens, float* acc) {
+    VFS_HANDLE(h);
+    const int rc = m.get_state(0, pos, vel, dens, nullptr);
+    if (rc) return rc;
+    return m.get_acc(0, acc);
+}
+
+int vfs_model_get_ids(vfs_model* h, uint32_t* ids) {
+    VFS_HANDLE(h);
+    if (!ids) return fail(VFS_ERR_INVALID_ARGUMENT, "NULL ids");
+    return m.get_state(0, nullptr, nullptr, nullptr, ids);
+}
+
+int vfs_model_get_neighbor_arrays(vfs_model* h, uint32_t* keys, uint32_t* sorted_indices,
+                                  uint32_t* offsets) {
+    VFS_HANDLE(h);
+    return m.get_neighbors(0, keys, sorted_indices, offsets);
+}
+
+int vfs_model_get_boundary_fields(vfs_model* h, float* bdens, float* bgrad) {
+    VFS_HANDLE(h);
+    return m.get_boundary(0, bdens, bgrad);
+}
+
+int vfs_model_record_fields(vfs_model* h, int32_t enable) {
+    VFS_HANDLE(h);
+    m.record = enable != 0;
+    m.invalidate_graph();
+    return VFS_OK;
+}
+
+int vfs_model_step(vfs_model* h) {
+    VFS_HANDLE(h);
+    return m.run_substeps(m.scenes[0].sph.iterations);
+}
+
+int vfs_model_substeps(vfs_model* h, int32_t count) {
+    VFS_HANDLE(h);
+    return m.run_substeps(count);
+}
+
+int vfs_model_use_graph(vfs_model* h, int32_t enable) {
+    VFS_HANDLE(h);
+    m.use_graph = enable != 0;
+    m.invalidate_graph();
+    return VFS_OK;
+}
+
+int vfs_model_synchronize(vfs_model* h) {
+    VFS_HANDLE(h);
+    return m.check_device();
+}
+
+int vfs_model_profile_substeps(vfs_model* h, int32_t count, float* phase_ms) {
+    VFS_HANDLE(h);
+    return vfs::profile(m, count, phase_ms);
+}
+
+int vfs_model_set_sort_config(vfs_model* h, int32_t digit_bits, int32_t tile_items) {
+    VFS_HANDLE(h);
+    return vfs::set_sort_config(m, digit_bits, tile_items);
+}
+
 int vfs_model_get_sort_config(const vfs_model* h, int32_t* digit_bits, int32_t* tile_items,
                               int32_t* passes) {
-    if (!h) return fail(VFS_ERR_INVALID_ARGUMENT, "NULL model");
-    if (digit_bits) *digit_bits = h->m.sc.digit_bits;
-    if (tile_items) *tile_items = h->m.sc.tile / 256;
-    if (passes) *passes = h->m.sc.passes;
+    VFS_HANDLE(h);
+    if (digit_bits) *digit_bits = m.sc.digit_bits;
+    if (tile_items) *tile_items = m.sc.tile / 256;
+    if (passes) *passes = m.sc.passes;
     return VFS_OK;
 }
 
 int vfs_model_device_state(vfs_model* h, void** pos4, void** vel4) {
-    if (!h) return fail(VFS_ERR_INVALID_ARGUMENT, "NULL model");
-    if (pos4) *pos4 = h->m.pos[h->m.cur];
-    if (vel4) *vel4 = h->m.vel[h->m.cur];
+    VFS_HANDLE(h);
+    if (pos4) *pos4 = m.pos[m.cur];
+    if (vel4) *vel4 = m.vel[m.cur];
     return VFS_OK;
+}
+
+// ---------------------------------------------------------------- batches of scenes
+
+int vfs_batch_create(int32_t n_scenes, const vfs_sim_params* sims, const vfs_sph_params* sphs,
+                     const vfs_wcsph_params* wcsphs, vfs_batch** out) {
+    try {
+        if (!sims || !sphs || !wcsphs || !out) return fail(VFS_ERR_INVALID_ARGUMENT, "NULL argument");
+        *out = nullptr;
+        if (n_scenes < 1 || (uint32_t)n_scenes > vfs::kMaxScenes)
+            return fail(VFS_ERR_CAPACITY, "n_scenes must be in [1, 65535]");
+        std::vector<vfs::SceneHost> scenes((size_t)n_scenes);
+        for (int32_t s = 0; s < n_scenes; s++) {
+            const int rc = vfs::validate(&sims[s], &sphs[s]);
+            if (rc) return fail(rc, "scene " + std::to_string(s) + ": " + vfs::g_last_error);
+            scenes[s].sim = sims[s];
+            scenes[s].sph = sphs[s];
+            scenes[s].wcsph = wcsphs[s];
+        }
+        vfs::Model* m = nullptr;
+        const int rc = vfs::create_model(scenes, &m);
+        if (rc) return rc;
+        vfs_batch* h = new vfs_batch();
+        h->m = m;
+        *out = h;
+        return VFS_OK;
+    } catch (const std::exception& e) {
+        return fail(VFS_ERR_OUT_OF_MEMORY, e.what());
+    }
+}
+
+int vfs_batch_destroy(vfs_batch* h) {
+    delete h;
+    return VFS_OK;
+}
+
+int32_t vfs_batch_num_scenes(const vfs_batch* h) {
+    return h && h->m ? (int32_t)h->m->scenes.size() : 0;
+}
+
+uint32_t vfs_batch_num_particles(const vfs_batch* h, int32_t scene) {
+    if (!h || !h->m || scene < 0 || (size_t)scene >= h->m->scenes.size()) return 0u;
+    return h->m->scenes[scene].n;
+}
+
+int vfs_batch_set_stream(vfs_batch* h, void* stream) {
+    VFS_HANDLE(h);
+    return vfs::set_stream(m, stream);
+}
+
+int vfs_batch_set_scene_parameters(vfs_batch* h, int32_t scene, const vfs_sim_params* sim,
+                                   const vfs_sph_params* sph, const vfs_wcsph_params* wc) {
+    VFS_HANDLE(h);
+    return vfs::set_scene_parameters(m, (uint32_t)scene, sim, sph, wc);
+}
+
+int vfs_batch_add_boundary_object(vfs_batch* h, int32_t scene, const vfs_boundary_object* obj) {
+    VFS_HANDLE(h);
+    if (!obj) return fail(VFS_ERR_INVALID_ARGUMENT, "NULL object");
+    return m.add_object((uint32_t)scene, *obj, nullptr, nullptr);
+}
+
+int vfs_batch_add_analytic_object(vfs_batch* h, int32_t scene, const vfs_analytic_object* obj) {
+    VFS_HANDLE(h);
+    if (!obj) return fail(VFS_ERR_INVALID_ARGUMENT, "NULL object");
+    return m.add_analytic((uint32_t)scene, *obj);
+}
+
+int vfs_batch_get_boundary_object(const vfs_batch* h, int32_t scene, uint32_t idx,
+                                  vfs_boundary_object* info, float* sdf_out, float* vm_out) {
+    VFS_HANDLE(h);
+    return get_object(m, (uint32_t)scene, idx, info, sdf_out, vm_out);
+}
+
+int vfs_batch_set_particle_state(vfs_batch* h, int32_t scene, const float* pos, const float* vel,
+                                 uint32_t offset, int64_t count) {
+    VFS_HANDLE(h);
+    return m.set_state((uint32_t)scene, pos, vel, offset, count);
+}
+
+int vfs_batch_copy_data_buffers(vfs_batch* h, int32_t scene, float* pos, float* vel, float* dens,
+                                float* acc) {
+    VFS_HANDLE(h);
+    const int rc = m.get_state((uint32_t)scene, pos, vel, dens, nullptr);
+    if (rc) return rc;
+    return m.get_acc((uint32_t)scene, acc);
+}
+
+int vfs_batch_get_ids(vfs_batch* h, int32_t scene, uint32_t* ids) {
+    VFS_HANDLE(h);
+    if (!ids) return fail(VFS_ERR_INVALID_ARGUMENT, "NULL ids");
+    return m.get_state((uint32_t)scene, nullptr, nullptr, nullptr, ids);
+}
+
+int vfs_batch_get_neighbor_arrays(vfs_batch* h, int32_t scene, uint32_t* keys,
+                                  uint32_t* sorted_indices, uint32_t* offsets) {
+    VFS_HANDLE(h);
+    return m.get_neighbors((uint32_t)scene, keys, sorted_indices, offsets);
+}
+
+int vfs_batch_get_boundary_fields(vfs_batch* h, int32_t scene, float* bdens, float* bgrad) {
+    VFS_HANDLE(h);
+    return m.get_boundary((uint32_t)scene, bdens, bgrad);
+}
+
+int vfs_batch_record_fields(vfs_batch* h, int32_t enable) {
+    VFS_HANDLE(h);
+    m.record = enable != 0;
+    m.invalidate_graph();
+    return VFS_OK;
+}
+
+int vfs_batch_substeps(vfs_batch* h, int32_t count) {
+    VFS_HANDLE(h);
+    return m.run_substeps(count);
+}
+
+int vfs_batch_use_graph(vfs_batch* h, int32_t enable) {
+    VFS_HANDLE(h);
+    m.use_graph = enable != 0;
+    m.invalidate_graph();
+    return VFS_OK;
+}
+
+int vfs_batch_synchronize(vfs_batch* h) {
+    VFS_HANDLE(h);
+    return m.check_device();
+}
+
+int vfs_batch_profile_substeps(vfs_batch* h, int32_t count, float* phase_ms) {
+    VFS_HANDLE(h);
+    return vfs::profile(m, count, phase_ms);
+}
+
+int vfs_batch_set_sort_config(vfs_batch* h, int32_t digit_bits, int32_t tile_items) {
+    VFS_HANDLE(h);
+    return vfs::set_sort_config(m, digit_bits, tile_items);
 }
 
 }  // extern "C"

@@ -6,7 +6,8 @@
 
 namespace vfs {
 
-constexpr int kMaxObjects = 8;      // boundary objects per model (kernel-parameter resident)
+constexpr int kMaxObjects = 8;      // boundary objects per scene
+constexpr uint32_t kMaxScenes = 65535;  // scene ids are 16-bit
 constexpr int kMaxSortPasses = 4;   // 32-bit keys at >= 8-bit digits
 constexpr int kMaxSortBins = 256;   // digit width <= 8 bits
 constexpr uint32_t kFlagAggregate = 1u << 30;
@@ -31,12 +32,13 @@ struct DevObject {
     const float* vm;
 };
 
-// Per-substep constants. Derived on the host once, from the same float expressions the
+// Per-scene, per-substep constants. Derived on the host once, from the same float expressions the
 // reference host and shaders use (src/models/model.cpp:225-234, wcsph_with_boundary_model.slang:39-41).
-struct StepParams {
-    uint32_t n;
-    uint32_t n_objects;
-    uint64_t mod_magic;  // ceil(2^64 / n): key = hash % n by multiply-high
+// A scene owns particles [off, off + n) and keys [off, off + n): key = off + HashCell3D % n.
+struct SceneParams {
+    uint32_t n;          // particles of the scene = its hash-table size
+    uint32_t off;        // first particle index and first key of the scene
+    uint64_t mod_magic;  // ceil(2^64 / n): hash % n by multiply-high
     float h, h2, inv_h;
     float cubic;        // 8 / (pi h^3)
     float grad_over_h;  // 48 / (pi h^4) / h (the shader's extra 1/h)
@@ -51,7 +53,18 @@ struct StepParams {
     float bnd_eighth;   // 0.125 h
     float bnd_half;     // 0.5 h
     uint32_t nbr_cap;   // neighbour-list slots per particle
-    DevObject obj[kMaxObjects];
+    uint32_t n_objects;
+    const DevObject* objects;  // device array of n_objects
+};
+
+// What every pass of one substep needs: a single scene passed inline, or (batched) a device table
+// of scenes with the scene id of every particle.
+struct StepLaunch {
+    uint32_t total;              // particles of all scenes
+    uint32_t n_scenes;
+    const SceneParams* scenes;   // device, n_scenes entries (batched launches)
+    const uint16_t* scene_of;    // device, scene id per particle (batched launches)
+    SceneParams one;             // the scene of a single-scene launch
 };
 
 // Scratch of one onesweep sort: global digit histograms, tile counters, look-back status words.
@@ -77,8 +90,9 @@ int key_bits_for(uint32_t max_key);
 SortConfig make_sort_config(uint32_t n, int digit_bits, int tile_items, int key_bits = 0);
 size_t sort_scratch_words(const SortConfig& c);
 
-// keys[i] = HashCell3D(floor(pos[i] / h)) % n and the per-pass digit histograms.
-cudaError_t launch_keys(const StepParams& p, const float4* pos, uint32_t* keys,
+// keys[i] = off + HashCell3D(floor(pos[i] / h)) % n of i's scene, and the per-pass digit
+// histograms.
+cudaError_t launch_keys(const StepLaunch& L, const float4* pos, uint32_t* keys,
                         const SortConfig& sc, uint32_t* ghist, cudaStream_t s);
 // Per-pass digit histograms of caller-provided keys.
 cudaError_t launch_digit_hist(const uint32_t* keys, uint32_t n, const SortConfig& sc,
@@ -92,11 +106,11 @@ cudaError_t launch_cells_reorder(uint32_t n, const uint32_t* skeys, const uint32
                                  uint32_t* cell_scan, const float4* pos_in, const float4* vel_in,
                                  float4* pos_out, float4* vel_out, cudaStream_t s);
 // Boundary volume + density + EOS epilogue; writes each particle's neighbour list.
-cudaError_t launch_density(const StepParams& p, const float4* pos, const uint32_t* cell_scan,
+cudaError_t launch_density(const StepLaunch& L, const float4* pos, const uint32_t* cell_scan,
                            float4* aux, float4* bnd, uint32_t* nbr, uint32_t* nbr_count,
                            cudaStream_t s);
 // Pressure + viscosity + wall + symplectic Euler over the density pass's neighbour lists.
-cudaError_t launch_force(const StepParams& p, const float4* pos, const float4* vel,
+cudaError_t launch_force(const StepLaunch& L, const float4* pos, const float4* vel,
                          const float4* aux, const float4* bnd, const uint32_t* cell_scan,
                          const uint32_t* nbr, const uint32_t* nbr_count, float4* pos_out,
                          float4* vel_out, float4* acc_out, cudaStream_t s);
@@ -105,8 +119,9 @@ cudaError_t launch_force(const StepParams& p, const float4* pos, const float4* v
 int enqueue_sort_pairs(uint32_t* items, uint32_t* keys, uint32_t n, const SortConfig& sc,
                        uint32_t* tmp_keys, uint32_t* tmp_items, uint32_t* scratch,
                        cudaStream_t s);
-// spatial_offsets[k] = cell start or n for empty keys (reference layout).
-cudaError_t launch_offsets(uint32_t n, const uint32_t* cell_scan, uint32_t* offsets,
+// Scene-local spatial_offsets[k] = cell start - off, or n for empty keys (reference layout), for
+// the scene owning keys [off, off + n).
+cudaError_t launch_offsets(uint32_t n, uint32_t off, const uint32_t* cell_scan, uint32_t* offsets,
                            cudaStream_t s);
 
 }  // namespace vfs

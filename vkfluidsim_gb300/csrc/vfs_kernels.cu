@@ -135,12 +135,12 @@ __device__ __forceinline__ float mat_row(const float* M, int r, float x, float y
 }
 
 // CalculateBoundaryVolume for one particle (wcsph_with_boundary_model.slang:102-151).
-__device__ __forceinline__ void boundary_terms(const StepParams& p, float px, float py, float pz,
+__device__ __forceinline__ void boundary_terms(const SceneParams& p, float px, float py, float pz,
                                                float& bd, float& bgx, float& bgy, float& bgz) {
     bd = 0.0f;
     bgx = bgy = bgz = 0.0f;
     for (uint32_t oi = 0; oi < p.n_objects; oi++) {
-        const DevObject& o = p.obj[oi];
+        const DevObject& o = p.objects[oi];
         const float lx = mat_row(o.T, 0, px, py, pz);
         const float ly = mat_row(o.T, 1, px, py, pz);
         const float lz = mat_row(o.T, 2, px, py, pz);
@@ -206,9 +206,22 @@ __device__ __forceinline__ void boundary_terms(const StepParams& p, float px, fl
 
 // ---------------------------------------------------------------- neighbour ranges
 
+// ---------------------------------------------------------------- scenes
+
+// Parameters of the scene owning particle i: the inline scene of a single-scene launch, or the
+// scene-table entry of a batched one.
+template <bool kBatch>
+__device__ __forceinline__ const SceneParams& scene_params(const StepLaunch& L, uint32_t i) {
+    if constexpr (kBatch)
+        return L.scenes[__ldg(L.scene_of + i)];
+    else
+        return L.one;
+}
+
 // ---------------------------------------------------------------- kernels
 
-__global__ void __launch_bounds__(256) k_keys(StepParams p, const float4* __restrict__ pos,
+template <bool kBatch>
+__global__ void __launch_bounds__(256) k_keys(StepLaunch L, const float4* __restrict__ pos,
                                               uint32_t* __restrict__ keys, int passes,
                                               int digit_bits, uint32_t* __restrict__ ghist) {
     __shared__ uint32_t s_h[kMaxSortPasses * kMaxSortBins];
@@ -216,12 +229,13 @@ __global__ void __launch_bounds__(256) k_keys(StepParams p, const float4* __rest
     const uint32_t mask = (uint32_t)bins - 1u;
     for (int e = threadIdx.x; e < passes * bins; e += blockDim.x) s_h[e] = 0u;
     __syncthreads();
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < p.n;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < L.total;
          i += gridDim.x * blockDim.x) {
+        const SceneParams& p = scene_params<kBatch>(L, i);
         const float4 x = pos[i];
-        const uint32_t key = key_mod(
-            hash_cell(cell_coord(x.x, p.h), cell_coord(x.y, p.h), cell_coord(x.z, p.h)),
-            p.mod_magic, p.n);
+        const uint32_t key = p.off + key_mod(hash_cell(cell_coord(x.x, p.h), cell_coord(x.y, p.h),
+                                                       cell_coord(x.z, p.h)),
+                                             p.mod_magic, p.n);
         keys[i] = key;
         for (int ps = 0; ps < passes; ps++)
             atomicAdd(&s_h[ps * bins + ((key >> (ps * digit_bits)) & mask)], 1u);
@@ -463,11 +477,12 @@ __global__ void __launch_bounds__(kCellBlock)
 }
 
 __global__ void __launch_bounds__(256)
-    k_offsets(uint32_t n, const uint32_t* __restrict__ scan, uint32_t* __restrict__ offsets) {
+    k_offsets(uint32_t n, uint32_t off, const uint32_t* __restrict__ scan,
+              uint32_t* __restrict__ offsets) {
     const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
-    const uint32_t a = scan[k], b = scan[k + 1];
-    offsets[k] = b > a ? a : n;
+    const uint32_t a = scan[off + k], b = scan[off + k + 1];
+    offsets[k] = b > a ? a - off : n;
 }
 
 // ---------------------------------------------------------------- neighbour passes
@@ -503,7 +518,7 @@ constexpr float kPruneLimit = 1.002f;
 // and calls visit(j, q) for each, with q = pos[j]; four positions are fetched per iteration and
 // batch_end() runs after each group of at most four (where a full list is drained).
 template <typename Visit, typename BatchEnd>
-__device__ __forceinline__ void for_each_candidate(const StepParams& p,
+__device__ __forceinline__ void for_each_candidate(const SceneParams& p,
                                                    const uint32_t* __restrict__ scan,
                                                    const float4* __restrict__ pos,
                                                    const float4& xi, uint32_t cx, uint32_t cy,
@@ -532,20 +547,21 @@ __device__ __forceinline__ void for_each_candidate(const StepParams& p,
         // Cells cx-1..cx+1 share a hash block iff (cell + 25) / 50 agrees at both ends (this also
         // covers the wrap of cell + 25 at 2^32 near cell -26).
         const bool same_block = (cx + 24u) / 50u == (cx + 26u) / 50u && hA <= 0xFFFFFFFDu;
+        const uint32_t* sc = scan + p.off;  // the scene's keys are off + local key
         if (same_block && kA + 2u < p.n) {
             // Buckets kA, kA+1, kA+2 are adjacent: one range, trimmed at either end.
-            b0 = __ldg(scan + kA + (skip_l ? 1u : 0u));
-            e0 = __ldg(scan + kA + (skip_r ? 2u : 3u));
+            b0 = __ldg(sc + kA + (skip_l ? 1u : 0u));
+            e0 = __ldg(sc + kA + (skip_r ? 2u : 3u));
         } else {
             const uint32_t kB = key_mod(hash_cell(cx, ry, rz), p.mod_magic, p.n);
             const uint32_t kC = key_mod(hash_cell(cx + 1u, ry, rz), p.mod_magic, p.n);
-            b0 = __ldg(scan + kA);
-            e0 = skip_l ? b0 : __ldg(scan + kA + 1u);
-            b1 = __ldg(scan + kB);
-            e1 = __ldg(scan + kB + 1u);
+            b0 = __ldg(sc + kA);
+            e0 = skip_l ? b0 : __ldg(sc + kA + 1u);
+            b1 = __ldg(sc + kB);
+            e1 = __ldg(sc + kB + 1u);
             if (!skip_r) {
-                b2 = __ldg(scan + kC);
-                e2 = __ldg(scan + kC + 1u);
+                b2 = __ldg(sc + kC);
+                e2 = __ldg(sc + kC + 1u);
             }
         }
 #pragma unroll 1
@@ -576,13 +592,15 @@ __device__ __forceinline__ void for_each_candidate(const StepParams& p,
 // (nbr[s * n + i], so a warp's lanes store and later load consecutive words), and its length in
 // nbr_count[i] (a length above nbr_cap means the list overflowed and was truncated). Positions
 // do not change before the force pass, so that list is exactly the force pass's neighbour set.
+template <bool kBatch>
 __global__ void __launch_bounds__(kNbrBlock, 6)
-    k_density(StepParams p, const float4* __restrict__ pos, const uint32_t* __restrict__ scan,
+    k_density(StepLaunch L, const float4* __restrict__ pos, const uint32_t* __restrict__ scan,
               float4* __restrict__ aux, float4* __restrict__ bnd, uint32_t* __restrict__ nbr,
               uint32_t* __restrict__ nbr_count) {
     __shared__ uint32_t s_j[kListCap * kNbrBlock];
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= p.n) return;
+    if (i >= L.total) return;
+    const SceneParams& p = scene_params<kBatch>(L, i);
     const int tid = threadIdx.x;
     const float4 xi = __ldg(pos + i);
     const uint32_t cx = cell_coord(xi.x, p.h), cy = cell_coord(xi.y, p.h),
@@ -600,7 +618,7 @@ __global__ void __launch_bounds__(kNbrBlock, 6)
             const float r = r2 > 0.0f ? r2 * rsqrtf(r2) : 0.0f;
             rho += p.mass * cubic_w(r * p.inv_h, p.cubic);
             if (j != i) {
-                if (listed < p.nbr_cap) nbr[(size_t)listed * p.n + i] = j;
+                if (listed < p.nbr_cap) nbr[(size_t)listed * L.total + i] = j;
                 listed++;
             }
         }
@@ -635,7 +653,7 @@ struct ForceAcc {
 
 // Pressure and viscosity contributions of one in-range neighbour (PressureAccel slang:234-249,
 // ViscousAccel slang:301-318).
-__device__ __forceinline__ void force_term(const StepParams& p, const float4& xi, const float4& vi,
+__device__ __forceinline__ void force_term(const SceneParams& p, const float4& xi, const float4& vi,
                                            float pdi, const float4& xj, const float2& aj,
                                            const float4& vj, ForceAcc& f) {
     const float xx = xi.x - xj.x, xy = xi.y - xj.y, xz = xi.z - xj.z;
@@ -660,7 +678,7 @@ __device__ __forceinline__ void force_term(const StepParams& p, const float4& xi
 }
 
 // Phase B of the force pass over the first cnt listed neighbours.
-__device__ __forceinline__ void force_drain(const StepParams& p, const float4* __restrict__ pos,
+__device__ __forceinline__ void force_drain(const SceneParams& p, const float4* __restrict__ pos,
                                             const float4* __restrict__ vel,
                                             const float2* __restrict__ aux2,
                                             const uint32_t* s_j, int tid, int cnt,
@@ -686,15 +704,17 @@ __device__ __forceinline__ void force_drain(const StepParams& p, const float4* _
 // CalculatePressureAccel + CalculateViscousAccel + UpdatePositions
 // (wcsph_with_boundary_model.slang:205-360), fused: both sums are accumulated separately in the
 // reference's visiting order, then a = ((g - P) + V) + wall, v += a dt, x += v dt.
+template <bool kBatch>
 __global__ void __launch_bounds__(kNbrBlock, 6)
-    k_force(StepParams p, const float4* __restrict__ pos, const float4* __restrict__ vel,
+    k_force(StepLaunch L, const float4* __restrict__ pos, const float4* __restrict__ vel,
             const float4* __restrict__ aux, const float4* __restrict__ bnd,
             const uint32_t* __restrict__ scan, const uint32_t* __restrict__ nbr,
             const uint32_t* __restrict__ nbr_count, float4* __restrict__ pos_out,
             float4* __restrict__ vel_out, float4* __restrict__ acc_out) {
     __shared__ uint32_t s_j[kListCap * kNbrBlock];
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= p.n) return;
+    if (i >= L.total) return;
+    const SceneParams& p = scene_params<kBatch>(L, i);
     const int tid = threadIdx.x;
     const float4 xi = __ldg(pos + i);
     const float4 vi = __ldg(vel + i);
@@ -709,7 +729,7 @@ __global__ void __launch_bounds__(kNbrBlock, 6)
         uint32_t k = 0;
 #pragma unroll 1
         for (; k + 2u <= listed; k += 2u) {
-            const uint32_t j0 = nbr[(size_t)k * p.n + i], j1 = nbr[(size_t)(k + 1u) * p.n + i];
+            const uint32_t j0 = nbr[(size_t)k * L.total + i], j1 = nbr[(size_t)(k + 1u) * L.total + i];
             const float4 x0 = __ldg(pos + j0), x1 = __ldg(pos + j1);
             const float4 v0 = __ldg(vel + j0), v1 = __ldg(vel + j1);
             const float2 a0 = __ldg(aux2 + 2 * (size_t)j0), a1 = __ldg(aux2 + 2 * (size_t)j1);
@@ -717,7 +737,7 @@ __global__ void __launch_bounds__(kNbrBlock, 6)
             force_term(p, xi, vi, pdi, x1, a1, v1, f);
         }
         if (k < listed) {
-            const uint32_t j0 = nbr[(size_t)k * p.n + i];
+            const uint32_t j0 = nbr[(size_t)k * L.total + i];
             force_term(p, xi, vi, pdi, __ldg(pos + j0), __ldg(aux2 + 2 * (size_t)j0),
                        __ldg(vel + j0), f);
         }
@@ -808,12 +828,15 @@ size_t sort_scratch_words(const SortConfig& c) {
     return (size_t)c.passes * c.bins + (size_t)c.passes + (size_t)c.passes * c.tiles * c.bins;
 }
 
-cudaError_t launch_keys(const StepParams& p, const float4* pos, uint32_t* keys,
+cudaError_t launch_keys(const StepLaunch& L, const float4* pos, uint32_t* keys,
                         const SortConfig& sc, uint32_t* ghist, cudaStream_t s) {
-    if (p.n == 0) return cudaSuccess;
-    uint32_t blocks = (p.n + 255u) / 256u;
+    if (L.total == 0) return cudaSuccess;
+    uint32_t blocks = (L.total + 255u) / 256u;
     if (blocks > 152u * 8u) blocks = 152u * 8u;
-    k_keys<<<blocks, 256, 0, s>>>(p, pos, keys, sc.passes, sc.digit_bits, ghist);
+    if (L.n_scenes > 1)
+        k_keys<true><<<blocks, 256, 0, s>>>(L, pos, keys, sc.passes, sc.digit_bits, ghist);
+    else
+        k_keys<false><<<blocks, 256, 0, s>>>(L, pos, keys, sc.passes, sc.digit_bits, ghist);
     return cudaGetLastError();
 }
 
@@ -862,29 +885,37 @@ cudaError_t launch_cells_reorder(uint32_t n, const uint32_t* skeys, const uint32
     return cudaGetLastError();
 }
 
-cudaError_t launch_density(const StepParams& p, const float4* pos, const uint32_t* cell_scan,
+cudaError_t launch_density(const StepLaunch& L, const float4* pos, const uint32_t* cell_scan,
                            float4* aux, float4* bnd, uint32_t* nbr, uint32_t* nbr_count,
                            cudaStream_t s) {
-    if (p.n == 0) return cudaSuccess;
-    k_density<<<(p.n + kNbrBlock - 1) / kNbrBlock, kNbrBlock, 0, s>>>(p, pos, cell_scan, aux, bnd,
-                                                                      nbr, nbr_count);
+    if (L.total == 0) return cudaSuccess;
+    const uint32_t blocks = (L.total + kNbrBlock - 1) / kNbrBlock;
+    if (L.n_scenes > 1)
+        k_density<true><<<blocks, kNbrBlock, 0, s>>>(L, pos, cell_scan, aux, bnd, nbr, nbr_count);
+    else
+        k_density<false><<<blocks, kNbrBlock, 0, s>>>(L, pos, cell_scan, aux, bnd, nbr, nbr_count);
     return cudaGetLastError();
 }
 
-cudaError_t launch_force(const StepParams& p, const float4* pos, const float4* vel,
+cudaError_t launch_force(const StepLaunch& L, const float4* pos, const float4* vel,
                          const float4* aux, const float4* bnd, const uint32_t* cell_scan,
                          const uint32_t* nbr, const uint32_t* nbr_count, float4* pos_out,
                          float4* vel_out, float4* acc_out, cudaStream_t s) {
-    if (p.n == 0) return cudaSuccess;
-    k_force<<<(p.n + kNbrBlock - 1) / kNbrBlock, kNbrBlock, 0, s>>>(
-        p, pos, vel, aux, bnd, cell_scan, nbr, nbr_count, pos_out, vel_out, acc_out);
+    if (L.total == 0) return cudaSuccess;
+    const uint32_t blocks = (L.total + kNbrBlock - 1) / kNbrBlock;
+    if (L.n_scenes > 1)
+        k_force<true><<<blocks, kNbrBlock, 0, s>>>(L, pos, vel, aux, bnd, cell_scan, nbr, nbr_count,
+                                                   pos_out, vel_out, acc_out);
+    else
+        k_force<false><<<blocks, kNbrBlock, 0, s>>>(L, pos, vel, aux, bnd, cell_scan, nbr,
+                                                    nbr_count, pos_out, vel_out, acc_out);
     return cudaGetLastError();
 }
 
-cudaError_t launch_offsets(uint32_t n, const uint32_t* cell_scan, uint32_t* offsets,
+cudaError_t launch_offsets(uint32_t n, uint32_t off, const uint32_t* cell_scan, uint32_t* offsets,
                            cudaStream_t s) {
     if (n == 0) return cudaSuccess;
-    k_offsets<<<(n + 255u) / 256u, 256, 0, s>>>(n, cell_scan, offsets);
+    k_offsets<<<(n + 255u) / 256u, 256, 0, s>>>(n, off, cell_scan, offsets);
     return cudaGetLastError();
 }
 

@@ -1,4 +1,4 @@
-// Host-side model state behind the vfs_model handle (C++ only).
+// Host-side state behind the vfs_model / vfs_batch handles (C++ only).
 #pragma once
 
 #include <cuda_runtime.h>
@@ -25,11 +25,23 @@ struct FluidBlock {
     float pos[3];
 };
 
-struct Model {
+// One independent simulation: the reference's scene + model parameters, its boundary objects and
+// its slice [off, off + n) of the particle and key arrays.
+struct SceneHost {
     vfs_sim_params sim{};
     vfs_sph_params sph{};
     vfs_wcsph_params wcsph{};
     uint32_t n = 0;
+    uint32_t off = 0;
+    std::vector<ObjectStore> objects;
+    std::vector<FluidBlock> blocks;  // set by vfs_scene_load for vfs_scene_reset
+    SceneParams params{};
+};
+
+// The engine behind both handles: a plain model is one scene, a batch is many advanced together.
+struct Model {
+    std::vector<SceneHost> scenes;
+    uint32_t n = 0;  // particles of all scenes
 
     cudaStream_t stream = nullptr;
     bool own_stream = false;
@@ -49,19 +61,20 @@ struct Model {
     float4* acc = nullptr;
     uint32_t* nbr = nullptr;        // kNbrCap slot-major neighbour lists
     uint32_t* nbr_count = nullptr;  // list length per particle
-    float* stage = nullptr;  // 32 bytes per particle of host-transfer staging
+    float* stage = nullptr;         // 32 bytes per particle of host-transfer staging
     uint32_t* scratch = nullptr;
     size_t scratch_words = 0;
     uint32_t* err = nullptr;
+    SceneParams* d_scenes = nullptr;   // batched launches: the scene table
+    uint16_t* d_scene_of = nullptr;    // batched launches: scene id per particle
+    DevObject* d_objects = nullptr;    // boundary objects of all scenes
+    size_t d_objects_cap = 0;
 
     int digit_bits = 8;
     int tile_items = 16;
     SortConfig sc{};
     SortScratch sort_scratch{};
-    StepParams params{};
-
-    std::vector<ObjectStore> objects;
-    std::vector<FluidBlock> blocks;  // set by vfs_scene_load for vfs_scene_reset
+    StepLaunch launch{};
 
     bool record = false;
     bool use_graph = true;
@@ -70,17 +83,26 @@ struct Model {
 
     ~Model();
     int init();
-    void refresh_params();
+    int refresh_params();
     void invalidate_graph();
     int alloc_sort_scratch();
     int enqueue_substep(cudaEvent_t* ev);
     int run_substeps(int count);
     int check_device();
-    int set_state(const float* pos3, const float* vel3, uint32_t offset, int64_t count);
-    int get_state(float* pos3, float* vel3, float* dens, uint32_t* ids);
-    int add_object(const vfs_boundary_object& src, const float* d_sdf, const float* d_vm);
-    int add_analytic(const vfs_analytic_object& a);
+    // Scene-relative state I/O (offset and ids are scene-local).
+    int set_state(uint32_t scene, const float* pos3, const float* vel3, uint32_t offset,
+                  int64_t count);
+    int get_state(uint32_t scene, float* pos3, float* vel3, float* dens, uint32_t* ids);
+    int get_acc(uint32_t scene, float* acc3);
+    int get_neighbors(uint32_t scene, uint32_t* keys, uint32_t* perm, uint32_t* offsets);
+    int get_boundary(uint32_t scene, float* bdens, float* bgrad);
+    int add_object(uint32_t scene, const vfs_boundary_object& src, const float* d_sdf,
+                   const float* d_vm);
+    int add_analytic(uint32_t scene, const vfs_analytic_object& a);
 };
+
+// Builds a model of the given scenes (sizes from each sph.n_particles) and allocates it.
+int create_model(const std::vector<SceneHost>& scenes, Model** out);
 
 }  // namespace vfs
 

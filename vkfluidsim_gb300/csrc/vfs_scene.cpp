@@ -256,28 +256,30 @@ std::vector<float> spawn_random(const float size[3], const float pos[3], uint32_
     return out;
 }
 
-int spawn_in_box(Model& m, const float size[3], const float pos[3], uint32_t offset, int64_t count,
-                 int32_t mode, uint64_t seed) {
+int spawn_in_box(Model& m, uint32_t scene, const float size[3], const float pos[3],
+                 uint32_t offset, int64_t count, int32_t mode, uint64_t seed) {
     if (count == 0) return VFS_OK;
-    const uint32_t cnt = count > 0 ? (uint32_t)count : m.n;
-    if ((uint64_t)offset + cnt > m.n) return fail(VFS_ERR_CAPACITY, "spawn exceeds the model's particle count");
+    if (scene >= m.scenes.size()) return fail(VFS_ERR_INVALID_ARGUMENT, "scene index out of range");
+    const SceneHost& sh = m.scenes[scene];
+    const uint32_t cnt = count > 0 ? (uint32_t)count : sh.n;
+    if ((uint64_t)offset + cnt > sh.n) return fail(VFS_ERR_CAPACITY, "spawn exceeds the scene's particle count");
     std::vector<float> p = mode == 1 ? spawn_random(size, pos, cnt, seed)
-                                     : spawn_compact(size, pos, cnt, m.sph.target_density);
+                                     : spawn_compact(size, pos, cnt, sh.sph.target_density);
     std::vector<float> v((size_t)cnt * 3, 0.0f);
-    return m.set_state(p.data(), v.data(), offset, cnt);
+    return m.set_state(scene, p.data(), v.data(), offset, cnt);
 }
 
 // GenericScene::Reset, src/scenes/generic_scene.cpp:42-57.
 int reset_blocks(Model& m) {
-    const float density = m.sph.target_density;
+    const float density = m.scenes[0].sph.target_density;
     const float particle_volume = 1 / density;
     const float particle_diam = std::cbrt(particle_volume);
     uint32_t offset = 0;
-    for (const FluidBlock& b : m.blocks) {
+    for (const FluidBlock& b : m.scenes[0].blocks) {
         const uint32_t count = b.size[0] * b.size[1] * b.size[2];
         float size[3];
         for (int a = 0; a < 3; a++) size[a] = particle_diam * (float)(b.size[a] + 1u);
-        const int rc = spawn_in_box(m, size, b.pos, offset, count, 0, 0);
+        const int rc = spawn_in_box(m, 0, size, b.pos, offset, count, 0, 0);
         if (rc) return rc;
         offset += count;
     }
@@ -296,7 +298,7 @@ int vfs_model_set_particles_in_box(vfs_model* h, const float box_size[3], const 
     vfs::Model* m = vfs_model_impl(h);
     if (!m || !box_size || !box_pos) return fail(VFS_ERR_INVALID_ARGUMENT, "NULL argument");
     try {
-        return vfs::spawn_in_box(*m, box_size, box_pos, offset, count, mode, seed);
+        return vfs::spawn_in_box(*m, 0, box_size, box_pos, offset, count, mode, seed);
     } catch (const std::exception& e) {
         return fail(VFS_ERR_OUT_OF_MEMORY, e.what());
     }
@@ -403,13 +405,13 @@ int vfs_scene_load(const char* json_path, const char* resources_dir, vfs_model**
     if (rc) return rc;
     Model* m = vfs_model_impl(h);
     for (const auto& a : objects) {
-        rc = m->add_analytic(a);
+        rc = m->add_analytic(0, a);
         if (rc) {
             vfs_model_destroy(h);
             return rc;
         }
     }
-    m->blocks = blocks;
+    m->scenes[0].blocks = blocks;
     rc = reset_blocks(*m);
     if (rc) {
         vfs_model_destroy(h);

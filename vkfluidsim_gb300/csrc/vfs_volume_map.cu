@@ -61,7 +61,13 @@ __global__ void __launch_bounds__(128) k_volume_map(VolumeMapParams P, float* __
     sdf_out[lin] = __double2float_rn(node_sdf);
     double value = 0.0;
     const float sr = P.h;
-    if (!(node_sdf > 2.0 * (double)sr)) {
+    // sdf is 1-Lipschitz, so below -h (with a margin for the float rounding of x + xi) every
+    // quadrature point is inside the solid and the node takes the precomputed full-ball value.
+    const double deep = -((double)sr + 4e-6 * (1.0 + fabs((double)fx) + fabs((double)fy) +
+                                               fabs((double)fz)));
+    if (node_sdf < deep) {
+        value = P.full_ball;
+    } else if (!(node_sdf > 2.0 * (double)sr)) {
         const double w_zero = kernel_w(0.0, (double)sr, P.w_factor);
         const float sr2 = __fmul_rn(sr, sr);
         double integral = 0.0;
@@ -97,6 +103,29 @@ __global__ void __launch_bounds__(128) k_volume_map(VolumeMapParams P, float* __
 }
 
 }  // namespace
+
+double volume_map_full_ball(const VolumeMapParams& p) {
+    const float sr = p.h;
+    const float sr2 = sr * sr;
+    double integral = 0.0;
+    for (int a = 0; a < p.qn; a++) {
+        const double wa = p.gw[a];
+        const float xa = (float)(p.c0 * p.gx[a] + p.c1);
+        for (int b = 0; b < p.qn; b++) {
+            const double wab = wa * p.gw[b];
+            const float xb = (float)(p.c0 * p.gx[b] + p.c1);
+            const float xab2 = xa * xa + xb * xb;
+            for (int c = 0; c < p.qn; c++) {
+                const double wabc = wab * p.gw[c];
+                const float xc = (float)(p.c0 * p.gx[c] + p.c1);
+                const float len2 = xab2 + xc * xc;
+                integral = integral + wabc * (!(len2 > sr2) ? 1.0 : 0.0);
+            }
+        }
+    }
+    integral = integral * ((p.c0 * p.c0) * p.c0);
+    return 0.8 * integral;
+}
 
 cudaError_t launch_volume_map(const VolumeMapParams& p, float* sdf, float* vm, cudaStream_t s) {
     const uint64_t total = (uint64_t)p.res[0] * p.res[1] * p.res[2];

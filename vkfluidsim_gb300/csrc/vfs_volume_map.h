@@ -19,7 +19,12 @@ struct VolumeMapParams {
     double gx[kMaxQuadrature], gw[kMaxQuadrature];
     double c0, c1;      // integration-domain half width and centre
     double w_factor;    // 8 / (pi h^3) in double
+    double full_ball;   // the integral when every quadrature point lies inside the solid
 };
+
+// Quadrature sum of a node whose whole h-ball lies inside the solid (integrand 1 wherever
+// |xi| <= h), accumulated in the kernel's order so it equals the per-node sum bit for bit.
+double volume_map_full_ball(const VolumeMapParams& p);
 
 cudaError_t launch_volume_map(const VolumeMapParams& p, float* sdf, float* vm, cudaStream_t s);
 

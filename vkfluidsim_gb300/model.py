@@ -20,7 +20,7 @@ from ._abi import check, load_library
 
 __all__ = [
     "SimulationParameters", "SPHParameters", "WCSPHParameters", "WCSPHWithBoundaryModel",
-    "AnalyticObject", "load_scene", "generate_lattice", "generate_uniform_blob",
+    "AnalyticObject", "Batch", "load_scene", "generate_lattice", "generate_uniform_blob",
     "generate_fourier_velocity",
 ]
 
@@ -320,3 +320,124 @@ def generate_fourier_velocity(pos, modes: int, amplitude: float, seed: int) -> n
     check(lib.vfs_generate_fourier_velocity(pos.shape[0], _fp(pos), modes, amplitude, seed,
                                             _fp(out)))
     return out
+
+
+class Batch:
+    """Many independent scenes advanced together (vfs_batch): every pass is one launch over all
+    scenes; each scene's results equal those of its own WCSPHWithBoundaryModel."""
+
+    def __init__(self, scenes):
+        """scenes: sequence of (SimulationParameters, SPHParameters, WCSPHParameters)."""
+        self._lib = load_library()
+        k = len(scenes)
+        sims = (_abi.SimParams * k)(*[s[0].to_c() for s in scenes])
+        sphs = (_abi.SphParams * k)(*[s[1].to_c() for s in scenes])
+        wcs = (_abi.WcsphParams * k)(*[s[2].to_c() for s in scenes])
+        h = C.c_void_p()
+        check(self._lib.vfs_batch_create(k, sims, sphs, wcs, C.byref(h)))
+        self._h = h
+
+    def clear(self) -> None:
+        if getattr(self, "_h", None) and self._h.value:
+            self._lib.vfs_batch_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.clear()
+        except Exception:
+            pass
+
+    @property
+    def n_scenes(self) -> int:
+        return int(self._lib.vfs_batch_num_scenes(self._h))
+
+    def n_particles(self, scene: int) -> int:
+        return int(self._lib.vfs_batch_num_particles(self._h, scene))
+
+    def set_stream(self, stream_handle: int) -> None:
+        check(self._lib.vfs_batch_set_stream(self._h, C.c_void_p(stream_handle)))
+
+    def set_scene_parameters(self, scene: int, sim=None, sph=None, wcsph=None) -> None:
+        a = C.byref(sim.to_c()) if sim else None
+        b = C.byref(sph.to_c()) if sph else None
+        c = C.byref(wcsph.to_c()) if wcsph else None
+        check(self._lib.vfs_batch_set_scene_parameters(self._h, scene, a, b, c))
+
+    def add_analytic_object(self, scene: int, obj: AnalyticObject) -> None:
+        check(self._lib.vfs_batch_add_analytic_object(self._h, scene, C.byref(obj.to_c())))
+
+    def get_boundary_object(self, scene: int, idx: int) -> BoundaryObjectInfo:
+        info = _abi.BoundaryObject()
+        check(self._lib.vfs_batch_get_boundary_object(self._h, scene, idx, C.byref(info), None,
+                                                      None))
+        res = tuple(int(x) for x in info.resolution)
+        cnt = res[0] * res[1] * res[2]
+        sdf = np.empty(cnt, np.float32)
+        vm = np.empty(cnt, np.float32)
+        check(self._lib.vfs_batch_get_boundary_object(self._h, scene, idx, None, _fp(sdf),
+                                                      _fp(vm)))
+        return BoundaryObjectInfo(np.array(info.transform[:], np.float32),
+                                  np.array(info.rotation[:], np.float32),
+                                  np.array(info.box_size[:], np.float32),
+                                  np.array(info.box_pos[:], np.float32), res, sdf, vm)
+
+    def set_particle_state(self, scene: int, pos, vel, offset: int = 0, count: int = -1) -> None:
+        pos = _f32(pos, (-1, 3))
+        vel = _f32(vel, (-1, 3))
+        if count < 0:
+            count = pos.shape[0]
+        check(self._lib.vfs_batch_set_particle_state(self._h, scene, _fp(pos), _fp(vel), offset,
+                                                     count))
+
+    def copy_data_buffers(self, scene: int, with_acc: bool = False) -> dict:
+        n = self.n_particles(scene)
+        pos = np.empty((n, 3), np.float32)
+        vel = np.empty((n, 3), np.float32)
+        dens = np.empty(n, np.float32)
+        acc = np.empty((n, 3), np.float32) if with_acc else None
+        check(self._lib.vfs_batch_copy_data_buffers(self._h, scene, _fp(pos), _fp(vel), _fp(dens),
+                                                    _fp(acc)))
+        out = {"positions": pos, "velocities": vel, "densities": dens}
+        if with_acc:
+            out["accelerations"] = acc
+        return out
+
+    def get_ids(self, scene: int) -> np.ndarray:
+        ids = np.empty(self.n_particles(scene), np.uint32)
+        check(self._lib.vfs_batch_get_ids(self._h, scene, _up(ids)))
+        return ids
+
+    def get_neighbor_arrays(self, scene: int):
+        n = self.n_particles(scene)
+        keys, perm, offs = (np.empty(n, np.uint32) for _ in range(3))
+        check(self._lib.vfs_batch_get_neighbor_arrays(self._h, scene, _up(keys), _up(perm),
+                                                      _up(offs)))
+        return keys, perm, offs
+
+    def get_boundary_fields(self, scene: int):
+        n = self.n_particles(scene)
+        bd = np.empty(n, np.float32)
+        bg = np.empty((n, 3), np.float32)
+        check(self._lib.vfs_batch_get_boundary_fields(self._h, scene, _fp(bd), _fp(bg)))
+        return bd, bg
+
+    def record_fields(self, enable: bool = True) -> None:
+        check(self._lib.vfs_batch_record_fields(self._h, int(enable)))
+
+    def substeps(self, count: int) -> None:
+        check(self._lib.vfs_batch_substeps(self._h, count))
+
+    def use_graph(self, enable: bool) -> None:
+        check(self._lib.vfs_batch_use_graph(self._h, int(enable)))
+
+    def synchronize(self) -> None:
+        check(self._lib.vfs_batch_synchronize(self._h))
+
+    def profile_substeps(self, count: int) -> dict:
+        ms = (C.c_float * 6)()
+        check(self._lib.vfs_batch_profile_substeps(self._h, count, ms))
+        return dict(zip(WCSPHWithBoundaryModel.PHASES, (float(x) for x in ms)))
+
+    def set_sort_config(self, digit_bits: int, tile_items: int) -> None:
+        check(self._lib.vfs_batch_set_sort_config(self._h, digit_bits, tile_items))

@@ -114,3 +114,41 @@ WORKLOADS = {
     "stress_4m": stress_4m,
     "dam_break_64k": dam_break_64k,
 }
+
+
+def batched_scenes(n_scenes=256, n_min=2048, n_max=65536, map_res=64, seed=3, steps=500):
+    """Independent dam-break scenes of uneven size: N_s log-uniform in [n_min, n_max] (jittered
+    lattices, spacing 0.02, h = 0.04, the column in the low corner octant of its own box), nu_s
+    log-uniform in [1e-3, 5e-2], stiffness uniform in [20, 100], each with its own container volume
+    map at map_res^3, dt = 2e-4."""
+    rng = np.random.default_rng(seed)
+    sizes = np.exp(rng.uniform(np.log(n_min), np.log(n_max), n_scenes)).astype(np.int64)
+    nus = np.exp(rng.uniform(np.log(1e-3), np.log(5e-2), n_scenes))
+    ks = rng.uniform(20.0, 100.0, n_scenes)
+    spacing = 0.02
+    out = []
+    for s in range(n_scenes):
+        n = int(sizes[s])
+        side = int(np.ceil(np.cbrt(n)))
+        nz = int(np.ceil(n / (side * side)))
+        pos = generate_lattice((side, side, nz), (0.0, 0.0, 0.0), spacing, 0.1, seed * 100003 + s)[:n]
+        box = (2 * side * spacing, 2 * side * spacing, 2 * nz * spacing)
+        sim = SimulationParameters((0.0, 0.0, -9.81), 2 * spacing)
+        sph = SPHParameters(1.0, 1, n, 2e-4, 1000.0, box, (0.0, 0.0, 0.0))
+        wc = WCSPHParameters(1e4, float(ks[s]), 7.0, float(nus[s]))
+        objs = [_container((0, 0, 0), box, (map_res,) * 3)] if map_res else []
+        out.append(Workload(f"batch_scene_{s}", sim, sph, wc, objs, np.ascontiguousarray(pos),
+                            np.zeros_like(pos), steps))
+    return out
+
+
+def build_batch(scenes):
+    """One vfs_batch holding every workload of `scenes` (parameters, objects, initial state)."""
+    from .model import Batch
+
+    b = Batch([(w.sim, replace(w.sph, n_particles=w.n), w.wcsph) for w in scenes])
+    for s, w in enumerate(scenes):
+        for o in w.objects:
+            b.add_analytic_object(s, o)
+        b.set_particle_state(s, w.pos, w.vel)
+    return b
