@@ -218,6 +218,23 @@ int vfs_batch_synchronize(vfs_batch* b);
 int vfs_batch_profile_substeps(vfs_batch* b, int32_t count, float* phase_ms);
 int vfs_batch_set_sort_config(vfs_batch* b, int32_t digit_bits, int32_t tile_items);
 
+/* ---- differentiable rollouts (an extension: the reference has no differentiation) ----
+ * A rollout advances a single-scene model `steps` substeps from its current state, keeping the
+ * state every `checkpoint_every` substeps. The backward pass recomputes each segment from its
+ * checkpoint (keeping that segment's sorted inputs, permutations, density products and neighbour
+ * lists on the device) and runs the adjoint kernels of integration, force, EOS, density and the
+ * volume-map terms in reverse. Gradients are by particle id (the order state was first set in):
+ * dl_dx_final / dl_dv_final (3N floats, either may be NULL) seed d loss / d final state; dl_dv0 and
+ * dl_dx0 receive d loss / d initial velocities and positions; dl_dparams[0..1] receive
+ * d loss / d viscosity_strenght and d loss / d stiffness. Neighbour lists longer than 128 entries
+ * make the backward pass fail with VFS_ERR_CAPACITY. */
+typedef struct vfs_rollout vfs_rollout;
+int vfs_rollout_create(vfs_model* m, int32_t steps, int32_t checkpoint_every, vfs_rollout** out);
+int vfs_rollout_destroy(vfs_rollout* r);
+int vfs_rollout_forward(vfs_rollout* r);
+int vfs_rollout_backward(vfs_rollout* r, const float* dl_dx_final, const float* dl_dv_final,
+                         float* dl_dv0, float* dl_dx0, double* dl_dparams);
+
 /* ---- scene: LoadScene / GenericScene (src/util/scene_loader.cpp:113-140,
  * src/scenes/generic_scene.cpp:10-57) ---- */
 

@@ -135,6 +135,10 @@ SIGNATURES = {
     "vfs_batch_synchronize": (_I, [_P]),
     "vfs_batch_profile_substeps": (_I, [_P, C.c_int32, _F]),
     "vfs_batch_set_sort_config": (_I, [_P, C.c_int32, C.c_int32]),
+    "vfs_rollout_create": (_I, [_P, C.c_int32, C.c_int32, C.POINTER(_P)]),
+    "vfs_rollout_destroy": (_I, [_P]),
+    "vfs_rollout_forward": (_I, [_P]),
+    "vfs_rollout_backward": (_I, [_P, _F, _F, _F, _F, C.POINTER(C.c_double)]),
     "vfs_scene_load": (_I, [C.c_char_p, C.c_char_p, C.POINTER(_P)]),
     "vfs_scene_reset": (_I, [_P]),
     "vfs_sort_pairs": (_I, [_P, _P, _U32, _U32, _P]),

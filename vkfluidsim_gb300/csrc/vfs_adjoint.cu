@@ -1,0 +1,648 @@
+// Reverse-mode (adjoint) kernels of the WCSPH substep and the checkpointed rollout around them.
+//
+// The forward substep (src/models/wcsph_with_boundary_model.cpp:93-116; shaders
+// wcsph_with_boundary_model.slang:102-360) is differentiated as a smooth function of the sorted
+// positions x', velocities v', viscosity nu and stiffness k: neighbour sets, the sort and branch
+// choices are piecewise constant and carry no gradient. Notation, per ordered pair (i, j) of the
+// density pass's neighbour list, x = x_i - x_j, r = |x|, n = x / r, gw = the shader's kernel
+// gradient (with its extra 1/h), W = the cubic spline, c = adjoint of a_i:
+//   pressure   a_i -= m (pd_i + pd_j) gw(r) n          -> d(-c.T)/dx, d/dpd_i, d/dpd_j
+//   viscosity  a_i += 10 nu mr_j (v_ij.x) gw(r) n / (r^2 + 0.01 h^2)
+//   boundary   a_i -= (pd_i + pb_i) rho0 G_i, rho_i += rho0 Psi_i (volume-map terms)
+//   wall       a_i -= k_w diff(x_i)
+//   EOS        pd = p / rho^2, pb = p / rho0^2, mr = m / max(rho, 1e-6), p = k ((rho/rho0)^g - 1)
+//   density    rho_i = sum_j m W(r_ij) + rho0 Psi_i
+// Pair contributions to the other particle j are scattered with atomics (the list of i holds j
+// with the reference's multiplicity, which need not be symmetric under hash collisions).
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <string>
+#include <vector>
+
+#include "vfs_cuda.h"
+#include "vfs_internal.h"
+#include "vfs_model.h"
+
+namespace vfs {
+namespace {
+
+constexpr uint32_t kErrAdjointOverflow = 2u;  // a neighbour list longer than its capacity
+
+__device__ __forceinline__ float3 f3(const float4& a) { return make_float3(a.x, a.y, a.z); }
+__device__ __forceinline__ float dot3(float3 a, float3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ float3 operator+(float3 a, float3 b) { return make_float3(a.x + b.x, a.y + b.y, a.z + b.z); }
+__device__ __forceinline__ float3 operator-(float3 a, float3 b) { return make_float3(a.x - b.x, a.y - b.y, a.z - b.z); }
+__device__ __forceinline__ float3 operator*(float s, float3 a) { return make_float3(s * a.x, s * a.y, s * a.z); }
+
+__device__ __forceinline__ void atomic_add3(float4* p, float3 v) {
+    atomicAdd(&p->x, v.x);
+    atomicAdd(&p->y, v.y);
+    atomicAdd(&p->z, v.z);
+}
+
+// Shader kernel gradient gw(r) and its derivative d gw / dr (kernels_3d.slang:78-91).
+__device__ __forceinline__ void gw_and_deriv(const SceneParams& p, float r, float& gw, float& dgw) {
+    const float q = r * p.inv_h;
+    gw = 0.0f;
+    dgw = 0.0f;
+    if (r > 1e-9f && q <= 1.0f) {
+        const float G = p.grad_over_h;
+        if (q > 0.5f) {
+            const float t = 1.0f - q;
+            gw = -G * t * t;
+            dgw = 2.0f * G * t * p.inv_h;
+        } else {
+            gw = G * q * (3.0f * q - 2.0f);
+            dgw = G * (6.0f * q - 2.0f) * p.inv_h;
+        }
+    }
+}
+
+// dW/dr of the cubic spline (kernels_3d.slang:62-76): h * gw(r) inside the support.
+__device__ __forceinline__ float dW_dr(const SceneParams& p, float r) {
+    float gw, dgw;
+    gw_and_deriv(p, r, gw, dgw);
+    return p.h * gw;
+}
+
+__device__ __forceinline__ float cubic_W(const SceneParams& p, float r) {
+    const float q = r * p.inv_h;
+    if (q > 1.0f) return 0.0f;
+    if (q > 0.5f) {
+        const float t = 1.0f - q;
+        return p.cubic * 2.0f * t * t * t;
+    }
+    return p.cubic * (6.0f * q * q * q - 6.0f * q * q + 1.0f);
+}
+
+// ---- trilinear grid sampling with its gradient (SampleGrid, slang:51-66, cells clamped) ----
+
+struct GridSample {
+    float v;
+    float3 g;  // d value / d local coordinates
+};
+
+__device__ __forceinline__ GridSample sample_grad(const float* __restrict__ grid, const DevObject& o,
+                                                  float3 l) {
+    const float u[3] = {(l.x - o.box_pos[0]) / o.box_size[0], (l.y - o.box_pos[1]) / o.box_size[1],
+                        (l.z - o.box_pos[2]) / o.box_size[2]};
+    uint32_t cell[3];
+    float chi[3], dchi[3];
+    for (int a = 0; a < 3; a++) {
+        const uint32_t n = o.res[a];
+        const float x = ((float)n - 1.0f) * u[a];
+        float f = floorf(x);
+        if (!(f >= 0.0f)) f = 0.0f;
+        if (f > (float)(n - 2u)) f = (float)(n - 2u);
+        cell[a] = (uint32_t)f;
+        chi[a] = 2.0f * (x - f) - 1.0f;
+        dchi[a] = 2.0f * ((float)n - 1.0f) / o.box_size[a];  // d chi / d local
+    }
+    const size_t sy = o.res[0], sz = (size_t)o.res[0] * o.res[1];
+    const size_t b = cell[0] + sy * cell[1] + sz * cell[2];
+    float v = 0.0f, gx = 0.0f, gy = 0.0f, gz = 0.0f;
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+        const int ox = i >> 2, oy = i & 1, oz = (i >> 1) & 1;
+        const float sx = ox ? 1.0f : -1.0f, sy_ = oy ? 1.0f : -1.0f, sz_ = oz ? 1.0f : -1.0f;
+        const float fx = 1.0f + sx * chi[0], fy = 1.0f + sy_ * chi[1], fz = 1.0f + sz_ * chi[2];
+        const float gval = __ldg(grid + b + ox + oy * sy + oz * sz);
+        v += gval * fx * fy * fz;
+        gx += gval * sx * fy * fz;
+        gy += gval * fx * sy_ * fz;
+        gz += gval * fx * fy * sz_;
+    }
+    GridSample s;
+    s.v = v * 0.125f;
+    s.g = make_float3(gx * 0.125f * dchi[0], gy * 0.125f * dchi[1], gz * 0.125f * dchi[2]);
+    return s;
+}
+
+__device__ __forceinline__ float3 mat3_row_apply(const float* M, float3 v) {  // rows of a 3x4
+    return make_float3(M[0] * v.x + M[1] * v.y + M[2] * v.z, M[4] * v.x + M[5] * v.y + M[6] * v.z,
+                       M[8] * v.x + M[9] * v.y + M[10] * v.z);
+}
+__device__ __forceinline__ float3 mat3_T_apply(const float* M, float3 v) {  // transpose of a 3x4
+    return make_float3(M[0] * v.x + M[4] * v.y + M[8] * v.z, M[1] * v.x + M[5] * v.y + M[9] * v.z,
+                       M[2] * v.x + M[6] * v.y + M[10] * v.z);
+}
+
+// Adjoint of CalculateBoundaryVolume (slang:102-151) for one particle: returns d L / d x given
+// psi_bar = d L / d Psi_i and G_bar = d L / d G_i.
+__device__ float3 boundary_adjoint(const SceneParams& p, float3 x, float psi_bar, float3 G_bar) {
+    float3 xbar = make_float3(0.f, 0.f, 0.f);
+    for (uint32_t oi = 0; oi < p.n_objects; oi++) {
+        const DevObject& o = p.objects[oi];
+        const float3 l = make_float3(o.T[0] * x.x + o.T[1] * x.y + o.T[2] * x.z + o.T[3],
+                                     o.T[4] * x.x + o.T[5] * x.y + o.T[6] * x.z + o.T[7],
+                                     o.T[8] * x.x + o.T[9] * x.y + o.T[10] * x.z + o.T[11]);
+        if (l.x < o.box_pos[0] || l.y < o.box_pos[1] || l.z < o.box_pos[2] ||
+            l.x > o.box_pos[0] + o.box_size[0] || l.y > o.box_pos[1] + o.box_size[1] ||
+            l.z > o.box_pos[2] + o.box_size[2])
+            continue;
+        const GridSample S = sample_grad(o.sdf, o, l);
+        if (!(S.v >= 0.0f && S.v < p.h)) continue;
+        const GridSample V = sample_grad(o.vm, o, l);
+        if (!(V.v > 0.0f)) continue;
+        const float e = p.grad_eps;
+        const float3 ex = make_float3(e, 0.f, 0.f), ey = make_float3(0.f, e, 0.f),
+                     ez = make_float3(0.f, 0.f, e);
+        const GridSample sxp = sample_grad(o.sdf, o, l + ex), sxm = sample_grad(o.sdf, o, l - ex);
+        const GridSample syp = sample_grad(o.sdf, o, l + ey), sym = sample_grad(o.sdf, o, l - ey);
+        const GridSample szp = sample_grad(o.sdf, o, l + ez), szm = sample_grad(o.sdf, o, l - ez);
+        const float inv2e = 1.0f / (2.0f * e);
+        const float3 g = make_float3((sxp.v - sxm.v) * inv2e, (syp.v - sym.v) * inv2e,
+                                     (szp.v - szm.v) * inv2e);
+        const float modn = sqrtf(dot3(g, g));
+        if (!(modn > 1e-9f)) continue;
+        const float3 ghat = (1.0f / modn) * g;
+        const float3 nrm = mat3_row_apply(o.R, ghat);
+        const bool d_active = S.v + p.bnd_eighth > p.bnd_half;
+        const float d = d_active ? S.v + p.bnd_eighth : p.bnd_half;
+        float gw, dgw;
+        gw_and_deriv(p, d, gw, dgw);
+        const float Wd = cubic_W(p, d);
+        const float dWd = p.h * gw;
+        const float3 grad_d = d_active ? S.g : make_float3(0.f, 0.f, 0.f);
+        // d Psi / d l = W(d) grad V + V W'(d) grad d.
+        float3 lbar = psi_bar * (Wd * V.g + (V.v * dWd) * grad_d);
+        // G = V gw(d) n: (G_bar . n)(gw grad V + V gw' grad d) + V gw (dn/dl)^T G_bar.
+        const float gn = dot3(G_bar, nrm);
+        lbar = lbar + gn * (gw * V.g + (V.v * dgw) * grad_d);
+        const float3 rg = mat3_T_apply(o.R, G_bar);         // R^T G_bar
+        const float3 w = (1.0f / modn) * (rg - dot3(rg, ghat) * ghat);  // (I - gg^T)/|g| R^T G_bar
+        // J_g^T w with J_g[a][b] = (dS/dl_b(l + e e_a) - dS/dl_b(l - e e_a)) / 2e.
+        const float3 jt = (w.x * inv2e) * (sxp.g - sxm.g) + (w.y * inv2e) * (syp.g - sym.g) +
+                          (w.z * inv2e) * (szp.g - szm.g);
+        lbar = lbar + (V.v * gw) * jt;
+        xbar = xbar + mat3_T_apply(o.T, lbar);  // d l / d x = T (linear part)
+    }
+    return xbar;
+}
+
+// ---- the reverse substep, one thread per sorted particle ----
+
+struct AdjBuffers {
+    const float4* pos;   // x' (sorted positions of the substep)
+    const float4* vel;   // v'
+    const float4* aux;   // (pd, mr, rho, pb)
+    const float4* bnd;   // (G, Psi)
+    const uint32_t* nbr;
+    const uint32_t* nbr_count;
+    float4* xbar;        // accumulates d L / d x' (sorted order)
+    float4* vbar;        // accumulates d L / d v'
+    float4* abar;        // d L / d a
+    float* pdbar;
+    float* pbbar;
+    float* mrbar;
+    float* rhobar;
+    float4* gbar;        // d L / d G
+    double* dparams;     // [d nu, d k]
+    uint32_t* err;
+};
+
+// Symplectic Euler, reversed: x_out = x' + v_out dt, v_out = v' + a dt.
+__global__ void k_adj_integrate(SceneParams p, uint32_t n, const float4* __restrict__ xbar_out,
+                                const float4* __restrict__ vbar_out, AdjBuffers B) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 xo = xbar_out[i], vo = vbar_out[i];
+    const float vx = vo.x + p.dt * xo.x, vy = vo.y + p.dt * xo.y, vz = vo.z + p.dt * xo.z;
+    B.xbar[i] = make_float4(xo.x, xo.y, xo.z, 0.f);
+    B.vbar[i] = make_float4(vx, vy, vz, 0.f);
+    B.abar[i] = make_float4(p.dt * vx, p.dt * vy, p.dt * vz, 0.f);
+    B.pdbar[i] = 0.f;
+    B.mrbar[i] = 0.f;
+}
+
+__device__ __forceinline__ void block_add_double(double v, double* dst) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0 && v != 0.0) atomicAdd(dst, v);
+}
+
+// Adjoint of the force pass: pressure, viscosity, boundary pressure and wall terms.
+__global__ void __launch_bounds__(128) k_adj_force(SceneParams p, uint32_t n, AdjBuffers B) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    double dnu = 0.0;
+    if (i < n) {
+        const float3 xi = f3(B.pos[i]), vi = f3(B.vel[i]);
+        const float4 ai = B.aux[i];
+        const float3 c = f3(B.abar[i]);
+        const float pdi = ai.x, pbi = ai.w;
+        float3 xbi = make_float3(0.f, 0.f, 0.f), vbi = make_float3(0.f, 0.f, 0.f);
+        float pdbar_i = 0.f;
+        const uint32_t cnt = B.nbr_count[i];
+        if (cnt > p.nbr_cap) atomicOr(B.err, kErrAdjointOverflow);
+        const uint32_t listed = min(cnt, p.nbr_cap);
+        const float nus = p.visc_scale;
+        for (uint32_t k = 0; k < listed; k++) {
+            const uint32_t j = B.nbr[(size_t)k * n + i];
+            const float3 xj = f3(B.pos[j]), vj = f3(B.vel[j]);
+            const float2 aj = *reinterpret_cast<const float2*>(B.aux + j);  // (pd_j, mr_j)
+            const float3 x = xi - xj;
+            const float r2 = dot3(x, x);
+            const float r = sqrtf(r2);
+            if (!(r > 1e-9f)) continue;
+            float gw, dgw;
+            gw_and_deriv(p, r, gw, dgw);
+            const float3 nn = (1.0f / r) * x;
+            const float cn = dot3(c, nn);
+            // Pressure: L-term = -m (pd_i + pd_j) gw (c . n).
+            const float alpha = pdi + aj.x;
+            const float3 dfp = (dgw * cn) * nn + (gw / r) * (c - cn * nn);
+            const float3 gxp = (-p.mass * alpha) * dfp;
+            const float pbar = -p.mass * gw * cn;
+            pdbar_i += pbar;
+            atomicAdd(&B.pdbar[j], pbar);
+            // Viscosity: L-term = nus mr_j (v.x)(c.x) u(r), u = gw / (r (r^2 + eps)).
+            const float3 v = vi - vj;
+            const float den = r2 + p.visc_eps;
+            const float u = gw / (r * den);
+            const float du = (dgw * r * den - gw * (3.0f * r2 + p.visc_eps)) / (r * r * den * den);
+            const float vx = dot3(v, x), cx = dot3(c, x);
+            const float s = nus * aj.y;
+            const float3 gxv = s * ((cx * u) * v + (vx * u) * c + (vx * cx * du) * nn);
+            const float3 gvv = (s * cx * u) * x;
+            atomicAdd(&B.mrbar[j], nus * vx * cx * u);
+            dnu += 10.0 * (double)aj.y * (double)vx * (double)cx * (double)u;
+            const float3 gx = gxp + gxv;
+            xbi = xbi + gx;
+            vbi = vbi + gvv;
+            atomic_add3(&B.xbar[j], -1.0f * gx);
+            atomic_add3(&B.vbar[j], -1.0f * gvv);
+        }
+        // Boundary pressure: L-term = -(pd_i + pb_i) rho0 (c . G_i).
+        const float3 G = f3(B.bnd[i]);
+        const float cg = dot3(c, G);
+        pdbar_i += -p.rho0 * cg;
+        B.pbbar[i] = -p.rho0 * cg;
+        const float sg = -(pdi + pbi) * p.rho0;
+        B.gbar[i] = make_float4(sg * c.x, sg * c.y, sg * c.z, 0.f);
+        // Wall penalty: a -= k_w diff(x), d diff / dx = 1 outside [lo, hi].
+        const float xs[3] = {xi.x, xi.y, xi.z};
+        const float cs[3] = {c.x, c.y, c.z};
+        float wb[3];
+        for (int a = 0; a < 3; a++)
+            wb[a] = (xs[a] < p.lo[a] || xs[a] > p.hi[a]) ? -p.wall_k * cs[a] : 0.0f;
+        xbi = xbi + make_float3(wb[0], wb[1], wb[2]);
+        atomic_add3(&B.xbar[i], xbi);
+        atomic_add3(&B.vbar[i], vbi);
+        atomicAdd(&B.pdbar[i], pdbar_i);
+    }
+    block_add_double(dnu, &B.dparams[0]);
+}
+
+// Adjoint of the EOS epilogue: rho_bar from pd_bar, pb_bar, mr_bar; d L / d k.
+__global__ void k_adj_eos(SceneParams p, uint32_t n, AdjBuffers B) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    double dk = 0.0;
+    if (i < n) {
+        const float4 ai = B.aux[i];
+        const float rho = ai.z;
+        const float pr = rho > 0.0f ? ai.x * rho * rho : 0.0f;  // p = pd rho^2
+        const float ratio = fmaxf(rho, p.rho0) / p.rho0;
+        const float f = powf(ratio, p.expoent) - 1.0f;  // p = k f
+        const float dp = rho > p.rho0 ? p.stiffness * p.expoent * powf(ratio, p.expoent - 1.0f) / p.rho0 : 0.0f;
+        const float pdb = B.pdbar[i], pbb = B.pbbar[i], mrb = B.mrbar[i];
+        float rb = 0.0f;
+        if (rho > 0.0f) rb += pdb * (dp / (rho * rho) - 2.0f * pr / (rho * rho * rho));
+        rb += pbb * dp / (p.rho0 * p.rho0);
+        if (rho > 1e-6f) rb += mrb * (-p.mass / (rho * rho));
+        B.rhobar[i] = rb;
+        if (rho > 0.0f) dk += (double)pdb * (double)f / ((double)rho * (double)rho);
+        dk += (double)pbb * (double)f / ((double)p.rho0 * (double)p.rho0);
+    }
+    block_add_double(dk, &B.dparams[1]);
+}
+
+// Adjoint of the density sum and of the volume-map terms.
+__global__ void __launch_bounds__(128) k_adj_density(SceneParams p, uint32_t n, AdjBuffers B) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float3 xi = f3(B.pos[i]);
+    const float rb = B.rhobar[i];
+    float3 xbi = make_float3(0.f, 0.f, 0.f);
+    const uint32_t listed = min(B.nbr_count[i], p.nbr_cap);
+    if (rb != 0.0f) {
+        for (uint32_t k = 0; k < listed; k++) {
+            const uint32_t j = B.nbr[(size_t)k * n + i];
+            const float3 x = xi - f3(B.pos[j]);
+            const float r = sqrtf(dot3(x, x));
+            if (!(r > 1e-9f)) continue;
+            const float3 g = (rb * p.mass * dW_dr(p, r) / r) * x;
+            xbi = xbi + g;
+            atomic_add3(&B.xbar[j], -1.0f * g);
+        }
+    }
+    const float4 gb = B.gbar[i];
+    const float psib = rb * p.rho0;
+    if (p.n_objects && (psib != 0.0f || gb.x != 0.0f || gb.y != 0.0f || gb.z != 0.0f))
+        xbi = xbi + boundary_adjoint(p, xi, psib, f3(gb));
+    atomic_add3(&B.xbar[i], xbi);
+}
+
+// Back through the reorder x' = x[perm]: scatter into the previous order.
+__global__ void k_adj_unsort(uint32_t n, const uint32_t* __restrict__ perm,
+                             const float4* __restrict__ xs, const float4* __restrict__ vs,
+                             float4* __restrict__ xprev, float4* __restrict__ vprev) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t src = perm[i];
+    if (src >= n) return;
+    xprev[src] = xs[i];
+    vprev[src] = vs[i];
+}
+
+// Places a by-id host gradient onto the particles of a state whose ids are in pos.w.
+__global__ void k_adj_by_id(uint32_t n, const float4* __restrict__ pos, const float* __restrict__ g3,
+                            float4* __restrict__ out) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t id = __float_as_uint(pos[i].w);
+    out[i] = id < n && g3 ? make_float4(g3[3 * id], g3[3 * id + 1], g3[3 * id + 2], 0.f)
+                          : make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
+// Gathers a per-particle float4 field into by-id float3 order.
+__global__ void k_to_id(uint32_t n, const float4* __restrict__ pos, const float4* __restrict__ f,
+                        float* __restrict__ out3) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t id = __float_as_uint(pos[i].w);
+    if (id >= n) return;
+    out3[3 * id] = f[i].x;
+    out3[3 * id + 1] = f[i].y;
+    out3[3 * id + 2] = f[i].z;
+}
+
+}  // namespace
+
+#define VFS_ADJ_TRY(expr)                                                                 \
+    do {                                                                                  \
+        cudaError_t e_ = (expr);                                                          \
+        if (e_ != cudaSuccess)                                                            \
+            return ::vfs::fail(VFS_ERR_CUDA, std::string(#expr) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+// A checkpointed differentiable rollout of a single-scene model.
+struct Rollout {
+    Model* m = nullptr;
+    int steps = 0, every = 0;
+    std::vector<float4*> ck_pos, ck_vel;  // state before steps 0, every, 2 every, ...
+    float4 *fin_pos = nullptr, *fin_vel = nullptr;  // state after the last step
+    // One segment of per-substep records.
+    std::vector<float4*> s_pos, s_vel, s_aux, s_bnd;
+    std::vector<uint32_t*> s_perm, s_nbr, s_cnt;
+    float4 *xbar = nullptr, *vbar = nullptr, *xs = nullptr, *vs = nullptr, *abar = nullptr, *gbar = nullptr;
+    float *pdbar = nullptr, *pbbar = nullptr, *mrbar = nullptr, *rhobar = nullptr;
+    float* host_io = nullptr;  // 3N floats on the device for host transfers
+    double* dparams = nullptr;
+    bool forward_done = false;
+
+    ~Rollout() {
+        for (auto* p : ck_pos) cudaFree(p);
+        for (auto* p : ck_vel) cudaFree(p);
+        for (auto* p : s_pos) cudaFree(p);
+        for (auto* p : s_vel) cudaFree(p);
+        for (auto* p : s_aux) cudaFree(p);
+        for (auto* p : s_bnd) cudaFree(p);
+        for (auto* p : s_perm) cudaFree(p);
+        for (auto* p : s_nbr) cudaFree(p);
+        for (auto* p : s_cnt) cudaFree(p);
+        cudaFree(fin_pos);
+        cudaFree(fin_vel);
+        cudaFree(xbar);
+        cudaFree(vbar);
+        cudaFree(xs);
+        cudaFree(vs);
+        cudaFree(abar);
+        cudaFree(gbar);
+        cudaFree(pdbar);
+        cudaFree(pbbar);
+        cudaFree(mrbar);
+        cudaFree(rhobar);
+        cudaFree(host_io);
+        cudaFree(dparams);
+    }
+
+    int init(Model* model, int n_steps, int ck_every) {
+        m = model;
+        steps = n_steps;
+        every = ck_every < 1 ? 1 : ck_every;
+        const size_t N = m->n ? m->n : 1;
+        const int n_ck = (steps + every - 1) / every;
+        ck_pos.resize(n_ck, nullptr);
+        ck_vel.resize(n_ck, nullptr);
+        for (int c = 0; c < n_ck; c++) {
+            VFS_ADJ_TRY(cudaMalloc(&ck_pos[c], N * sizeof(float4)));
+            VFS_ADJ_TRY(cudaMalloc(&ck_vel[c], N * sizeof(float4)));
+        }
+        const int seg = every < steps ? every : steps;
+        s_pos.resize(seg, nullptr);
+        s_vel.resize(seg, nullptr);
+        s_aux.resize(seg, nullptr);
+        s_bnd.resize(seg, nullptr);
+        s_perm.resize(seg, nullptr);
+        s_nbr.resize(seg, nullptr);
+        s_cnt.resize(seg, nullptr);
+        for (int t = 0; t < seg; t++) {
+            VFS_ADJ_TRY(cudaMalloc(&s_pos[t], N * sizeof(float4)));
+            VFS_ADJ_TRY(cudaMalloc(&s_vel[t], N * sizeof(float4)));
+            VFS_ADJ_TRY(cudaMalloc(&s_aux[t], N * sizeof(float4)));
+            VFS_ADJ_TRY(cudaMalloc(&s_bnd[t], N * sizeof(float4)));
+            VFS_ADJ_TRY(cudaMalloc(&s_perm[t], N * 4));
+            VFS_ADJ_TRY(cudaMalloc(&s_nbr[t], N * kNbrCap * 4));
+            VFS_ADJ_TRY(cudaMalloc(&s_cnt[t], N * 4));
+        }
+        for (float4** b : {&fin_pos, &fin_vel, &xbar, &vbar, &xs, &vs, &abar, &gbar})
+            VFS_ADJ_TRY(cudaMalloc(b, N * sizeof(float4)));
+        for (float** b : {&pdbar, &pbbar, &mrbar, &rhobar}) VFS_ADJ_TRY(cudaMalloc(b, N * 4));
+        VFS_ADJ_TRY(cudaMalloc(&host_io, N * 12));
+        VFS_ADJ_TRY(cudaMalloc(&dparams, 2 * sizeof(double)));
+        return VFS_OK;
+    }
+
+    int save(float4* dp, float4* dv) {
+        const size_t bytes = (size_t)m->n * sizeof(float4);
+        VFS_ADJ_TRY(cudaMemcpyAsync(dp, m->pos[m->cur], bytes, cudaMemcpyDeviceToDevice, m->stream));
+        VFS_ADJ_TRY(cudaMemcpyAsync(dv, m->vel[m->cur], bytes, cudaMemcpyDeviceToDevice, m->stream));
+        return VFS_OK;
+    }
+    int restore(const float4* dp, const float4* dv) {
+        const size_t bytes = (size_t)m->n * sizeof(float4);
+        VFS_ADJ_TRY(cudaMemcpyAsync(m->pos[m->cur], dp, bytes, cudaMemcpyDeviceToDevice, m->stream));
+        VFS_ADJ_TRY(cudaMemcpyAsync(m->vel[m->cur], dv, bytes, cudaMemcpyDeviceToDevice, m->stream));
+        return VFS_OK;
+    }
+
+    int forward() {
+        for (int t = 0; t < steps; t++) {
+            if (t % every == 0) {
+                const int rc = save(ck_pos[t / every], ck_vel[t / every]);
+                if (rc) return rc;
+            }
+            const int rc = m->run_substeps(1);
+            if (rc) return rc;
+        }
+        const int rc = save(fin_pos, fin_vel);
+        if (rc) return rc;
+        forward_done = true;
+        return m->check_device();
+    }
+
+    // Recomputes substeps [t0, t0 + len) from checkpoint t0 / every, keeping each substep's
+    // sorted inputs, permutation, density products and neighbour lists.
+    int record_segment(int t0, int len) {
+        int rc = restore(ck_pos[t0 / every], ck_vel[t0 / every]);
+        if (rc) return rc;
+        const size_t N = m->n;
+        const int o = 1 - m->cur;
+        for (int t = 0; t < len; t++) {
+            rc = m->enqueue_substep(nullptr);
+            if (rc) return rc;
+            cudaStream_t s = m->stream;
+            VFS_ADJ_TRY(cudaMemcpyAsync(s_pos[t], m->pos[o], N * 16, cudaMemcpyDeviceToDevice, s));
+            VFS_ADJ_TRY(cudaMemcpyAsync(s_vel[t], m->vel[o], N * 16, cudaMemcpyDeviceToDevice, s));
+            VFS_ADJ_TRY(cudaMemcpyAsync(s_aux[t], m->aux, N * 16, cudaMemcpyDeviceToDevice, s));
+            VFS_ADJ_TRY(cudaMemcpyAsync(s_bnd[t], m->bnd, N * 16, cudaMemcpyDeviceToDevice, s));
+            VFS_ADJ_TRY(cudaMemcpyAsync(s_perm[t], m->sperm, N * 4, cudaMemcpyDeviceToDevice, s));
+            VFS_ADJ_TRY(cudaMemcpyAsync(s_nbr[t], m->nbr, N * kNbrCap * 4, cudaMemcpyDeviceToDevice, s));
+            VFS_ADJ_TRY(cudaMemcpyAsync(s_cnt[t], m->nbr_count, N * 4, cudaMemcpyDeviceToDevice, s));
+        }
+        return VFS_OK;
+    }
+
+    // One reverse substep: (xbar, vbar) hold the adjoint of the substep's output state; on return
+    // they hold the adjoint of its input state.
+    int reverse_substep(int t) {
+        const uint32_t n = m->n;
+        const SceneParams& p = m->scenes[0].params;
+        cudaStream_t s = m->stream;
+        AdjBuffers B;
+        B.pos = s_pos[t];
+        B.vel = s_vel[t];
+        B.aux = s_aux[t];
+        B.bnd = s_bnd[t];
+        B.nbr = s_nbr[t];
+        B.nbr_count = s_cnt[t];
+        B.xbar = xs;
+        B.vbar = vs;
+        B.abar = abar;
+        B.pdbar = pdbar;
+        B.pbbar = pbbar;
+        B.mrbar = mrbar;
+        B.rhobar = rhobar;
+        B.gbar = gbar;
+        B.dparams = dparams;
+        B.err = m->err;
+        const unsigned g256 = (n + 255) / 256, g128 = (n + 127) / 128;
+        k_adj_integrate<<<g256, 256, 0, s>>>(p, n, xbar, vbar, B);
+        k_adj_force<<<g128, 128, 0, s>>>(p, n, B);
+        k_adj_eos<<<g256, 256, 0, s>>>(p, n, B);
+        k_adj_density<<<g128, 128, 0, s>>>(p, n, B);
+        k_adj_unsort<<<g256, 256, 0, s>>>(n, s_perm[t], xs, vs, xbar, vbar);
+        VFS_ADJ_TRY(cudaGetLastError());
+        return VFS_OK;
+    }
+
+    int backward(const float* gx_host, const float* gv_host, float* dv0, float* dx0, double* dpar) {
+        if (!forward_done) return fail(VFS_ERR_NOT_READY, "run the rollout forward first");
+        const uint32_t n = m->n;
+        cudaStream_t s = m->stream;
+        const unsigned g256 = (n + 255) / 256;
+        VFS_ADJ_TRY(cudaMemsetAsync(dparams, 0, 2 * sizeof(double), s));
+        // Seed: by-id gradients of the final state, placed in its (sorted) order.
+        for (int which = 0; which < 2; which++) {
+            const float* h = which == 0 ? gx_host : gv_host;
+            float4* dst = which == 0 ? xbar : vbar;
+            if (h) {
+                VFS_ADJ_TRY(cudaMemcpyAsync(host_io, h, (size_t)n * 12, cudaMemcpyHostToDevice, s));
+                k_adj_by_id<<<g256, 256, 0, s>>>(n, fin_pos, host_io, dst);
+            } else {
+                VFS_ADJ_TRY(cudaMemsetAsync(dst, 0, (size_t)n * sizeof(float4), s));
+            }
+        }
+        VFS_ADJ_TRY(cudaGetLastError());
+        for (int t0 = ((steps - 1) / every) * every; t0 >= 0; t0 -= every) {
+            const int len = t0 + every <= steps ? every : steps - t0;
+            int rc = record_segment(t0, len);
+            if (rc) return rc;
+            for (int t = len - 1; t >= 0; t--) {
+                rc = reverse_substep(t);
+                if (rc) return rc;
+            }
+        }
+        // xbar / vbar now hold the adjoint of the rollout's initial state, in its order.
+        if (dv0) {
+            k_to_id<<<g256, 256, 0, s>>>(n, ck_pos[0], vbar, host_io);
+            VFS_ADJ_TRY(cudaMemcpyAsync(dv0, host_io, (size_t)n * 12, cudaMemcpyDeviceToHost, s));
+        }
+        if (dx0) {
+            k_to_id<<<g256, 256, 0, s>>>(n, ck_pos[0], xbar, host_io);
+            VFS_ADJ_TRY(cudaMemcpyAsync(dx0, host_io, (size_t)n * 12, cudaMemcpyDeviceToHost, s));
+        }
+        double dp[2] = {0.0, 0.0};
+        VFS_ADJ_TRY(cudaMemcpyAsync(dp, dparams, sizeof(dp), cudaMemcpyDeviceToHost, s));
+        int rc = restore(fin_pos, fin_vel);  // leave the model at the end of the rollout
+        if (rc) return rc;
+        rc = m->check_device();
+        if (rc) {
+            uint32_t e = 0;
+            cudaMemcpy(&e, m->err, 4, cudaMemcpyDeviceToHost);
+            if (e & kErrAdjointOverflow)
+                return fail(VFS_ERR_CAPACITY, "a neighbour list exceeded 128 entries: the adjoint needs "
+                                              "complete lists");
+            return rc;
+        }
+        if (dpar) {
+            dpar[0] = dp[0];
+            dpar[1] = dp[1];
+        }
+        return VFS_OK;
+    }
+};
+
+}  // namespace vfs
+
+using vfs::fail;
+
+extern "C" {
+
+struct vfs_rollout {
+    vfs::Rollout r;
+};
+
+int vfs_rollout_create(vfs_model* model, int32_t steps, int32_t checkpoint_every,
+                       vfs_rollout** out) {
+    vfs::Model* m = vfs_model_impl(model);
+    if (!m || !out) return fail(VFS_ERR_INVALID_ARGUMENT, "NULL argument");
+    *out = nullptr;
+    if (steps < 1) return fail(VFS_ERR_INVALID_ARGUMENT, "steps must be >= 1");
+    vfs_rollout* h = new vfs_rollout();
+    const int rc = h->r.init(m, steps, checkpoint_every);
+    if (rc) {
+        delete h;
+        return rc;
+    }
+    *out = h;
+    return VFS_OK;
+}
+
+int vfs_rollout_destroy(vfs_rollout* r) {
+    delete r;
+    return VFS_OK;
+}
+
+int vfs_rollout_forward(vfs_rollout* r) {
+    if (!r) return fail(VFS_ERR_INVALID_ARGUMENT, "NULL rollout");
+    return r->r.forward();
+}
+
+int vfs_rollout_backward(vfs_rollout* r, const float* dl_dx_final, const float* dl_dv_final,
+                         float* dl_dv0, float* dl_dx0, double* dl_dparams) {
+    if (!r) return fail(VFS_ERR_INVALID_ARGUMENT, "NULL rollout");
+    return r->r.backward(dl_dx_final, dl_dv_final, dl_dv0, dl_dx0, dl_dparams);
+}
+
+}  // extern "C"

@@ -14,7 +14,7 @@ constexpr uint32_t kFlagAggregate = 1u << 30;
 constexpr uint32_t kFlagPrefix = 2u << 30;
 constexpr uint32_t kCountMask = (1u << 30) - 1u;
 constexpr uint32_t kMaxParticles = 1u << 30;
-constexpr uint32_t kNbrCap = 64;  // neighbour-list slots per particle (overflow falls back)
+constexpr uint32_t kNbrCap = 128;  // neighbour-list slots per particle (overflow falls back)
 
 // Error bits of the per-model device error word.
 constexpr uint32_t kErrLookbackTimeout = 1u;
