@@ -27,6 +27,7 @@ import statistics
 import subprocess
 import sys
 import time
+from dataclasses import replace
 from pathlib import Path
 
 import numpy as np
@@ -217,6 +218,53 @@ def time_batched(args, stream, torch):
                       "working set > L2"}
 
 
+def time_adjoint(args, stream, torch):
+    """Differentiable rollout (BASELINE config 4: 65,536 particles, 300 substeps, checkpoint every
+    25). The target is the rollout with viscosity 0.02, stiffness 60 and a smooth initial velocity
+    (8 Fourier modes, 0.5 m/s); the optimised run starts from viscosity 0.01, stiffness 50, zero
+    velocity; loss = MSE of final positions by id. Times the plain forward rollout against forward
+    + checkpointed adjoint (wall clock around synchronised C-ABI calls on the model's stream)."""
+    import vkfluidsim_gb300 as vfs
+    from vkfluidsim_gb300 import workloads as W
+    from vkfluidsim_gb300.adjoint import Rollout
+
+    base = W.dam_break_64k()
+    steps, every = base.steps, 25
+    tw = replace(base, vel=vfs.generate_fourier_velocity(base.pos, 8, 0.5, 4),
+                 wcsph=replace(base.wcsph, viscosity_strenght=0.02, stiffness=60.0))
+    tm = W.build_model(tw)
+    tm.set_stream(stream.cuda_stream)
+    tm.substeps(steps)
+    ts = tm.copy_data_buffers()
+    target = np.empty_like(ts["positions"])
+    target[tm.get_ids()] = ts["positions"]
+    del tm
+    m = W.build_model(base)
+    m.set_stream(stream.cuda_stream)
+    m.substeps(3)  # warm-up (graph capture)
+    m.set_particle_state(base.pos, base.vel)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    m.substeps(steps)
+    m.synchronize()
+    t_fwd = time.perf_counter() - t0
+    m.set_particle_state(base.pos, base.vel)
+    ro = Rollout(m, steps, every)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ro.forward()
+    xf = ro.final_positions_by_id()
+    g = ro.backward(2.0 * (xf - target) / xf.size)
+    t_all = time.perf_counter() - t0
+    return {"particles": base.n, "steps": steps, "checkpoint_every": every,
+            "forward_ms_per_step": 1e3 * t_fwd / steps,
+            "fwd_adjoint_ms_per_step": 1e3 * t_all / steps,
+            "cost_vs_forward": t_all / t_fwd,
+            "value": base.n * steps / t_all,
+            "loss": float(np.mean((xf - target) ** 2)),
+            "grads": {"dnu": g["dnu"], "dk": g["dk"], "dv0_max": float(np.abs(g["dv0"]).max())}}
+
+
 def run_gpu(args):
     import torch
 
@@ -323,6 +371,7 @@ def run_gpu(args):
     batched = None
     if args.batch_scenes > 0:
         batched = time_batched(args, stream, torch)
+    adjoint = time_adjoint(args, stream, torch) if args.adjoint else None
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -353,6 +402,8 @@ def run_gpu(args):
         }
         if batched:
             line["batched"] = batched
+        if adjoint:
+            line["fwd_adjoint"] = adjoint
         if cpu:
             line["cpu_baseline"] = cpu
         print(json.dumps(line), flush=True)
@@ -371,6 +422,7 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--batch-scenes", type=int, default=256)
+    ap.add_argument("--adjoint", type=int, default=1)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -35,10 +35,9 @@ __device__ __forceinline__ float3 operator+(float3 a, float3 b) { return make_fl
 __device__ __forceinline__ float3 operator-(float3 a, float3 b) { return make_float3(a.x - b.x, a.y - b.y, a.z - b.z); }
 __device__ __forceinline__ float3 operator*(float s, float3 a) { return make_float3(s * a.x, s * a.y, s * a.z); }
 
+// One 16-byte vector atomic (sm_90 and later) instead of three scalar ones.
 __device__ __forceinline__ void atomic_add3(float4* p, float3 v) {
-    atomicAdd(&p->x, v.x);
-    atomicAdd(&p->y, v.y);
-    atomicAdd(&p->z, v.z);
+    atomicAdd(p, make_float4(v.x, v.y, v.z, 0.0f));
 }
 
 // Shader kernel gradient gw(r) and its derivative d gw / dr (kernels_3d.slang:78-91).
@@ -193,9 +192,8 @@ struct AdjBuffers {
     float4* xbar;        // accumulates d L / d x' (sorted order)
     float4* vbar;        // accumulates d L / d v'
     float4* abar;        // d L / d a
-    float* pdbar;
+    float2* pmbar;       // (d L / d pd, d L / d mr)
     float* pbbar;
-    float* mrbar;
     float* rhobar;
     float4* gbar;        // d L / d G
     double* dparams;     // [d nu, d k]
@@ -212,13 +210,23 @@ __global__ void k_adj_integrate(SceneParams p, uint32_t n, const float4* __restr
     B.xbar[i] = make_float4(xo.x, xo.y, xo.z, 0.f);
     B.vbar[i] = make_float4(vx, vy, vz, 0.f);
     B.abar[i] = make_float4(p.dt * vx, p.dt * vy, p.dt * vz, 0.f);
-    B.pdbar[i] = 0.f;
-    B.mrbar[i] = 0.f;
+    B.pmbar[i] = make_float2(0.f, 0.f);
 }
 
+// Sums v over the block and adds it to *dst with one atomic (one address is shared by the whole
+// grid, so per-warp atomics would serialise). Every thread of the block must call it.
 __device__ __forceinline__ void block_add_double(double v, double* dst) {
+    __shared__ double s_part[32];
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    if ((threadIdx.x & 31) == 0 && v != 0.0) atomicAdd(dst, v);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) s_part[warp] = v;
+    __syncthreads();
+    if (warp == 0) {
+        const int nw = (blockDim.x + 31) >> 5;
+        double t = lane < nw ? s_part[lane] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+        if (lane == 0 && t != 0.0) atomicAdd(dst, t);
+    }
 }
 
 // Adjoint of the force pass: pressure, viscosity, boundary pressure and wall terms.
@@ -254,7 +262,6 @@ __global__ void __launch_bounds__(128) k_adj_force(SceneParams p, uint32_t n, Ad
             const float3 gxp = (-p.mass * alpha) * dfp;
             const float pbar = -p.mass * gw * cn;
             pdbar_i += pbar;
-            atomicAdd(&B.pdbar[j], pbar);
             // Viscosity: L-term = nus mr_j (v.x)(c.x) u(r), u = gw / (r (r^2 + eps)).
             const float3 v = vi - vj;
             const float den = r2 + p.visc_eps;
@@ -264,7 +271,7 @@ __global__ void __launch_bounds__(128) k_adj_force(SceneParams p, uint32_t n, Ad
             const float s = nus * aj.y;
             const float3 gxv = s * ((cx * u) * v + (vx * u) * c + (vx * cx * du) * nn);
             const float3 gvv = (s * cx * u) * x;
-            atomicAdd(&B.mrbar[j], nus * vx * cx * u);
+            atomicAdd(&B.pmbar[j], make_float2(pbar, nus * vx * cx * u));
             dnu += 10.0 * (double)aj.y * (double)vx * (double)cx * (double)u;
             const float3 gx = gxp + gxv;
             xbi = xbi + gx;
@@ -288,7 +295,7 @@ __global__ void __launch_bounds__(128) k_adj_force(SceneParams p, uint32_t n, Ad
         xbi = xbi + make_float3(wb[0], wb[1], wb[2]);
         atomic_add3(&B.xbar[i], xbi);
         atomic_add3(&B.vbar[i], vbi);
-        atomicAdd(&B.pdbar[i], pdbar_i);
+        atomicAdd(&B.pmbar[i], make_float2(pdbar_i, 0.0f));
     }
     block_add_double(dnu, &B.dparams[0]);
 }
@@ -304,7 +311,8 @@ __global__ void k_adj_eos(SceneParams p, uint32_t n, AdjBuffers B) {
         const float ratio = fmaxf(rho, p.rho0) / p.rho0;
         const float f = powf(ratio, p.expoent) - 1.0f;  // p = k f
         const float dp = rho > p.rho0 ? p.stiffness * p.expoent * powf(ratio, p.expoent - 1.0f) / p.rho0 : 0.0f;
-        const float pdb = B.pdbar[i], pbb = B.pbbar[i], mrb = B.mrbar[i];
+        const float2 pm = B.pmbar[i];
+        const float pdb = pm.x, pbb = B.pbbar[i], mrb = pm.y;
         float rb = 0.0f;
         if (rho > 0.0f) rb += pdb * (dp / (rho * rho) - 2.0f * pr / (rho * rho * rho));
         rb += pbb * dp / (p.rho0 * p.rho0);
@@ -395,12 +403,15 @@ struct Rollout {
     std::vector<float4*> s_pos, s_vel, s_aux, s_bnd;
     std::vector<uint32_t*> s_perm, s_nbr, s_cnt;
     float4 *xbar = nullptr, *vbar = nullptr, *xs = nullptr, *vs = nullptr, *abar = nullptr, *gbar = nullptr;
-    float *pdbar = nullptr, *pbbar = nullptr, *mrbar = nullptr, *rhobar = nullptr;
+    float2* pmbar = nullptr;
+    float *pbbar = nullptr, *rhobar = nullptr;
     float* host_io = nullptr;  // 3N floats on the device for host transfers
     double* dparams = nullptr;
     bool forward_done = false;
+    cudaGraphExec_t seg_graph = nullptr;  // recompute + reverse of one full segment
 
     ~Rollout() {
+        if (seg_graph) cudaGraphExecDestroy(seg_graph);
         for (auto* p : ck_pos) cudaFree(p);
         for (auto* p : ck_vel) cudaFree(p);
         for (auto* p : s_pos) cudaFree(p);
@@ -418,9 +429,8 @@ struct Rollout {
         cudaFree(vs);
         cudaFree(abar);
         cudaFree(gbar);
-        cudaFree(pdbar);
+        cudaFree(pmbar);
         cudaFree(pbbar);
-        cudaFree(mrbar);
         cudaFree(rhobar);
         cudaFree(host_io);
         cudaFree(dparams);
@@ -457,7 +467,8 @@ struct Rollout {
         }
         for (float4** b : {&fin_pos, &fin_vel, &xbar, &vbar, &xs, &vs, &abar, &gbar})
             VFS_ADJ_TRY(cudaMalloc(b, N * sizeof(float4)));
-        for (float** b : {&pdbar, &pbbar, &mrbar, &rhobar}) VFS_ADJ_TRY(cudaMalloc(b, N * 4));
+        for (float** b : {&pbbar, &rhobar}) VFS_ADJ_TRY(cudaMalloc(b, N * 4));
+        VFS_ADJ_TRY(cudaMalloc(&pmbar, N * sizeof(float2)));
         VFS_ADJ_TRY(cudaMalloc(&host_io, N * 12));
         VFS_ADJ_TRY(cudaMalloc(&dparams, 2 * sizeof(double)));
         return VFS_OK;
@@ -491,25 +502,69 @@ struct Rollout {
         return m->check_device();
     }
 
-    // Recomputes substeps [t0, t0 + len) from checkpoint t0 / every, keeping each substep's
-    // sorted inputs, permutation, density products and neighbour lists.
-    int record_segment(int t0, int len) {
-        int rc = restore(ck_pos[t0 / every], ck_vel[t0 / every]);
-        if (rc) return rc;
-        const size_t N = m->n;
+    // Recomputes `len` substeps from the state in the model, keeping each substep's sorted inputs,
+    // permutation, density products and neighbour lists: the model's buffers for those are pointed
+    // at the segment's per-substep records, so the passes write them in place.
+    int record_segment(int len) {
+        float4* own_aux = m->aux;
+        float4* own_bnd = m->bnd;
+        uint32_t* own_nbr = m->nbr;
+        uint32_t* own_cnt = m->nbr_count;
         const int o = 1 - m->cur;
-        for (int t = 0; t < len; t++) {
+        float4* own_pos = m->pos[o];
+        float4* own_vel = m->vel[o];
+        int rc = VFS_OK;
+        for (int t = 0; t < len && rc == VFS_OK; t++) {
+            m->aux = s_aux[t];
+            m->bnd = s_bnd[t];
+            m->nbr = s_nbr[t];
+            m->nbr_count = s_cnt[t];
+            m->pos[o] = s_pos[t];
+            m->vel[o] = s_vel[t];
             rc = m->enqueue_substep(nullptr);
-            if (rc) return rc;
-            cudaStream_t s = m->stream;
-            VFS_ADJ_TRY(cudaMemcpyAsync(s_pos[t], m->pos[o], N * 16, cudaMemcpyDeviceToDevice, s));
-            VFS_ADJ_TRY(cudaMemcpyAsync(s_vel[t], m->vel[o], N * 16, cudaMemcpyDeviceToDevice, s));
-            VFS_ADJ_TRY(cudaMemcpyAsync(s_aux[t], m->aux, N * 16, cudaMemcpyDeviceToDevice, s));
-            VFS_ADJ_TRY(cudaMemcpyAsync(s_bnd[t], m->bnd, N * 16, cudaMemcpyDeviceToDevice, s));
-            VFS_ADJ_TRY(cudaMemcpyAsync(s_perm[t], m->sperm, N * 4, cudaMemcpyDeviceToDevice, s));
-            VFS_ADJ_TRY(cudaMemcpyAsync(s_nbr[t], m->nbr, N * kNbrCap * 4, cudaMemcpyDeviceToDevice, s));
-            VFS_ADJ_TRY(cudaMemcpyAsync(s_cnt[t], m->nbr_count, N * 4, cudaMemcpyDeviceToDevice, s));
+            if (rc == VFS_OK) {
+                const cudaError_t e = cudaMemcpyAsync(s_perm[t], m->sperm, (size_t)m->n * 4,
+                                                      cudaMemcpyDeviceToDevice, m->stream);
+                if (e != cudaSuccess) rc = fail(VFS_ERR_CUDA, cudaGetErrorString(e));
+            }
         }
+        m->aux = own_aux;
+        m->bnd = own_bnd;
+        m->nbr = own_nbr;
+        m->nbr_count = own_cnt;
+        m->pos[o] = own_pos;
+        m->vel[o] = own_vel;
+        return rc;
+    }
+
+    // Recompute + reverse of one segment of `len` substeps whose input state is in the model.
+    int segment_body(int len) {
+        int rc = record_segment(len);
+        for (int t = len - 1; t >= 0 && rc == VFS_OK; t--) rc = reverse_substep(t);
+        return rc;
+    }
+
+    // Full segments replay one captured graph; a shorter last segment runs without one.
+    int run_segment(int len) {
+        if (len != every) return segment_body(len);
+        if (!seg_graph) {
+            cudaGraph_t g = nullptr;
+            VFS_ADJ_TRY(cudaStreamBeginCapture(m->stream, cudaStreamCaptureModeThreadLocal));
+            const int rc = segment_body(len);
+            const cudaError_t e = cudaStreamEndCapture(m->stream, &g);
+            if (rc) {
+                if (g) cudaGraphDestroy(g);
+                return rc;
+            }
+            if (e != cudaSuccess) return fail(VFS_ERR_CUDA, std::string("segment capture: ") + cudaGetErrorString(e));
+            const cudaError_t ei = cudaGraphInstantiate(&seg_graph, g, 0);
+            cudaGraphDestroy(g);
+            if (ei != cudaSuccess) {
+                seg_graph = nullptr;
+                return fail(VFS_ERR_CUDA, std::string("segment graph: ") + cudaGetErrorString(ei));
+            }
+        }
+        VFS_ADJ_TRY(cudaGraphLaunch(seg_graph, m->stream));
         return VFS_OK;
     }
 
@@ -529,9 +584,8 @@ struct Rollout {
         B.xbar = xs;
         B.vbar = vs;
         B.abar = abar;
-        B.pdbar = pdbar;
+        B.pmbar = pmbar;
         B.pbbar = pbbar;
-        B.mrbar = mrbar;
         B.rhobar = rhobar;
         B.gbar = gbar;
         B.dparams = dparams;
@@ -566,12 +620,10 @@ struct Rollout {
         VFS_ADJ_TRY(cudaGetLastError());
         for (int t0 = ((steps - 1) / every) * every; t0 >= 0; t0 -= every) {
             const int len = t0 + every <= steps ? every : steps - t0;
-            int rc = record_segment(t0, len);
+            int rc = restore(ck_pos[t0 / every], ck_vel[t0 / every]);
             if (rc) return rc;
-            for (int t = len - 1; t >= 0; t--) {
-                rc = reverse_substep(t);
-                if (rc) return rc;
-            }
+            rc = run_segment(len);
+            if (rc) return rc;
         }
         // xbar / vbar now hold the adjoint of the rollout's initial state, in its order.
         if (dv0) {
