@@ -30,6 +30,39 @@ def target(w):
     return (w.pos + 0.01 * np.sin(7.0 * w.pos[:, [1, 2, 0]])).astype(np.float64)
 
 
+def straddling_scene():
+    """Scene A's lattice moved to x in [0.85, 1.19] inside a 2 x 1 x 1 container: cells 24..26 on
+    x have neighbour cells in two 50^3 hash blocks, so particles with and without distinct neighbour
+    keys interact (both the gathered and the scattered adjoint pair terms run)."""
+    w = W.dam_break(dims=(18, 18, 18), spacing=0.019, box=(2.0, 1.0, 1.0), map_res=24,
+                    stiffness=20.0, viscosity=0.02, seed=7, dt=1e-4)
+    w.sim = replace(w.sim, smooth_radius=0.04)
+    w.pos = (w.pos + np.array([0.85, 0.0, 0.0], np.float32)).astype(np.float32)
+    w.vel = vfs.generate_fourier_velocity(w.pos, 8, 0.5, 11)
+    return w
+
+
+def small_scene():
+    """1,440 particles (12 x 12 x 10): N <= 5102, so neighbour keys may collide everywhere and
+    every adjoint pair term is scattered."""
+    w = W.dam_break(dims=(12, 12, 10), spacing=0.019, map_res=24, stiffness=20.0,
+                    viscosity=0.02, seed=5, dt=1e-4)
+    w.sim = replace(w.sim, smooth_radius=0.04)
+    w.vel = vfs.generate_fourier_velocity(w.pos, 8, 0.5, 13)
+    return w
+
+
+SCENES = {"one_block": scene, "straddling": straddling_scene, "small": small_scene}
+
+
+def distinct_key_mask(w):
+    """Per particle: are its 27 neighbour-cell keys certainly distinct (N > 5102 and all 27 cells
+    in one 50^3 hash block, the condition the GPU kernels test)?"""
+    c = np.floor(w.pos.astype(np.float64) / float(np.float32(w.sim.smooth_radius))).astype(np.int64)
+    same = (((c + 24) // 50) == ((c + 26) // 50)).all(axis=1)
+    return same & (w.n > 5102)
+
+
 def cpu_objects(w):
     """The scene's boundary objects with grids from the oracle's CPU volume-map generator."""
     from oracle import binding as ob

@@ -55,3 +55,11 @@ def test_torch_autograd_matches_fp64_finite_differences(setup):
     assert abs(float(nu.grad) - float(fd_nu)) <= 1e-5 * abs(float(fd_nu))
     assert abs(float(k.grad) - float(fd_k)) <= 1e-5 * abs(float(fd_k))
     assert abs(float((vv.grad * delta).sum()) - float(fd_dir)) <= 1e-5 * abs(float(fd_dir))
+
+
+def test_adjoint_scenes_cover_both_pair_rules():
+    """The GPU adjoint tests' scenes: all keys distinct, mixed, none distinct."""
+    frac = {k: float(S.distinct_key_mask(f()).mean()) for k, f in S.SCENES.items()}
+    assert frac["one_block"] == 1.0
+    assert 0.2 < frac["straddling"] < 0.9
+    assert frac["small"] == 0.0

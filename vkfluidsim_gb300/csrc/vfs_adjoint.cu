@@ -28,6 +28,7 @@ namespace vfs {
 namespace {
 
 constexpr uint32_t kErrAdjointOverflow = 2u;  // a neighbour list longer than its capacity
+constexpr int kAdjLanes = 4;                     // lanes sharing one particle's neighbour list
 
 __device__ __forceinline__ float3 f3(const float4& a) { return make_float3(a.x, a.y, a.z); }
 __device__ __forceinline__ float dot3(float3 a, float3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
@@ -229,125 +230,181 @@ __device__ __forceinline__ void block_add_double(double v, double* dst) {
     }
 }
 
+// Sums v over the kLanes lanes of a particle group (consecutive lanes of one warp). Every lane of
+// the warp must call it.
+template <int kLanes>
+__device__ __forceinline__ float group_sum(float v) {
+#pragma unroll
+    for (int o = kLanes / 2; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+template <int kLanes>
+__device__ __forceinline__ float3 group_sum3(float3 v) {
+    return make_float3(group_sum<kLanes>(v.x), group_sum<kLanes>(v.y), group_sum<kLanes>(v.z));
+}
+
 // Adjoint of the force pass: pressure, viscosity, boundary pressure and wall terms.
+//
+// Pair (j, i) of j's force, with x = x_j - x_i, v = v_j - v_i, n = x / r, c_j = d L / d a_j:
+//   pressure  L-term -m (pd_j + pd_i) gw(r) (c_j . n)
+//   viscosity L-term  s_i (v . x)(c_j . x) u(r),  s_i = 10 nu mr_i,  u = gw / (r (r^2 + eps)).
+// Both are linear in c_j, and pair (i, j) of i's force is the same expression with c_i, s_j and
+// (x, v) negated. Particle j's list is split over kLanes lanes. When i and j both have distinct
+// neighbour keys and adjacent cells, each lists the other exactly once, so j also gathers the part
+// of pair (i, j) that falls on j, which is the own-pair expression evaluated at c_j - c_i (pressure)
+// and s_i c_j - s_j c_i (viscosity). Otherwise i's part is left to i, which scatters its own
+// pair's reverse to j with atomics (c_i counted as zero here).
+template <int kLanes>
 __global__ void __launch_bounds__(128) k_adj_force(SceneParams p, uint32_t n, AdjBuffers B) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    double dnu = 0.0;
-    if (i < n) {
-        const float3 xi = f3(B.pos[i]), vi = f3(B.vel[i]);
-        const float4 ai = B.aux[i];
-        const float3 c = f3(B.abar[i]);
-        const float pdi = ai.x, pbi = ai.w;
-        float3 xbi = make_float3(0.f, 0.f, 0.f), vbi = make_float3(0.f, 0.f, 0.f);
-        float pdbar_i = 0.f;
-        const uint32_t cnt = B.nbr_count[i];
-        if (cnt > p.nbr_cap) atomicOr(B.err, kErrAdjointOverflow);
-        const uint32_t listed = min(cnt, p.nbr_cap);
-        const float nus = p.visc_scale;
-        for (uint32_t k = 0; k < listed; k++) {
-            const uint32_t j = B.nbr[(size_t)k * n + i];
-            const float3 xj = f3(B.pos[j]), vj = f3(B.vel[j]);
-            const float2 aj = *reinterpret_cast<const float2*>(B.aux + j);  // (pd_j, mr_j)
-            const float3 x = xi - xj;
+    const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t j = (uint32_t)(t / kLanes), lane = (uint32_t)(t % kLanes);
+    float3 xb = make_float3(0.f, 0.f, 0.f), vb = make_float3(0.f, 0.f, 0.f);
+    float pdb = 0.f, mrb = 0.f, dnu_f = 0.f;
+    float3 xj = xb, cj = xb;
+    float pdj = 0.f, pbj = 0.f;
+    if (j < n) {
+        xj = f3(B.pos[j]);
+        const float3 vj = f3(B.vel[j]);
+        const float4 aj = B.aux[j];
+        cj = f3(B.abar[j]);
+        pdj = aj.x;
+        pbj = aj.w;
+        const float s_j = p.visc_scale * aj.y;
+        const uint32_t cnt = B.nbr_count[j];
+        const bool dj = (cnt & kNbrDistinct) != 0u;
+        if (lane == 0 && (cnt & kNbrCountMask) > p.nbr_cap) atomicOr(B.err, kErrAdjointOverflow);
+        const uint32_t listed = min(cnt & kNbrCountMask, p.nbr_cap);
+        for (uint32_t k = lane; k < listed; k += kLanes) {
+            const uint32_t i = B.nbr[(size_t)k * n + j];
+            const float3 x = xj - f3(B.pos[i]);
             const float r2 = dot3(x, x);
-            const float r = sqrtf(r2);
-            if (!(r > 1e-9f)) continue;
+            if (!(r2 > 1e-18f)) continue;
+            const float inv_r = rsqrtf(r2);
+            const float r = r2 * inv_r;
+            const float3 v = vj - f3(B.vel[i]);
+            const float2 ai = *reinterpret_cast<const float2*>(B.aux + i);  // (pd_i, mr_i)
+            const uint32_t ci_word = B.nbr_count[i];
+            const bool gather = dj && (ci_word & kNbrDistinct) != 0u && nbr_cells_adjacent(cnt, ci_word);
+            const float3 ci = gather ? f3(B.abar[i]) : make_float3(0.f, 0.f, 0.f);
             float gw, dgw;
             gw_and_deriv(p, r, gw, dgw);
-            const float3 nn = (1.0f / r) * x;
-            const float cn = dot3(c, nn);
-            // Pressure: L-term = -m (pd_i + pd_j) gw (c . n).
-            const float alpha = pdi + aj.x;
-            const float3 dfp = (dgw * cn) * nn + (gw / r) * (c - cn * nn);
-            const float3 gxp = (-p.mass * alpha) * dfp;
-            const float pbar = -p.mass * gw * cn;
-            pdbar_i += pbar;
-            // Viscosity: L-term = nus mr_j (v.x)(c.x) u(r), u = gw / (r (r^2 + eps)).
-            const float3 v = vi - vj;
-            const float den = r2 + p.visc_eps;
-            const float u = gw / (r * den);
-            const float du = (dgw * r * den - gw * (3.0f * r2 + p.visc_eps)) / (r * r * den * den);
-            const float vx = dot3(v, x), cx = dot3(c, x);
-            const float s = nus * aj.y;
-            const float3 gxv = s * ((cx * u) * v + (vx * u) * c + (vx * cx * du) * nn);
-            const float3 gvv = (s * cx * u) * x;
-            atomicAdd(&B.pmbar[j], make_float2(pbar, nus * vx * cx * u));
-            dnu += 10.0 * (double)aj.y * (double)vx * (double)cx * (double)u;
-            const float3 gx = gxp + gxv;
-            xbi = xbi + gx;
-            vbi = vbi + gvv;
-            atomic_add3(&B.xbar[j], -1.0f * gx);
-            atomic_add3(&B.vbar[j], -1.0f * gvv);
+            const float inv_den = 1.0f / (r2 + p.visc_eps);
+            const float u = gw * inv_r * inv_den;
+            const float du = (dgw * r - gw * (3.0f * r2 + p.visc_eps) * inv_den) * inv_r * inv_r * inv_den;
+            const float s_i = p.visc_scale * ai.y;
+            const float3 nn = inv_r * x;
+            const float3 dc = cj - ci;
+            const float3 cv = s_i * cj - s_j * ci;
+            const float dcn = dot3(dc, nn), cvx = dot3(cv, x), vx = dot3(v, x), cjx = dot3(cj, x);
+            const float3 dx = (-p.mass * (pdj + ai.x)) * ((dgw * dcn) * nn + (gw * inv_r) * (dc - dcn * nn)) +
+                              (cvx * u) * v + (vx * u) * cv + (vx * cvx * du) * nn;
+            const float3 dv = (cvx * u) * x;
+            const float dp = -p.mass * gw * dcn;
+            xb = xb + dx;
+            vb = vb + dv;
+            pdb += dp;
+            dnu_f += ai.y * vx * cjx * u;
+            if (gather) {
+                mrb -= p.visc_scale * vx * dot3(ci, x) * u;
+            } else {
+                atomic_add3(&B.xbar[i], -1.0f * dx);
+                atomic_add3(&B.vbar[i], -1.0f * dv);
+                atomicAdd(&B.pmbar[i], make_float2(dp, p.visc_scale * vx * cjx * u));
+            }
         }
-        // Boundary pressure: L-term = -(pd_i + pb_i) rho0 (c . G_i).
-        const float3 G = f3(B.bnd[i]);
-        const float cg = dot3(c, G);
-        pdbar_i += -p.rho0 * cg;
-        B.pbbar[i] = -p.rho0 * cg;
-        const float sg = -(pdi + pbi) * p.rho0;
-        B.gbar[i] = make_float4(sg * c.x, sg * c.y, sg * c.z, 0.f);
+    }
+    xb = group_sum3<kLanes>(xb);
+    vb = group_sum3<kLanes>(vb);
+    pdb = group_sum<kLanes>(pdb);
+    mrb = group_sum<kLanes>(mrb);
+    if (j < n && lane == 0) {
+        // Boundary pressure: L-term = -(pd_j + pb_j) rho0 (c . G_j).
+        const float3 G = f3(B.bnd[j]);
+        const float cg = dot3(cj, G);
+        pdb += -p.rho0 * cg;
+        B.pbbar[j] = -p.rho0 * cg;
+        const float sg = -(pdj + pbj) * p.rho0;
+        B.gbar[j] = make_float4(sg * cj.x, sg * cj.y, sg * cj.z, 0.f);
         // Wall penalty: a -= k_w diff(x), d diff / dx = 1 outside [lo, hi].
-        const float xs[3] = {xi.x, xi.y, xi.z};
-        const float cs[3] = {c.x, c.y, c.z};
+        const float xs[3] = {xj.x, xj.y, xj.z};
+        const float cs[3] = {cj.x, cj.y, cj.z};
         float wb[3];
         for (int a = 0; a < 3; a++)
             wb[a] = (xs[a] < p.lo[a] || xs[a] > p.hi[a]) ? -p.wall_k * cs[a] : 0.0f;
-        xbi = xbi + make_float3(wb[0], wb[1], wb[2]);
-        atomic_add3(&B.xbar[i], xbi);
-        atomic_add3(&B.vbar[i], vbi);
-        atomicAdd(&B.pmbar[i], make_float2(pdbar_i, 0.0f));
+        xb = xb + make_float3(wb[0], wb[1], wb[2]);
+        atomic_add3(&B.xbar[j], xb);
+        atomic_add3(&B.vbar[j], vb);
+        atomicAdd(&B.pmbar[j], make_float2(pdb, mrb));
     }
-    block_add_double(dnu, &B.dparams[0]);
+    block_add_double(10.0 * (double)dnu_f, &B.dparams[0]);
 }
 
 // Adjoint of the EOS epilogue: rho_bar from pd_bar, pb_bar, mr_bar; d L / d k.
 __global__ void k_adj_eos(SceneParams p, uint32_t n, AdjBuffers B) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    double dk = 0.0;
+    float dk = 0.0f;
     if (i < n) {
         const float4 ai = B.aux[i];
         const float rho = ai.z;
-        const float pr = rho > 0.0f ? ai.x * rho * rho : 0.0f;  // p = pd rho^2
-        const float ratio = fmaxf(rho, p.rho0) / p.rho0;
-        const float f = powf(ratio, p.expoent) - 1.0f;  // p = k f
-        const float dp = rho > p.rho0 ? p.stiffness * p.expoent * powf(ratio, p.expoent - 1.0f) / p.rho0 : 0.0f;
+        const float inv_rho0 = 1.0f / p.rho0;
+        const float ratio = fmaxf(rho, p.rho0) * inv_rho0;
+        const float pw = powf(ratio, p.expoent);  // ratio^gamma
+        const float f = pw - 1.0f;                // p = k f
+        const float pr = p.stiffness * f;
+        const float dp = rho > p.rho0 ? p.stiffness * p.expoent * pw / fmaxf(rho, p.rho0) : 0.0f;
         const float2 pm = B.pmbar[i];
         const float pdb = pm.x, pbb = B.pbbar[i], mrb = pm.y;
-        float rb = 0.0f;
-        if (rho > 0.0f) rb += pdb * (dp / (rho * rho) - 2.0f * pr / (rho * rho * rho));
-        rb += pbb * dp / (p.rho0 * p.rho0);
-        if (rho > 1e-6f) rb += mrb * (-p.mass / (rho * rho));
+        const float inv_rho = rho > 0.0f ? 1.0f / rho : 0.0f;
+        float rb = pdb * (dp - 2.0f * pr * inv_rho) * inv_rho * inv_rho;
+        rb += pbb * dp * inv_rho0 * inv_rho0;
+        if (rho > 1e-6f) rb -= mrb * p.mass * inv_rho * inv_rho;
         B.rhobar[i] = rb;
-        if (rho > 0.0f) dk += (double)pdb * (double)f / ((double)rho * (double)rho);
-        dk += (double)pbb * (double)f / ((double)p.rho0 * (double)p.rho0);
+        dk = (pdb * inv_rho * inv_rho + pbb * inv_rho0 * inv_rho0) * f;
     }
-    block_add_double(dk, &B.dparams[1]);
+    block_add_double((double)dk, &B.dparams[1]);
 }
 
-// Adjoint of the density sum and of the volume-map terms.
+// Adjoint of the density sum and of the volume-map terms, the list split over kLanes lanes as in
+// k_adj_force; the reverse half of each pair is gathered or scattered under the same rule.
+template <int kLanes>
 __global__ void __launch_bounds__(128) k_adj_density(SceneParams p, uint32_t n, AdjBuffers B) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const float3 xi = f3(B.pos[i]);
-    const float rb = B.rhobar[i];
-    float3 xbi = make_float3(0.f, 0.f, 0.f);
-    const uint32_t listed = min(B.nbr_count[i], p.nbr_cap);
-    if (rb != 0.0f) {
-        for (uint32_t k = 0; k < listed; k++) {
-            const uint32_t j = B.nbr[(size_t)k * n + i];
-            const float3 x = xi - f3(B.pos[j]);
-            const float r = sqrtf(dot3(x, x));
-            if (!(r > 1e-9f)) continue;
-            const float3 g = (rb * p.mass * dW_dr(p, r) / r) * x;
-            xbi = xbi + g;
-            atomic_add3(&B.xbar[j], -1.0f * g);
+    const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t j = (uint32_t)(t / kLanes), lane = (uint32_t)(t % kLanes);
+    float3 xb = make_float3(0.f, 0.f, 0.f), xj = xb;
+    float rbj = 0.0f;
+    if (j < n) {
+        xj = f3(B.pos[j]);
+        rbj = B.rhobar[j];
+        const uint32_t cnt = B.nbr_count[j];
+        const bool dj = (cnt & kNbrDistinct) != 0u;
+        const uint32_t listed = min(cnt & kNbrCountMask, p.nbr_cap);
+        for (uint32_t k = lane; k < listed; k += kLanes) {
+            const uint32_t i = B.nbr[(size_t)k * n + j];
+            const float3 x = xj - f3(B.pos[i]);
+            const float r2 = dot3(x, x);
+            if (!(r2 > 1e-18f)) continue;
+            const float inv_r = rsqrtf(r2);
+            const float w = p.mass * dW_dr(p, r2 * inv_r) * inv_r;
+            const uint32_t ci_word = B.nbr_count[i];
+            const bool gather = dj && (ci_word & kNbrDistinct) != 0u && nbr_cells_adjacent(cnt, ci_word);
+            // Own pair: d rho_j / d x_j = m W'(r) n, d rho_j / d x_i = -m W'(r) n.
+            if (gather)
+                xb = xb + ((rbj + B.rhobar[i]) * w) * x;  // with i's pair (i, j): d rho_i / d x_j
+            else {
+                xb = xb + (rbj * w) * x;
+                if (rbj != 0.0f) atomic_add3(&B.xbar[i], (-rbj * w) * x);
+            }
         }
     }
-    const float4 gb = B.gbar[i];
-    const float psib = rb * p.rho0;
-    if (p.n_objects && (psib != 0.0f || gb.x != 0.0f || gb.y != 0.0f || gb.z != 0.0f))
-        xbi = xbi + boundary_adjoint(p, xi, psib, f3(gb));
-    atomic_add3(&B.xbar[i], xbi);
+    xb = group_sum3<kLanes>(xb);
+    if (j < n && lane == 0) {
+        const float4 gb = B.gbar[j];
+        const float psib = rbj * p.rho0;
+        if (p.n_objects && (psib != 0.0f || gb.x != 0.0f || gb.y != 0.0f || gb.z != 0.0f))
+            xb = xb + boundary_adjoint(p, xj, psib, f3(gb));
+        atomic_add3(&B.xbar[j], xb);
+    }
 }
 
 // Back through the reorder x' = x[perm]: scatter into the previous order.
@@ -408,6 +465,7 @@ struct Rollout {
     float* host_io = nullptr;  // 3N floats on the device for host transfers
     double* dparams = nullptr;
     bool forward_done = false;
+    bool last_recorded = false;  // the segment records hold the last segment (set by forward)
     cudaGraphExec_t seg_graph = nullptr;  // recompute + reverse of one full segment
 
     ~Rollout() {
@@ -487,8 +545,16 @@ struct Rollout {
         return VFS_OK;
     }
 
+    // First substep of the last segment, and its length.
+    int last_t0() const { return ((steps - 1) / every) * every; }
+    int last_len() const { return steps - last_t0(); }
+
+    // Runs the rollout from the model's state, saving a checkpoint every `every` substeps. The last
+    // segment is recorded as it runs, so the adjoint starts without recomputing it.
     int forward() {
-        for (int t = 0; t < steps; t++) {
+        forward_done = false;
+        const int t_last = last_t0();
+        for (int t = 0; t < t_last; t++) {
             if (t % every == 0) {
                 const int rc = save(ck_pos[t / every], ck_vel[t / every]);
                 if (rc) return rc;
@@ -496,10 +562,15 @@ struct Rollout {
             const int rc = m->run_substeps(1);
             if (rc) return rc;
         }
-        const int rc = save(fin_pos, fin_vel);
+        int rc = save(ck_pos[t_last / every], ck_vel[t_last / every]);
+        if (rc == VFS_OK) rc = record_segment(last_len());
+        if (rc == VFS_OK) rc = save(fin_pos, fin_vel);
+        if (rc) return rc;
+        rc = m->check_device();
         if (rc) return rc;
         forward_done = true;
-        return m->check_device();
+        last_recorded = true;
+        return VFS_OK;
     }
 
     // Recomputes `len` substeps from the state in the model, keeping each substep's sorted inputs,
@@ -590,11 +661,12 @@ struct Rollout {
         B.gbar = gbar;
         B.dparams = dparams;
         B.err = m->err;
-        const unsigned g256 = (n + 255) / 256, g128 = (n + 127) / 128;
+        const unsigned g256 = (n + 255) / 256;
         k_adj_integrate<<<g256, 256, 0, s>>>(p, n, xbar, vbar, B);
-        k_adj_force<<<g128, 128, 0, s>>>(p, n, B);
+        const unsigned gl = (unsigned)(((size_t)n * kAdjLanes + 127) / 128);
+        k_adj_force<kAdjLanes><<<gl, 128, 0, s>>>(p, n, B);
         k_adj_eos<<<g256, 256, 0, s>>>(p, n, B);
-        k_adj_density<<<g128, 128, 0, s>>>(p, n, B);
+        k_adj_density<kAdjLanes><<<gl, 128, 0, s>>>(p, n, B);
         k_adj_unsort<<<g256, 256, 0, s>>>(n, s_perm[t], xs, vs, xbar, vbar);
         VFS_ADJ_TRY(cudaGetLastError());
         return VFS_OK;
@@ -618,13 +690,18 @@ struct Rollout {
             }
         }
         VFS_ADJ_TRY(cudaGetLastError());
-        for (int t0 = ((steps - 1) / every) * every; t0 >= 0; t0 -= every) {
+        for (int t0 = last_t0(); t0 >= 0; t0 -= every) {
             const int len = t0 + every <= steps ? every : steps - t0;
-            int rc = restore(ck_pos[t0 / every], ck_vel[t0 / every]);
-            if (rc) return rc;
-            rc = run_segment(len);
+            int rc = VFS_OK;
+            if (t0 == last_t0() && last_recorded) {
+                for (int t = len - 1; t >= 0 && rc == VFS_OK; t--) rc = reverse_substep(t);
+            } else {
+                rc = restore(ck_pos[t0 / every], ck_vel[t0 / every]);
+                if (rc == VFS_OK) rc = run_segment(len);
+            }
             if (rc) return rc;
         }
+        last_recorded = false;  // the records now hold the first segment
         // xbar / vbar now hold the adjoint of the rollout's initial state, in its order.
         if (dv0) {
             k_to_id<<<g256, 256, 0, s>>>(n, ck_pos[0], vbar, host_io);

@@ -15,6 +15,28 @@ constexpr uint32_t kFlagPrefix = 2u << 30;
 constexpr uint32_t kCountMask = (1u << 30) - 1u;
 constexpr uint32_t kMaxParticles = 1u << 30;
 constexpr uint32_t kNbrCap = 128;  // neighbour-list slots per particle (overflow falls back)
+// nbr_count[i] holds the list length in its low 25 bits, particle i's cell coordinates mod 4 in
+// bits 25-26 (x), 27-28 (y), 29-30 (z), and in the top bit whether its 27 neighbour cells have 27
+// distinct keys (then every in-range neighbour appears once in its list).
+constexpr uint32_t kNbrDistinct = 0x80000000u;
+constexpr uint32_t kNbrCountMask = 0x01FFFFFFu;
+constexpr uint32_t kNbrCellShift = 25;
+
+__host__ __device__ inline uint32_t nbr_word(uint32_t listed, uint32_t cx, uint32_t cy, uint32_t cz,
+                                             bool distinct) {
+    return (listed < kNbrCountMask ? listed : kNbrCountMask) | ((cx & 3u) << kNbrCellShift) |
+           ((cy & 3u) << (kNbrCellShift + 2)) | ((cz & 3u) << (kNbrCellShift + 4)) |
+           (distinct ? kNbrDistinct : 0u);
+}
+
+// For two particles within h of each other (cells at most 2 apart per axis): are their cells
+// adjacent (at most 1 apart on every axis)? Decided from the cell residues of their words.
+__host__ __device__ inline bool nbr_cells_adjacent(uint32_t a, uint32_t b) {
+    bool adj = true;
+    for (uint32_t s = kNbrCellShift; s < kNbrCellShift + 6; s += 2)
+        adj = adj && (((a >> s) - (b >> s)) & 3u) != 2u;
+    return adj;
+}
 
 // Error bits of the per-model device error word.
 constexpr uint32_t kErrLookbackTimeout = 1u;

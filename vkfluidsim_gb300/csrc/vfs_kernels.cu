@@ -514,6 +514,16 @@ __device__ __forceinline__ float face_dist2(uint32_t d, float f) {
 // skipped. The 2e-3 margin keeps the float cell fractions conservative.
 constexpr float kPruneLimit = 1.002f;
 
+// True when the 27 neighbour cells of (cx, cy, cz) provably have 27 distinct keys (see above).
+__device__ __forceinline__ bool distinct_keys(const SceneParams& p, uint32_t cx, uint32_t cy,
+                                              uint32_t cz) {
+    const uint32_t h_lo = hash_cell(cx - 1u, cy - 1u, cz - 1u);
+    const uint32_t h_hi = hash_cell(cx + 1u, cy + 1u, cz + 1u);
+    return p.n > 5102u && (cx + 24u) / 50u == (cx + 26u) / 50u &&
+           (cy + 24u) / 50u == (cy + 26u) / 50u && (cz + 24u) / 50u == (cz + 26u) / 50u &&
+           h_hi >= h_lo;
+}
+
 // Walks the candidates of the 27 neighbour buckets of cell (cx, cy, cz) in the reference's order
 // and calls visit(j, q) for each, with q = pos[j]; four positions are fetched per iteration and
 // batch_end() runs after each group of at most four (where a full list is drained).
@@ -524,11 +534,7 @@ __device__ __forceinline__ void for_each_candidate(const SceneParams& p,
                                                    const float4& xi, uint32_t cx, uint32_t cy,
                                                    uint32_t cz, Visit&& visit,
                                                    BatchEnd&& batch_end) {
-    const uint32_t h_lo = hash_cell(cx - 1u, cy - 1u, cz - 1u);
-    const uint32_t h_hi = hash_cell(cx + 1u, cy + 1u, cz + 1u);
-    const bool interior = p.n > 5102u && (cx + 24u) / 50u == (cx + 26u) / 50u &&
-                          (cy + 24u) / 50u == (cy + 26u) / 50u &&
-                          (cz + 24u) / 50u == (cz + 26u) / 50u && h_hi >= h_lo;
+    const bool interior = distinct_keys(p, cx, cy, cz);
     const float lim = interior ? kPruneLimit : 1e30f;
     const float fx = fmaf(-(float)(int)cx, p.h, xi.x) * p.inv_h;
     const float fy = fmaf(-(float)(int)cy, p.h, xi.y) * p.inv_h;
@@ -635,7 +641,7 @@ __global__ void __launch_bounds__(kNbrBlock, 6)
         if (cnt > kDrainAt) drain();
     });
     drain();
-    nbr_count[i] = listed;
+    nbr_count[i] = nbr_word(listed, cx, cy, cz, distinct_keys(p, cx, cy, cz));
     float bd, bgx, bgy, bgz;
     boundary_terms(p, xi.x, xi.y, xi.z, bd, bgx, bgy, bgz);
     rho += p.rho0 * bd;
@@ -723,7 +729,7 @@ __global__ void __launch_bounds__(kNbrBlock, 6)
     const float pdi = ai.x;
 
     ForceAcc f{0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
-    const uint32_t listed = nbr_count[i];
+    const uint32_t listed = nbr_count[i] & kNbrCountMask;
     if (listed <= p.nbr_cap) {
         // The density pass's list: the in-range neighbours in the reference's visiting order.
         uint32_t k = 0;
