@@ -109,6 +109,27 @@ def dist_env():
     return world, rank, local
 
 
+def max_over_ranks(x: float, world: int, device=None) -> float:
+    """The largest x over all ranks (the job's time is its slowest replica's); x itself at N=1."""
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(units_per_rank: int, steps: int, total_ms: float, world: int,
+                       device=None) -> tuple[float, float]:
+    """Whole-job throughput of `world` independent replicas, each processing units_per_rank units
+    per step for `steps` steps: all ranks' units over the slowest rank's time. Returns (value,
+    max total ms)."""
+    ms = max_over_ranks(total_ms, world, device)
+    return world * units_per_rank * steps / (ms / 1e3), ms
+
+
 def oracle_for_workload(w, model=None):
     """CPU oracle of the workload; boundary grids from the GPU model or built on the CPU."""
     from oracle import binding as ob
@@ -181,6 +202,7 @@ def time_batched(args, stream, torch):
     total = sum(w.n for w in scenes)
     b = W.build_batch(scenes)
     b.set_stream(stream.cuda_stream)
+    tuned = b.autotune(repeats=2) if args.autotune else b.get_tune_config()
     for _ in range(args.warmup):
         b.substeps(1)
     torch.cuda.synchronize()
@@ -212,7 +234,7 @@ def time_batched(args, stream, torch):
     return {"scenes": len(scenes), "particles": total,
             "value": total / (t_batch * 1e-3), "ms_per_step": t_batch,
             "loop_value": total / (t_loop * 1e-3), "loop_ms_per_step": t_loop,
-            "speedup_vs_loop": t_loop / t_batch, "phase_ms": prof,
+            "speedup_vs_loop": t_loop / t_batch, "phase_ms": prof, "launch_shapes": tuned,
             "config": "N_s log-uniform [2048, 65536], nu_s log-uniform [1e-3, 5e-2], "
                       "k_s uniform [20, 100], own 64^3 container map per scene, dt 2e-4; "
                       "working set > L2"}
@@ -267,6 +289,50 @@ def time_adjoint(args, stream, torch):
             "grads": {"dnu": g["dnu"], "dk": g["dk"], "dv0_max": float(np.abs(g["dv0"]).max())}}
 
 
+def time_stress(args, stream, torch):
+    """Stress workload (4,194,304 uniform particles in a 4 x 2 x 2 box plus a 419,430-particle
+    Gaussian blob, sigma 0.1, h = 0.02, 128^3 container volume map): one substep from the same
+    initial state, repeated (state re-uploaded untimed before each repeat). Reports the sort's
+    pair throughput (N x 16 B per pass-equivalent: read + write of key and value) and the
+    density/force fractions of the HBM roofline."""
+    from vkfluidsim_gb300 import workloads as W
+
+    w = W.stress_4m()
+    m = W.build_model(w)
+    m.set_stream(stream.cuda_stream)
+    reps = max(3, min(args.steps, 10))
+    for _ in range(args.warmup):
+        m.set_particle_state(w.pos, w.vel)
+        m.substeps(1)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ms = []
+    for _ in range(reps):
+        m.set_particle_state(w.pos, w.vel)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        m.substeps(1)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    phase = {}
+    for _ in range(3):
+        m.set_particle_state(w.pos, w.vel)
+        for k, v in m.profile_substeps(1).items():
+            phase.setdefault(k, []).append(v)
+    phase = {k: float(np.median(v)) for k, v in phase.items()}
+    hbm, _ = peaks()
+    n = w.n
+    digits, items, passes = m.get_sort_config()
+    frac = {k: B_PHASE[k] * n / (phase[k] * 1e-3) / 1e9 / hbm for k in ("density", "force") if k in phase}
+    del m
+    return {"workload": w.name, "particles": n, "repeats": reps,
+            "ms_per_step": float(np.median(ms)), "value": n / (float(np.median(ms)) * 1e-3),
+            "phase_ms": phase,
+            "sort": {"digit_bits": digits, "passes": passes,
+                     "pair_gbs": 16 * n / (phase["sort"] * 1e-3) / 1e9},
+            "roofline_frac": frac}
+
+
 def run_gpu(args):
     import torch
 
@@ -284,6 +350,7 @@ def run_gpu(args):
     m = W.build_model(w)
     m.set_stream(stream.cuda_stream)
     n = w.n
+    tuned = m.autotune(repeats=3) if args.autotune else m.get_tune_config()
     flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
 
     def barrier():
@@ -311,14 +378,7 @@ def run_gpu(args):
         barrier()
         t_wall = time.perf_counter() - t_wall0
     step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
-    total_ms = sum(step_ms)
-    if world > 1:
-        import torch.distributed as dist
-
-        t = torch.tensor([total_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = world * n * args.steps / (total_ms / 1e3)
+    value, total_ms = replica_throughput(n, args.steps, sum(step_ms), world, device="cuda")
     ms_per_step = total_ms / args.steps
 
     # ---- per-kernel timing (same stream, CUDA events between the passes).
@@ -360,20 +420,16 @@ def run_gpu(args):
         check(lib.vfs_model_substeps(m._h, 1))
         check(lib.vfs_model_copy_data_buffers(m._h, fp(hp), fp(hv), fp(hd), None))
     barrier()
-    e2e_s = time.perf_counter() - t0
-    if world > 1:
-        import torch.distributed as dist
-
-        t = torch.tensor([e2e_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e = {"value": world * n * args.steps / e2e_s, "unit": UNIT,
+    e2e_value, _ = replica_throughput(n, args.steps, 1e3 * (time.perf_counter() - t0), world,
+                                      device="cuda")
+    e2e = {"value": e2e_value, "unit": UNIT,
            "h2d_bytes_per_step": 24 * n, "d2h_bytes_per_step": 28 * n}
 
     batched = None
     if args.batch_scenes > 0:
         batched = time_batched(args, stream, torch)
     adjoint = time_adjoint(args, stream, torch) if args.adjoint else None
+    stress = time_stress(args, stream, torch) if args.stress else None
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -389,6 +445,7 @@ def run_gpu(args):
                        "dt": w.sph.fixed_dt, "boundary": "sphere r=0.2, 128^3 volume map",
                        "l2": "flushed between timed steps (256 MiB write)",
                        "sort": {"digit_bits": digits, "tile_items": items, "passes": passes},
+                       "launch_shapes": tuned, "autotuned": bool(args.autotune),
                        "cuda_graph": True, "parallelism": f"replicas x{world}"},
             "e2e": e2e,
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm,
@@ -406,6 +463,8 @@ def run_gpu(args):
             line["batched"] = batched
         if adjoint:
             line["fwd_adjoint"] = adjoint
+        if stress:
+            line["stress"] = stress
         if cpu:
             line["cpu_baseline"] = cpu
         print(json.dumps(line), flush=True)
@@ -425,6 +484,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--batch-scenes", type=int, default=256)
     ap.add_argument("--adjoint", type=int, default=1)
+    ap.add_argument("--stress", type=int, default=1)
+    ap.add_argument("--autotune", type=int, default=1)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

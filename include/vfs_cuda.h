@@ -182,6 +182,30 @@ int vfs_model_get_sort_config(const vfs_model* m, int32_t* digit_bits, int32_t* 
 /* Device pointers of the current state: float4 (x, y, z, id bits) and (vx, vy, vz, 0). */
 int vfs_model_device_state(vfs_model* m, void** pos4, void** vel4);
 
+/* ---- autotuner (an extension: the reference's dispatch sizes are fixed in its shaders'
+ * numthreads, e.g. assets/shaders/simulation/wcsph_with_boundary_model.slang:92) ----
+ * Launch shapes of one substep. None changes any result: the sort is stable for every digit
+ * width, and each particle's sums are accumulated by one thread in the same order for every
+ * block shape. */
+typedef struct vfs_tune_config {
+    int32_t sort_digit_bits; /* 4..8 (the tuner tries 6, 7, 8) */
+    int32_t sort_tile_items; /* 8, 12 or 16 keys per thread of a onesweep tile */
+    int32_t nbr_block;       /* neighbour passes: threads per block ... */
+    int32_t nbr_min_blocks;  /* ... and minimum resident blocks per SM: 128x6, 128x8, 256x3, 64x12 */
+    int32_t cell_block;      /* keys per block of the cell-range / reorder kernel: 128, 256, 512 */
+} vfs_tune_config;
+/* Times every candidate of each stage (sort, neighbour passes, cell ranges) for `repeats`
+ * substeps from the model's current state, keeps the fastest, and restores the state (the
+ * neighbour arrays then need a new substep). With use_cache, a choice cached in this process for
+ * the same device and workload size is applied without timing. `chosen` may be NULL. */
+int vfs_model_autotune(vfs_model* m, int32_t repeats, int32_t use_cache, vfs_tune_config* chosen);
+int vfs_model_set_tune_config(vfs_model* m, const vfs_tune_config* c);
+int vfs_model_get_tune_config(vfs_model* m, vfs_tune_config* c);
+/* The process-wide cache of autotuner choices, as a text file (one line per workload key). */
+int vfs_tune_cache_save(const char* path);
+int vfs_tune_cache_load(const char* path);
+int vfs_tune_cache_clear(void);
+
 /* ---- batches: many independent scenes advanced by one launch per pass ----
  * Each scene is a complete reference simulation (its own parameters, particle count N_s = its
  * hash-table size, boundary objects). Scene s owns particles and keys [off_s, off_s + N_s): its
@@ -217,6 +241,9 @@ int vfs_batch_use_graph(vfs_batch* b, int32_t enable);
 int vfs_batch_synchronize(vfs_batch* b);
 int vfs_batch_profile_substeps(vfs_batch* b, int32_t count, float* phase_ms);
 int vfs_batch_set_sort_config(vfs_batch* b, int32_t digit_bits, int32_t tile_items);
+int vfs_batch_autotune(vfs_batch* b, int32_t repeats, int32_t use_cache, vfs_tune_config* chosen);
+int vfs_batch_set_tune_config(vfs_batch* b, const vfs_tune_config* c);
+int vfs_batch_get_tune_config(vfs_batch* b, vfs_tune_config* c);
 
 /* ---- differentiable rollouts (an extension: the reference has no differentiation) ----
  * A rollout advances a single-scene model `steps` substeps from its current state, keeping the
@@ -263,6 +290,17 @@ int vfs_sort_pairs(uint32_t* items, uint32_t* keys, uint32_t n, uint32_t max_val
  * looks up that array's device address (cudaGetSymbolAddress) and should come before any stream
  * capture. All calls share the array, so calls whose work overlaps on the GPU (other streams,
  * other threads) race; serialise them on one stream. */
+/* ---- failure detection ----
+ * Self-test of the radix sort's decoupled look-back wait (the sort's counterpart of the
+ * reference's global-atomic scan, src/compute/sort.cpp:57-86, which has no wait to fail). 32
+ * threads each wait on a predecessor tile's status word, with the same bounded-poll code the sort
+ * uses. With predecessor_published = 0 nothing ever publishes: after spin_limit polls (1..2^20)
+ * each sets the timeout bit of the error word and returns, and the call returns
+ * VFS_ERR_DEVICE_CHECK with err_word = 1 while the CUDA context stays usable. With 1, the
+ * predecessor has published prefix b + 1 for digit b: exclusive[b] = b + 1 and VFS_OK. */
+int vfs_selftest_lookback(int32_t predecessor_published, int32_t spin_limit, uint32_t* err_word,
+                          uint32_t* exclusive);
+
 #define VFS_SORT_NOALLOC_MAX_PAIRS 262144u
 int vfs_sort_pairs_noalloc(uint32_t* items, uint32_t* keys, uint32_t n, uint32_t max_value,
                            void* stream);

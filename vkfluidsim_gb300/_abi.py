@@ -86,6 +86,11 @@ _I = C.c_int
 _U32 = C.c_uint32
 
 # name -> (restype, argtypes)
+class TuneConfig(C.Structure):
+    _fields_ = [("sort_digit_bits", C.c_int32), ("sort_tile_items", C.c_int32),
+                ("nbr_block", C.c_int32), ("nbr_min_blocks", C.c_int32), ("cell_block", C.c_int32)]
+
+
 SIGNATURES = {
     "vfs_last_error": (C.c_char_p, []),
     "vfs_version": (C.c_char_p, []),
@@ -135,6 +140,16 @@ SIGNATURES = {
     "vfs_batch_synchronize": (_I, [_P]),
     "vfs_batch_profile_substeps": (_I, [_P, C.c_int32, _F]),
     "vfs_batch_set_sort_config": (_I, [_P, C.c_int32, C.c_int32]),
+    "vfs_batch_autotune": (_I, [_P, C.c_int32, C.c_int32, C.POINTER(TuneConfig)]),
+    "vfs_batch_set_tune_config": (_I, [_P, C.POINTER(TuneConfig)]),
+    "vfs_batch_get_tune_config": (_I, [_P, C.POINTER(TuneConfig)]),
+    "vfs_model_autotune": (_I, [_P, C.c_int32, C.c_int32, C.POINTER(TuneConfig)]),
+    "vfs_model_set_tune_config": (_I, [_P, C.POINTER(TuneConfig)]),
+    "vfs_model_get_tune_config": (_I, [_P, C.POINTER(TuneConfig)]),
+    "vfs_tune_cache_save": (_I, [C.c_char_p]),
+    "vfs_selftest_lookback": (_I, [C.c_int32, C.c_int32, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]),
+    "vfs_tune_cache_load": (_I, [C.c_char_p]),
+    "vfs_tune_cache_clear": (_I, []),
     "vfs_rollout_create": (_I, [_P, C.c_int32, C.c_int32, C.POINTER(_P)]),
     "vfs_rollout_destroy": (_I, [_P]),
     "vfs_rollout_forward": (_I, [_P]),

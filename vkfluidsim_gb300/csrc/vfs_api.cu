@@ -317,12 +317,12 @@ int Model::enqueue_substep(cudaEvent_t* ev) {
     if (ev) VFS_CUDA_TRY(cudaEventRecord(ev[2], s));
     VFS_CUDA_TRY(launch_sort(n, sc, sort_scratch, keys, keys_alt, vals, vals_alt, &skeys, &sperm, s));
     if (ev) VFS_CUDA_TRY(cudaEventRecord(ev[3], s));
-    VFS_CUDA_TRY(launch_cells_reorder(n, skeys, sperm, cell_scan, pos[c], vel[c], pos[o], vel[o], s));
+    VFS_CUDA_TRY(launch_cells_reorder(n, skeys, sperm, cell_scan, pos[c], vel[c], pos[o], vel[o], kc, s));
     if (ev) VFS_CUDA_TRY(cudaEventRecord(ev[4], s));
-    VFS_CUDA_TRY(launch_density(launch, pos[o], cell_scan, aux, bnd, nbr, nbr_count, s));
+    VFS_CUDA_TRY(launch_density(launch, pos[o], cell_scan, aux, bnd, nbr, nbr_count, kc, s));
     if (ev) VFS_CUDA_TRY(cudaEventRecord(ev[5], s));
     VFS_CUDA_TRY(launch_force(launch, pos[o], vel[o], aux, bnd, cell_scan, nbr, nbr_count, pos[c],
-                              vel[c], record ? acc : nullptr, s));
+                              vel[c], record ? acc : nullptr, kc, s));
     if (ev) VFS_CUDA_TRY(cudaEventRecord(ev[6], s));
     return VFS_OK;
 }
@@ -667,7 +667,7 @@ int Model::add_analytic(uint32_t scene, const vfs_analytic_object& a) {
     return rc;
 }
 
-static int profile(Model& m, int32_t count, float* phase_ms) {
+int profile_phases(Model& m, int32_t count, float* phase_ms) {
     if (!phase_ms || count < 1) return fail(VFS_ERR_INVALID_ARGUMENT, "bad argument");
     for (int k = 0; k < 6; k++) phase_ms[k] = 0.0f;
     if (m.n == 0) return VFS_OK;
@@ -718,7 +718,7 @@ static int set_stream(Model& m, void* stream) {
     return VFS_OK;
 }
 
-static int set_sort_config(Model& m, int32_t digit_bits, int32_t tile_items) {
+int set_sort_config(Model& m, int32_t digit_bits, int32_t tile_items) {
     if (digit_bits < 4 || digit_bits > 8) return fail(VFS_ERR_INVALID_ARGUMENT, "digit_bits must be in [4, 8]");
     if (tile_items != 8 && tile_items != 12 && tile_items != 16)
         return fail(VFS_ERR_INVALID_ARGUMENT, "tile_items must be 8, 12 or 16");
@@ -776,6 +776,7 @@ struct vfs_batch {
 }  // extern "C"
 
 vfs::Model* vfs_model_impl(vfs_model* h) { return h ? h->m : nullptr; }
+vfs::Model* vfs_batch_impl(vfs_batch* h) { return h ? h->m : nullptr; }
 
 #define VFS_HANDLE(h)                                                    \
     if (!(h) || !(h)->m) return fail(VFS_ERR_INVALID_ARGUMENT, "NULL handle"); \
@@ -943,7 +944,7 @@ int vfs_model_synchronize(vfs_model* h) {
 
 int vfs_model_profile_substeps(vfs_model* h, int32_t count, float* phase_ms) {
     VFS_HANDLE(h);
-    return vfs::profile(m, count, phase_ms);
+    return vfs::profile_phases(m, count, phase_ms);
 }
 
 int vfs_model_set_sort_config(vfs_model* h, int32_t digit_bits, int32_t tile_items) {
@@ -1096,7 +1097,7 @@ int vfs_batch_synchronize(vfs_batch* h) {
 
 int vfs_batch_profile_substeps(vfs_batch* h, int32_t count, float* phase_ms) {
     VFS_HANDLE(h);
-    return vfs::profile(m, count, phase_ms);
+    return vfs::profile_phases(m, count, phase_ms);
 }
 
 int vfs_batch_set_sort_config(vfs_batch* h, int32_t digit_bits, int32_t tile_items) {

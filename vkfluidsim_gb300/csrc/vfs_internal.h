@@ -110,6 +110,14 @@ struct SortConfig {
 int key_bits_for(uint32_t max_key);
 // key_bits <= 0: keys are spatial-hash keys, < n.
 SortConfig make_sort_config(uint32_t n, int digit_bits, int tile_items, int key_bits = 0);
+
+// Launch shapes of the neighbour passes: threads per block x minimum resident blocks per SM.
+enum NbrShape : int { kNbr128x6 = 0, kNbr128x8 = 1, kNbr256x3 = 2, kNbr64x12 = 3, kNumNbrShapes = 4 };
+// Launch shapes chosen per model (by default or by the autotuner); none changes any result.
+struct KernelConfig {
+    int nbr_shape = kNbr128x6;
+    int cell_block = 256;  // keys per block of the cell-range / reorder kernel: 128, 256 or 512
+};
 size_t sort_scratch_words(const SortConfig& c);
 
 // keys[i] = off + HashCell3D(floor(pos[i] / h)) % n of i's scene, and the per-pass digit
@@ -126,16 +134,20 @@ cudaError_t launch_sort(uint32_t n, const SortConfig& sc, const SortScratch& scr
 // cell_scan[k] = first sorted index with key >= k (k in [0, n]); gathers pos/vel by perm.
 cudaError_t launch_cells_reorder(uint32_t n, const uint32_t* skeys, const uint32_t* perm,
                                  uint32_t* cell_scan, const float4* pos_in, const float4* vel_in,
-                                 float4* pos_out, float4* vel_out, cudaStream_t s);
+                                 float4* pos_out, float4* vel_out, const KernelConfig& kc,
+                                 cudaStream_t s);
+// Failure-detection self-test of the sort's bounded look-back wait (d_work: 96 words).
+cudaError_t launch_lookback_selftest(bool published, uint32_t spin_limit, uint32_t* d_work,
+                                     uint32_t* err, cudaStream_t s);
 // Boundary volume + density + EOS epilogue; writes each particle's neighbour list.
 cudaError_t launch_density(const StepLaunch& L, const float4* pos, const uint32_t* cell_scan,
                            float4* aux, float4* bnd, uint32_t* nbr, uint32_t* nbr_count,
-                           cudaStream_t s);
+                           const KernelConfig& kc, cudaStream_t s);
 // Pressure + viscosity + wall + symplectic Euler over the density pass's neighbour lists.
 cudaError_t launch_force(const StepLaunch& L, const float4* pos, const float4* vel,
                          const float4* aux, const float4* bnd, const uint32_t* cell_scan,
                          const uint32_t* nbr, const uint32_t* nbr_count, float4* pos_out,
-                         float4* vel_out, float4* acc_out, cudaStream_t s);
+                         float4* vel_out, float4* acc_out, const KernelConfig& kc, cudaStream_t s);
 // Stable in-place sort of (keys, items) with caller-provided temporaries (n words each) and
 // sort scratch (sort_scratch_words(sc) + 1 words, zeroed here); items become the permutation.
 int enqueue_sort_pairs(uint32_t* items, uint32_t* keys, uint32_t n, const SortConfig& sc,

@@ -298,6 +298,43 @@ __device__ __forceinline__ uint32_t block_excl_scan256(uint32_t v, uint32_t* s_w
 
 constexpr uint32_t kLookbackSpinLimit = 1u << 20;
 
+// Decoupled look-back of tile `tile` for digit `bin`: sums the predecessors' published counts,
+// walking back until a tile with an inclusive prefix. A predecessor that has published nothing is
+// polled at most spin_limit times; then kErrLookbackTimeout is set in *err and the partial sum is
+// returned (the caller's scatter is guarded, and the host reports the error word).
+__device__ __forceinline__ uint32_t lookback_exclusive(const uint32_t* status, int bins,
+                                                       uint32_t tile, int bin, uint32_t spin_limit,
+                                                       uint32_t* err) {
+    uint32_t excl = 0u;
+    uint32_t t = tile - 1u;
+    uint32_t spins = 0u;
+    while (true) {
+        const uint32_t s = ld_volatile(status + (size_t)t * bins + bin);
+        const uint32_t flag = s & ~kCountMask;
+        if (flag == 0u) {
+            if (++spins > spin_limit) {
+                atomicOr(err, kErrLookbackTimeout);
+                break;
+            }
+            __nanosleep(32);
+            continue;
+        }
+        excl += s & kCountMask;
+        if (flag == kFlagPrefix || t == 0u) break;
+        t--;
+    }
+    return excl;
+}
+
+// Failure-detection self-test of the look-back wait: thread b plays tile 1 of digit b over a
+// status table whose tile 0 has published (prefix b + 1) or not (nothing). exclusive[b] gets the
+// look-back result.
+__global__ void k_lookback_selftest(const uint32_t* status, int bins, uint32_t spin_limit,
+                                    uint32_t* exclusive, uint32_t* err) {
+    const int b = threadIdx.x;
+    if (b < bins) exclusive[b] = lookback_exclusive(status, bins, 1u, b, spin_limit, err);
+}
+
 // One stable LSD radix pass (onesweep: Adinets & Merrill 2022). Tiles are claimed in launch
 // order through an atomic counter, so every predecessor of a tile is already resident and the
 // bounded look-back always terminates; a timeout sets an error bit instead of hanging.
@@ -374,23 +411,7 @@ __global__ void __launch_bounds__(BLOCK)
             st_volatile(st, kFlagPrefix | cnt);
         } else {
             st_volatile(st, kFlagAggregate | cnt);
-            uint32_t t = tile - 1u;
-            uint32_t spins = 0u;
-            while (true) {
-                const uint32_t s = ld_volatile(status + (size_t)t * bins + tid);
-                const uint32_t flag = s & ~kCountMask;
-                if (flag == 0u) {
-                    if (++spins > kLookbackSpinLimit) {
-                        atomicOr(err, kErrLookbackTimeout);
-                        break;
-                    }
-                    __nanosleep(32);
-                    continue;
-                }
-                excl += s & kCountMask;
-                if (flag == kFlagPrefix || t == 0u) break;
-                t--;
-            }
+            excl = lookback_exclusive(status, bins, tile, tid, kLookbackSpinLimit, err);
             st_volatile(st, kFlagPrefix | ((excl + cnt) & kCountMask));
         }
         s_gofs[tid] = gbase + excl;
@@ -434,7 +455,6 @@ __device__ __forceinline__ uint32_t lower_bound_keys(const uint32_t* __restrict_
     return lo;
 }
 
-constexpr uint32_t kCellBlock = 256;
 
 // Block b owns keys [256 b, 256 b + 256) of cell_scan (n + 1 entries: cell_scan[k] is the first
 // sorted index with key >= k, so bucket k is [cell_scan[k], cell_scan[k + 1])) and gathers the
@@ -442,6 +462,7 @@ constexpr uint32_t kCellBlock = 256;
 // of the sorted keys; each element of the slice writes the entries between its predecessor's key
 // and its own, which never leave the block's range, so no thread loops over more than 256
 // entries however the keys cluster.
+template <uint32_t kCellBlock>
 __global__ void __launch_bounds__(kCellBlock)
     k_cells_reorder(uint32_t n, const uint32_t* __restrict__ skeys,
                     const uint32_t* __restrict__ perm, uint32_t* __restrict__ scan,
@@ -494,7 +515,6 @@ __global__ void __launch_bounds__(256)
 // candidate order, so the sums are accumulated in the reference's visiting order. A list that
 // fills up (dense regions) is drained early and refilled.
 
-constexpr int kNbrBlock = 128;
 constexpr int kListCap = 48;
 constexpr int kDrainAt = kListCap - 4;  // a batch of four never overflows the list
 
@@ -598,8 +618,8 @@ __device__ __forceinline__ void for_each_candidate(const SceneParams& p,
 // (nbr[s * n + i], so a warp's lanes store and later load consecutive words), and its length in
 // nbr_count[i] (a length above nbr_cap means the list overflowed and was truncated). Positions
 // do not change before the force pass, so that list is exactly the force pass's neighbour set.
-template <bool kBatch>
-__global__ void __launch_bounds__(kNbrBlock, 6)
+template <bool kBatch, int kNbrBlock, int kMinBlocks>
+__global__ void __launch_bounds__(kNbrBlock, kMinBlocks)
     k_density(StepLaunch L, const float4* __restrict__ pos, const uint32_t* __restrict__ scan,
               float4* __restrict__ aux, float4* __restrict__ bnd, uint32_t* __restrict__ nbr,
               uint32_t* __restrict__ nbr_count) {
@@ -684,6 +704,7 @@ __device__ __forceinline__ void force_term(const SceneParams& p, const float4& x
 }
 
 // Phase B of the force pass over the first cnt listed neighbours.
+template <int kNbrBlock>
 __device__ __forceinline__ void force_drain(const SceneParams& p, const float4* __restrict__ pos,
                                             const float4* __restrict__ vel,
                                             const float2* __restrict__ aux2,
@@ -710,8 +731,8 @@ __device__ __forceinline__ void force_drain(const SceneParams& p, const float4* 
 // CalculatePressureAccel + CalculateViscousAccel + UpdatePositions
 // (wcsph_with_boundary_model.slang:205-360), fused: both sums are accumulated separately in the
 // reference's visiting order, then a = ((g - P) + V) + wall, v += a dt, x += v dt.
-template <bool kBatch>
-__global__ void __launch_bounds__(kNbrBlock, 6)
+template <bool kBatch, int kNbrBlock, int kMinBlocks>
+__global__ void __launch_bounds__(kNbrBlock, kMinBlocks)
     k_force(StepLaunch L, const float4* __restrict__ pos, const float4* __restrict__ vel,
             const float4* __restrict__ aux, const float4* __restrict__ bnd,
             const uint32_t* __restrict__ scan, const uint32_t* __restrict__ nbr,
@@ -761,11 +782,11 @@ __global__ void __launch_bounds__(kNbrBlock, 6)
             }
         }, [&]() {
             if (cnt > kDrainAt) {
-                force_drain(p, pos, vel, aux2, s_j, tid, cnt, xi, vi, pdi, f);
+                force_drain<kNbrBlock>(p, pos, vel, aux2, s_j, tid, cnt, xi, vi, pdi, f);
                 cnt = 0;
             }
         });
-        force_drain(p, pos, vel, aux2, s_j, tid, cnt, xi, vi, pdi, f);
+        force_drain<kNbrBlock>(p, pos, vel, aux2, s_j, tid, cnt, xi, vi, pdi, f);
     }
     const float4 bi = __ldg(bnd + i);
     const float sb = (pdi + ai.w) * p.rho0;
@@ -805,6 +826,23 @@ cudaError_t launch_onesweep_t(uint32_t n, const SortConfig& sc, const SortScratc
 }
 
 }  // namespace
+
+cudaError_t launch_lookback_selftest(bool published, uint32_t spin_limit, uint32_t* d_work,
+                                     uint32_t* err, cudaStream_t s) {
+    constexpr int bins = 32;
+    uint32_t h[2 * bins];
+    for (int b = 0; b < bins; b++) {
+        h[b] = published ? (kFlagPrefix | (uint32_t)(b + 1)) : 0u;  // tile 0
+        h[bins + b] = 0u;                                           // tile 1 (the waiter)
+    }
+    cudaError_t e = cudaMemcpyAsync(d_work, h, sizeof(h), cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) return e;
+    e = cudaStreamSynchronize(s);  // h is a stack buffer
+    if (e != cudaSuccess) return e;
+    k_lookback_selftest<<<1, bins, 0, s>>>(d_work, bins, spin_limit, d_work + 2 * bins, err);
+    return cudaGetLastError();
+}
+
 
 int key_bits_for(uint32_t max_key) {
     int bits = 1;
@@ -884,37 +922,80 @@ cudaError_t launch_sort(uint32_t n, const SortConfig& sc, const SortScratch& scr
 
 cudaError_t launch_cells_reorder(uint32_t n, const uint32_t* skeys, const uint32_t* perm,
                                  uint32_t* cell_scan, const float4* pos_in, const float4* vel_in,
-                                 float4* pos_out, float4* vel_out, cudaStream_t s) {
+                                 float4* pos_out, float4* vel_out, const KernelConfig& kc,
+                                 cudaStream_t s) {
     if (n == 0) return cudaSuccess;
-    k_cells_reorder<<<(n + kCellBlock) / kCellBlock, kCellBlock, 0, s>>>(
-        n, skeys, perm, cell_scan, pos_in, vel_in, pos_out, vel_out);
+    switch (kc.cell_block) {
+        case 128:
+            k_cells_reorder<128><<<(n + 128u) / 128u, 128, 0, s>>>(n, skeys, perm, cell_scan, pos_in,
+                                                                 vel_in, pos_out, vel_out);
+            break;
+        case 512:
+            k_cells_reorder<512><<<(n + 512u) / 512u, 512, 0, s>>>(n, skeys, perm, cell_scan, pos_in,
+                                                                 vel_in, pos_out, vel_out);
+            break;
+        default:
+            k_cells_reorder<256><<<(n + 256u) / 256u, 256, 0, s>>>(n, skeys, perm, cell_scan, pos_in,
+                                                                 vel_in, pos_out, vel_out);
+    }
     return cudaGetLastError();
+}
+
+template <int B, int M>
+void density_shape(const StepLaunch& L, const float4* pos, const uint32_t* cell_scan, float4* aux,
+                   float4* bnd, uint32_t* nbr, uint32_t* nbr_count, cudaStream_t s) {
+    const uint32_t blocks = (L.total + B - 1) / B;
+    if (L.n_scenes > 1)
+        k_density<true, B, M><<<blocks, B, 0, s>>>(L, pos, cell_scan, aux, bnd, nbr, nbr_count);
+    else
+        k_density<false, B, M><<<blocks, B, 0, s>>>(L, pos, cell_scan, aux, bnd, nbr, nbr_count);
+}
+
+template <int B, int M>
+void force_shape(const StepLaunch& L, const float4* pos, const float4* vel, const float4* aux,
+                 const float4* bnd, const uint32_t* cell_scan, const uint32_t* nbr,
+                 const uint32_t* nbr_count, float4* pos_out, float4* vel_out, float4* acc_out,
+                 cudaStream_t s) {
+    const uint32_t blocks = (L.total + B - 1) / B;
+    if (L.n_scenes > 1)
+        k_force<true, B, M><<<blocks, B, 0, s>>>(L, pos, vel, aux, bnd, cell_scan, nbr, nbr_count,
+                                                 pos_out, vel_out, acc_out);
+    else
+        k_force<false, B, M><<<blocks, B, 0, s>>>(L, pos, vel, aux, bnd, cell_scan, nbr, nbr_count,
+                                                  pos_out, vel_out, acc_out);
 }
 
 cudaError_t launch_density(const StepLaunch& L, const float4* pos, const uint32_t* cell_scan,
                            float4* aux, float4* bnd, uint32_t* nbr, uint32_t* nbr_count,
-                           cudaStream_t s) {
+                           const KernelConfig& kc, cudaStream_t s) {
     if (L.total == 0) return cudaSuccess;
-    const uint32_t blocks = (L.total + kNbrBlock - 1) / kNbrBlock;
-    if (L.n_scenes > 1)
-        k_density<true><<<blocks, kNbrBlock, 0, s>>>(L, pos, cell_scan, aux, bnd, nbr, nbr_count);
-    else
-        k_density<false><<<blocks, kNbrBlock, 0, s>>>(L, pos, cell_scan, aux, bnd, nbr, nbr_count);
+    switch (kc.nbr_shape) {
+        case kNbr128x8: density_shape<128, 8>(L, pos, cell_scan, aux, bnd, nbr, nbr_count, s); break;
+        case kNbr256x3: density_shape<256, 3>(L, pos, cell_scan, aux, bnd, nbr, nbr_count, s); break;
+        case kNbr64x12: density_shape<64, 12>(L, pos, cell_scan, aux, bnd, nbr, nbr_count, s); break;
+        default: density_shape<128, 6>(L, pos, cell_scan, aux, bnd, nbr, nbr_count, s);
+    }
     return cudaGetLastError();
 }
 
 cudaError_t launch_force(const StepLaunch& L, const float4* pos, const float4* vel,
                          const float4* aux, const float4* bnd, const uint32_t* cell_scan,
                          const uint32_t* nbr, const uint32_t* nbr_count, float4* pos_out,
-                         float4* vel_out, float4* acc_out, cudaStream_t s) {
+                         float4* vel_out, float4* acc_out, const KernelConfig& kc, cudaStream_t s) {
     if (L.total == 0) return cudaSuccess;
-    const uint32_t blocks = (L.total + kNbrBlock - 1) / kNbrBlock;
-    if (L.n_scenes > 1)
-        k_force<true><<<blocks, kNbrBlock, 0, s>>>(L, pos, vel, aux, bnd, cell_scan, nbr, nbr_count,
-                                                   pos_out, vel_out, acc_out);
-    else
-        k_force<false><<<blocks, kNbrBlock, 0, s>>>(L, pos, vel, aux, bnd, cell_scan, nbr,
-                                                    nbr_count, pos_out, vel_out, acc_out);
+    switch (kc.nbr_shape) {
+        case kNbr128x8:
+            force_shape<128, 8>(L, pos, vel, aux, bnd, cell_scan, nbr, nbr_count, pos_out, vel_out, acc_out, s);
+            break;
+        case kNbr256x3:
+            force_shape<256, 3>(L, pos, vel, aux, bnd, cell_scan, nbr, nbr_count, pos_out, vel_out, acc_out, s);
+            break;
+        case kNbr64x12:
+            force_shape<64, 12>(L, pos, vel, aux, bnd, cell_scan, nbr, nbr_count, pos_out, vel_out, acc_out, s);
+            break;
+        default:
+            force_shape<128, 6>(L, pos, vel, aux, bnd, cell_scan, nbr, nbr_count, pos_out, vel_out, acc_out, s);
+    }
     return cudaGetLastError();
 }
 

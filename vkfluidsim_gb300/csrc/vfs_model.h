@@ -74,6 +74,7 @@ struct Model {
     int tile_items = 16;
     SortConfig sc{};
     SortScratch sort_scratch{};
+    KernelConfig kc{};
     StepLaunch launch{};
 
     bool record = false;
@@ -104,7 +105,14 @@ struct Model {
 // Builds a model of the given scenes (sizes from each sph.n_particles) and allocates it.
 int create_model(const std::vector<SceneHost>& scenes, Model** out);
 
+// Runs `count` substeps with events between the passes; phase_ms[6] = mean ms of keys, sort,
+// cells+reorder, density, force, clear.
+int profile_phases(Model& m, int32_t count, float* phase_ms);
+int set_sort_config(Model& m, int32_t digit_bits, int32_t tile_items);
+
 }  // namespace vfs
 
 struct vfs_model;
 vfs::Model* vfs_model_impl(vfs_model* h);
+struct vfs_batch;
+vfs::Model* vfs_batch_impl(vfs_batch* h);

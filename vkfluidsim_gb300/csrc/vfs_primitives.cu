@@ -117,4 +117,26 @@ int vfs_reorder_float3(const uint32_t* sorted_indices, const float* src, float* 
     return VFS_OK;
 }
 
+int vfs_selftest_lookback(int32_t predecessor_published, int32_t spin_limit, uint32_t* err_word,
+                          uint32_t* exclusive) {
+    if (spin_limit < 1 || spin_limit > (1 << 20))
+        return fail(VFS_ERR_INVALID_ARGUMENT, "spin_limit must be in [1, 2^20]");
+    uint32_t* d = nullptr;
+    VFS_PRIM_TRY(cudaMalloc(&d, 97 * sizeof(uint32_t)));  // status 2 x 32, exclusive 32, error word
+    uint32_t h[33];
+    cudaError_t e = cudaMemset(d, 0, 97 * sizeof(uint32_t));
+    if (e == cudaSuccess)
+        e = vfs::launch_lookback_selftest(predecessor_published != 0, (uint32_t)spin_limit, d, d + 96,
+                                          nullptr);
+    if (e == cudaSuccess) e = cudaMemcpy(h, d + 64, sizeof(h), cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e != cudaSuccess) return fail(VFS_ERR_CUDA, cudaGetErrorString(e));
+    if (exclusive)
+        for (int b = 0; b < 32; b++) exclusive[b] = h[b];
+    if (err_word) *err_word = h[32];
+    if (h[32]) return fail(VFS_ERR_DEVICE_CHECK, "device error word set: " + std::to_string(h[32]) +
+                                                     " (look-back timeout)");
+    return VFS_OK;
+}
+
 }  // extern "C"

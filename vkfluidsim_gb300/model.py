@@ -108,6 +108,22 @@ class BoundaryObjectInfo:
     volume_map: np.ndarray = field(repr=False)
 
 
+def tune_dict(c) -> dict:
+    return {k: int(getattr(c, k)) for k, _ in _abi.TuneConfig._fields_}
+
+
+def tune_cache_save(path: str) -> None:
+    check(load_library().vfs_tune_cache_save(str(path).encode()))
+
+
+def tune_cache_load(path: str) -> None:
+    check(load_library().vfs_tune_cache_load(str(path).encode()))
+
+
+def tune_cache_clear() -> None:
+    check(load_library().vfs_tune_cache_clear())
+
+
 class WCSPHWithBoundaryModel:
     """A WCSPH-with-boundary model on the GPU (one handle of libvfs_cuda)."""
 
@@ -277,6 +293,21 @@ class WCSPHWithBoundaryModel:
         check(self._lib.vfs_model_get_sort_config(self._h, C.byref(d), C.byref(t), C.byref(p)))
         return d.value, t.value, p.value
 
+    def autotune(self, repeats: int = 3, use_cache: bool = True) -> dict:
+        """Runs the autotuner (vfs_model_autotune) and returns the chosen launch shapes."""
+        c = _abi.TuneConfig()
+        check(self._lib.vfs_model_autotune(self._h, repeats, int(use_cache), C.byref(c)))
+        return tune_dict(c)
+
+    def get_tune_config(self) -> dict:
+        c = _abi.TuneConfig()
+        check(self._lib.vfs_model_get_tune_config(self._h, C.byref(c)))
+        return tune_dict(c)
+
+    def set_tune_config(self, **kw) -> None:
+        c = _abi.TuneConfig(**{**self.get_tune_config(), **kw})
+        check(self._lib.vfs_model_set_tune_config(self._h, C.byref(c)))
+
     def device_state(self):
         p, v = C.c_void_p(), C.c_void_p()
         check(self._lib.vfs_model_device_state(self._h, C.byref(p), C.byref(v)))
@@ -441,3 +472,18 @@ class Batch:
 
     def set_sort_config(self, digit_bits: int, tile_items: int) -> None:
         check(self._lib.vfs_batch_set_sort_config(self._h, digit_bits, tile_items))
+
+    def autotune(self, repeats: int = 3, use_cache: bool = True) -> dict:
+        """Runs the autotuner (vfs_batch_autotune) and returns the chosen launch shapes."""
+        c = _abi.TuneConfig()
+        check(self._lib.vfs_batch_autotune(self._h, repeats, int(use_cache), C.byref(c)))
+        return tune_dict(c)
+
+    def get_tune_config(self) -> dict:
+        c = _abi.TuneConfig()
+        check(self._lib.vfs_batch_get_tune_config(self._h, C.byref(c)))
+        return tune_dict(c)
+
+    def set_tune_config(self, **kw) -> None:
+        c = _abi.TuneConfig(**{**self.get_tune_config(), **kw})
+        check(self._lib.vfs_batch_set_tune_config(self._h, C.byref(c)))
