@@ -182,6 +182,30 @@ int vfs_model_get_sort_config(const vfs_model* m, int32_t* digit_bits, int32_t* 
 /* Device pointers of the current state: float4 (x, y, z, id bits) and (vx, vy, vz, 0). */
 int vfs_model_device_state(vfs_model* m, void** pos4, void** vel4);
 
+/* ---- headless state export (the "record particle positions" roadmap item, README.md:30, in
+ * place of the render hand-off SPHModel::CopyDataBuffers, src/models/model.cpp:158-170) ----
+ * A snapshot is `<prefix>.bin` (positions f32[N][3], velocities f32[N][3], densities f32[N], each
+ * indexed by particle id, little-endian, back to back) and `<prefix>.json` (format
+ * "vkfluidsim_gb300.state" version 1: offsets, shapes, substep count, simulation parameters). */
+int vfs_model_export_state(vfs_model* m, const char* path_prefix);
+/* Loads a snapshot of the same particle count (positions and velocities, ids = file order). */
+int vfs_model_import_state(vfs_model* m, const char* path_prefix);
+/* Runs `substeps` substeps, writing a snapshot `<prefix>_f<frame, 6 digits>` every `every`
+ * substeps; file writes overlap the following substeps (two pinned buffers, a writer thread). */
+int vfs_model_record(vfs_model* m, int32_t substeps, int32_t every, const char* path_prefix);
+
+/* ---- headless rendering (the particle pass of src/gui/scene_renderer.cpp:101-109 and
+ * assets/shaders/draw/particles_3d.slang, into a host RGBA8 image instead of a swapchain) ----
+ * model_view, proj: column-major 4x4 (glm layout), as the reference's Particle3DDrawPipeline push
+ * constants. Each particle is a screen-facing quad of side quad_side (view units; the reference
+ * draws 0.15) shaded as a sphere impostor: colour = IDL Mac-style colour map of |v| / v_max
+ * (reference 6.5) times max(0, n . normalize(0, 1, 1)), depth of view + depth_radius * n
+ * (reference 0.15), nearest wins (LESS_OR_EQUAL). rgba: width * height * 4 bytes, row 0 at NDC
+ * y = -1; depth (optional): width * height floats, 1 where no particle. */
+int vfs_model_render_particles(vfs_model* m, const float* model_view, const float* proj,
+                               int32_t width, int32_t height, float quad_side, float depth_radius,
+                               float v_max, uint8_t* rgba, float* depth);
+
 /* ---- autotuner (an extension: the reference's dispatch sizes are fixed in its shaders'
  * numthreads, e.g. assets/shaders/simulation/wcsph_with_boundary_model.slang:92) ----
  * Launch shapes of one substep. None changes any result: the sort is stable for every digit
@@ -241,6 +265,13 @@ int vfs_batch_use_graph(vfs_batch* b, int32_t enable);
 int vfs_batch_synchronize(vfs_batch* b);
 int vfs_batch_profile_substeps(vfs_batch* b, int32_t count, float* phase_ms);
 int vfs_batch_set_sort_config(vfs_batch* b, int32_t digit_bits, int32_t tile_items);
+int vfs_batch_export_state(vfs_batch* b, int32_t scene, const char* path_prefix);
+int vfs_batch_import_state(vfs_batch* b, int32_t scene, const char* path_prefix);
+/* As vfs_model_record; the snapshots are `<prefix>_s<scene>_f<frame>`. */
+int vfs_batch_record(vfs_batch* b, int32_t substeps, int32_t every, const char* path_prefix);
+int vfs_batch_render_particles(vfs_batch* b, int32_t scene, const float* model_view,
+                               const float* proj, int32_t width, int32_t height, float quad_side,
+                               float depth_radius, float v_max, uint8_t* rgba, float* depth);
 int vfs_batch_autotune(vfs_batch* b, int32_t repeats, int32_t use_cache, vfs_tune_config* chosen);
 int vfs_batch_set_tune_config(vfs_batch* b, const vfs_tune_config* c);
 int vfs_batch_get_tune_config(vfs_batch* b, vfs_tune_config* c);

@@ -6,12 +6,13 @@ only binds it. Importing works without a GPU; every model call needs the library
 from ._abi import LIB_PATH, VfsError, load_library, SHAPE_SPHERE, SHAPE_BOX, SHAPE_CONTAINER
 from .model import (AnalyticObject, Batch, SimulationParameters, SPHParameters, WCSPHParameters,
                     WCSPHWithBoundaryModel, generate_fourier_velocity, generate_lattice,
-                    generate_uniform_blob, load_scene, tune_cache_clear, tune_cache_load,
-                    tune_cache_save)
+                    generate_uniform_blob, load_scene, look_at, perspective, read_state,
+                    tune_cache_clear, tune_cache_load, tune_cache_save, write_ppm)
 
 __all__ = [
     "LIB_PATH", "VfsError", "load_library", "SHAPE_SPHERE", "SHAPE_BOX", "SHAPE_CONTAINER",
     "AnalyticObject", "Batch", "SimulationParameters", "SPHParameters", "WCSPHParameters",
     "WCSPHWithBoundaryModel", "generate_fourier_velocity", "generate_lattice",
-    "generate_uniform_blob", "load_scene", "tune_cache_clear", "tune_cache_load", "tune_cache_save",
+    "generate_uniform_blob", "load_scene", "look_at", "perspective", "read_state",
+    "tune_cache_clear", "tune_cache_load", "tune_cache_save", "write_ppm",
 ]

@@ -147,6 +147,18 @@ SIGNATURES = {
     "vfs_model_set_tune_config": (_I, [_P, C.POINTER(TuneConfig)]),
     "vfs_model_get_tune_config": (_I, [_P, C.POINTER(TuneConfig)]),
     "vfs_tune_cache_save": (_I, [C.c_char_p]),
+    "vfs_model_export_state": (_I, [_P, C.c_char_p]),
+    "vfs_model_render_particles": (_I, [_P, C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_int32,
+                                        C.c_int32, C.c_float, C.c_float, C.c_float,
+                                        C.POINTER(C.c_uint8), C.POINTER(C.c_float)]),
+    "vfs_batch_render_particles": (_I, [_P, C.c_int32, C.POINTER(C.c_float), C.POINTER(C.c_float),
+                                        C.c_int32, C.c_int32, C.c_float, C.c_float, C.c_float,
+                                        C.POINTER(C.c_uint8), C.POINTER(C.c_float)]),
+    "vfs_model_import_state": (_I, [_P, C.c_char_p]),
+    "vfs_model_record": (_I, [_P, C.c_int32, C.c_int32, C.c_char_p]),
+    "vfs_batch_export_state": (_I, [_P, C.c_int32, C.c_char_p]),
+    "vfs_batch_import_state": (_I, [_P, C.c_int32, C.c_char_p]),
+    "vfs_batch_record": (_I, [_P, C.c_int32, C.c_int32, C.c_char_p]),
     "vfs_selftest_lookback": (_I, [C.c_int32, C.c_int32, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]),
     "vfs_tune_cache_load": (_I, [C.c_char_p]),
     "vfs_tune_cache_clear": (_I, []),

@@ -29,6 +29,7 @@
 namespace vfs {
 
 thread_local std::string g_last_error;
+std::string last_error_message() { return g_last_error; }
 
 int fail(int code, const std::string& msg) {
     g_last_error = msg;
@@ -336,6 +337,7 @@ int Model::run_substeps(int count) {
             if (rc) return rc;
         }
         stepped = true;
+        substeps_done += (uint64_t)count;
         return VFS_OK;
     }
     if (!graph_exec) {
@@ -357,6 +359,7 @@ int Model::run_substeps(int count) {
     }
     for (int i = 0; i < count; i++) VFS_CUDA_TRY(cudaGraphLaunch(graph_exec, stream));
     stepped = true;
+    substeps_done += (uint64_t)count;
     return VFS_OK;
 }
 

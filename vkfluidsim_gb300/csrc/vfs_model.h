@@ -12,6 +12,7 @@
 namespace vfs {
 
 int fail(int code, const std::string& msg);
+std::string last_error_message();  // this thread's last error
 
 struct ObjectStore {
     vfs_boundary_object info;  // grid pointers cleared; grids live on the device
@@ -78,6 +79,7 @@ struct Model {
     StepLaunch launch{};
 
     bool record = false;
+    uint64_t substeps_done = 0;  // substeps run by run_substeps (the snapshot sidecar's counter)
     bool use_graph = true;
     bool stepped = false;
     cudaGraphExec_t graph_exec = nullptr;

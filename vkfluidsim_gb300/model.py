@@ -108,6 +108,71 @@ class BoundaryObjectInfo:
     volume_map: np.ndarray = field(repr=False)
 
 
+def read_state(prefix) -> dict:
+    """Reads a snapshot written by export_state / record: {"positions" (N, 3), "velocities" (N, 3),
+    "densities" (N,), each by particle id, plus the sidecar's "substeps", "time", "parameters"}."""
+    import json
+    from pathlib import Path
+
+    meta = json.loads(Path(f"{prefix}.json").read_text())
+    if meta.get("format") != "vkfluidsim_gb300.state" or meta.get("version") != 1:
+        raise ValueError(f"{prefix}.json is not a version-1 state sidecar")
+    raw = np.fromfile(Path(f"{prefix}.json").parent / meta["binary"], dtype="<u1")
+    out = {k: meta[k] for k in ("substeps", "time", "parameters", "particles")}
+    for name, a in meta["arrays"].items():
+        count = int(np.prod(a["shape"]))
+        out[name] = np.frombuffer(raw, dtype=a["dtype"], count=count,
+                                  offset=a["offset"]).reshape(a["shape"])
+    return out
+
+
+def perspective(fovy: float, aspect: float, near: float, far: float, y_down: bool = True):
+    """glm::perspective with depth in [0, 1] (GLM_FORCE_DEPTH_ZERO_TO_ONE), y optionally flipped
+    as gfx::Camera does for Vulkan; column-major float32[16]."""
+    f = 1.0 / np.tan(fovy / 2.0)
+    m = np.zeros((4, 4), np.float64)  # m[col][row]
+    m[0][0] = f / aspect
+    m[1][1] = -f if y_down else f
+    m[2][2] = far / (near - far)
+    m[2][3] = -1.0
+    m[3][2] = -(far * near) / (far - near)
+    return m.astype(np.float32).ravel()
+
+
+def look_at(eye, center, up=(0.0, 0.0, 1.0)):
+    """glm::lookAt (right-handed); column-major float32[16]."""
+    eye, center, up = (np.asarray(v, np.float64) for v in (eye, center, up))
+    f = center - eye
+    f /= np.linalg.norm(f)
+    s = np.cross(f, up)
+    s /= np.linalg.norm(s)
+    u = np.cross(s, f)
+    m = np.eye(4)  # m[col][row]
+    m[0][0], m[1][0], m[2][0] = s
+    m[0][1], m[1][1], m[2][1] = u
+    m[0][2], m[1][2], m[2][2] = -f
+    m[3][0], m[3][1], m[3][2] = -s @ eye, -u @ eye, f @ eye
+    return m.astype(np.float32).ravel()
+
+
+def write_ppm(path, rgba) -> None:
+    """Writes the RGB channels of an (H, W, 4) uint8 image as a binary PPM."""
+    rgb = np.ascontiguousarray(np.asarray(rgba)[..., :3], dtype=np.uint8)
+    with open(path, "wb") as f:
+        f.write(b"P6\n%d %d\n255\n" % (rgb.shape[1], rgb.shape[0]))
+        f.write(rgb.tobytes())
+
+
+def _render(lib_fn, args, width, height, quad_side, depth_radius, v_max, with_depth):
+    mv = np.ascontiguousarray(args[-2], np.float32)
+    pj = np.ascontiguousarray(args[-1], np.float32)
+    img = np.empty((height, width, 4), np.uint8)
+    dep = np.empty((height, width), np.float32) if with_depth else None
+    check(lib_fn(*args[:-2], _fp(mv), _fp(pj), width, height, quad_side, depth_radius, v_max,
+                 img.ctypes.data_as(C.POINTER(C.c_uint8)), _fp(dep)))
+    return (img, dep) if with_depth else img
+
+
 def tune_dict(c) -> dict:
     return {k: int(getattr(c, k)) for k, _ in _abi.TuneConfig._fields_}
 
@@ -293,6 +358,24 @@ class WCSPHWithBoundaryModel:
         check(self._lib.vfs_model_get_sort_config(self._h, C.byref(d), C.byref(t), C.byref(p)))
         return d.value, t.value, p.value
 
+    def export_state(self, prefix) -> None:
+        """Writes `<prefix>.bin` + `<prefix>.json` (state by particle id; see read_state)."""
+        check(self._lib.vfs_model_export_state(self._h, str(prefix).encode()))
+
+    def import_state(self, prefix) -> None:
+        check(self._lib.vfs_model_import_state(self._h, str(prefix).encode()))
+
+    def record(self, substeps: int, every: int, prefix) -> None:
+        """Runs `substeps` substeps, writing a snapshot `<prefix>_f<frame:06d>` every `every`."""
+        check(self._lib.vfs_model_record(self._h, substeps, every, str(prefix).encode()))
+
+    def render_particles(self, model_view, proj, width: int, height: int, quad_side: float = 0.15,
+                         depth_radius: float = 0.15, v_max: float = 6.5, with_depth: bool = False):
+        """The reference's particle pass into an (height, width, 4) uint8 RGBA image (row 0 at
+        NDC y = -1), optionally with the depth buffer."""
+        return _render(self._lib.vfs_model_render_particles, (self._h, model_view, proj), width,
+                       height, quad_side, depth_radius, v_max, with_depth)
+
     def autotune(self, repeats: int = 3, use_cache: bool = True) -> dict:
         """Runs the autotuner (vfs_model_autotune) and returns the chosen launch shapes."""
         c = _abi.TuneConfig()
@@ -472,6 +555,22 @@ class Batch:
 
     def set_sort_config(self, digit_bits: int, tile_items: int) -> None:
         check(self._lib.vfs_batch_set_sort_config(self._h, digit_bits, tile_items))
+
+    def export_state(self, scene: int, prefix) -> None:
+        check(self._lib.vfs_batch_export_state(self._h, scene, str(prefix).encode()))
+
+    def import_state(self, scene: int, prefix) -> None:
+        check(self._lib.vfs_batch_import_state(self._h, scene, str(prefix).encode()))
+
+    def record(self, substeps: int, every: int, prefix) -> None:
+        """Snapshots `<prefix>_s<scene>_f<frame:06d>` of every scene every `every` substeps."""
+        check(self._lib.vfs_batch_record(self._h, substeps, every, str(prefix).encode()))
+
+    def render_particles(self, scene: int, model_view, proj, width: int, height: int,
+                         quad_side: float = 0.15, depth_radius: float = 0.15, v_max: float = 6.5,
+                         with_depth: bool = False):
+        return _render(self._lib.vfs_batch_render_particles, (self._h, scene, model_view, proj),
+                       width, height, quad_side, depth_radius, v_max, with_depth)
 
     def autotune(self, repeats: int = 3, use_cache: bool = True) -> dict:
         """Runs the autotuner (vfs_batch_autotune) and returns the chosen launch shapes."""
