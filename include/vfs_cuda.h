@@ -79,7 +79,7 @@ typedef struct vfs_boundary_object {
 /* An analytic boundary shape whose SDF grid and volume map the library builds on the GPU, in
  * place of the reference's OBJ mesh -> MeshSDF -> GenerateVolumeMap chain
  * (src/scenes/generic_scene.cpp:88-124, src/util/volume_map.cpp:9-54). The placement fields are
- * the scene JSON's boundaryObjects[] keys (src/util/scene_loader.cpp:59-95). */
+ * the scene JSON's boundaryObjects[] keys (src/util/scene_loader.cpp:75-111). */
 #define VFS_SHAPE_SPHERE 0    /* params[0] = radius */
 #define VFS_SHAPE_BOX 1       /* params[0..2] = half extents, solid */
 #define VFS_SHAPE_CONTAINER 2 /* params[0..2] = half extents, fluid inside (inverted box) */
@@ -92,6 +92,22 @@ typedef struct vfs_analytic_object {
     float scale[3];
     uint32_t resolution[3];
 } vfs_analytic_object;
+
+/* A triangle-mesh boundary object: GenericScene's ObjectDef (src/scenes/generic_scene.h) with the
+ * mesh given as an OBJ file (its last object, polygons triangulated as fans; LoadObjMesh,
+ * src/util/mesh_loader.cpp) or as arrays (obj_path NULL). */
+typedef struct vfs_mesh_object {
+    const char* obj_path;
+    const float* vertices;      /* n_vertices x 3 */
+    uint32_t n_vertices;
+    const uint32_t* triangles;  /* n_triangles x 3 vertex indices */
+    uint32_t n_triangles;
+    float position[3];
+    float rotation_angle_deg;
+    float rotation_axis[3];
+    float scale[3];
+    uint32_t resolution[3];
+} vfs_mesh_object;
 
 /* Thread-local message of the last failing call on this thread. */
 const char* vfs_last_error(void);
@@ -111,7 +127,7 @@ int vfs_model_destroy(vfs_model* m);
 /* The CUDA stream (a cudaStream_t passed as void*) all later work is enqueued on; NULL selects
  * the handle's own non-blocking stream. */
 int vfs_model_set_stream(vfs_model* m, void* stream);
-/* Simulation::SetGlobalParameters (src/simulation.cpp:46-50) and the parameter edits of
+/* Simulation::SetGlobalParameters (src/simulation.cpp:47-51) and the parameter edits of
  * DrawDebugUI (src/models/model.cpp:236-263, wcsph_with_boundary_model.cpp:119-141). Any
  * argument may be NULL. n_particles is ignored (the capacity is fixed at create). */
 int vfs_model_set_parameters(vfs_model* m, const vfs_sim_params* sim, const vfs_sph_params* sph,
@@ -125,8 +141,13 @@ uint32_t vfs_model_num_particles(const vfs_model* m);
 int vfs_model_add_boundary_object(vfs_model* m, const vfs_boundary_object* obj);
 /* The same from an analytic shape: SDF grid and 16^3-point Gauss-Legendre volume map are
  * generated on the GPU over the shape's box grown by a margin of 8h
- * (src/util/mesh_sdf.cpp:69-86 with margin 8h from generic_scene.cpp:101). */
+ * (MeshSDF::Build, src/util/mesh_sdf.cpp:28-44, with margin 8h from generic_scene.cpp:100). */
 int vfs_model_add_analytic_object(vfs_model* m, const vfs_analytic_object* obj);
+/* The same for a triangle mesh (GenericScene::AddBoundaryObject, src/scenes/generic_scene.cpp:89-124):
+ * the SDF grid holds the mesh's signed distance (nearest triangle through a BVH, sign from
+ * angle-weighted pseudonormals; SignedDistanceToMesh, src/util/geometry.cpp:267-328) at the nodes
+ * of the mesh bounds grown by 8h, and the volume map integrates it, both on the GPU. */
+int vfs_model_add_mesh_object(vfs_model* m, const vfs_mesh_object* obj);
 uint32_t vfs_model_num_boundary_objects(const vfs_model* m);
 /* Reads back boundary object idx: matrices and box into *info (grid pointers set to NULL), and
  * the grids into sdf_out / vm_out when they are not NULL. */
@@ -247,6 +268,7 @@ int vfs_batch_set_scene_parameters(vfs_batch* b, int32_t scene, const vfs_sim_pa
                                    const vfs_sph_params* sph, const vfs_wcsph_params* wcsph);
 int vfs_batch_add_boundary_object(vfs_batch* b, int32_t scene, const vfs_boundary_object* obj);
 int vfs_batch_add_analytic_object(vfs_batch* b, int32_t scene, const vfs_analytic_object* obj);
+int vfs_batch_add_mesh_object(vfs_batch* b, int32_t scene, const vfs_mesh_object* obj);
 int vfs_batch_get_boundary_object(const vfs_batch* b, int32_t scene, uint32_t idx,
                                   vfs_boundary_object* info, float* sdf_out, float* vm_out);
 int vfs_batch_set_particle_state(vfs_batch* b, int32_t scene, const float* pos, const float* vel,
@@ -321,6 +343,12 @@ int vfs_sort_pairs(uint32_t* items, uint32_t* keys, uint32_t n, uint32_t max_val
  * looks up that array's device address (cudaGetSymbolAddress) and should come before any stream
  * capture. All calls share the array, so calls whose work overlaps on the GPU (other streams,
  * other threads) race; serialise them on one stream. */
+/* Signed distances (double) of n_points points (x, y, z floats) to a triangle mesh, computed on
+ * the GPU exactly as the mesh objects' SDF grids are (the primitive behind them). */
+int vfs_mesh_signed_distance(const float* vertices, uint32_t n_vertices, const uint32_t* triangles,
+                             uint32_t n_triangles, const float* points, uint32_t n_points,
+                             double* distances);
+
 /* ---- failure detection ----
  * Self-test of the radix sort's decoupled look-back wait (the sort's counterpart of the
  * reference's global-atomic scan, src/compute/sort.cpp:57-86, which has no wait to fail). 32

@@ -63,6 +63,9 @@ def load() -> C.CDLL:
         "vfs_oracle_gauss_legendre": (None, [C.c_int, _D, _D]),
         "vfs_oracle_volume_map": (C.c_int, [C.c_int, _D, C.c_float, _U, C.c_float, C.c_int, _F, _F,
                                             _F, _F]),
+        "vfs_oracle_mesh_distance": (C.c_int, [_F, C.c_uint32, _U, C.c_uint32, _F, C.c_uint32, _D]),
+        "vfs_oracle_mesh_volume_map": (C.c_int, [_F, C.c_uint32, _U, C.c_uint32, C.c_float, _U,
+                                                 C.c_float, C.c_int, _F, _F, _F, _F]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -130,6 +133,39 @@ def volume_map(shape: int, params, h: float, res, margin: float, quad_n: int = 1
                                       _fp(sdf), _fp(vm))
     if rc != 0:
         raise ValueError("oracle volume map rejected its arguments")
+    return bs, bp, sdf, vm
+
+
+def _mesh_args(vertices, triangles):
+    v = np.ascontiguousarray(vertices, np.float32).reshape(-1, 3)
+    t = np.ascontiguousarray(triangles, np.uint32).reshape(-1, 3)
+    return v, t
+
+
+def mesh_distance(vertices, triangles, points):
+    """Oracle signed distances (double) of points to a triangle mesh."""
+    v, t = _mesh_args(vertices, triangles)
+    p = np.ascontiguousarray(points, np.float32).reshape(-1, 3)
+    out = np.empty(len(p), np.float64)
+    rc = load().vfs_oracle_mesh_distance(_fp(v), len(v), _up(t), len(t), _fp(p), len(p), _dp(out))
+    if rc != 0:
+        raise ValueError("oracle rejected the mesh")
+    return out
+
+
+def mesh_volume_map(vertices, triangles, h: float, res, margin: float, quad_n: int = 16):
+    """Oracle SDF grid + volume map of a triangle mesh, with its grid box."""
+    v, t = _mesh_args(vertices, triangles)
+    r = np.asarray(res, np.uint32)
+    cnt = int(r[0]) * int(r[1]) * int(r[2])
+    bs = np.empty(3, np.float32)
+    bp = np.empty(3, np.float32)
+    sdf = np.empty(cnt, np.float32)
+    vm = np.empty(cnt, np.float32)
+    rc = load().vfs_oracle_mesh_volume_map(_fp(v), len(v), _up(t), len(t), h, _up(r), margin,
+                                           quad_n, _fp(bs), _fp(bp), _fp(sdf), _fp(vm))
+    if rc != 0:
+        raise ValueError("oracle rejected the mesh")
     return bs, bp, sdf, vm
 
 

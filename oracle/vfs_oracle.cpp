@@ -33,6 +33,7 @@
 #include <cstring>
 #include <limits>
 #include <memory>
+#include <map>
 #include <vector>
 
 #ifdef _OPENMP
@@ -573,7 +574,7 @@ struct Handle {
 };
 
 // ---- Volume maps from analytic SDFs (src/util/volume_map.cpp:9-54, discretization.cpp:16-57,
-// mesh_sdf.cpp:69-86, gaussian_quadrature.cpp:2293-2334) ----
+// mesh_sdf.cpp:28-44, gaussian_quadrature.cpp:2293-2334) ----
 
 // Gauss-Legendre nodes and weights on [-1, 1] by Newton iteration on P_n (own computation of
 // the published rule; checked against the reference's table in tests/golden).
@@ -643,6 +644,204 @@ struct KernelD {
     }
 };
 
+// A triangle mesh with the reference's pseudonormals (MeshPseudonormals::Build,
+// src/util/mesh_pseudonormals.cpp:11-88: face normals; vertex normals weighted by acos(|cos|) of
+// the corner angle; edge normals the normalised sum of the faces on the edge) and the
+// closest-point query of DistancePointToTriangle (src/util/geometry.cpp, Eberly's region method).
+struct OracleMesh {
+    struct V {
+        double x, y, z;
+    };
+    std::vector<V> p;
+    std::vector<uint32_t> t;
+    std::vector<V> fn, vn, en;  // en: 3 per triangle (edges 01, 12, 02)
+    float lo[3], hi[3];
+
+    static V sub(V a, V b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+    static double dot(V a, V b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+
+    bool build(const float* v, uint32_t nv, const uint32_t* tri, uint32_t nt) {
+        if (nv < 3 || nt < 1) return false;
+        for (uint32_t k = 0; k < 3 * nt; k++)
+            if (tri[k] >= nv) return false;
+        p.resize(nv);
+        for (uint32_t k = 0; k < nv; k++) p[k] = {v[3 * k], v[3 * k + 1], v[3 * k + 2]};
+        t.assign(tri, tri + 3 * (size_t)nt);
+        for (int a = 0; a < 3; a++) {
+            lo[a] = INFINITY;
+            hi[a] = -INFINITY;
+        }
+        for (uint32_t k = 0; k < 3 * nt; k++) {
+            const float q[3] = {v[3 * t[k]], v[3 * t[k] + 1], v[3 * t[k] + 2]};
+            for (int a = 0; a < 3; a++) {
+                lo[a] = std::min(lo[a], q[a]);
+                hi[a] = std::max(hi[a], q[a]);
+            }
+        }
+        // Float math like the reference's glm::vec3 pseudonormals.
+        struct F {
+            float x, y, z;
+        };
+        auto fs = [](F a, F b) { return F{a.x - b.x, a.y - b.y, a.z - b.z}; };
+        auto fd = [](F a, F b) { return a.x * b.x + a.y * b.y + a.z * b.z; };
+        auto fnorm = [&](F a) {
+            const float l = std::sqrt(fd(a, a));
+            return F{a.x / l, a.y / l, a.z / l};
+        };
+        auto P = [&](uint32_t i) { return F{v[3 * i], v[3 * i + 1], v[3 * i + 2]}; };
+        std::vector<F> vacc(nv, F{0, 0, 0});
+        std::map<uint64_t, F> edges;
+        std::vector<F> fnf(nt);
+        auto key = [&](uint32_t a, uint32_t b) { return (uint64_t)std::max(a, b) + (uint64_t)std::min(a, b) * nv; };
+        for (uint32_t i = 0; i < nt; i++) {
+            const uint32_t ia = t[3 * i], ib = t[3 * i + 1], ic = t[3 * i + 2];
+            const F a = P(ia), b = P(ib), c = P(ic);
+            const F e1 = fs(b, a), e2 = fs(c, a);
+            const F cr = {e1.y * e2.z - e1.z * e2.y, e1.z * e2.x - e1.x * e2.z, e1.x * e2.y - e1.y * e2.x};
+            if (!(fd(cr, cr) > 0.0f)) return false;
+            const F n = fnorm(cr);
+            fnf[i] = n;
+            const float a0 = std::acos(std::fabs(fd(fnorm(fs(b, a)), fnorm(fs(c, a)))));
+            const float a1 = std::acos(std::fabs(fd(fnorm(fs(a, b)), fnorm(fs(c, b)))));
+            const float a2 = std::acos(std::fabs(fd(fnorm(fs(b, c)), fnorm(fs(a, c)))));
+            for (auto pr : {std::make_pair(ia, a0), std::make_pair(ib, a1), std::make_pair(ic, a2)}) {
+                F& q = vacc[pr.first];
+                q = F{q.x + pr.second * n.x, q.y + pr.second * n.y, q.z + pr.second * n.z};
+            }
+            for (auto e : {std::make_pair(ia, ib), std::make_pair(ib, ic), std::make_pair(ia, ic)}) {
+                F& q = edges[key(e.first, e.second)];
+                q = F{q.x + n.x, q.y + n.y, q.z + n.z};
+            }
+        }
+        fn.resize(nt);
+        en.resize(3 * (size_t)nt);
+        vn.assign(nv, V{0, 0, 0});
+        for (uint32_t k = 0; k < nv; k++)
+            if (fd(vacc[k], vacc[k]) > 0.0f) {
+                const F n = fnorm(vacc[k]);
+                vn[k] = {n.x, n.y, n.z};
+            }
+        for (uint32_t i = 0; i < nt; i++) {
+            fn[i] = {fnf[i].x, fnf[i].y, fnf[i].z};
+            const uint32_t ia = t[3 * i], ib = t[3 * i + 1], ic = t[3 * i + 2];
+            const uint64_t ks[3] = {key(ia, ib), key(ib, ic), key(ia, ic)};
+            for (int e = 0; e < 3; e++) {
+                const F s = edges[ks[e]];
+                const F n = fd(s, s) > 0.0f ? fnorm(s) : fnf[i];
+                en[3 * i + e] = {n.x, n.y, n.z};
+            }
+        }
+        return true;
+    }
+
+    // Squared distance and closest entity (0-2 vertices, 3 E01, 4 E12, 5 E02, 6 face).
+    static double closest(V pt, V v0, V v1, V v2, double& s, double& u, int& ent) {
+        const V e0 = sub(v1, v0), e1 = sub(v2, v0), d = sub(v0, pt);
+        const double a00 = dot(e0, e0), a01 = dot(e0, e1), a11 = dot(e1, e1);
+        const double b0 = dot(d, e0), b1 = dot(d, e1);
+        const double det = std::max(a00 * a11 - a01 * a01, 0.0);
+        s = a01 * b1 - a11 * b0;
+        u = a01 * b0 - a00 * b1;
+        auto edge_s0 = [&]() {  // s = 0: t in [0, 1]
+            s = 0;
+            if (b1 >= 0) { u = 0; ent = 0; }
+            else if (-b1 >= a11) { u = 1; ent = 2; }
+            else { u = -b1 / a11; ent = 5; }
+        };
+        auto edge_t0 = [&]() {  // t = 0: s in [0, 1]
+            u = 0;
+            if (b0 >= 0) { s = 0; ent = 0; }
+            else if (-b0 >= a00) { s = 1; ent = 1; }
+            else { s = -b0 / a00; ent = 3; }
+        };
+        if (s + u <= det) {
+            if (s < 0) {
+                if (u < 0) {
+                    if (b0 < 0) {
+                        u = 0;
+                        if (-b0 >= a00) { s = 1; ent = 1; }
+                        else { s = -b0 / a00; ent = 3; }
+                    } else {
+                        edge_s0();
+                    }
+                } else {
+                    edge_s0();
+                }
+            } else if (u < 0) {
+                edge_t0();
+            } else {
+                s /= det;
+                u /= det;
+                ent = 6;
+            }
+        } else if (s < 0) {
+            const double t0 = a01 + b0, t1 = a11 + b1;
+            if (t1 > t0) {
+                const double num = t1 - t0, den = a00 - 2 * a01 + a11;
+                if (num >= den) { s = 1; u = 0; ent = 1; }
+                else { s = num / den; u = 1 - s; ent = 4; }
+            } else {
+                s = 0;
+                if (t1 <= 0) { u = 1; ent = 2; }
+                else if (b1 >= 0) { u = 0; ent = 0; }
+                else { u = -b1 / a11; ent = 5; }
+            }
+        } else if (u < 0) {
+            const double t0 = a01 + b1, t1 = a00 + b0;
+            if (t1 > t0) {
+                const double num = t1 - t0, den = a00 - 2 * a01 + a11;
+                if (num >= den) { u = 1; s = 0; ent = 2; }
+                else { u = num / den; s = 1 - u; ent = 4; }
+            } else {
+                u = 0;
+                if (t1 <= 0) { s = 1; ent = 1; }
+                else if (b0 >= 0) { s = 0; ent = 0; }
+                else { s = -b0 / a00; ent = 3; }
+            }
+        } else {
+            const double num = a11 + b1 - a01 - b0;
+            if (num <= 0) { s = 0; u = 1; ent = 2; }
+            else {
+                const double den = a00 - 2 * a01 + a11;
+                if (num >= den) { s = 1; u = 0; ent = 1; }
+                else { s = num / den; u = 1 - s; ent = 4; }
+            }
+        }
+        const V q = {v0.x + s * e0.x + u * e1.x - pt.x, v0.y + s * e0.y + u * e1.y - pt.y,
+                     v0.z + s * e0.z + u * e1.z - pt.z};
+        return dot(q, q);
+    }
+
+    double signed_distance(float x, float y, float z) const {
+        const V pt = {x, y, z};
+        double best = INFINITY, bs = 0, bu = 0;
+        size_t bt = 0;
+        int be = 6;
+        for (size_t i = 0; i < t.size() / 3; i++) {
+            double s, u;
+            int ent;
+            const double d2 = closest(pt, p[t[3 * i]], p[t[3 * i + 1]], p[t[3 * i + 2]], s, u, ent);
+            if (d2 < best) {
+                best = d2;
+                bt = i;
+                be = ent;
+                bs = s;
+                bu = u;
+            }
+        }
+        const V a = p[t[3 * bt]], b = p[t[3 * bt + 1]], c = p[t[3 * bt + 2]];
+        const V cp = {a.x + bs * (b.x - a.x) + bu * (c.x - a.x), a.y + bs * (b.y - a.y) + bu * (c.y - a.y),
+                      a.z + bs * (b.z - a.z) + bu * (c.z - a.z)};
+        V n;
+        if (be <= 2) n = vn[t[3 * bt + be]];
+        else if (be <= 5) n = en[3 * bt + (be - 3)];
+        else n = fn[bt];
+        const double d = std::sqrt(best);
+        return dot(sub(pt, cp), n) >= 0 ? d : -d;
+    }
+};
+
+
 template <typename T>
 void set_state_t(Model<T>* m, const float* pos, const float* vel, const uint32_t* ids) {
     for (uint32_t i = 0; i < m->n; i++) {
@@ -688,6 +887,89 @@ void get_fields_t(Model<T>* m, float* acc, float* bdens, float* bgrad) {
 }
 
 }  // namespace
+
+// Grid box, SDF grid and volume map of a shape given by its local bounds and signed-distance
+// function, following MeshSDF::Build (src/util/mesh_sdf.cpp:28-44, tolerance 0, margin passed in:
+// the scene uses 8h, src/scenes/generic_scene.cpp:88-124), LinearLagrangeDiscreteGrid::Init
+// (src/util/discretization.cpp:16-32) and GenerateVolumeMap (src/util/volume_map.cpp:9-54) with
+// a 16-point Gauss-Legendre rule per axis (gaussian_quadrature.cpp:2293-2334). The float
+// roundings of the reference (node and quadrature points passed as glm::vec3, the grid step
+// computed in float) are kept.
+template <typename Sdf>
+int volume_map_of(const Sdf& sdf_fn, const float lo[3], const float hi[3], float support_radius,
+                  const uint32_t* res, float margin, int quad_n, float* box_size_out,
+                  float* box_pos_out, float* sdf_out, float* vm_out) {
+    if (res[0] < 2 || res[1] < 2 || res[2] < 2) return -1;
+    if (quad_n < 2) quad_n = 2;
+    if (quad_n > 64) quad_n = 64;
+    float bpos[3], bsize[3];
+    for (int a = 0; a < 3; a++) {
+        const float size = hi[a] - lo[a];
+        bsize[a] = size + 2.0f * margin;
+        bpos[a] = lo[a] - margin;
+        box_size_out[a] = bsize[a];
+        box_pos_out[a] = bpos[a];
+    }
+    float dmin[3], dmax[3];
+    double step[3];
+    for (int a = 0; a < 3; a++) {
+        dmin[a] = bpos[a];
+        dmax[a] = bpos[a] + bsize[a];
+        step[a] = (double)((dmax[a] - dmin[a]) / (float)(res[a] - 1u));
+    }
+    std::vector<double> gx(quad_n), gw(quad_n);
+    gauss_legendre(quad_n, gx.data(), gw.data());
+    const float sr = support_radius;
+    const KernelD kern((double)sr);
+    // Integration domain [-h, h]^3: c0 = 0.5 (max - min), c1 = 0.5 (max + min) (both float
+    // vectors converted to double).
+    const double c0 = 0.5 * (double)(sr - (-sr));
+    const double c1 = 0.5 * (double)(sr + (-sr));
+    const int64_t total = (int64_t)res[0] * res[1] * res[2];
+#pragma omp parallel for schedule(dynamic, 16)
+    for (int64_t lin = 0; lin < total; lin++) {
+        const uint32_t i = (uint32_t)(lin % res[0]);
+        const uint32_t j = (uint32_t)((lin / res[0]) % res[1]);
+        const uint32_t k = (uint32_t)(lin / ((int64_t)res[0] * res[1]));
+        const double ex = step[0] * (double)i + (double)dmin[0];
+        const double ey = step[1] * (double)j + (double)dmin[1];
+        const double ez = step[2] * (double)k + (double)dmin[2];
+        const float fx = (float)ex, fy = (float)ey, fz = (float)ez;  // func(const glm::vec3&)
+        const double node_sdf = sdf_fn(fx, fy, fz);
+        sdf_out[lin] = (float)node_sdf;
+        double value = 0.0;
+        if (!(node_sdf > 2.0 * (double)sr)) {
+            double integral = 0.0;
+            for (int a = 0; a < quad_n; a++) {
+                const double wa = gw[a];
+                for (int b = 0; b < quad_n; b++) {
+                    const double wab = wa * gw[b];
+                    for (int cidx = 0; cidx < quad_n; cidx++) {
+                        const double wabc = wab * gw[cidx];
+                        const float xi_x = (float)(c0 * gx[a] + c1);
+                        const float xi_y = (float)(c0 * gx[b] + c1);
+                        const float xi_z = (float)(c0 * gx[cidx] + c1);
+                        double f = 0.0;
+                        const float len2 = xi_x * xi_x + xi_y * xi_y + xi_z * xi_z;
+                        if (!(len2 > sr * sr)) {
+                            const float px = fx + xi_x, py = fy + xi_y, pz = fz + xi_z;
+                            const double di = sdf_fn(px, py, pz);
+                            if (di <= 0.0)
+                                f = 1.0;
+                            else if (di < (double)sr)
+                                f = kern.W(di) / kern.w_zero;
+                        }
+                        integral += wabc * f;
+                    }
+                }
+            }
+            integral *= c0 * c0 * c0;
+            value = 0.8 * integral;
+        }
+        vm_out[lin] = (float)value;
+    }
+    return 0;
+}
 
 extern "C" {
 
@@ -838,88 +1120,44 @@ int32_t vfs_oracle_cell_coord(float x, float h) { return cell_coord<float>(x, h)
 
 void vfs_oracle_gauss_legendre(int n, double* x, double* w) { gauss_legendre(n, x, w); }
 
-// Grid box, SDF grid and volume map of an analytic shape, following MeshSDF::Build
-// (src/util/mesh_sdf.cpp:69-86, tolerance 0, margin passed in: the scene uses 8h,
-// src/scenes/generic_scene.cpp:88-124), LinearLagrangeDiscreteGrid::Init
-// (src/util/discretization.cpp:16-32) and GenerateVolumeMap (src/util/volume_map.cpp:9-54)
-// with a 16-point Gauss-Legendre rule per axis (gaussian_quadrature.cpp:2293-2334). The float
-// roundings of the reference (node and quadrature points passed as glm::vec3, the grid step
-// computed in float) are kept.
+// Grid box, SDF grid and volume map of an analytic shape (volume_map_of above).
 int vfs_oracle_volume_map(int kind, const double* shape_params, float support_radius,
                           const uint32_t* res, float margin, int quad_n, float* box_size_out,
                           float* box_pos_out, float* sdf_out, float* vm_out) {
-    if (res[0] < 2 || res[1] < 2 || res[2] < 2) return -1;
-    if (quad_n < 2) quad_n = 2;
-    if (quad_n > 64) quad_n = 64;
     float lo[3], hi[3];
     shape_aabb(kind, shape_params, lo, hi);
-    float bpos[3], bsize[3];
-    for (int a = 0; a < 3; a++) {
-        const float size = hi[a] - lo[a];
-        bsize[a] = size + 2.0f * margin;
-        bpos[a] = lo[a] - margin;
-        box_size_out[a] = bsize[a];
-        box_pos_out[a] = bpos[a];
-    }
-    float dmin[3], dmax[3];
-    double step[3];
-    for (int a = 0; a < 3; a++) {
-        dmin[a] = bpos[a];
-        dmax[a] = bpos[a] + bsize[a];
-        step[a] = (double)((dmax[a] - dmin[a]) / (float)(res[a] - 1u));
-    }
-    std::vector<double> gx(quad_n), gw(quad_n);
-    gauss_legendre(quad_n, gx.data(), gw.data());
-    const float sr = support_radius;
-    const KernelD kern((double)sr);
-    // Integration domain [-h, h]^3: c0 = 0.5 (max - min), c1 = 0.5 (max + min) (both float
-    // vectors converted to double).
-    const double c0 = 0.5 * (double)(sr - (-sr));
-    const double c1 = 0.5 * (double)(sr + (-sr));
-    const int64_t total = (int64_t)res[0] * res[1] * res[2];
-#pragma omp parallel for schedule(dynamic, 16)
-    for (int64_t lin = 0; lin < total; lin++) {
-        const uint32_t i = (uint32_t)(lin % res[0]);
-        const uint32_t j = (uint32_t)((lin / res[0]) % res[1]);
-        const uint32_t k = (uint32_t)(lin / ((int64_t)res[0] * res[1]));
-        const double ex = step[0] * (double)i + (double)dmin[0];
-        const double ey = step[1] * (double)j + (double)dmin[1];
-        const double ez = step[2] * (double)k + (double)dmin[2];
-        const float fx = (float)ex, fy = (float)ey, fz = (float)ez;  // func(const glm::vec3&)
-        const double node_sdf = analytic_sdf(kind, shape_params, fx, fy, fz);
-        sdf_out[lin] = (float)node_sdf;
-        double value = 0.0;
-        if (!(node_sdf > 2.0 * (double)sr)) {
-            double integral = 0.0;
-            for (int a = 0; a < quad_n; a++) {
-                const double wa = gw[a];
-                for (int b = 0; b < quad_n; b++) {
-                    const double wab = wa * gw[b];
-                    for (int cidx = 0; cidx < quad_n; cidx++) {
-                        const double wabc = wab * gw[cidx];
-                        const float xi_x = (float)(c0 * gx[a] + c1);
-                        const float xi_y = (float)(c0 * gx[b] + c1);
-                        const float xi_z = (float)(c0 * gx[cidx] + c1);
-                        double f = 0.0;
-                        const float len2 = xi_x * xi_x + xi_y * xi_y + xi_z * xi_z;
-                        if (!(len2 > sr * sr)) {
-                            const float px = fx + xi_x, py = fy + xi_y, pz = fz + xi_z;
-                            const double di = analytic_sdf(kind, shape_params, px, py, pz);
-                            if (di <= 0.0)
-                                f = 1.0;
-                            else if (di < (double)sr)
-                                f = kern.W(di) / kern.w_zero;
-                        }
-                        integral += wabc * f;
-                    }
-                }
-            }
-            integral *= c0 * c0 * c0;
-            value = 0.8 * integral;
-        }
-        vm_out[lin] = (float)value;
-    }
+    auto fn = [&](float x, float y, float z) { return analytic_sdf(kind, shape_params, x, y, z); };
+    return volume_map_of(fn, lo, hi, support_radius, res, margin, quad_n, box_size_out,
+                         box_pos_out, sdf_out, vm_out);
+}
+
+// Signed distances of points to a triangle mesh (brute force over the triangles), restating
+// SignedDistanceToMesh (src/util/geometry.cpp:267-328) with the pseudonormals of
+// MeshPseudonormals::Build (src/util/mesh_pseudonormals.cpp:11-88). Returns -1 for a mesh with a
+// degenerate triangle or an out-of-range index.
+int vfs_oracle_mesh_distance(const float* vertices, uint32_t n_vertices, const uint32_t* triangles,
+                             uint32_t n_triangles, const float* points, uint32_t n_points,
+                             double* out) {
+    OracleMesh mesh;
+    if (!mesh.build(vertices, n_vertices, triangles, n_triangles)) return -1;
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < (int64_t)n_points; i++)
+        out[i] = mesh.signed_distance(points[3 * i], points[3 * i + 1], points[3 * i + 2]);
     return 0;
+}
+
+// Grid box, SDF grid and volume map of a triangle mesh (GenericScene::AddBoundaryObject,
+// src/scenes/generic_scene.cpp:89-124), all in double like the reference.
+int vfs_oracle_mesh_volume_map(const float* vertices, uint32_t n_vertices,
+                               const uint32_t* triangles, uint32_t n_triangles,
+                               float support_radius, const uint32_t* res, float margin,
+                               int quad_n, float* box_size_out, float* box_pos_out,
+                               float* sdf_out, float* vm_out) {
+    OracleMesh mesh;
+    if (!mesh.build(vertices, n_vertices, triangles, n_triangles)) return -1;
+    auto fn = [&](float x, float y, float z) { return mesh.signed_distance(x, y, z); };
+    return volume_map_of(fn, mesh.lo, mesh.hi, support_radius, res, margin, quad_n, box_size_out,
+                         box_pos_out, sdf_out, vm_out);
 }
 
 }  // extern "C"

@@ -86,6 +86,21 @@ _I = C.c_int
 _U32 = C.c_uint32
 
 # name -> (restype, argtypes)
+class MeshObject(C.Structure):
+    _fields_ = [
+        ("obj_path", C.c_char_p),
+        ("vertices", C.POINTER(C.c_float)),
+        ("n_vertices", C.c_uint32),
+        ("triangles", C.POINTER(C.c_uint32)),
+        ("n_triangles", C.c_uint32),
+        ("position", C.c_float * 3),
+        ("rotation_angle_deg", C.c_float),
+        ("rotation_axis", C.c_float * 3),
+        ("scale", C.c_float * 3),
+        ("resolution", C.c_uint32 * 3),
+    ]
+
+
 class TuneConfig(C.Structure):
     _fields_ = [("sort_digit_bits", C.c_int32), ("sort_tile_items", C.c_int32),
                 ("nbr_block", C.c_int32), ("nbr_min_blocks", C.c_int32), ("cell_block", C.c_int32)]
@@ -148,6 +163,11 @@ SIGNATURES = {
     "vfs_model_get_tune_config": (_I, [_P, C.POINTER(TuneConfig)]),
     "vfs_tune_cache_save": (_I, [C.c_char_p]),
     "vfs_model_export_state": (_I, [_P, C.c_char_p]),
+    "vfs_model_add_mesh_object": (_I, [_P, C.POINTER(MeshObject)]),
+    "vfs_batch_add_mesh_object": (_I, [_P, C.c_int32, C.POINTER(MeshObject)]),
+    "vfs_mesh_signed_distance": (_I, [C.POINTER(C.c_float), C.c_uint32, C.POINTER(C.c_uint32),
+                                      C.c_uint32, C.POINTER(C.c_float), C.c_uint32,
+                                      C.POINTER(C.c_double)]),
     "vfs_model_render_particles": (_I, [_P, C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_int32,
                                         C.c_int32, C.c_float, C.c_float, C.c_float,
                                         C.POINTER(C.c_uint8), C.POINTER(C.c_float)]),

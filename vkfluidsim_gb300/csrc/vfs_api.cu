@@ -24,6 +24,7 @@
 #include "vfs_cuda.h"
 #include "vfs_internal.h"
 #include "vfs_model.h"
+#include "vfs_mesh.h"
 #include "vfs_volume_map.h"
 
 namespace vfs {
@@ -626,7 +627,7 @@ int Model::add_analytic(uint32_t scene, const vfs_analytic_object& a) {
         info.rotation[k] = (float)R.a[k];
     }
     // MeshSDF::Build box: shape AABB grown by tolerance (0) + margin (8h), in float
-    // (src/util/mesh_sdf.cpp:69-86, src/scenes/generic_scene.cpp:100).
+    // (src/util/mesh_sdf.cpp:28-44, src/scenes/generic_scene.cpp:100).
     const float margin = (float)(8.0 * (double)h);
     float lo[3], hi[3];
     for (int k = 0; k < 3; k++) {
@@ -665,6 +666,134 @@ int Model::add_analytic(uint32_t scene, const vfs_analytic_object& a) {
         return fail(VFS_ERR_CUDA, std::string("volume map: ") + cudaGetErrorString(e));
     }
     const int rc = add_object(scene, info, d_sdf, d_vm);
+    cudaFree(d_sdf);
+    cudaFree(d_vm);
+    return rc;
+}
+
+namespace {
+
+// Device copy of a host mesh; free() releases it.
+struct MeshUpload {
+    MeshDev dev{};
+    void* blocks[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    void free() {
+        for (void*& b : blocks) {
+            if (b) cudaFree(b);
+            b = nullptr;
+        }
+    }
+};
+
+template <typename T>
+std::vector<T> rows4(const std::vector<T>& v, size_t width) {
+    std::vector<T> out(v.size() / width * 4, T(0));
+    for (size_t r = 0; r < v.size() / width; r++)
+        for (size_t c = 0; c < width; c++) out[4 * r + c] = v[width * r + c];
+    return out;
+}
+
+int upload_mesh(const MeshHost& mh, MeshUpload& up) {
+    const auto pos4 = rows4(mh.pos, 3);
+    const auto tri4 = rows4(mh.tri, 3);
+    const auto tn4 = rows4(mh.tri_normal, 3);
+    const auto en4 = rows4(mh.edge_normal, 3);
+    const auto vn4 = rows4(mh.vertex_normal, 3);
+    const void* src[6] = {pos4.data(), tri4.data(), tn4.data(), en4.data(), vn4.data(), mh.nodes.data()};
+    const size_t bytes[6] = {pos4.size() * 4, tri4.size() * 4, tn4.size() * 4, en4.size() * 4,
+                             vn4.size() * 4, mh.nodes.size() * sizeof(BvhNode)};
+    for (int k = 0; k < 6; k++) {
+        cudaError_t e = cudaMalloc(&up.blocks[k], bytes[k]);
+        if (e == cudaSuccess) e = cudaMemcpy(up.blocks[k], src[k], bytes[k], cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) {
+            up.free();
+            return fail(VFS_ERR_CUDA, std::string("mesh upload: ") + cudaGetErrorString(e));
+        }
+    }
+    up.dev.pos = static_cast<const float4*>(up.blocks[0]);
+    up.dev.tri = static_cast<const uint4*>(up.blocks[1]);
+    up.dev.tri_normal = static_cast<const float4*>(up.blocks[2]);
+    up.dev.edge_normal = static_cast<const float4*>(up.blocks[3]);
+    up.dev.vertex_normal = static_cast<const float4*>(up.blocks[4]);
+    up.dev.nodes = static_cast<const BvhNode*>(up.blocks[5]);
+    return VFS_OK;
+}
+
+}  // namespace
+
+// GenericScene::AddBoundaryObject for an OBJ mesh (src/scenes/generic_scene.cpp:89-124): the mesh
+// SDF box is the mesh bounds grown by tolerance 0 + margin 8h (MeshSDF::Init/Build,
+// src/util/mesh_sdf.cpp:14-44), the SDF grid holds the mesh's signed distance at the nodes and the
+// volume map integrates it (GenerateVolumeMap, src/util/volume_map.cpp:9-54), both on the GPU.
+int Model::add_mesh(uint32_t scene, const vfs_mesh_object& a) {
+    if (scene >= scenes.size()) return fail(VFS_ERR_INVALID_ARGUMENT, "scene index out of range");
+    for (int k = 0; k < 3; k++)
+        if (a.resolution[k] < 2) return fail(VFS_ERR_INVALID_ARGUMENT, "grid resolution must be >= 2 per axis");
+    std::vector<float> pos;
+    std::vector<uint32_t> tri;
+    std::string err;
+    if (a.obj_path) {
+        if (!load_obj(a.obj_path, pos, tri, err)) return fail(VFS_ERR_IO, err);
+    } else {
+        if (!a.vertices || !a.triangles) return fail(VFS_ERR_INVALID_ARGUMENT, "mesh without an OBJ path or arrays");
+        pos.assign(a.vertices, a.vertices + 3 * (size_t)a.n_vertices);
+        tri.assign(a.triangles, a.triangles + 3 * (size_t)a.n_triangles);
+    }
+    MeshHost mh;
+    if (!build_mesh(pos, tri, mh, err)) return fail(VFS_ERR_INVALID_ARGUMENT, "mesh: " + err);
+    const float h = scenes[scene].sim.smooth_radius;
+    M4 T = m4_identity();
+    T.a[12] = a.position[0];
+    T.a[13] = a.position[1];
+    T.a[14] = a.position[2];
+    const M4 R = m4_rotation(a.rotation_angle_deg, a.rotation_axis);
+    M4 S = m4_identity();
+    for (int k = 0; k < 3; k++) S.a[k * 5] = (a.scale[k] == 0.0f) ? 1.0 : (double)a.scale[k];
+    const M4 W = m4_mul(m4_mul(T, R), S);
+    M4 Wi;
+    if (!m4_inverse(W, Wi)) return fail(VFS_ERR_INVALID_ARGUMENT, "object transform is singular");
+    vfs_boundary_object info{};
+    for (int k = 0; k < 16; k++) {
+        info.transform[k] = (float)Wi.a[k];
+        info.rotation[k] = (float)R.a[k];
+    }
+    const float margin = (float)(0.0 + 8.0 * (double)h);
+    for (int k = 0; k < 3; k++) {
+        info.box_size[k] = (mh.hi[k] - mh.lo[k]) + 2.0f * margin;
+        info.box_pos[k] = mh.lo[k] - margin;
+        info.resolution[k] = a.resolution[k];
+    }
+    VolumeMapParams vp{};
+    vp.h = h;
+    for (int k = 0; k < 3; k++) {
+        vp.res[k] = a.resolution[k];
+        vp.dmin[k] = info.box_pos[k];
+        const float dmax = info.box_pos[k] + info.box_size[k];
+        vp.step[k] = (double)((dmax - vp.dmin[k]) / (float)(a.resolution[k] - 1u));
+    }
+    vp.qn = 16;
+    gauss_legendre_nodes(vp.qn, vp.gx, vp.gw);
+    vp.c0 = 0.5 * (double)(h - (-h));
+    vp.c1 = 0.5 * (double)(h + (-h));
+    const double hd = (double)h;
+    vp.w_factor = 8.0 / (pi_d() * hd * hd * hd);
+    vp.full_ball = volume_map_full_ball(vp);
+    MeshUpload up;
+    int rc = upload_mesh(mh, up);
+    if (rc) return rc;
+    const size_t cnt = (size_t)a.resolution[0] * a.resolution[1] * a.resolution[2];
+    float *d_sdf = nullptr, *d_vm = nullptr;
+    cudaError_t e = cudaMalloc(&d_sdf, cnt * 4);
+    if (e == cudaSuccess) e = cudaMalloc(&d_vm, cnt * 4);
+    if (e == cudaSuccess) e = launch_mesh_volume_map(vp, up.dev, d_sdf, d_vm, stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+    up.free();
+    if (e != cudaSuccess) {
+        if (d_sdf) cudaFree(d_sdf);
+        if (d_vm) cudaFree(d_vm);
+        return fail(VFS_ERR_CUDA, std::string("mesh volume map: ") + cudaGetErrorString(e));
+    }
+    rc = add_object(scene, info, d_sdf, d_vm);
     cudaFree(d_sdf);
     cudaFree(d_vm);
     return rc;
@@ -863,6 +992,40 @@ int vfs_model_add_analytic_object(vfs_model* h, const vfs_analytic_object* obj) 
     return m.add_analytic(0, *obj);
 }
 
+int vfs_model_add_mesh_object(vfs_model* h, const vfs_mesh_object* obj) {
+    VFS_HANDLE(h);
+    if (!obj) return fail(VFS_ERR_INVALID_ARGUMENT, "NULL object");
+    return m.add_mesh(0, *obj);
+}
+
+int vfs_mesh_signed_distance(const float* vertices, uint32_t n_vertices, const uint32_t* triangles,
+                             uint32_t n_triangles, const float* points, uint32_t n_points,
+                             double* distances) {
+    if (!vertices || !triangles || (n_points && (!points || !distances)))
+        return fail(VFS_ERR_INVALID_ARGUMENT, "NULL argument");
+    std::vector<float> pos(vertices, vertices + 3 * (size_t)n_vertices);
+    std::vector<uint32_t> tri(triangles, triangles + 3 * (size_t)n_triangles);
+    vfs::MeshHost mh;
+    std::string err;
+    if (!vfs::build_mesh(pos, tri, mh, err)) return fail(VFS_ERR_INVALID_ARGUMENT, "mesh: " + err);
+    if (n_points == 0) return VFS_OK;
+    vfs::MeshUpload up;
+    int rc = vfs::upload_mesh(mh, up);
+    if (rc) return rc;
+    float* dp = nullptr;
+    double* dd = nullptr;
+    cudaError_t e = cudaMalloc(&dp, (size_t)n_points * 12);
+    if (e == cudaSuccess) e = cudaMalloc(&dd, (size_t)n_points * 8);
+    if (e == cudaSuccess) e = cudaMemcpy(dp, points, (size_t)n_points * 12, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = vfs::launch_mesh_distance(up.dev, dp, n_points, dd, nullptr);
+    if (e == cudaSuccess) e = cudaMemcpy(distances, dd, (size_t)n_points * 8, cudaMemcpyDeviceToHost);
+    up.free();
+    if (dp) cudaFree(dp);
+    if (dd) cudaFree(dd);
+    if (e != cudaSuccess) return fail(VFS_ERR_CUDA, std::string("mesh distance: ") + cudaGetErrorString(e));
+    return VFS_OK;
+}
+
 uint32_t vfs_model_num_boundary_objects(const vfs_model* h) {
     return h && h->m ? (uint32_t)h->m->scenes[0].objects.size() : 0u;
 }
@@ -1035,6 +1198,12 @@ int vfs_batch_add_analytic_object(vfs_batch* h, int32_t scene, const vfs_analyti
     VFS_HANDLE(h);
     if (!obj) return fail(VFS_ERR_INVALID_ARGUMENT, "NULL object");
     return m.add_analytic((uint32_t)scene, *obj);
+}
+
+int vfs_batch_add_mesh_object(vfs_batch* h, int32_t scene, const vfs_mesh_object* obj) {
+    VFS_HANDLE(h);
+    if (!obj || scene < 0) return fail(VFS_ERR_INVALID_ARGUMENT, "NULL object or negative scene");
+    return m.add_mesh((uint32_t)scene, *obj);
 }
 
 int vfs_batch_get_boundary_object(const vfs_batch* h, int32_t scene, uint32_t idx,

@@ -102,6 +102,7 @@ struct Model {
     int add_object(uint32_t scene, const vfs_boundary_object& src, const float* d_sdf,
                    const float* d_vm);
     int add_analytic(uint32_t scene, const vfs_analytic_object& a);
+    int add_mesh(uint32_t scene, const vfs_mesh_object& a);
 };
 
 // Builds a model of the given scenes (sizes from each sph.n_particles) and allocates it.

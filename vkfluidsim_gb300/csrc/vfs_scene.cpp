@@ -325,6 +325,7 @@ int vfs_scene_load(const char* json_path, const char* resources_dir, vfs_model**
     vfs_wcsph_params wc{};
     std::vector<FluidBlock> blocks;
     std::vector<vfs_analytic_object> objects;
+    std::vector<std::string> mesh_paths;  // per object: the OBJ path, or empty for an analytic shape
     try {
         // Simulation::Init defaults (src/simulation.cpp:20-27), overridden when present.
         sim.gravity[0] = 0.0f;
@@ -387,14 +388,15 @@ int vfs_scene_load(const char* json_path, const char* resources_dir, vfs_model**
                 } else {
                     throw SceneError{"unknown shape type '" + type + "'"};
                 }
-            } else {
-                const Json& rp = need(o, "resourcePath");
-                std::string path = rp.str;
+            }
+            std::string path;
+            if (!o.get("shape")) {
+                // Platform::Info::ResourcePath: the path is relative to the resources directory.
+                path = need(o, "resourcePath").str;
                 if (resources_dir && *resources_dir) path = std::string(resources_dir) + "/" + path;
-                throw SceneError{"OBJ-mesh boundary objects are not supported by this build ('" + path +
-                                 "'); use an analytic 'shape'"};
             }
             objects.push_back(a);
+            mesh_paths.push_back(path);
         }
     } catch (const SceneError& e) {
         return fail(VFS_ERR_PARSE, "scene JSON: " + e.msg);
@@ -404,8 +406,22 @@ int vfs_scene_load(const char* json_path, const char* resources_dir, vfs_model**
     int rc = vfs_model_create(&sim, &sph, &wc, &h);
     if (rc) return rc;
     Model* m = vfs_model_impl(h);
-    for (const auto& a : objects) {
-        rc = m->add_analytic(0, a);
+    for (size_t k = 0; k < objects.size(); k++) {
+        const vfs_analytic_object& a = objects[k];
+        if (mesh_paths[k].empty()) {
+            rc = m->add_analytic(0, a);
+        } else {
+            vfs_mesh_object mo{};
+            mo.obj_path = mesh_paths[k].c_str();
+            for (int c = 0; c < 3; c++) {
+                mo.position[c] = a.position[c];
+                mo.rotation_axis[c] = a.rotation_axis[c];
+                mo.scale[c] = a.scale[c];
+                mo.resolution[c] = a.resolution[c];
+            }
+            mo.rotation_angle_deg = a.rotation_angle_deg;
+            rc = m->add_mesh(0, mo);
+        }
         if (rc) {
             vfs_model_destroy(h);
             return rc;

@@ -1,4 +1,4 @@
-// GPU SDF + volume-map generation for analytic boundary shapes.
+// GPU SDF + volume-map generation for analytic boundary shapes and triangle meshes.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -27,5 +27,14 @@ struct VolumeMapParams {
 double volume_map_full_ball(const VolumeMapParams& p);
 
 cudaError_t launch_volume_map(const VolumeMapParams& p, float* sdf, float* vm, cudaStream_t s);
+
+struct MeshDev;
+// The same grids for a triangle mesh (p.shape unused): node SDF values from the mesh's exact
+// signed distance in double, quadrature points in float.
+cudaError_t launch_mesh_volume_map(const VolumeMapParams& p, const MeshDev& mesh, float* sdf,
+                                   float* vm, cudaStream_t s);
+// Signed distances of n points (3 floats each, device) to the mesh, in double.
+cudaError_t launch_mesh_distance(const MeshDev& mesh, const float* points, uint32_t n,
+                                 double* out, cudaStream_t s);
 
 }  // namespace vfs

@@ -98,6 +98,53 @@ class AnalyticObject:
 
 
 @dataclass
+class MeshObject:
+    """A triangle-mesh boundary object (GenericScene ObjectDef with an OBJ resourcePath): either
+    `obj_path` or `vertices` (V, 3) + `triangles` (T, 3)."""
+    obj_path: Optional[str] = None
+    vertices: Optional[np.ndarray] = None
+    triangles: Optional[np.ndarray] = None
+    position: Sequence[float] = (0.0, 0.0, 0.0)
+    rotation_angle_deg: float = 0.0
+    rotation_axis: Sequence[float] = (0.0, 0.0, 1.0)
+    scale: Sequence[float] = (1.0, 1.0, 1.0)
+    resolution: Sequence[int] = (32, 32, 32)
+
+    def to_c(self):
+        m = _abi.MeshObject()
+        keep = []
+        if self.obj_path is not None:
+            m.obj_path = str(self.obj_path).encode()
+        else:
+            v = np.ascontiguousarray(self.vertices, np.float32).reshape(-1, 3)
+            t = np.ascontiguousarray(self.triangles, np.uint32).reshape(-1, 3)
+            keep += [v, t]
+            m.vertices = v.ctypes.data_as(C.POINTER(C.c_float))
+            m.n_vertices = len(v)
+            m.triangles = t.ctypes.data_as(C.POINTER(C.c_uint32))
+            m.n_triangles = len(t)
+        m.position[:] = list(self.position)
+        m.rotation_angle_deg = self.rotation_angle_deg
+        m.rotation_axis[:] = list(self.rotation_axis)
+        m.scale[:] = list(self.scale)
+        m.resolution[:] = [int(r) for r in self.resolution]
+        return m, keep
+
+
+def mesh_signed_distance(vertices, triangles, points) -> np.ndarray:
+    """Signed distances (double) of points to a triangle mesh, computed on the GPU."""
+    v = np.ascontiguousarray(vertices, np.float32).reshape(-1, 3)
+    t = np.ascontiguousarray(triangles, np.uint32).reshape(-1, 3)
+    p = np.ascontiguousarray(points, np.float32).reshape(-1, 3)
+    out = np.empty(len(p), np.float64)
+    check(load_library().vfs_mesh_signed_distance(
+        v.ctypes.data_as(C.POINTER(C.c_float)), len(v), t.ctypes.data_as(C.POINTER(C.c_uint32)),
+        len(t), p.ctypes.data_as(C.POINTER(C.c_float)), len(p),
+        out.ctypes.data_as(C.POINTER(C.c_double))))
+    return out
+
+
+@dataclass
 class BoundaryObjectInfo:
     transform: np.ndarray
     rotation: np.ndarray
@@ -259,6 +306,11 @@ class WCSPHWithBoundaryModel:
 
     def add_analytic_object(self, obj: AnalyticObject) -> None:
         check(self._lib.vfs_model_add_analytic_object(self._h, C.byref(obj.to_c())))
+
+    def add_mesh_object(self, obj: MeshObject) -> None:
+        m, keep = obj.to_c()
+        check(self._lib.vfs_model_add_mesh_object(self._h, C.byref(m)))
+        del keep
 
     @property
     def n_boundary_objects(self) -> int:
@@ -480,6 +532,11 @@ class Batch:
 
     def add_analytic_object(self, scene: int, obj: AnalyticObject) -> None:
         check(self._lib.vfs_batch_add_analytic_object(self._h, scene, C.byref(obj.to_c())))
+
+    def add_mesh_object(self, scene: int, obj: MeshObject) -> None:
+        m, keep = obj.to_c()
+        check(self._lib.vfs_batch_add_mesh_object(self._h, scene, C.byref(m)))
+        del keep
 
     def get_boundary_object(self, scene: int, idx: int) -> BoundaryObjectInfo:
         info = _abi.BoundaryObject()
