@@ -650,13 +650,14 @@ __global__ void __launch_bounds__(kNbrBlock, kMinBlocks)
         }
         cnt = 0;
     };
+    // Branch-free append: every candidate is stored at the list's end and kept only when in
+    // range (the next one overwrites it otherwise). Lists are drained above kDrainAt, so the slot
+    // index stays below kListCap.
     for_each_candidate(p, scan, pos, xi, cx, cy, cz, [&](uint32_t j, const float4& xj) {
         const float dx = xj.x - xi.x, dy = xj.y - xi.y, dz = xj.z - xi.z;
         const float r2 = dx * dx + dy * dy + dz * dz;
-        if (r2 <= p.h2) {
-            s_j[cnt * kNbrBlock + tid] = j;
-            cnt++;
-        }
+        s_j[cnt * kNbrBlock + tid] = j;
+        cnt += r2 <= p.h2 ? 1 : 0;
     }, [&]() {
         if (cnt > kDrainAt) drain();
     });
