@@ -236,7 +236,7 @@ typedef struct vfs_tune_config {
     int32_t sort_digit_bits; /* 4..8 (the tuner tries 6, 7, 8) */
     int32_t sort_tile_items; /* 8, 12 or 16 keys per thread of a onesweep tile */
     int32_t nbr_block;       /* neighbour passes: threads per block ... */
-    int32_t nbr_min_blocks;  /* ... and minimum resident blocks per SM: 128x6, 128x8, 256x3, 64x12 */
+    int32_t nbr_min_blocks;  /* ... and minimum resident blocks per SM: 128x6, 128x8, 96x8, 64x12 */
     int32_t cell_block;      /* keys per block of the cell-range / reorder kernel: 128, 256, 512 */
 } vfs_tune_config;
 /* Times every candidate of each stage (sort, neighbour passes, cell ranges) for `repeats`

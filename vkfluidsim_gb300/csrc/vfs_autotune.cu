@@ -36,7 +36,7 @@ namespace {
 struct Shape {
     int threads, min_blocks;
 };
-constexpr Shape kShapes[kNumNbrShapes] = {{128, 6}, {128, 8}, {256, 3}, {64, 12}};
+constexpr Shape kShapes[kNumNbrShapes] = {{128, 6}, {128, 8}, {96, 8}, {64, 12}};
 
 std::mutex g_cache_mu;
 std::map<std::string, vfs_tune_config> g_cache;
@@ -86,7 +86,7 @@ int apply_tune_config(Model& m, const vfs_tune_config& c) {
     const int shape = shape_of(c.nbr_block, c.nbr_min_blocks);
     if (shape < 0)
         return fail(VFS_ERR_INVALID_ARGUMENT,
-                    "neighbour block shape must be 128x6, 128x8, 256x3 or 64x12 (threads x blocks/SM)");
+                    "neighbour block shape must be 128x6, 128x8, 96x8 or 64x12 (threads x blocks/SM)");
     if (c.cell_block != 128 && c.cell_block != 256 && c.cell_block != 512)
         return fail(VFS_ERR_INVALID_ARGUMENT, "cell_block must be 128, 256 or 512");
     if (c.sort_digit_bits != m.digit_bits || c.sort_tile_items != m.tile_items) {

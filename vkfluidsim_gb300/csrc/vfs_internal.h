@@ -112,7 +112,7 @@ int key_bits_for(uint32_t max_key);
 SortConfig make_sort_config(uint32_t n, int digit_bits, int tile_items, int key_bits = 0);
 
 // Launch shapes of the neighbour passes: threads per block x minimum resident blocks per SM.
-enum NbrShape : int { kNbr128x6 = 0, kNbr128x8 = 1, kNbr256x3 = 2, kNbr64x12 = 3, kNumNbrShapes = 4 };
+enum NbrShape : int { kNbr128x6 = 0, kNbr128x8 = 1, kNbr96x8 = 2, kNbr64x12 = 3, kNumNbrShapes = 4 };
 // Launch shapes chosen per model (by default or by the autotuner); none changes any result.
 struct KernelConfig {
     int nbr_shape = kNbr128x6;

@@ -653,6 +653,7 @@ __global__ void __launch_bounds__(kNbrBlock, kMinBlocks)
     // Branch-free append: every candidate is stored at the list's end and kept only when in
     // range (the next one overwrites it otherwise). Lists are drained above kDrainAt, so the slot
     // index stays below kListCap.
+    const bool distinct = distinct_keys(p, cx, cy, cz);
     for_each_candidate(p, scan, pos, xi, cx, cy, cz, [&](uint32_t j, const float4& xj) {
         const float dx = xj.x - xi.x, dy = xj.y - xi.y, dz = xj.z - xi.z;
         const float r2 = dx * dx + dy * dy + dz * dz;
@@ -662,7 +663,7 @@ __global__ void __launch_bounds__(kNbrBlock, kMinBlocks)
         if (cnt > kDrainAt) drain();
     });
     drain();
-    nbr_count[i] = nbr_word(listed, cx, cy, cz, distinct_keys(p, cx, cy, cz));
+    nbr_count[i] = nbr_word(listed, cx, cy, cz, distinct);
     float bd, bgx, bgy, bgz;
     boundary_terms(p, xi.x, xi.y, xi.z, bd, bgx, bgy, bgz);
     rho += p.rho0 * bd;
@@ -972,7 +973,7 @@ cudaError_t launch_density(const StepLaunch& L, const float4* pos, const uint32_
     if (L.total == 0) return cudaSuccess;
     switch (kc.nbr_shape) {
         case kNbr128x8: density_shape<128, 8>(L, pos, cell_scan, aux, bnd, nbr, nbr_count, s); break;
-        case kNbr256x3: density_shape<256, 3>(L, pos, cell_scan, aux, bnd, nbr, nbr_count, s); break;
+        case kNbr96x8: density_shape<96, 8>(L, pos, cell_scan, aux, bnd, nbr, nbr_count, s); break;
         case kNbr64x12: density_shape<64, 12>(L, pos, cell_scan, aux, bnd, nbr, nbr_count, s); break;
         default: density_shape<128, 6>(L, pos, cell_scan, aux, bnd, nbr, nbr_count, s);
     }
@@ -988,8 +989,8 @@ cudaError_t launch_force(const StepLaunch& L, const float4* pos, const float4* v
         case kNbr128x8:
             force_shape<128, 8>(L, pos, vel, aux, bnd, cell_scan, nbr, nbr_count, pos_out, vel_out, acc_out, s);
             break;
-        case kNbr256x3:
-            force_shape<256, 3>(L, pos, vel, aux, bnd, cell_scan, nbr, nbr_count, pos_out, vel_out, acc_out, s);
+        case kNbr96x8:
+            force_shape<96, 8>(L, pos, vel, aux, bnd, cell_scan, nbr, nbr_count, pos_out, vel_out, acc_out, s);
             break;
         case kNbr64x12:
             force_shape<64, 12>(L, pos, vel, aux, bnd, cell_scan, nbr, nbr_count, pos_out, vel_out, acc_out, s);
