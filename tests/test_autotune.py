@@ -12,12 +12,12 @@ from vkfluidsim_gb300 import workloads as W
 def test_tune_cache_file_round_trip(tmp_path):
     vfs.tune_cache_clear()
     f = tmp_path / "tune.txt"
-    f.write_text("# header\nsm103_152sms_n32768_s1_00000000000000aa 7 12 256 3 512\n")
+    f.write_text("# header\nsm103_152sms_n32768_s1_00000000000000aa 7 12 96 8 512\n")
     vfs.tune_cache_load(str(f))
     out = tmp_path / "out.txt"
     vfs.tune_cache_save(str(out))
     lines = [ln for ln in out.read_text().splitlines() if not ln.startswith("#")]
-    assert lines == ["sm103_152sms_n32768_s1_00000000000000aa 7 12 256 3 512"]
+    assert lines == ["sm103_152sms_n32768_s1_00000000000000aa 7 12 96 8 512"]
     vfs.tune_cache_clear()
 
 
