@@ -595,10 +595,11 @@ __device__ __forceinline__ void for_each_candidate(const SceneParams& p,
             const uint32_t b = seg == 0 ? b0 : (seg == 1 ? b1 : b2);
             const uint32_t e = seg == 0 ? e0 : (seg == 1 ? e1 : e2);
             uint32_t j = b;
+            const float4* pp = pos + b;
 #pragma unroll 1
-            for (; j + 4u <= e; j += 4u) {
-                const float4 q0 = __ldg(pos + j), q1 = __ldg(pos + j + 1u);
-                const float4 q2 = __ldg(pos + j + 2u), q3 = __ldg(pos + j + 3u);
+            for (; j + 4u <= e; j += 4u, pp += 4) {
+                const float4 q0 = __ldg(pp), q1 = __ldg(pp + 1);
+                const float4 q2 = __ldg(pp + 2), q3 = __ldg(pp + 3);
                 visit(j, q0);
                 visit(j + 1u, q1);
                 visit(j + 2u, q2);
@@ -606,7 +607,7 @@ __device__ __forceinline__ void for_each_candidate(const SceneParams& p,
                 batch_end();
             }
 #pragma unroll 1
-            for (; j < e; j++) visit(j, __ldg(pos + j));
+            for (; j < e; j++, pp++) visit(j, __ldg(pp));
             batch_end();
         }
     }
@@ -632,9 +633,10 @@ __global__ void __launch_bounds__(kNbrBlock, kMinBlocks)
     const uint32_t cx = cell_coord(xi.x, p.h), cy = cell_coord(xi.y, p.h),
                    cz = cell_coord(xi.z, p.h);
     float rho = 0.0f;
-    int cnt = 0;
+    uint32_t s_end = tid;  // shared-memory word one past the last kept candidate (stride kNbrBlock)
     uint32_t listed = 0;
     auto drain = [&]() {
+        const int cnt = (int)((s_end - tid) / kNbrBlock);
 #pragma unroll 2
         for (int k = 0; k < cnt; k++) {
             const uint32_t j = s_j[k * kNbrBlock + tid];
@@ -648,7 +650,7 @@ __global__ void __launch_bounds__(kNbrBlock, kMinBlocks)
                 listed++;
             }
         }
-        cnt = 0;
+        s_end = tid;
     };
     // Branch-free append: every candidate is stored at the list's end and kept only when in
     // range (the next one overwrites it otherwise). Lists are drained above kDrainAt, so the slot
@@ -657,10 +659,10 @@ __global__ void __launch_bounds__(kNbrBlock, kMinBlocks)
     for_each_candidate(p, scan, pos, xi, cx, cy, cz, [&](uint32_t j, const float4& xj) {
         const float dx = xj.x - xi.x, dy = xj.y - xi.y, dz = xj.z - xi.z;
         const float r2 = dx * dx + dy * dy + dz * dz;
-        s_j[cnt * kNbrBlock + tid] = j;
-        cnt += r2 <= p.h2 ? 1 : 0;
+        s_j[s_end] = j;
+        s_end += r2 <= p.h2 ? kNbrBlock : 0u;
     }, [&]() {
-        if (cnt > kDrainAt) drain();
+        if (s_end > tid + kDrainAt * kNbrBlock) drain();
     });
     drain();
     nbr_count[i] = nbr_word(listed, cx, cy, cz, distinct);
