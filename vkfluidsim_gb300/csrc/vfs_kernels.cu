@@ -635,18 +635,21 @@ __global__ void __launch_bounds__(kNbrBlock, kMinBlocks)
     float rho = 0.0f;
     uint32_t s_end = tid;  // shared-memory word one past the last kept candidate (stride kNbrBlock)
     uint32_t listed = 0;
+    uint32_t* nbr_out = nbr + i;  // slot `listed` of particle i's list
     auto drain = [&]() {
-        const int cnt = (int)((s_end - tid) / kNbrBlock);
 #pragma unroll 2
-        for (int k = 0; k < cnt; k++) {
-            const uint32_t j = s_j[k * kNbrBlock + tid];
+        for (uint32_t o = tid; o < s_end; o += kNbrBlock) {
+            const uint32_t j = s_j[o];
             const float4 xj = __ldg(pos + j);
             const float dx = xj.x - xi.x, dy = xj.y - xi.y, dz = xj.z - xi.z;
             const float r2 = dx * dx + dy * dy + dz * dz;
             const float r = r2 > 0.0f ? r2 * rsqrtf(r2) : 0.0f;
             rho += p.mass * cubic_w(r * p.inv_h, p.cubic);
             if (j != i) {
-                if (listed < p.nbr_cap) nbr[(size_t)listed * L.total + i] = j;
+                if (listed < p.nbr_cap) {
+                    *nbr_out = j;
+                    nbr_out += L.total;
+                }
                 listed++;
             }
         }
@@ -758,9 +761,11 @@ __global__ void __launch_bounds__(kNbrBlock, kMinBlocks)
     if (listed <= p.nbr_cap) {
         // The density pass's list: the in-range neighbours in the reference's visiting order.
         uint32_t k = 0;
+        const uint32_t* nl = nbr + i;  // slot k of particle i's list
+        const size_t stride = L.total;
 #pragma unroll 1
-        for (; k + 2u <= listed; k += 2u) {
-            const uint32_t j0 = nbr[(size_t)k * L.total + i], j1 = nbr[(size_t)(k + 1u) * L.total + i];
+        for (; k + 2u <= listed; k += 2u, nl += 2 * stride) {
+            const uint32_t j0 = __ldg(nl), j1 = __ldg(nl + stride);
             const float4 x0 = __ldg(pos + j0), x1 = __ldg(pos + j1);
             const float4 v0 = __ldg(vel + j0), v1 = __ldg(vel + j1);
             const float2 a0 = __ldg(aux2 + 2 * (size_t)j0), a1 = __ldg(aux2 + 2 * (size_t)j1);
@@ -768,7 +773,7 @@ __global__ void __launch_bounds__(kNbrBlock, kMinBlocks)
             force_term(p, xi, vi, pdi, x1, a1, v1, f);
         }
         if (k < listed) {
-            const uint32_t j0 = nbr[(size_t)k * L.total + i];
+            const uint32_t j0 = __ldg(nl);
             force_term(p, xi, vi, pdi, __ldg(pos + j0), __ldg(aux2 + 2 * (size_t)j0),
                        __ldg(vel + j0), f);
         }
