@@ -321,9 +321,9 @@ int Model::enqueue_substep(cudaEvent_t* ev) {
     if (ev) VFS_CUDA_TRY(cudaEventRecord(ev[3], s));
     VFS_CUDA_TRY(launch_cells_reorder(n, skeys, sperm, cell_scan, pos[c], vel[c], pos[o], vel[o], kc, s));
     if (ev) VFS_CUDA_TRY(cudaEventRecord(ev[4], s));
-    VFS_CUDA_TRY(launch_density(launch, pos[o], cell_scan, aux, bnd, nbr, nbr_count, kc, s));
+    VFS_CUDA_TRY(launch_density(launch, pos[o], vel[o], rec, cell_scan, aux, bnd, nbr, nbr_count, kc, s));
     if (ev) VFS_CUDA_TRY(cudaEventRecord(ev[5], s));
-    VFS_CUDA_TRY(launch_force(launch, pos[o], vel[o], aux, bnd, cell_scan, nbr, nbr_count, pos[c],
+    VFS_CUDA_TRY(launch_force(launch, pos[o], vel[o], aux, rec, bnd, cell_scan, nbr, nbr_count, pos[c],
                               vel[c], record ? acc : nullptr, kc, s));
     if (ev) VFS_CUDA_TRY(cudaEventRecord(ev[6], s));
     return VFS_OK;
@@ -385,6 +385,7 @@ Model::~Model() {
     cudaFree(vals_alt);
     cudaFree(cell_scan);
     cudaFree(aux);
+    cudaFree(rec);
     cudaFree(bnd);
     cudaFree(acc);
     cudaFree(stage);
@@ -425,6 +426,7 @@ int Model::init() {
     VFS_CUDA_TRY(cudaMalloc(&vals_alt, N * 4));
     VFS_CUDA_TRY(cudaMalloc(&cell_scan, (N + 1) * 4));
     VFS_CUDA_TRY(cudaMalloc(&aux, N * sizeof(float4)));
+    VFS_CUDA_TRY(cudaMalloc(&rec, 2 * N * sizeof(float4)));
     VFS_CUDA_TRY(cudaMalloc(&bnd, N * sizeof(float4)));
     VFS_CUDA_TRY(cudaMalloc(&acc, N * sizeof(float4)));
     VFS_CUDA_TRY(cudaMalloc(&stage, N * 32));

@@ -140,12 +140,13 @@ cudaError_t launch_cells_reorder(uint32_t n, const uint32_t* skeys, const uint32
 cudaError_t launch_lookback_selftest(bool published, uint32_t spin_limit, uint32_t* d_work,
                                      uint32_t* err, cudaStream_t s);
 // Boundary volume + density + EOS epilogue; writes each particle's neighbour list.
-cudaError_t launch_density(const StepLaunch& L, const float4* pos, const uint32_t* cell_scan,
-                           float4* aux, float4* bnd, uint32_t* nbr, uint32_t* nbr_count,
-                           const KernelConfig& kc, cudaStream_t s);
+// Also writes rec[2i], rec[2i+1] = (x, y, z, p/rho^2), (v, m/max(rho, 1e-6)) for the force pass.
+cudaError_t launch_density(const StepLaunch& L, const float4* pos, const float4* vel, float4* rec,
+                           const uint32_t* cell_scan, float4* aux, float4* bnd, uint32_t* nbr,
+                           uint32_t* nbr_count, const KernelConfig& kc, cudaStream_t s);
 // Pressure + viscosity + wall + symplectic Euler over the density pass's neighbour lists.
 cudaError_t launch_force(const StepLaunch& L, const float4* pos, const float4* vel,
-                         const float4* aux, const float4* bnd, const uint32_t* cell_scan,
+                         const float4* aux, const float4* rec, const float4* bnd, const uint32_t* cell_scan,
                          const uint32_t* nbr, const uint32_t* nbr_count, float4* pos_out,
                          float4* vel_out, float4* acc_out, const KernelConfig& kc, cudaStream_t s);
 // Stable in-place sort of (keys, items) with caller-provided temporaries (n words each) and

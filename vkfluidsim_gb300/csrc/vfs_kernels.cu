@@ -621,7 +621,8 @@ __device__ __forceinline__ void for_each_candidate(const SceneParams& p,
 // do not change before the force pass, so that list is exactly the force pass's neighbour set.
 template <bool kBatch, int kNbrBlock, int kMinBlocks>
 __global__ void __launch_bounds__(kNbrBlock, kMinBlocks)
-    k_density(StepLaunch L, const float4* __restrict__ pos, const uint32_t* __restrict__ scan,
+    k_density(StepLaunch L, const float4* __restrict__ pos, const float4* __restrict__ vel,
+              float4* __restrict__ rec, const uint32_t* __restrict__ scan,
               float4* __restrict__ aux, float4* __restrict__ bnd, uint32_t* __restrict__ nbr,
               uint32_t* __restrict__ nbr_count) {
     __shared__ uint32_t s_j[kListCap * kNbrBlock];
@@ -677,6 +678,10 @@ __global__ void __launch_bounds__(kNbrBlock, kMinBlocks)
     const float mr = p.mass / fmaxf(rho, 1e-6f);
     const float pb = rho > 0.0f ? pr / (p.rho0 * p.rho0) : 0.0f;
     aux[i] = make_float4(pd, mr, rho, pb);
+    // The force pass's neighbour record of i: one 32-byte sector per gathered neighbour.
+    const float4 vi = __ldg(vel + i);
+    rec[2 * (size_t)i] = make_float4(xi.x, xi.y, xi.z, pd);
+    rec[2 * (size_t)i + 1] = make_float4(vi.x, vi.y, vi.z, mr);
     bnd[i] = make_float4(bgx, bgy, bgz, bd);
 }
 
@@ -710,29 +715,24 @@ __device__ __forceinline__ void force_term(const SceneParams& p, const float4& x
     f.Vz += (tv * (nz * gw)) * iden;
 }
 
+// One neighbour's term from its force record: rec[2j] = (x, y, z, p/rho^2), rec[2j+1] =
+// (vx, vy, vz, m/max(rho, 1e-6)), the same values as pos, vel and aux hold.
+__device__ __forceinline__ void force_term_rec(const SceneParams& p, const float4& xi,
+                                               const float4& vi, float pdi,
+                                               const float4* __restrict__ rec, uint32_t j,
+                                               ForceAcc& f) {
+    const float4 r0 = __ldg(rec + 2 * (size_t)j), r1 = __ldg(rec + 2 * (size_t)j + 1);
+    force_term(p, xi, vi, pdi, r0, make_float2(r0.w, r1.w), r1, f);
+}
+
 // Phase B of the force pass over the first cnt listed neighbours.
 template <int kNbrBlock>
-__device__ __forceinline__ void force_drain(const SceneParams& p, const float4* __restrict__ pos,
-                                            const float4* __restrict__ vel,
-                                            const float2* __restrict__ aux2,
+__device__ __forceinline__ void force_drain(const SceneParams& p, const float4* __restrict__ rec,
                                             const uint32_t* s_j, int tid, int cnt,
                                             const float4& xi, const float4& vi, float pdi,
                                             ForceAcc& f) {
-    int k = 0;
-#pragma unroll 1
-    for (; k + 2 <= cnt; k += 2) {
-        const uint32_t j0 = s_j[k * kNbrBlock + tid], j1 = s_j[(k + 1) * kNbrBlock + tid];
-        const float4 x0 = __ldg(pos + j0), x1 = __ldg(pos + j1);
-        const float4 v0 = __ldg(vel + j0), v1 = __ldg(vel + j1);
-        const float2 a0 = __ldg(aux2 + 2 * (size_t)j0), a1 = __ldg(aux2 + 2 * (size_t)j1);
-        force_term(p, xi, vi, pdi, x0, a0, v0, f);
-        force_term(p, xi, vi, pdi, x1, a1, v1, f);
-    }
-    if (k < cnt) {
-        const uint32_t j0 = s_j[k * kNbrBlock + tid];
-        force_term(p, xi, vi, pdi, __ldg(pos + j0), __ldg(aux2 + 2 * (size_t)j0),
-                   __ldg(vel + j0), f);
-    }
+#pragma unroll 2
+    for (int k = 0; k < cnt; k++) force_term_rec(p, xi, vi, pdi, rec, s_j[k * kNbrBlock + tid], f);
 }
 
 // CalculatePressureAccel + CalculateViscousAccel + UpdatePositions
@@ -741,7 +741,8 @@ __device__ __forceinline__ void force_drain(const SceneParams& p, const float4* 
 template <bool kBatch, int kNbrBlock, int kMinBlocks>
 __global__ void __launch_bounds__(kNbrBlock, kMinBlocks)
     k_force(StepLaunch L, const float4* __restrict__ pos, const float4* __restrict__ vel,
-            const float4* __restrict__ aux, const float4* __restrict__ bnd,
+            const float4* __restrict__ aux, const float4* __restrict__ rec,
+            const float4* __restrict__ bnd,
             const uint32_t* __restrict__ scan, const uint32_t* __restrict__ nbr,
             const uint32_t* __restrict__ nbr_count, float4* __restrict__ pos_out,
             float4* __restrict__ vel_out, float4* __restrict__ acc_out) {
@@ -753,7 +754,6 @@ __global__ void __launch_bounds__(kNbrBlock, kMinBlocks)
     const float4 xi = __ldg(pos + i);
     const float4 vi = __ldg(vel + i);
     const float4 ai = __ldg(aux + i);
-    const float2* __restrict__ aux2 = reinterpret_cast<const float2*>(aux);
     const float pdi = ai.x;
 
     ForceAcc f{0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
@@ -766,17 +766,12 @@ __global__ void __launch_bounds__(kNbrBlock, kMinBlocks)
 #pragma unroll 1
         for (; k + 2u <= listed; k += 2u, nl += 2 * stride) {
             const uint32_t j0 = __ldg(nl), j1 = __ldg(nl + stride);
-            const float4 x0 = __ldg(pos + j0), x1 = __ldg(pos + j1);
-            const float4 v0 = __ldg(vel + j0), v1 = __ldg(vel + j1);
-            const float2 a0 = __ldg(aux2 + 2 * (size_t)j0), a1 = __ldg(aux2 + 2 * (size_t)j1);
-            force_term(p, xi, vi, pdi, x0, a0, v0, f);
-            force_term(p, xi, vi, pdi, x1, a1, v1, f);
+            const float4 a0 = __ldg(rec + 2 * (size_t)j0), b0 = __ldg(rec + 2 * (size_t)j0 + 1);
+            const float4 a1 = __ldg(rec + 2 * (size_t)j1), b1 = __ldg(rec + 2 * (size_t)j1 + 1);
+            force_term(p, xi, vi, pdi, a0, make_float2(a0.w, b0.w), b0, f);
+            force_term(p, xi, vi, pdi, a1, make_float2(a1.w, b1.w), b1, f);
         }
-        if (k < listed) {
-            const uint32_t j0 = __ldg(nl);
-            force_term(p, xi, vi, pdi, __ldg(pos + j0), __ldg(aux2 + 2 * (size_t)j0),
-                       __ldg(vel + j0), f);
-        }
+        if (k < listed) force_term_rec(p, xi, vi, pdi, rec, __ldg(nl), f);
     } else {
         // Overflowed list (very dense neighbourhood): walk the candidates again.
         const uint32_t cx = cell_coord(xi.x, p.h), cy = cell_coord(xi.y, p.h),
@@ -791,11 +786,11 @@ __global__ void __launch_bounds__(kNbrBlock, kMinBlocks)
             }
         }, [&]() {
             if (cnt > kDrainAt) {
-                force_drain<kNbrBlock>(p, pos, vel, aux2, s_j, tid, cnt, xi, vi, pdi, f);
+                force_drain<kNbrBlock>(p, rec, s_j, tid, cnt, xi, vi, pdi, f);
                 cnt = 0;
             }
         });
-        force_drain<kNbrBlock>(p, pos, vel, aux2, s_j, tid, cnt, xi, vi, pdi, f);
+        force_drain<kNbrBlock>(p, rec, s_j, tid, cnt, xi, vi, pdi, f);
     }
     const float4 bi = __ldg(bnd + i);
     const float sb = (pdi + ai.w) * p.rho0;
@@ -951,59 +946,60 @@ cudaError_t launch_cells_reorder(uint32_t n, const uint32_t* skeys, const uint32
 }
 
 template <int B, int M>
-void density_shape(const StepLaunch& L, const float4* pos, const uint32_t* cell_scan, float4* aux,
-                   float4* bnd, uint32_t* nbr, uint32_t* nbr_count, cudaStream_t s) {
+void density_shape(const StepLaunch& L, const float4* pos, const float4* vel, float4* rec,
+                   const uint32_t* cell_scan, float4* aux, float4* bnd, uint32_t* nbr,
+                   uint32_t* nbr_count, cudaStream_t s) {
     const uint32_t blocks = (L.total + B - 1) / B;
     if (L.n_scenes > 1)
-        k_density<true, B, M><<<blocks, B, 0, s>>>(L, pos, cell_scan, aux, bnd, nbr, nbr_count);
+        k_density<true, B, M><<<blocks, B, 0, s>>>(L, pos, vel, rec, cell_scan, aux, bnd, nbr, nbr_count);
     else
-        k_density<false, B, M><<<blocks, B, 0, s>>>(L, pos, cell_scan, aux, bnd, nbr, nbr_count);
+        k_density<false, B, M><<<blocks, B, 0, s>>>(L, pos, vel, rec, cell_scan, aux, bnd, nbr, nbr_count);
 }
 
 template <int B, int M>
 void force_shape(const StepLaunch& L, const float4* pos, const float4* vel, const float4* aux,
-                 const float4* bnd, const uint32_t* cell_scan, const uint32_t* nbr,
+                 const float4* rec, const float4* bnd, const uint32_t* cell_scan, const uint32_t* nbr,
                  const uint32_t* nbr_count, float4* pos_out, float4* vel_out, float4* acc_out,
                  cudaStream_t s) {
     const uint32_t blocks = (L.total + B - 1) / B;
     if (L.n_scenes > 1)
-        k_force<true, B, M><<<blocks, B, 0, s>>>(L, pos, vel, aux, bnd, cell_scan, nbr, nbr_count,
+        k_force<true, B, M><<<blocks, B, 0, s>>>(L, pos, vel, aux, rec, bnd, cell_scan, nbr, nbr_count,
                                                  pos_out, vel_out, acc_out);
     else
-        k_force<false, B, M><<<blocks, B, 0, s>>>(L, pos, vel, aux, bnd, cell_scan, nbr, nbr_count,
+        k_force<false, B, M><<<blocks, B, 0, s>>>(L, pos, vel, aux, rec, bnd, cell_scan, nbr, nbr_count,
                                                   pos_out, vel_out, acc_out);
 }
 
-cudaError_t launch_density(const StepLaunch& L, const float4* pos, const uint32_t* cell_scan,
-                           float4* aux, float4* bnd, uint32_t* nbr, uint32_t* nbr_count,
-                           const KernelConfig& kc, cudaStream_t s) {
+cudaError_t launch_density(const StepLaunch& L, const float4* pos, const float4* vel, float4* rec,
+                           const uint32_t* cell_scan, float4* aux, float4* bnd, uint32_t* nbr,
+                           uint32_t* nbr_count, const KernelConfig& kc, cudaStream_t s) {
     if (L.total == 0) return cudaSuccess;
     switch (kc.nbr_shape) {
-        case kNbr128x8: density_shape<128, 8>(L, pos, cell_scan, aux, bnd, nbr, nbr_count, s); break;
-        case kNbr96x8: density_shape<96, 8>(L, pos, cell_scan, aux, bnd, nbr, nbr_count, s); break;
-        case kNbr64x12: density_shape<64, 12>(L, pos, cell_scan, aux, bnd, nbr, nbr_count, s); break;
-        default: density_shape<128, 6>(L, pos, cell_scan, aux, bnd, nbr, nbr_count, s);
+        case kNbr128x8: density_shape<128, 8>(L, pos, vel, rec, cell_scan, aux, bnd, nbr, nbr_count, s); break;
+        case kNbr96x8: density_shape<96, 8>(L, pos, vel, rec, cell_scan, aux, bnd, nbr, nbr_count, s); break;
+        case kNbr64x12: density_shape<64, 12>(L, pos, vel, rec, cell_scan, aux, bnd, nbr, nbr_count, s); break;
+        default: density_shape<128, 6>(L, pos, vel, rec, cell_scan, aux, bnd, nbr, nbr_count, s);
     }
     return cudaGetLastError();
 }
 
 cudaError_t launch_force(const StepLaunch& L, const float4* pos, const float4* vel,
-                         const float4* aux, const float4* bnd, const uint32_t* cell_scan,
+                         const float4* aux, const float4* rec, const float4* bnd, const uint32_t* cell_scan,
                          const uint32_t* nbr, const uint32_t* nbr_count, float4* pos_out,
                          float4* vel_out, float4* acc_out, const KernelConfig& kc, cudaStream_t s) {
     if (L.total == 0) return cudaSuccess;
     switch (kc.nbr_shape) {
         case kNbr128x8:
-            force_shape<128, 8>(L, pos, vel, aux, bnd, cell_scan, nbr, nbr_count, pos_out, vel_out, acc_out, s);
+            force_shape<128, 8>(L, pos, vel, aux, rec, bnd, cell_scan, nbr, nbr_count, pos_out, vel_out, acc_out, s);
             break;
         case kNbr96x8:
-            force_shape<96, 8>(L, pos, vel, aux, bnd, cell_scan, nbr, nbr_count, pos_out, vel_out, acc_out, s);
+            force_shape<96, 8>(L, pos, vel, aux, rec, bnd, cell_scan, nbr, nbr_count, pos_out, vel_out, acc_out, s);
             break;
         case kNbr64x12:
-            force_shape<64, 12>(L, pos, vel, aux, bnd, cell_scan, nbr, nbr_count, pos_out, vel_out, acc_out, s);
+            force_shape<64, 12>(L, pos, vel, aux, rec, bnd, cell_scan, nbr, nbr_count, pos_out, vel_out, acc_out, s);
             break;
         default:
-            force_shape<128, 6>(L, pos, vel, aux, bnd, cell_scan, nbr, nbr_count, pos_out, vel_out, acc_out, s);
+            force_shape<128, 6>(L, pos, vel, aux, rec, bnd, cell_scan, nbr, nbr_count, pos_out, vel_out, acc_out, s);
     }
     return cudaGetLastError();
 }

@@ -58,6 +58,7 @@ struct Model {
     uint32_t* sperm = nullptr;  // sorted_indices of the last substep (aliases vals / vals_alt)
     uint32_t* cell_scan = nullptr;
     float4* aux = nullptr;
+    float4* rec = nullptr;  // 2 float4 per particle: the force pass's neighbour records
     float4* bnd = nullptr;
     float4* acc = nullptr;
     uint32_t* nbr = nullptr;        // kNbrCap slot-major neighbour lists
