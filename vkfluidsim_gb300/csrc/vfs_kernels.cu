@@ -642,10 +642,22 @@ __global__ void __launch_bounds__(kNbrBlock, kMinBlocks)
         for (uint32_t o = tid; o < s_end; o += kNbrBlock) {
             const uint32_t j = s_j[o];
             const float4 xj = __ldg(pos + j);
-            const float dx = xj.x - xi.x, dy = xj.y - xi.y, dz = xj.z - xi.z;
-            const float r2 = dx * dx + dy * dy + dz * dz;
-            const float r = r2 > 0.0f ? r2 * rsqrtf(r2) : 0.0f;
-            rho += p.mass * cubic_w(r * p.inv_h, p.cubic);
+            // Explicit rounding: the same sums for every launch shape.
+            const float dx = __fsub_rn(xj.x, xi.x), dy = __fsub_rn(xj.y, xi.y), dz = __fsub_rn(xj.z, xi.z);
+            const float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+            const float r = r2 > 0.0f ? __fmul_rn(r2, rsqrtf(r2)) : 0.0f;
+            const float q = __fmul_rn(r, p.inv_h);
+            float w = 0.0f;
+            if (q <= 1.0f) {
+                if (q > 0.5f) {
+                    const float t = __fsub_rn(1.0f, q);
+                    w = __fmul_rn(__fmul_rn(p.cubic, 2.0f), __fmul_rn(__fmul_rn(t, t), t));
+                } else {
+                    const float q2 = __fmul_rn(q, q);
+                    w = __fmul_rn(p.cubic, __fmaf_rn(6.0f, __fmul_rn(q2, q), __fmaf_rn(-6.0f, q2, 1.0f)));
+                }
+            }
+            rho = __fmaf_rn(p.mass, w, rho);
             if (j != i) {
                 if (listed < p.nbr_cap) {
                     *nbr_out = j;
@@ -691,28 +703,40 @@ struct ForceAcc {
 
 // Pressure and viscosity contributions of one in-range neighbour (PressureAccel slang:234-249,
 // ViscousAccel slang:301-318).
+// Written with explicit round-to-nearest intrinsics so that no fusion is left to the compiler:
+// every launch shape of the force pass then gives bit-identical results.
 __device__ __forceinline__ void force_term(const SceneParams& p, const float4& xi, const float4& vi,
                                            float pdi, const float4& xj, const float2& aj,
                                            const float4& vj, ForceAcc& f) {
-    const float xx = xi.x - xj.x, xy = xi.y - xj.y, xz = xi.z - xj.z;
-    const float r2 = xx * xx + xy * xy + xz * xz;
+    const float xx = __fsub_rn(xi.x, xj.x), xy = __fsub_rn(xi.y, xj.y), xz = __fsub_rn(xi.z, xj.z);
+    const float r2 = __fmaf_rn(xz, xz, __fmaf_rn(xy, xy, __fmul_rn(xx, xx)));
     const bool pos_r = r2 > 0.0f;
     const float ir = pos_r ? rsqrtf(r2) : 0.0f;
-    const float r = r2 * ir;
-    const float nx = pos_r ? xx * ir : 0.0f;
-    const float ny = pos_r ? xy * ir : 1.0f;
-    const float nz = pos_r ? xz * ir : 0.0f;
-    const float gw = cubic_dw(r, r * p.inv_h, p.grad_over_h);
-    const float s = (p.mass * (pdi + aj.x)) * gw;
-    f.Px += s * nx;
-    f.Py += s * ny;
-    f.Pz += s * nz;
-    const float dv = (vi.x - vj.x) * xx + (vi.y - vj.y) * xy + (vi.z - vj.z) * xz;
-    const float tv = aj.y * dv;
-    const float iden = __fdividef(1.0f, r2 + p.visc_eps);
-    f.Vx += (tv * (nx * gw)) * iden;
-    f.Vy += (tv * (ny * gw)) * iden;
-    f.Vz += (tv * (nz * gw)) * iden;
+    const float r = __fmul_rn(r2, ir);
+    const float nx = pos_r ? __fmul_rn(xx, ir) : 0.0f;
+    const float ny = pos_r ? __fmul_rn(xy, ir) : 1.0f;
+    const float nz = pos_r ? __fmul_rn(xz, ir) : 0.0f;
+    const float q = __fmul_rn(r, p.inv_h);
+    float gw = 0.0f;
+    if ((r > 1e-9f) && (q <= 1.0f)) {
+        if (q > 0.5f) {
+            const float t = __fsub_rn(1.0f, q);
+            gw = __fmul_rn(-p.grad_over_h, __fmul_rn(t, t));
+        } else {
+            gw = __fmul_rn(__fmul_rn(p.grad_over_h, q), __fmaf_rn(3.0f, q, -2.0f));
+        }
+    }
+    const float s = __fmul_rn(__fmul_rn(p.mass, __fadd_rn(pdi, aj.x)), gw);
+    f.Px = __fmaf_rn(s, nx, f.Px);
+    f.Py = __fmaf_rn(s, ny, f.Py);
+    f.Pz = __fmaf_rn(s, nz, f.Pz);
+    const float dv = __fmaf_rn(__fsub_rn(vi.z, vj.z), xz,
+                               __fmaf_rn(__fsub_rn(vi.y, vj.y), xy, __fmul_rn(__fsub_rn(vi.x, vj.x), xx)));
+    const float tv = __fmul_rn(aj.y, dv);
+    const float iden = __fdividef(1.0f, __fadd_rn(r2, p.visc_eps));
+    f.Vx = __fmaf_rn(__fmul_rn(tv, __fmul_rn(nx, gw)), iden, f.Vx);
+    f.Vy = __fmaf_rn(__fmul_rn(tv, __fmul_rn(ny, gw)), iden, f.Vy);
+    f.Vz = __fmaf_rn(__fmul_rn(tv, __fmul_rn(nz, gw)), iden, f.Vz);
 }
 
 // One neighbour's term from its force record: rec[2j] = (x, y, z, p/rho^2), rec[2j+1] =
@@ -764,14 +788,21 @@ __global__ void __launch_bounds__(kNbrBlock, kMinBlocks)
         const uint32_t* nl = nbr + i;  // slot k of particle i's list
         const size_t stride = L.total;
 #pragma unroll 1
-        for (; k + 2u <= listed; k += 2u, nl += 2 * stride) {
-            const uint32_t j0 = __ldg(nl), j1 = __ldg(nl + stride);
-            const float4 a0 = __ldg(rec + 2 * (size_t)j0), b0 = __ldg(rec + 2 * (size_t)j0 + 1);
-            const float4 a1 = __ldg(rec + 2 * (size_t)j1), b1 = __ldg(rec + 2 * (size_t)j1 + 1);
-            force_term(p, xi, vi, pdi, a0, make_float2(a0.w, b0.w), b0, f);
-            force_term(p, xi, vi, pdi, a1, make_float2(a1.w, b1.w), b1, f);
+        for (; k + 4u <= listed; k += 4u, nl += 4 * stride) {
+            uint32_t j[4];
+            float4 a[4], b[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) j[u] = __ldg(nl + u * stride);
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                a[u] = __ldg(rec + 2 * (size_t)j[u]);
+                b[u] = __ldg(rec + 2 * (size_t)j[u] + 1);
+            }
+#pragma unroll
+            for (int u = 0; u < 4; u++) force_term(p, xi, vi, pdi, a[u], make_float2(a[u].w, b[u].w), b[u], f);
         }
-        if (k < listed) force_term_rec(p, xi, vi, pdi, rec, __ldg(nl), f);
+#pragma unroll 1
+        for (; k < listed; k++, nl += stride) force_term_rec(p, xi, vi, pdi, rec, __ldg(nl), f);
     } else {
         // Overflowed list (very dense neighbourhood): walk the candidates again.
         const uint32_t cx = cell_coord(xi.x, p.h), cy = cell_coord(xi.y, p.h),
