@@ -200,6 +200,12 @@ int vfs_model_profile_substeps(vfs_model* m, int32_t count, float* phase_ms);
 int vfs_model_set_sort_config(vfs_model* m, int32_t digit_bits, int32_t tile_items);
 int vfs_model_get_sort_config(const vfs_model* m, int32_t* digit_bits, int32_t* tile_items,
                               int32_t* passes);
+/* Neighbour-list slots per particle (default 128, range [16, 4096], 4 bytes per particle each).
+ * A particle with more in-range neighbours makes the force pass walk its candidates again and a
+ * differentiable rollout fail with VFS_ERR_CAPACITY, so dense scenes want more slots. Results do
+ * not depend on the capacity. The getter returns -1 for a NULL handle. */
+int vfs_model_set_neighbor_capacity(vfs_model* m, int32_t slots);
+int32_t vfs_model_get_neighbor_capacity(const vfs_model* m);
 /* Device pointers of the current state: float4 (x, y, z, id bits) and (vx, vy, vz, 0). */
 int vfs_model_device_state(vfs_model* m, void** pos4, void** vel4);
 
@@ -287,6 +293,7 @@ int vfs_batch_use_graph(vfs_batch* b, int32_t enable);
 int vfs_batch_synchronize(vfs_batch* b);
 int vfs_batch_profile_substeps(vfs_batch* b, int32_t count, float* phase_ms);
 int vfs_batch_set_sort_config(vfs_batch* b, int32_t digit_bits, int32_t tile_items);
+int vfs_batch_set_neighbor_capacity(vfs_batch* b, int32_t slots);
 int vfs_batch_export_state(vfs_batch* b, int32_t scene, const char* path_prefix);
 int vfs_batch_import_state(vfs_batch* b, int32_t scene, const char* path_prefix);
 /* As vfs_model_record; the snapshots are `<prefix>_s<scene>_f<frame>`. */

@@ -281,6 +281,26 @@ def test_dense_cluster_overflows_the_neighbour_list():
     assert g["densities"].max() > 50 * np.median(g["densities"])
 
 
+def test_neighbour_capacity_changes_no_result():
+    """The same dense cluster with 2048 list slots (no list overflows, so the force pass uses the
+    lists) and with 128 (most blob particles fall back to the walk): bit-identical steps."""
+    w = W.stress_4m(n_uniform=20000, n_blob=4000, map_res=0)
+    blob = vfs.generate_uniform_blob(0, (0, 0, 0), (1, 1, 1), 4000, (2.0, 1.0, 1.0), 0.008, 77)
+    w.pos[20000:] = blob
+    a = W.build_model(w)
+    b = W.build_model(w)
+    assert a.neighbor_capacity == 128
+    b.set_neighbor_capacity(2048)
+    assert b.neighbor_capacity == 2048
+    for m in (a, b):
+        m.substeps(2)
+    sa, sb = a.copy_data_buffers(), b.copy_data_buffers()
+    for k in ("positions", "velocities", "densities"):
+        assert np.array_equal(sa[k], sb[k]), k
+    with pytest.raises(vfs.VfsError):
+        b.set_neighbor_capacity(8)
+
+
 def test_negative_cells_and_hash_block_boundaries():
     """Particles spanning cells -31..31 cross the uint wrap of cell + 25 (cells -26/-25) and the
     50-cell hash-block boundaries, where the candidate walk must not skip any bucket."""

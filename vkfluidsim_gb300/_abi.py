@@ -155,6 +155,9 @@ SIGNATURES = {
     "vfs_batch_synchronize": (_I, [_P]),
     "vfs_batch_profile_substeps": (_I, [_P, C.c_int32, _F]),
     "vfs_batch_set_sort_config": (_I, [_P, C.c_int32, C.c_int32]),
+    "vfs_batch_set_neighbor_capacity": (_I, [_P, C.c_int32]),
+    "vfs_model_set_neighbor_capacity": (_I, [_P, C.c_int32]),
+    "vfs_model_get_neighbor_capacity": (C.c_int32, [_P]),
     "vfs_batch_autotune": (_I, [_P, C.c_int32, C.c_int32, C.POINTER(TuneConfig)]),
     "vfs_batch_set_tune_config": (_I, [_P, C.POINTER(TuneConfig)]),
     "vfs_batch_get_tune_config": (_I, [_P, C.POINTER(TuneConfig)]),

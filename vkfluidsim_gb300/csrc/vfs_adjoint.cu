@@ -465,6 +465,7 @@ struct Rollout {
     float* host_io = nullptr;  // 3N floats on the device for host transfers
     double* dparams = nullptr;
     bool forward_done = false;
+    uint32_t cap = 0;  // neighbour slots per particle of the segment records (the model's at creation)
     bool last_recorded = false;  // the segment records hold the last segment (set by forward)
     cudaGraphExec_t seg_graph = nullptr;  // recompute + reverse of one full segment
 
@@ -496,6 +497,7 @@ struct Rollout {
 
     int init(Model* model, int n_steps, int ck_every) {
         m = model;
+        cap = m->nbr_cap;
         steps = n_steps;
         every = ck_every < 1 ? 1 : ck_every;
         const size_t N = m->n ? m->n : 1;
@@ -520,7 +522,7 @@ struct Rollout {
             VFS_ADJ_TRY(cudaMalloc(&s_aux[t], N * sizeof(float4)));
             VFS_ADJ_TRY(cudaMalloc(&s_bnd[t], N * sizeof(float4)));
             VFS_ADJ_TRY(cudaMalloc(&s_perm[t], N * 4));
-            VFS_ADJ_TRY(cudaMalloc(&s_nbr[t], N * kNbrCap * 4));
+            VFS_ADJ_TRY(cudaMalloc(&s_nbr[t], N * (size_t)cap * 4));
             VFS_ADJ_TRY(cudaMalloc(&s_cnt[t], N * 4));
         }
         for (float4** b : {&fin_pos, &fin_vel, &xbar, &vbar, &xs, &vs, &abar, &gbar})
@@ -577,6 +579,8 @@ struct Rollout {
     // permutation, density products and neighbour lists: the model's buffers for those are pointed
     // at the segment's per-substep records, so the passes write them in place.
     int record_segment(int len) {
+        if (m->nbr_cap != cap)
+            return fail(VFS_ERR_INVALID_ARGUMENT, "the model's neighbour capacity changed after the rollout was created");
         float4* own_aux = m->aux;
         float4* own_bnd = m->bnd;
         uint32_t* own_nbr = m->nbr;
@@ -720,7 +724,8 @@ struct Rollout {
             uint32_t e = 0;
             cudaMemcpy(&e, m->err, 4, cudaMemcpyDeviceToHost);
             if (e & kErrAdjointOverflow)
-                return fail(VFS_ERR_CAPACITY, "a neighbour list exceeded 128 entries: the adjoint needs "
+                return fail(VFS_ERR_CAPACITY, "a neighbour list exceeded " + std::to_string(cap) +
+                                                  " entries: the adjoint needs "
                                               "complete lists");
             return rc;
         }

@@ -249,6 +249,7 @@ int Model::refresh_params() {
     std::vector<DevObject> objs;
     for (SceneHost& sh : scenes) {
         derive_scene_params(sh, sh.params);
+        sh.params.nbr_cap = nbr_cap;
         for (const ObjectStore& o : sh.objects) {
             DevObject d{};
             to_dev_object(o, d);
@@ -430,7 +431,7 @@ int Model::init() {
     VFS_CUDA_TRY(cudaMalloc(&bnd, N * sizeof(float4)));
     VFS_CUDA_TRY(cudaMalloc(&acc, N * sizeof(float4)));
     VFS_CUDA_TRY(cudaMalloc(&stage, N * 32));
-    VFS_CUDA_TRY(cudaMalloc(&nbr, N * kNbrCap * sizeof(uint32_t)));
+    VFS_CUDA_TRY(cudaMalloc(&nbr, N * nbr_cap * sizeof(uint32_t)));
     VFS_CUDA_TRY(cudaMalloc(&nbr_count, N * sizeof(uint32_t)));
     VFS_CUDA_TRY(cudaMalloc(&err, 4));
     VFS_CUDA_TRY(cudaMemset(err, 0, 4));
@@ -852,6 +853,23 @@ static int set_stream(Model& m, void* stream) {
     return VFS_OK;
 }
 
+// Neighbour-list slots per particle: lists longer than this make the force pass walk the
+// candidates again (and a differentiable rollout fail), so dense scenes want more slots; each slot
+// costs 4 bytes per particle.
+int set_neighbor_capacity(Model& m, int32_t slots) {
+    if (slots < 16 || slots > 4096) return fail(VFS_ERR_INVALID_ARGUMENT, "neighbour capacity must be in [16, 4096]");
+    VFS_CUDA_TRY(cudaStreamSynchronize(m.stream));
+    const size_t N = m.n ? m.n : 1;
+    uint32_t* fresh = nullptr;
+    VFS_CUDA_TRY(cudaMalloc(&fresh, N * (size_t)slots * sizeof(uint32_t)));
+    cudaFree(m.nbr);
+    m.nbr = fresh;
+    m.nbr_cap = (uint32_t)slots;
+    m.invalidate_graph();
+    m.stepped = false;
+    return m.refresh_params();
+}
+
 int set_sort_config(Model& m, int32_t digit_bits, int32_t tile_items) {
     if (digit_bits < 4 || digit_bits > 8) return fail(VFS_ERR_INVALID_ARGUMENT, "digit_bits must be in [4, 8]");
     if (tile_items != 8 && tile_items != 12 && tile_items != 16)
@@ -1120,6 +1138,15 @@ int vfs_model_set_sort_config(vfs_model* h, int32_t digit_bits, int32_t tile_ite
     return vfs::set_sort_config(m, digit_bits, tile_items);
 }
 
+int vfs_model_set_neighbor_capacity(vfs_model* h, int32_t slots) {
+    VFS_HANDLE(h);
+    return vfs::set_neighbor_capacity(m, slots);
+}
+
+int32_t vfs_model_get_neighbor_capacity(const vfs_model* h) {
+    return (h && h->m) ? (int32_t)h->m->nbr_cap : -1;
+}
+
 int vfs_model_get_sort_config(const vfs_model* h, int32_t* digit_bits, int32_t* tile_items,
                               int32_t* passes) {
     VFS_HANDLE(h);
@@ -1272,6 +1299,11 @@ int vfs_batch_synchronize(vfs_batch* h) {
 int vfs_batch_profile_substeps(vfs_batch* h, int32_t count, float* phase_ms) {
     VFS_HANDLE(h);
     return vfs::profile_phases(m, count, phase_ms);
+}
+
+int vfs_batch_set_neighbor_capacity(vfs_batch* h, int32_t slots) {
+    VFS_HANDLE(h);
+    return vfs::set_neighbor_capacity(m, slots);
 }
 
 int vfs_batch_set_sort_config(vfs_batch* h, int32_t digit_bits, int32_t tile_items) {

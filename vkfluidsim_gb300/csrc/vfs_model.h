@@ -61,7 +61,8 @@ struct Model {
     float4* rec = nullptr;  // 2 float4 per particle: the force pass's neighbour records
     float4* bnd = nullptr;
     float4* acc = nullptr;
-    uint32_t* nbr = nullptr;        // kNbrCap slot-major neighbour lists
+    uint32_t* nbr = nullptr;        // nbr_cap slot-major neighbour lists
+    uint32_t nbr_cap = kNbrCap;     // slots per particle (longer lists fall back to a walk)
     uint32_t* nbr_count = nullptr;  // list length per particle
     float* stage = nullptr;         // 32 bytes per particle of host-transfer staging
     uint32_t* scratch = nullptr;
@@ -113,6 +114,7 @@ int create_model(const std::vector<SceneHost>& scenes, Model** out);
 // cells+reorder, density, force, clear.
 int profile_phases(Model& m, int32_t count, float* phase_ms);
 int set_sort_config(Model& m, int32_t digit_bits, int32_t tile_items);
+int set_neighbor_capacity(Model& m, int32_t slots);
 
 }  // namespace vfs
 

@@ -405,6 +405,13 @@ class WCSPHWithBoundaryModel:
     def set_sort_config(self, digit_bits: int, tile_items: int) -> None:
         check(self._lib.vfs_model_set_sort_config(self._h, digit_bits, tile_items))
 
+    @property
+    def neighbor_capacity(self) -> int:
+        return int(self._lib.vfs_model_get_neighbor_capacity(self._h))
+
+    def set_neighbor_capacity(self, slots: int) -> None:
+        check(self._lib.vfs_model_set_neighbor_capacity(self._h, slots))
+
     def get_sort_config(self):
         d, t, p = C.c_int32(), C.c_int32(), C.c_int32()
         check(self._lib.vfs_model_get_sort_config(self._h, C.byref(d), C.byref(t), C.byref(p)))
@@ -612,6 +619,9 @@ class Batch:
 
     def set_sort_config(self, digit_bits: int, tile_items: int) -> None:
         check(self._lib.vfs_batch_set_sort_config(self._h, digit_bits, tile_items))
+
+    def set_neighbor_capacity(self, slots: int) -> None:
+        check(self._lib.vfs_batch_set_neighbor_capacity(self._h, slots))
 
     def export_state(self, scene: int, prefix) -> None:
         check(self._lib.vfs_batch_export_state(self._h, scene, str(prefix).encode()))
