@@ -570,6 +570,7 @@ __device__ __forceinline__ void for_each_candidate(const SceneParams& p,
         const uint32_t hA = hash_cell(cx - 1u, ry, rz);
         const uint32_t kA = key_mod(hA, p.mod_magic, p.n);
         uint32_t b0, e0, b1 = 0u, e1 = 0u, b2 = 0u, e2 = 0u;
+        int nseg = 1;
         // Cells cx-1..cx+1 share a hash block iff (cell + 25) / 50 agrees at both ends (this also
         // covers the wrap of cell + 25 at 2^32 near cell -26).
         const bool same_block = (cx + 24u) / 50u == (cx + 26u) / 50u && hA <= 0xFFFFFFFDu;
@@ -585,13 +586,14 @@ __device__ __forceinline__ void for_each_candidate(const SceneParams& p,
             e0 = skip_l ? b0 : __ldg(sc + kA + 1u);
             b1 = __ldg(sc + kB);
             e1 = __ldg(sc + kB + 1u);
+            nseg = 3;
             if (!skip_r) {
                 b2 = __ldg(sc + kC);
                 e2 = __ldg(sc + kC + 1u);
             }
         }
 #pragma unroll 1
-        for (int seg = 0; seg < 3; seg++) {
+        for (int seg = 0; seg < nseg; seg++) {
             const uint32_t b = seg == 0 ? b0 : (seg == 1 ? b1 : b2);
             const uint32_t e = seg == 0 ? e0 : (seg == 1 ? e1 : e2);
             uint32_t j = b;
