@@ -366,9 +366,10 @@ int Model::run_substeps(int count) {
 }
 
 int Model::check_device() {
+    // The error word rides the stream into pinned memory, so one synchronisation covers both.
+    VFS_CUDA_TRY(cudaMemcpyAsync(err_host, err, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
     VFS_CUDA_TRY(cudaStreamSynchronize(stream));
-    uint32_t e = 0;
-    VFS_CUDA_TRY(cudaMemcpy(&e, err, sizeof(e), cudaMemcpyDeviceToHost));
+    const uint32_t e = *err_host;
     if (e) return fail(VFS_ERR_DEVICE_CHECK, "device error word set: " + std::to_string(e) +
                                                  (e & kErrLookbackTimeout ? " (look-back timeout)" : ""));
     return VFS_OK;
@@ -394,6 +395,7 @@ Model::~Model() {
     cudaFree(nbr_count);
     cudaFree(scratch);
     cudaFree(err);
+    if (err_host) cudaFreeHost(err_host);
     cudaFree(d_scenes);
     cudaFree(d_scene_of);
     cudaFree(d_objects);
@@ -435,6 +437,7 @@ int Model::init() {
     VFS_CUDA_TRY(cudaMalloc(&nbr_count, N * sizeof(uint32_t)));
     VFS_CUDA_TRY(cudaMalloc(&err, 4));
     VFS_CUDA_TRY(cudaMemset(err, 0, 4));
+    VFS_CUDA_TRY(cudaMallocHost(&err_host, 4));
     for (int b = 0; b < 2; b++) {
         VFS_CUDA_TRY(cudaMemset(pos[b], 0, N * sizeof(float4)));
         VFS_CUDA_TRY(cudaMemset(vel[b], 0, N * sizeof(float4)));

@@ -68,6 +68,7 @@ struct Model {
     uint32_t* scratch = nullptr;
     size_t scratch_words = 0;
     uint32_t* err = nullptr;
+    uint32_t* err_host = nullptr;  // pinned copy of the error word read by check_device
     SceneParams* d_scenes = nullptr;   // batched launches: the scene table
     uint16_t* d_scene_of = nullptr;    // batched launches: scene id per particle
     DevObject* d_objects = nullptr;    // boundary objects of all scenes
