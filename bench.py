@@ -242,7 +242,7 @@ def time_batched(args, stream, torch):
 
 
 def time_adjoint(args, stream, torch):
-    """Differentiable rollout (BASELINE config 4: 65,536 particles, 300 substeps, checkpoint every
+    """Differentiable rollout (65,536-particle dam break, 300 substeps, checkpoint every
     25). The target is the rollout with viscosity 0.02, stiffness 60 and a smooth initial velocity
     (8 Fourier modes, 0.5 m/s); the optimised run starts from viscosity 0.01, stiffness 50, zero
     velocity; loss = MSE of final positions by id. Times the plain forward rollout against forward

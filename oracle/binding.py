@@ -1,7 +1,8 @@
 """ctypes binding of the CPU oracle (``oracle/_build/libvfs_oracle.so``).
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, ``__graft_entry__.smoke()`` and bench.py's
-CPU-baseline legs as the checker / CPU baseline. The product package never imports it.
+CPU-baseline legs, as the reference results and the timed CPU baseline. The product package never
+imports it.
 """
 from __future__ import annotations
 

@@ -1,7 +1,7 @@
 // The oracle: a CPU restatement of VkFluidSim's WCSPH-with-boundary substep.
 //
 // TEST INFRASTRUCTURE ONLY. Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline legs
-// load this library, and only as the checker / the timed CPU baseline. The product path
+// load this library, and only as the reference results / the timed CPU baseline. The product path
 // (vkfluidsim_gb300) never links, loads or calls it.
 //
 // PARITY UNPINNED: the reference publishes no golden vectors or known-answer tests for this path,

@@ -186,7 +186,7 @@ def test_graph_and_stream_launch_agree_bitwise(dam):
 
 
 def test_full_size_one_million_particles():
-    """BASELINE's plain configuration at full size: 1,048,576 particles with the sphere map."""
+    """The plain 1M workload at full size: 1,048,576 particles with the sphere map."""
     w = W.obstacle_1m(map_res=128)
     m = W.build_model(w)
     m.substeps(1)

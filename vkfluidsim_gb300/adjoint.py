@@ -2,7 +2,8 @@
 ``torch.autograd.Function`` over it.
 
 Gradients are returned by particle id (the order in which the state was first set). The loss of the
-BASELINE differentiable configuration is the mean squared error of the final positions by id.
+65,536-particle differentiable benchmark workload is the mean squared error of the final
+positions by id.
 """
 from __future__ import annotations
 
