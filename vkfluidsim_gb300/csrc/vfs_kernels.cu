@@ -741,13 +741,24 @@ __device__ __forceinline__ void force_term(const SceneParams& p, const float4& x
     f.Vz = __fmaf_rn(__fmul_rn(tv, __fmul_rn(nz, gw)), iden, f.Vz);
 }
 
+// A 32-byte force record in one 256-bit load (sm_100+; rec + 2j is 32-byte aligned because the
+// buffer comes from cudaMalloc and each record is 32 bytes).
+__device__ __forceinline__ void load_record(const float4* __restrict__ rec, uint32_t j, float4& a,
+                                            float4& b) {
+    const float4* q = rec + 2 * (size_t)j;
+    asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+        : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w)
+        : "l"(q));
+}
+
 // One neighbour's term from its force record: rec[2j] = (x, y, z, p/rho^2), rec[2j+1] =
 // (vx, vy, vz, m/max(rho, 1e-6)), the same values as pos, vel and aux hold.
 __device__ __forceinline__ void force_term_rec(const SceneParams& p, const float4& xi,
                                                const float4& vi, float pdi,
                                                const float4* __restrict__ rec, uint32_t j,
                                                ForceAcc& f) {
-    const float4 r0 = __ldg(rec + 2 * (size_t)j), r1 = __ldg(rec + 2 * (size_t)j + 1);
+    float4 r0, r1;
+    load_record(rec, j, r0, r1);
     force_term(p, xi, vi, pdi, r0, make_float2(r0.w, r1.w), r1, f);
 }
 
@@ -796,10 +807,7 @@ __global__ void __launch_bounds__(kNbrBlock, kMinBlocks)
 #pragma unroll
             for (int u = 0; u < 4; u++) j[u] = __ldg(nl + u * stride);
 #pragma unroll
-            for (int u = 0; u < 4; u++) {
-                a[u] = __ldg(rec + 2 * (size_t)j[u]);
-                b[u] = __ldg(rec + 2 * (size_t)j[u] + 1);
-            }
+            for (int u = 0; u < 4; u++) load_record(rec, j[u], a[u], b[u]);
 #pragma unroll
             for (int u = 0; u < 4; u++) force_term(p, xi, vi, pdi, a[u], make_float2(a[u].w, b[u].w), b[u], f);
         }
