@@ -335,6 +335,76 @@ def time_stress(args, stream, torch):
             "roofline_frac": frac}
 
 
+def time_next_rows(args, stream, torch, model, rank):
+    """Setup and output paths beside the step: GPU volume-map generation (analytic sphere at 128^3
+    and 64^3, a 320-triangle mesh at 64^3) against the oracle's OpenMP CPU generator at 64^3,
+    headless rendering of the 1M scene at 1920 x 1080, and one state snapshot (bin + JSON)."""
+    import tempfile
+
+    import vkfluidsim_gb300 as vfs
+    from vkfluidsim_gb300 import workloads as W
+
+    out = {}
+    probe = W.build_model(W.dam_break(dims=(4, 4, 4), map_res=0))
+    probe.set_stream(stream.cuda_stream)
+
+    def gpu_ms(fn):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        fn()
+        probe.synchronize()
+        return 1e3 * (time.perf_counter() - t0)
+
+    h = float(probe.get_parameters()[0].smooth_radius)
+    for res in (128, 64):
+        obj = vfs.AnalyticObject(vfs.SHAPE_SPHERE, (0.25,), resolution=(res,) * 3)
+        out[f"sphere_map_{res}_gpu_ms"] = gpu_ms(lambda: probe.add_analytic_object(obj))
+    # A 320-triangle icosphere (radius 0.25).
+    g = (1 + 5 ** 0.5) / 2
+    v = [(-1, g, 0), (1, g, 0), (-1, -g, 0), (1, -g, 0), (0, -1, g), (0, 1, g), (0, -1, -g),
+         (0, 1, -g), (g, 0, -1), (g, 0, 1), (-g, 0, -1), (-g, 0, 1)]
+    v = [np.array(q, np.float64) / np.linalg.norm(q) for q in v]
+    f = [(0, 11, 5), (0, 5, 1), (0, 1, 7), (0, 7, 10), (0, 10, 11), (1, 5, 9), (5, 11, 4),
+         (11, 10, 2), (10, 7, 6), (7, 1, 8), (3, 9, 4), (3, 4, 2), (3, 2, 6), (3, 6, 8), (3, 8, 9),
+         (4, 9, 5), (2, 4, 11), (6, 2, 10), (8, 6, 7), (9, 8, 1)]
+    for _ in range(2):
+        mid, nf = {}, []
+        for a, b, c in f:
+            ks = []
+            for x, y in ((a, b), (b, c), (c, a)):
+                k = (min(x, y), max(x, y))
+                if k not in mid:
+                    q = v[x] + v[y]
+                    v.append(q / np.linalg.norm(q))
+                    mid[k] = len(v) - 1
+                ks.append(mid[k])
+            nf += [(a, ks[0], ks[2]), (b, ks[1], ks[0]), (c, ks[2], ks[1]), tuple(ks)]
+        f = nf
+    mesh = vfs.MeshObject(vertices=np.array(v) * 0.25, triangles=np.array(f), resolution=(64,) * 3)
+    out["mesh_map_64_gpu_ms"] = gpu_ms(lambda: probe.add_mesh_object(mesh))
+    out["mesh_triangles"] = len(f)
+    if rank == 0 and not args.no_cpu:
+        from oracle import binding as ob
+
+        t0 = time.perf_counter()
+        ob.volume_map(0, (0.25,), h, (64, 64, 64), np.float32(8 * h))
+        out["sphere_map_64_cpu_oracle_ms"] = 1e3 * (time.perf_counter() - t0)
+        out["cpu_threads"] = ob.get_threads()
+    del probe
+    eye, center = (1.0, -1.6, 1.2), (1.0, 0.5, 0.25)
+    mv, pj = vfs.look_at(eye, center), vfs.perspective(0.8, 1920 / 1080, 0.05, 20.0)
+    model.render_particles(mv, pj, 1920, 1080, quad_side=0.01)  # warm-up
+    t0 = time.perf_counter()
+    model.render_particles(mv, pj, 1920, 1080, quad_side=0.01)
+    out["render_1920x1080_ms"] = 1e3 * (time.perf_counter() - t0)
+    with tempfile.TemporaryDirectory() as d:
+        t0 = time.perf_counter()
+        model.export_state(f"{d}/snap")
+        out["snapshot_ms"] = 1e3 * (time.perf_counter() - t0)
+    out["particles"] = model.n_particles
+    return out
+
+
 def run_gpu(args):
     import torch
 
@@ -432,6 +502,7 @@ def run_gpu(args):
         batched = time_batched(args, stream, torch)
     adjoint = time_adjoint(args, stream, torch) if args.adjoint else None
     stress = time_stress(args, stream, torch) if args.stress else None
+    next_rows = time_next_rows(args, stream, torch, m, rank) if args.next_rows else None
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -467,6 +538,8 @@ def run_gpu(args):
             line["fwd_adjoint"] = adjoint
         if stress:
             line["stress"] = stress
+        if next_rows:
+            line["next_rows"] = next_rows
         if cpu:
             line["cpu_baseline"] = cpu
         print(json.dumps(line), flush=True)
@@ -488,6 +561,7 @@ def main():
     ap.add_argument("--adjoint", type=int, default=1)
     ap.add_argument("--stress", type=int, default=1)
     ap.add_argument("--autotune", type=int, default=1)
+    ap.add_argument("--next-rows", type=int, default=1)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -658,6 +658,7 @@ int Model::add_analytic(uint32_t scene, const vfs_analytic_object& a) {
     gauss_legendre_nodes(vp.qn, vp.gx, vp.gw);
     vp.c0 = 0.5 * (double)(h - (-h));
     vp.c1 = 0.5 * (double)(h + (-h));
+    for (int k = 0; k < vp.qn; k++) vp.gxf[k] = (float)(vp.c0 * vp.gx[k] + vp.c1);
     const double hd = (double)h;
     vp.w_factor = 8.0 / (pi_d() * hd * hd * hd);
     vp.full_ball = volume_map_full_ball(vp);
@@ -781,6 +782,7 @@ int Model::add_mesh(uint32_t scene, const vfs_mesh_object& a) {
     gauss_legendre_nodes(vp.qn, vp.gx, vp.gw);
     vp.c0 = 0.5 * (double)(h - (-h));
     vp.c1 = 0.5 * (double)(h + (-h));
+    for (int k = 0; k < vp.qn; k++) vp.gxf[k] = (float)(vp.c0 * vp.gx[k] + vp.c1);
     const double hd = (double)h;
     vp.w_factor = 8.0 / (pi_d() * hd * hd * hd);
     vp.full_ball = volume_map_full_ball(vp);

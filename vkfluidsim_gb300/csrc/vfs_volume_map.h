@@ -17,6 +17,7 @@ struct VolumeMapParams {
     double step[3];     // grid step, computed in float then widened
     int qn;             // Gauss-Legendre points per axis
     double gx[kMaxQuadrature], gw[kMaxQuadrature];
+    float gxf[kMaxQuadrature];  // quadrature coordinates c0 * gx + c1 rounded to float (the points' offsets)
     double c0, c1;      // integration-domain half width and centre
     double w_factor;    // 8 / (pi h^3) in double
     double full_ball;   // the integral when every quadrature point lies inside the solid
