@@ -299,6 +299,8 @@ int Model::alloc_sort_scratch() {
         VFS_CUDA_TRY(cudaMalloc(&scratch, words * sizeof(uint32_t)));
         scratch_words = words;
     }
+    VFS_CUDA_TRY(cudaStreamSynchronize(stream));
+    VFS_CUDA_TRY(cudaMemset(scratch, 0, words * sizeof(uint32_t)));
     sort_scratch.ghist = scratch;
     sort_scratch.counters = scratch + (size_t)sc.passes * sc.bins;
     sort_scratch.status = sort_scratch.counters + sc.passes;
@@ -314,13 +316,14 @@ int Model::enqueue_substep(cudaEvent_t* ev) {
     cudaStream_t s = stream;
     const int c = cur, o = 1 - cur;
     if (ev) VFS_CUDA_TRY(cudaEventRecord(ev[0], s));
-    VFS_CUDA_TRY(cudaMemsetAsync(scratch, 0, sort_scratch_words(sc) * sizeof(uint32_t), s));
+    // The sort scratch is zero here: zeroed when allocated and by every substep's cell pass.
     if (ev) VFS_CUDA_TRY(cudaEventRecord(ev[1], s));
     VFS_CUDA_TRY(launch_keys(launch, pos[c], keys, sc, sort_scratch.ghist, s));
     if (ev) VFS_CUDA_TRY(cudaEventRecord(ev[2], s));
     VFS_CUDA_TRY(launch_sort(n, sc, sort_scratch, keys, keys_alt, vals, vals_alt, &skeys, &sperm, s));
     if (ev) VFS_CUDA_TRY(cudaEventRecord(ev[3], s));
-    VFS_CUDA_TRY(launch_cells_reorder(n, skeys, sperm, cell_scan, pos[c], vel[c], pos[o], vel[o], kc, s));
+    VFS_CUDA_TRY(launch_cells_reorder(n, skeys, sperm, cell_scan, pos[c], vel[c], pos[o], vel[o],
+                                      scratch, (uint32_t)sort_scratch_words(sc), kc, s));
     if (ev) VFS_CUDA_TRY(cudaEventRecord(ev[4], s));
     VFS_CUDA_TRY(launch_density(launch, pos[o], vel[o], rec, cell_scan, aux, bnd, nbr, nbr_count, kc, s));
     if (ev) VFS_CUDA_TRY(cudaEventRecord(ev[5], s));

@@ -131,11 +131,12 @@ cudaError_t launch_digit_hist(const uint32_t* keys, uint32_t n, const SortConfig
 cudaError_t launch_sort(uint32_t n, const SortConfig& sc, const SortScratch& scratch,
                         uint32_t* keys, uint32_t* keys_alt, uint32_t* vals, uint32_t* vals_alt,
                         uint32_t** sorted_keys, uint32_t** sorted_perm, cudaStream_t s);
-// cell_scan[k] = first sorted index with key >= k (k in [0, n]); gathers pos/vel by perm.
+// cell_scan[k] = first sorted index with key >= k (k in [0, n]); gathers pos/vel by perm; zeroes
+// zero[0, zero_words) (the sort scratch, for the next substep).
 cudaError_t launch_cells_reorder(uint32_t n, const uint32_t* skeys, const uint32_t* perm,
                                  uint32_t* cell_scan, const float4* pos_in, const float4* vel_in,
-                                 float4* pos_out, float4* vel_out, const KernelConfig& kc,
-                                 cudaStream_t s);
+                                 float4* pos_out, float4* vel_out, uint32_t* zero,
+                                 uint32_t zero_words, const KernelConfig& kc, cudaStream_t s);
 // Failure-detection self-test of the sort's bounded look-back wait (d_work: 96 words).
 cudaError_t launch_lookback_selftest(bool published, uint32_t spin_limit, uint32_t* d_work,
                                      uint32_t* err, cudaStream_t s);

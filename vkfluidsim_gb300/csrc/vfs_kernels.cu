@@ -467,8 +467,13 @@ __global__ void __launch_bounds__(kCellBlock)
     k_cells_reorder(uint32_t n, const uint32_t* __restrict__ skeys,
                     const uint32_t* __restrict__ perm, uint32_t* __restrict__ scan,
                     const float4* __restrict__ pos_in, const float4* __restrict__ vel_in,
-                    float4* __restrict__ pos_out, float4* __restrict__ vel_out) {
+                    float4* __restrict__ pos_out, float4* __restrict__ vel_out,
+                    uint32_t* __restrict__ zero, uint32_t zero_words) {
     __shared__ uint32_t s_lo, s_hi;
+    // The sort is done with its scratch (histograms, tile counters, look-back status): clear it
+    // for the next substep here instead of in a separate memset.
+    for (uint32_t w = blockIdx.x * kCellBlock + threadIdx.x; w < zero_words; w += gridDim.x * kCellBlock)
+        zero[w] = 0u;
     const uint32_t c0 = blockIdx.x * kCellBlock;
     const uint32_t c1 = min(c0 + kCellBlock, n + 1u);
     const uint32_t tid = threadIdx.x;
@@ -967,21 +972,21 @@ cudaError_t launch_sort(uint32_t n, const SortConfig& sc, const SortScratch& scr
 
 cudaError_t launch_cells_reorder(uint32_t n, const uint32_t* skeys, const uint32_t* perm,
                                  uint32_t* cell_scan, const float4* pos_in, const float4* vel_in,
-                                 float4* pos_out, float4* vel_out, const KernelConfig& kc,
-                                 cudaStream_t s) {
+                                 float4* pos_out, float4* vel_out, uint32_t* zero,
+                                 uint32_t zero_words, const KernelConfig& kc, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
     switch (kc.cell_block) {
         case 128:
             k_cells_reorder<128><<<(n + 128u) / 128u, 128, 0, s>>>(n, skeys, perm, cell_scan, pos_in,
-                                                                 vel_in, pos_out, vel_out);
+                                                                 vel_in, pos_out, vel_out, zero, zero_words);
             break;
         case 512:
             k_cells_reorder<512><<<(n + 512u) / 512u, 512, 0, s>>>(n, skeys, perm, cell_scan, pos_in,
-                                                                 vel_in, pos_out, vel_out);
+                                                                 vel_in, pos_out, vel_out, zero, zero_words);
             break;
         default:
             k_cells_reorder<256><<<(n + 256u) / 256u, 256, 0, s>>>(n, skeys, perm, cell_scan, pos_in,
-                                                                 vel_in, pos_out, vel_out);
+                                                                 vel_in, pos_out, vel_out, zero, zero_words);
     }
     return cudaGetLastError();
 }
