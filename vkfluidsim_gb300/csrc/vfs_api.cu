@@ -304,6 +304,9 @@ int Model::alloc_sort_scratch() {
     sort_scratch.ghist = scratch;
     sort_scratch.counters = scratch + (size_t)sc.passes * sc.bins;
     sort_scratch.status = sort_scratch.counters + sc.passes;
+    sort_scratch.dcounter = sort_scratch.status + (size_t)sc.passes * sc.tiles * sc.bins;
+    sort_scratch.mcount = sort_scratch.dcounter + 1;
+    sort_scratch.dstatus = sort_scratch.mcount + 1;
     sort_scratch.err = err;
     invalidate_graph();
     return VFS_OK;
@@ -318,12 +321,19 @@ int Model::enqueue_substep(cudaEvent_t* ev) {
     if (ev) VFS_CUDA_TRY(cudaEventRecord(ev[0], s));
     // The sort scratch is zero here: zeroed when allocated and by every substep's cell pass.
     if (ev) VFS_CUDA_TRY(cudaEventRecord(ev[1], s));
-    VFS_CUDA_TRY(launch_keys(launch, pos[c], keys, sc, sort_scratch.ghist, s));
+    // Incremental stable sort: keys + the particles whose key changed (compacted into keys/vals),
+    // a sort of those alone (count on the device), a merge with the rest.
+    VFS_CUDA_TRY(launch_keys_delta(launch, pos[c], pkeys, keys, vals, mprefix, sc, sort_scratch, s));
     if (ev) VFS_CUDA_TRY(cudaEventRecord(ev[2], s));
-    VFS_CUDA_TRY(launch_sort(n, sc, sort_scratch, keys, keys_alt, vals, vals_alt, &skeys, &sperm, s));
+    uint32_t *mk = nullptr, *mi = nullptr;
+    VFS_CUDA_TRY(launch_sort(n, sc, sort_scratch, keys, keys_alt, vals, vals_alt, &mk, &mi, s,
+                             /*vals_given=*/true, sort_scratch.mcount));
+    VFS_CUDA_TRY(launch_merge(n, pkeys, mprefix, sort_scratch.mcount, mk, mi, sk_buf, sp_buf, s));
+    skeys = sk_buf;
+    sperm = sp_buf;
     if (ev) VFS_CUDA_TRY(cudaEventRecord(ev[3], s));
     VFS_CUDA_TRY(launch_cells_reorder(n, skeys, sperm, cell_scan, pos[c], vel[c], pos[o], vel[o],
-                                      scratch, (uint32_t)sort_scratch_words(sc), kc, s));
+                                      scratch, (uint32_t)sort_scratch_words(sc), pkeys, kc, s));
     if (ev) VFS_CUDA_TRY(cudaEventRecord(ev[4], s));
     VFS_CUDA_TRY(launch_density(launch, pos[o], vel[o], rec, cell_scan, aux, bnd, nbr, nbr_count, kc, s));
     if (ev) VFS_CUDA_TRY(cudaEventRecord(ev[5], s));
@@ -391,6 +401,10 @@ Model::~Model() {
     cudaFree(cell_scan);
     cudaFree(aux);
     cudaFree(rec);
+    cudaFree(sk_buf);
+    cudaFree(sp_buf);
+    cudaFree(pkeys);
+    cudaFree(mprefix);
     cudaFree(bnd);
     cudaFree(acc);
     cudaFree(stage);
@@ -431,6 +445,11 @@ int Model::init() {
     VFS_CUDA_TRY(cudaMalloc(&vals, N * 4));
     VFS_CUDA_TRY(cudaMalloc(&vals_alt, N * 4));
     VFS_CUDA_TRY(cudaMalloc(&cell_scan, (N + 1) * 4));
+    VFS_CUDA_TRY(cudaMalloc(&sk_buf, N * 4));
+    VFS_CUDA_TRY(cudaMalloc(&sp_buf, N * 4));
+    VFS_CUDA_TRY(cudaMalloc(&pkeys, N * 4));
+    VFS_CUDA_TRY(cudaMemset(pkeys, 0xFF, N * 4));  // sorted, and no key equals it: all moved
+    VFS_CUDA_TRY(cudaMalloc(&mprefix, (N + 1) * 4));
     VFS_CUDA_TRY(cudaMalloc(&aux, N * sizeof(float4)));
     VFS_CUDA_TRY(cudaMalloc(&rec, 2 * N * sizeof(float4)));
     VFS_CUDA_TRY(cudaMalloc(&bnd, N * sizeof(float4)));

@@ -94,6 +94,9 @@ struct SortScratch {
     uint32_t* ghist;     // [passes][bins]
     uint32_t* counters;  // [passes]
     uint32_t* status;    // [passes][tiles][bins]
+    uint32_t* dcounter;  // key/delta pass: block claim counter [1]
+    uint32_t* dstatus;   // key/delta pass: look-back status per block [delta_blocks]
+    uint32_t* mcount;    // number of particles whose key changed [1]
     uint32_t* err;       // device error word
 };
 
@@ -103,6 +106,7 @@ struct SortConfig {
     int bins;
     int tile;        // elements per onesweep tile
     uint32_t tiles;
+    uint32_t delta_blocks;  // tiles of the key/delta pass (1024 particles each)
 };
 
 // ---- launch wrappers (vfs_kernels.cu) ----
@@ -127,16 +131,32 @@ cudaError_t launch_keys(const StepLaunch& L, const float4* pos, uint32_t* keys,
 // Per-pass digit histograms of caller-provided keys.
 cudaError_t launch_digit_hist(const uint32_t* keys, uint32_t n, const SortConfig& sc,
                               uint32_t* ghist, cudaStream_t s);
+// Incremental sort, pass 1: keys, moved flags (key != pkeys[i]), their exclusive prefix
+// mprefix[0..n], the moved (key, index) pairs compacted in index order, their digit histograms,
+// and the moved count in scr.mcount.
+cudaError_t launch_keys_delta(const StepLaunch& L, const float4* pos, const uint32_t* pkeys,
+                              uint32_t* mkeys, uint32_t* midx, uint32_t* mprefix,
+                              const SortConfig& sc, const SortScratch& scr, cudaStream_t s);
+// Incremental sort, last pass: merge of the unmoved particles with the sorted moved ones into the
+// stable sort of all (key, index) pairs.
+cudaError_t launch_merge(uint32_t n, const uint32_t* pkeys, const uint32_t* mprefix,
+                         const uint32_t* mcount, const uint32_t* mk, const uint32_t* mi,
+                         uint32_t* out_keys, uint32_t* out_perm, cudaStream_t s);
 // Stable LSD onesweep over sc.passes digits; returns the buffers holding sorted keys / perm.
+// vals_given: `vals` holds the values to carry (else the values are the indices); n_dev: an
+// optional device-side count (<= n) of elements to sort (the digit histograms must match it).
 cudaError_t launch_sort(uint32_t n, const SortConfig& sc, const SortScratch& scratch,
                         uint32_t* keys, uint32_t* keys_alt, uint32_t* vals, uint32_t* vals_alt,
-                        uint32_t** sorted_keys, uint32_t** sorted_perm, cudaStream_t s);
+                        uint32_t** sorted_keys, uint32_t** sorted_perm, cudaStream_t s,
+                        bool vals_given = false, const uint32_t* n_dev = nullptr);
 // cell_scan[k] = first sorted index with key >= k (k in [0, n]); gathers pos/vel by perm; zeroes
-// zero[0, zero_words) (the sort scratch, for the next substep).
+// zero[0, zero_words) (the sort scratch, for the next substep); copies skeys to pkeys_out (the next
+// substep's previous sorted keys) when pkeys_out is not NULL.
 cudaError_t launch_cells_reorder(uint32_t n, const uint32_t* skeys, const uint32_t* perm,
                                  uint32_t* cell_scan, const float4* pos_in, const float4* vel_in,
                                  float4* pos_out, float4* vel_out, uint32_t* zero,
-                                 uint32_t zero_words, const KernelConfig& kc, cudaStream_t s);
+                                 uint32_t zero_words, uint32_t* pkeys_out, const KernelConfig& kc,
+                                 cudaStream_t s);
 // Failure-detection self-test of the sort's bounded look-back wait (d_work: 96 words).
 cudaError_t launch_lookback_selftest(bool published, uint32_t spin_limit, uint32_t* d_work,
                                      uint32_t* err, cudaStream_t s);

@@ -344,10 +344,13 @@ __global__ void __launch_bounds__(BLOCK)
                uint32_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out, uint32_t n,
                int shift, int bins, const uint32_t* __restrict__ ghist,
                uint32_t* __restrict__ counter, uint32_t* __restrict__ status,
-               uint32_t* __restrict__ err) {
+               uint32_t* __restrict__ err, const uint32_t* __restrict__ n_dev) {
     static_assert(BLOCK == 256, "block scan assumes 256 threads");
     constexpr int WARPS = BLOCK / 32;
     constexpr int TILE = BLOCK * ITEMS;
+    // A device-side count (at most n) sorts only that prefix; the grid is sized for n and tiles
+    // past the count leave at once (no later tile waits on them: tiles are claimed in order).
+    if (n_dev) n = min(n, *n_dev);
     __shared__ uint32_t s_whist[WARPS][kMaxSortBins];
     __shared__ uint32_t s_dstart[kMaxSortBins];
     __shared__ uint32_t s_gofs[kMaxSortBins];
@@ -365,6 +368,7 @@ __global__ void __launch_bounds__(BLOCK)
     const uint32_t gcount = tid < bins ? __ldg(ghist + tid) : 0u;
     const uint32_t gbase = block_excl_scan256(gcount, s_scan);  // contains __syncthreads
     const uint32_t tile = s_tile;
+    if ((uint64_t)tile * TILE >= n) return;  // block-uniform, after the last barrier of the scan
     const uint32_t base = tile * (uint32_t)TILE + (uint32_t)warp * ITEMS * 32u;
     const uint32_t lt_mask = (1u << lane) - 1u;
 
@@ -468,7 +472,8 @@ __global__ void __launch_bounds__(kCellBlock)
                     const uint32_t* __restrict__ perm, uint32_t* __restrict__ scan,
                     const float4* __restrict__ pos_in, const float4* __restrict__ vel_in,
                     float4* __restrict__ pos_out, float4* __restrict__ vel_out,
-                    uint32_t* __restrict__ zero, uint32_t zero_words) {
+                    uint32_t* __restrict__ zero, uint32_t zero_words,
+                    uint32_t* __restrict__ pkeys_out) {
     __shared__ uint32_t s_lo, s_hi;
     // The sort is done with its scratch (histograms, tile counters, look-back status): clear it
     // for the next substep here instead of in a separate memset.
@@ -485,6 +490,7 @@ __global__ void __launch_bounds__(kCellBlock)
         if (src >= n) src = i;  // only after a reported sort failure
         pos_out[i] = __ldg(pos_in + src);
         vel_out[i] = __ldg(vel_in + src);
+        if (pkeys_out) pkeys_out[i] = skeys[i];
     }
     __syncthreads();
     const uint32_t lo = s_lo, hi = max(s_lo, s_hi);
@@ -863,15 +869,227 @@ __global__ void __launch_bounds__(kNbrBlock, kMinBlocks)
     pos_out[i] = make_float4(xi.x + nvx * p.dt, xi.y + nvy * p.dt, xi.z + nvz * p.dt, xi.w);
 }
 
+// ---------------------------------------------------------------- incremental sort
+// Particles move little per substep, so most keep the key they had in the previous substep, whose
+// stably sorted keys `pkeys` line up with the current (reordered) particles. The particles whose
+// key changed ("moved", in index order) are sorted stably by key and merged with the others by
+// (key, index): exactly the stable sort of all (key, index) pairs. The unmoved particles' keys are
+// pkeys[i], a subsequence of a sorted array, so they are already in order; this holds for any
+// sorted pkeys (all moved when pkeys is the all-ones fill of a fresh model), so no step ever
+// needs to know whether pkeys is current.
+
+// Keys, moved flags and the moved particles' compaction: mprefix[i] = number of moved particles
+// before i (mprefix[n] = total = *mcount), (mkeys, midx)[rank] for the moved ones in index order,
+// and the digit histograms of the moved keys. A tile is 256 threads x kDeltaItems particles
+// (particle tile * kDeltaTile + item * 256 + thread, so every load is coalesced); tiles are
+// claimed in order and chained by a bounded decoupled look-back over their moved counts.
+// Decoupled look-back of tile `tile` over single-counter status words, one warp wide: lane l reads
+// tile - 1 - l, so each step covers 32 predecessors. Sums aggregates up to and including the
+// nearest inclusive prefix. Each lane polls a word that has published nothing at most
+// kLookbackSpinLimit times, then sets kErrLookbackTimeout and counts it as zero. Called by a
+// whole warp; every lane returns the same sum.
+__device__ __forceinline__ uint32_t warp_lookback(const uint32_t* status, uint32_t tile, uint32_t* err) {
+    const int lane = threadIdx.x & 31;
+    uint32_t excl = 0u;
+    int64_t top = (int64_t)tile - 1;  // nearest predecessor not yet summed
+    while (top >= 0) {
+        const int64_t t = top - lane;
+        uint32_t v = kFlagPrefix;  // below tile 0: an empty prefix
+        if (t >= 0) {
+            uint32_t spins = 0u;
+            while (true) {
+                v = ld_volatile(status + t);
+                if ((v & ~kCountMask) != 0u) break;
+                if (++spins > kLookbackSpinLimit) {
+                    atomicOr(err, kErrLookbackTimeout);
+                    v = kFlagPrefix;
+                    break;
+                }
+                __nanosleep(32);
+            }
+        }
+        const uint32_t pre = __ballot_sync(0xffffffffu, (v & ~kCountMask) == kFlagPrefix);
+        const int stop = pre ? __ffs(pre) - 1 : 31;  // lanes 0..stop are summed
+        uint32_t c = lane <= stop ? (v & kCountMask) : 0u;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+        excl += c;
+        if (pre) break;
+        top -= 32;
+    }
+    return excl;
+}
+
+constexpr int kDeltaItems = 4;
+constexpr uint32_t kDeltaTile = 256u * kDeltaItems;
+
+template <bool kBatch>
+__global__ void __launch_bounds__(256)
+    k_keys_delta(StepLaunch L, const float4* __restrict__ pos, const uint32_t* __restrict__ pkeys,
+                 uint32_t* __restrict__ mkeys, uint32_t* __restrict__ midx,
+                 uint32_t* __restrict__ mprefix, int passes, int digit_bits,
+                 uint32_t* __restrict__ ghist, uint32_t* __restrict__ counter,
+                 uint32_t* __restrict__ status, uint32_t* __restrict__ mcount,
+                 uint32_t* __restrict__ err) {
+    __shared__ uint32_t s_h[kMaxSortPasses * kMaxSortBins];
+    __shared__ uint32_t s_cnt[kDeltaItems * 8];  // moved count per (item, warp), then its offset
+    __shared__ uint32_t s_blk, s_excl;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int bins = 1 << digit_bits;
+    const uint32_t mask = (uint32_t)bins - 1u;
+    if (tid == 0) s_blk = atomicAdd(counter, 1u);
+    for (int e = tid; e < passes * bins; e += 256) s_h[e] = 0u;
+    __syncthreads();
+    const uint32_t tile = s_blk;
+    const uint32_t base = tile * kDeltaTile + (uint32_t)tid;
+    uint32_t key[kDeltaItems];
+    uint32_t ball[kDeltaItems];
+#pragma unroll
+    for (int k = 0; k < kDeltaItems; k++) {
+        const uint32_t i = base + (uint32_t)k * 256u;
+        bool moved = false;
+        key[k] = 0u;
+        if (i < L.total) {
+            const SceneParams& p = scene_params<kBatch>(L, i);
+            const float4 x = pos[i];
+            key[k] = p.off + key_mod(hash_cell(cell_coord(x.x, p.h), cell_coord(x.y, p.h),
+                                               cell_coord(x.z, p.h)),
+                                     p.mod_magic, p.n);
+            moved = key[k] != pkeys[i];
+            if (moved)
+                for (int ps = 0; ps < passes; ps++)
+                    atomicAdd(&s_h[ps * bins + ((key[k] >> (ps * digit_bits)) & mask)], 1u);
+        }
+        ball[k] = __ballot_sync(0xffffffffu, moved);
+        if (lane == 0) s_cnt[k * 8 + warp] = __popc(ball[k]);
+    }
+    __syncthreads();
+    if (warp == 0) {
+        // Exclusive offsets in particle order (item-major, then warp): each lane scans 4 entries.
+        constexpr int kPerLane = kDeltaItems * 8 / 32;
+        static_assert(kDeltaItems % 4 == 0, "whole counters per lane");
+        uint32_t c[kPerLane], sum = 0u;
+#pragma unroll
+        for (int q = 0; q < kPerLane; q++) {
+            c[q] = s_cnt[lane * kPerLane + q];
+            sum += c[q];
+        }
+        uint32_t incl = sum;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += v;
+        }
+        uint32_t run = incl - sum;
+#pragma unroll
+        for (int q = 0; q < kPerLane; q++) {
+            s_cnt[lane * kPerLane + q] = run;
+            run += c[q];
+        }
+        const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+        uint32_t excl = 0u;
+        if (tile == 0u) {
+            if (lane == 0) st_volatile(status, kFlagPrefix | total);
+        } else {
+            if (lane == 0) st_volatile(status + tile, kFlagAggregate | total);
+            excl = warp_lookback(status, tile, err);
+            if (lane == 0) st_volatile(status + tile, kFlagPrefix | ((excl + total) & kCountMask));
+        }
+        if (lane == 0) {
+            s_excl = excl;
+            if (tile == gridDim.x - 1u) {
+                *mcount = excl + total;
+                mprefix[L.total] = excl + total;
+            }
+        }
+    }
+    __syncthreads();
+    const uint32_t lt = (1u << lane) - 1u;
+#pragma unroll
+    for (int k = 0; k < kDeltaItems; k++) {
+        const uint32_t i = base + (uint32_t)k * 256u;
+        if (i < L.total) {
+            const uint32_t rank = s_excl + s_cnt[k * 8 + warp] + __popc(ball[k] & lt);
+            mprefix[i] = rank;
+            if ((ball[k] >> lane) & 1u) {
+                mkeys[rank] = key[k];
+                midx[rank] = i;
+            }
+        }
+    }
+    for (int e = tid; e < passes * bins; e += 256)
+        if (s_h[e]) atomicAdd(&ghist[e], s_h[e]);
+}
+
+__device__ __forceinline__ uint32_t lower_bound_u32(const uint32_t* a, uint32_t n, uint32_t v) {
+    uint32_t lo = 0u, hi = n;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (a[mid] < v) lo = mid + 1u; else hi = mid;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ uint32_t upper_bound_u32(const uint32_t* a, uint32_t n, uint32_t v) {
+    uint32_t lo = 0u, hi = n;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (a[mid] <= v) lo = mid + 1u; else hi = mid;
+    }
+    return lo;
+}
+
+// Merge of the unmoved particles (keys pkeys[i], in index order) with the sorted moved ones
+// (mk, mi) by (key, index). Thread t < n places unmoved particle t; thread n + r places the moved
+// particle of sorted rank r. Every output position is computed independently.
+__global__ void __launch_bounds__(256)
+    k_merge(uint32_t n, const uint32_t* __restrict__ pkeys, const uint32_t* __restrict__ mprefix,
+            const uint32_t* __restrict__ mcount, const uint32_t* __restrict__ mk,
+            const uint32_t* __restrict__ mi, uint32_t* __restrict__ out_keys,
+            uint32_t* __restrict__ out_perm) {
+    const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t m = min(*mcount, n);
+    uint32_t key, idx, pos;
+    if (t < n) {
+        idx = (uint32_t)t;
+        const uint32_t before = mprefix[idx];
+        if (mprefix[idx + 1u] != before) return;  // moved: placed by its sorted rank
+        key = pkeys[idx];
+        uint32_t lo = 0u, hi = m;  // moved particles ordered before (key, idx)
+        while (lo < hi) {
+            const uint32_t mid = (lo + hi) >> 1;
+            const uint32_t k2 = mk[mid];
+            if (k2 < key || (k2 == key && mi[mid] < idx)) lo = mid + 1u; else hi = mid;
+        }
+        pos = (idx - before) + lo;
+    } else if (t < (uint64_t)n + m) {
+        const uint32_t r = (uint32_t)(t - n);
+        key = mk[r];
+        idx = mi[r];
+        // Unmoved particles ordered before (key, idx): pkeys is sorted and unmoved j has key
+        // pkeys[j], so they are the unmoved j below lower_bound(key) plus the unmoved j < idx in
+        // the equal-key range [L, R).
+        const uint32_t lb = lower_bound_u32(pkeys, n, key), ub = upper_bound_u32(pkeys, n, key);
+        const uint32_t e = idx > lb ? min(idx, ub) : lb;
+        pos = r + (lb - mprefix[lb]) + ((e - lb) - (mprefix[e] - mprefix[lb]));
+    } else {
+        return;
+    }
+    if (pos < n) {
+        out_keys[pos] = key;
+        out_perm[pos] = idx;
+    }
+}
+
 constexpr int kSortBlock = 256;
 
 template <int ITEMS>
 cudaError_t launch_onesweep_t(uint32_t n, const SortConfig& sc, const SortScratch& scr, int pass,
                               const uint32_t* kin, const uint32_t* vin, uint32_t* kout,
-                              uint32_t* vout, cudaStream_t s) {
+                              uint32_t* vout, const uint32_t* n_dev, cudaStream_t s) {
     k_onesweep<kSortBlock, ITEMS><<<sc.tiles, kSortBlock, 0, s>>>(
         kin, vin, kout, vout, n, pass * sc.digit_bits, sc.bins, scr.ghist + pass * sc.bins,
-        scr.counters + pass, scr.status + (size_t)pass * sc.tiles * sc.bins, scr.err);
+        scr.counters + pass, scr.status + (size_t)pass * sc.tiles * sc.bins, scr.err, n_dev);
     return cudaGetLastError();
 }
 
@@ -915,11 +1133,14 @@ SortConfig make_sort_config(uint32_t n, int digit_bits, int tile_items, int key_
     c.tile = kSortBlock * tile_items;
     c.tiles = (uint32_t)(((uint64_t)n + c.tile - 1) / c.tile);
     if (c.tiles == 0) c.tiles = 1;
+    c.delta_blocks = (uint32_t)(((uint64_t)n + kDeltaTile - 1u) / kDeltaTile);
+    if (c.delta_blocks == 0) c.delta_blocks = 1;
     return c;
 }
 
 size_t sort_scratch_words(const SortConfig& c) {
-    return (size_t)c.passes * c.bins + (size_t)c.passes + (size_t)c.passes * c.tiles * c.bins;
+    return (size_t)c.passes * c.bins + (size_t)c.passes + (size_t)c.passes * c.tiles * c.bins +
+           2u + (size_t)c.delta_blocks;
 }
 
 cudaError_t launch_keys(const StepLaunch& L, const float4* pos, uint32_t* keys,
@@ -934,6 +1155,31 @@ cudaError_t launch_keys(const StepLaunch& L, const float4* pos, uint32_t* keys,
     return cudaGetLastError();
 }
 
+cudaError_t launch_keys_delta(const StepLaunch& L, const float4* pos, const uint32_t* pkeys,
+                              uint32_t* mkeys, uint32_t* midx, uint32_t* mprefix,
+                              const SortConfig& sc, const SortScratch& scr, cudaStream_t s) {
+    if (L.total == 0) return cudaSuccess;
+    if (L.n_scenes > 1)
+        k_keys_delta<true><<<sc.delta_blocks, 256, 0, s>>>(L, pos, pkeys, mkeys, midx, mprefix,
+                                                          sc.passes, sc.digit_bits, scr.ghist,
+                                                          scr.dcounter, scr.dstatus, scr.mcount, scr.err);
+    else
+        k_keys_delta<false><<<sc.delta_blocks, 256, 0, s>>>(L, pos, pkeys, mkeys, midx, mprefix,
+                                                           sc.passes, sc.digit_bits, scr.ghist,
+                                                           scr.dcounter, scr.dstatus, scr.mcount, scr.err);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_merge(uint32_t n, const uint32_t* pkeys, const uint32_t* mprefix,
+                         const uint32_t* mcount, const uint32_t* mk, const uint32_t* mi,
+                         uint32_t* out_keys, uint32_t* out_perm, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    const uint64_t threads = 2ull * n;
+    k_merge<<<(unsigned)((threads + 255u) / 256u), 256, 0, s>>>(n, pkeys, mprefix, mcount, mk, mi,
+                                                                 out_keys, out_perm);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_digit_hist(const uint32_t* keys, uint32_t n, const SortConfig& sc,
                               uint32_t* ghist, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
@@ -945,20 +1191,21 @@ cudaError_t launch_digit_hist(const uint32_t* keys, uint32_t n, const SortConfig
 
 cudaError_t launch_sort(uint32_t n, const SortConfig& sc, const SortScratch& scr, uint32_t* keys,
                         uint32_t* keys_alt, uint32_t* vals, uint32_t* vals_alt,
-                        uint32_t** sorted_keys, uint32_t** sorted_perm, cudaStream_t s) {
+                        uint32_t** sorted_keys, uint32_t** sorted_perm, cudaStream_t s,
+                        bool vals_given, const uint32_t* n_dev) {
     const uint32_t* kin = keys;
-    const uint32_t* vin = nullptr;  // pass 0 ranks (key, index)
+    const uint32_t* vin = vals_given ? vals : nullptr;  // nullptr: pass 0 ranks (key, index)
     uint32_t* kout = keys_alt;
     uint32_t* vout = vals_alt;
     for (int pass = 0; pass < sc.passes; pass++) {
         cudaError_t e;
         const int items = sc.tile / kSortBlock;
         if (items == 8)
-            e = launch_onesweep_t<8>(n, sc, scr, pass, kin, vin, kout, vout, s);
+            e = launch_onesweep_t<8>(n, sc, scr, pass, kin, vin, kout, vout, n_dev, s);
         else if (items == 12)
-            e = launch_onesweep_t<12>(n, sc, scr, pass, kin, vin, kout, vout, s);
+            e = launch_onesweep_t<12>(n, sc, scr, pass, kin, vin, kout, vout, n_dev, s);
         else
-            e = launch_onesweep_t<16>(n, sc, scr, pass, kin, vin, kout, vout, s);
+            e = launch_onesweep_t<16>(n, sc, scr, pass, kin, vin, kout, vout, n_dev, s);
         if (e != cudaSuccess) return e;
         kin = kout;
         vin = vout;
@@ -973,20 +1220,21 @@ cudaError_t launch_sort(uint32_t n, const SortConfig& sc, const SortScratch& scr
 cudaError_t launch_cells_reorder(uint32_t n, const uint32_t* skeys, const uint32_t* perm,
                                  uint32_t* cell_scan, const float4* pos_in, const float4* vel_in,
                                  float4* pos_out, float4* vel_out, uint32_t* zero,
-                                 uint32_t zero_words, const KernelConfig& kc, cudaStream_t s) {
+                                 uint32_t zero_words, uint32_t* pkeys_out, const KernelConfig& kc,
+                                 cudaStream_t s) {
     if (n == 0) return cudaSuccess;
     switch (kc.cell_block) {
         case 128:
             k_cells_reorder<128><<<(n + 128u) / 128u, 128, 0, s>>>(n, skeys, perm, cell_scan, pos_in,
-                                                                 vel_in, pos_out, vel_out, zero, zero_words);
+                                                                 vel_in, pos_out, vel_out, zero, zero_words, pkeys_out);
             break;
         case 512:
             k_cells_reorder<512><<<(n + 512u) / 512u, 512, 0, s>>>(n, skeys, perm, cell_scan, pos_in,
-                                                                 vel_in, pos_out, vel_out, zero, zero_words);
+                                                                 vel_in, pos_out, vel_out, zero, zero_words, pkeys_out);
             break;
         default:
             k_cells_reorder<256><<<(n + 256u) / 256u, 256, 0, s>>>(n, skeys, perm, cell_scan, pos_in,
-                                                                 vel_in, pos_out, vel_out, zero, zero_words);
+                                                                 vel_in, pos_out, vel_out, zero, zero_words, pkeys_out);
     }
     return cudaGetLastError();
 }

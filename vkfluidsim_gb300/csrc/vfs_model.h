@@ -54,8 +54,12 @@ struct Model {
     uint32_t* keys_alt = nullptr;
     uint32_t* vals = nullptr;
     uint32_t* vals_alt = nullptr;
-    uint32_t* skeys = nullptr;  // sorted keys of the last substep (aliases keys / keys_alt)
-    uint32_t* sperm = nullptr;  // sorted_indices of the last substep (aliases vals / vals_alt)
+    uint32_t* skeys = nullptr;  // sorted keys of the last substep (sk_buf)
+    uint32_t* sperm = nullptr;  // sorted_indices of the last substep (sp_buf)
+    uint32_t* sk_buf = nullptr;   // merge output: sorted keys
+    uint32_t* sp_buf = nullptr;   // merge output: sorted_indices
+    uint32_t* pkeys = nullptr;    // previous substep's sorted keys (all ones in a fresh model)
+    uint32_t* mprefix = nullptr;  // n + 1: moved particles before each index
     uint32_t* cell_scan = nullptr;
     float4* aux = nullptr;
     float4* rec = nullptr;  // 2 float4 per particle: the force pass's neighbour records
