@@ -323,12 +323,12 @@ int Model::enqueue_substep(cudaEvent_t* ev) {
     if (ev) VFS_CUDA_TRY(cudaEventRecord(ev[1], s));
     // Incremental stable sort: keys + the particles whose key changed (compacted into keys/vals),
     // a sort of those alone (count on the device), a merge with the rest.
-    VFS_CUDA_TRY(launch_keys_delta(launch, pos[c], pkeys, keys, vals, mprefix, sc, sort_scratch, s));
+    VFS_CUDA_TRY(launch_keys_delta(launch, pos[c], pkeys, keys, vals, moved, sc, sort_scratch, s));
     if (ev) VFS_CUDA_TRY(cudaEventRecord(ev[2], s));
     uint32_t *mk = nullptr, *mi = nullptr;
     VFS_CUDA_TRY(launch_sort(n, sc, sort_scratch, keys, keys_alt, vals, vals_alt, &mk, &mi, s,
                              /*vals_given=*/true, sort_scratch.mcount));
-    VFS_CUDA_TRY(launch_merge(n, pkeys, mprefix, sort_scratch.mcount, mk, mi, sk_buf, sp_buf, s));
+    VFS_CUDA_TRY(launch_merge(n, pkeys, moved, sort_scratch.mcount, mk, mi, sk_buf, sp_buf, s));
     skeys = sk_buf;
     sperm = sp_buf;
     if (ev) VFS_CUDA_TRY(cudaEventRecord(ev[3], s));
@@ -404,7 +404,7 @@ Model::~Model() {
     cudaFree(sk_buf);
     cudaFree(sp_buf);
     cudaFree(pkeys);
-    cudaFree(mprefix);
+    cudaFree(moved);
     cudaFree(bnd);
     cudaFree(acc);
     cudaFree(stage);
@@ -449,7 +449,7 @@ int Model::init() {
     VFS_CUDA_TRY(cudaMalloc(&sp_buf, N * 4));
     VFS_CUDA_TRY(cudaMalloc(&pkeys, N * 4));
     VFS_CUDA_TRY(cudaMemset(pkeys, 0xFF, N * 4));  // sorted, and no key equals it: all moved
-    VFS_CUDA_TRY(cudaMalloc(&mprefix, (N + 1) * 4));
+    VFS_CUDA_TRY(cudaMalloc(&moved, (2 * ((N + 31) / 32) + 1) * 4));
     VFS_CUDA_TRY(cudaMalloc(&aux, N * sizeof(float4)));
     VFS_CUDA_TRY(cudaMalloc(&rec, 2 * N * sizeof(float4)));
     VFS_CUDA_TRY(cudaMalloc(&bnd, N * sizeof(float4)));

@@ -131,15 +131,15 @@ cudaError_t launch_keys(const StepLaunch& L, const float4* pos, uint32_t* keys,
 // Per-pass digit histograms of caller-provided keys.
 cudaError_t launch_digit_hist(const uint32_t* keys, uint32_t n, const SortConfig& sc,
                               uint32_t* ghist, cudaStream_t s);
-// Incremental sort, pass 1: keys, moved flags (key != pkeys[i]), their exclusive prefix
-// mprefix[0..n], the moved (key, index) pairs compacted in index order, their digit histograms,
-// and the moved count in scr.mcount.
+// Incremental sort, pass 1: keys, moved flags (key != pkeys[i]) as a bitmask bits[0, W) with the
+// moved count before each word in bits[W, 2W] (W = ceil(n / 32)), the moved (key, index) pairs
+// compacted in index order, their digit histograms, and the moved count in scr.mcount.
 cudaError_t launch_keys_delta(const StepLaunch& L, const float4* pos, const uint32_t* pkeys,
-                              uint32_t* mkeys, uint32_t* midx, uint32_t* mprefix,
+                              uint32_t* mkeys, uint32_t* midx, uint32_t* bits,
                               const SortConfig& sc, const SortScratch& scr, cudaStream_t s);
 // Incremental sort, last pass: merge of the unmoved particles with the sorted moved ones into the
 // stable sort of all (key, index) pairs.
-cudaError_t launch_merge(uint32_t n, const uint32_t* pkeys, const uint32_t* mprefix,
+cudaError_t launch_merge(uint32_t n, const uint32_t* pkeys, const uint32_t* bits,
                          const uint32_t* mcount, const uint32_t* mk, const uint32_t* mi,
                          uint32_t* out_keys, uint32_t* out_perm, cudaStream_t s);
 // Stable LSD onesweep over sc.passes digits; returns the buffers holding sorted keys / perm.

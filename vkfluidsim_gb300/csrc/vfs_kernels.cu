@@ -878,9 +878,10 @@ __global__ void __launch_bounds__(kNbrBlock, kMinBlocks)
 // sorted pkeys (all moved when pkeys is the all-ones fill of a fresh model), so no step ever
 // needs to know whether pkeys is current.
 
-// Keys, moved flags and the moved particles' compaction: mprefix[i] = number of moved particles
-// before i (mprefix[n] = total = *mcount), (mkeys, midx)[rank] for the moved ones in index order,
-// and the digit histograms of the moved keys. A tile is 256 threads x kDeltaItems particles
+// Keys, moved flags and the moved particles' compaction: the moved flags as a bitmask with one
+// word per 32 particles, bits[w], and the number of moved particles before each word, pre[w]
+// (pre[W] = total = *mcount, W = ceil(n / 32), pre = bits + W); (mkeys, midx)[rank] for the moved
+// ones in index order; and the digit histograms of the moved keys. A tile is 256 threads x kDeltaItems particles
 // (particle tile * kDeltaTile + item * 256 + thread, so every load is coalesced); tiles are
 // claimed in order and chained by a bounded decoupled look-back over their moved counts.
 // Decoupled look-back of tile `tile` over single-counter status words, one warp wide: lane l reads
@@ -927,7 +928,7 @@ template <bool kBatch>
 __global__ void __launch_bounds__(256)
     k_keys_delta(StepLaunch L, const float4* __restrict__ pos, const uint32_t* __restrict__ pkeys,
                  uint32_t* __restrict__ mkeys, uint32_t* __restrict__ midx,
-                 uint32_t* __restrict__ mprefix, int passes, int digit_bits,
+                 uint32_t* __restrict__ bits, int passes, int digit_bits,
                  uint32_t* __restrict__ ghist, uint32_t* __restrict__ counter,
                  uint32_t* __restrict__ status, uint32_t* __restrict__ mcount,
                  uint32_t* __restrict__ err) {
@@ -999,18 +1000,23 @@ __global__ void __launch_bounds__(256)
             s_excl = excl;
             if (tile == gridDim.x - 1u) {
                 *mcount = excl + total;
-                mprefix[L.total] = excl + total;
+                bits[2u * ((L.total + 31u) >> 5)] = excl + total;  // pre[W]
             }
         }
     }
     __syncthreads();
     const uint32_t lt = (1u << lane) - 1u;
+    const uint32_t W = (L.total + 31u) >> 5;
 #pragma unroll
     for (int k = 0; k < kDeltaItems; k++) {
         const uint32_t i = base + (uint32_t)k * 256u;
+        const uint32_t word = i >> 5;  // this warp's 32 particles of item k
+        if (lane == 0 && word < W) {
+            bits[word] = ball[k];
+            bits[W + word] = s_excl + s_cnt[k * 8 + warp];
+        }
         if (i < L.total) {
             const uint32_t rank = s_excl + s_cnt[k * 8 + warp] + __popc(ball[k] & lt);
-            mprefix[i] = rank;
             if ((ball[k] >> lane) & 1u) {
                 mkeys[rank] = key[k];
                 midx[rank] = i;
@@ -1042,18 +1048,28 @@ __device__ __forceinline__ uint32_t upper_bound_u32(const uint32_t* a, uint32_t 
 // Merge of the unmoved particles (keys pkeys[i], in index order) with the sorted moved ones
 // (mk, mi) by (key, index). Thread t < n places unmoved particle t; thread n + r places the moved
 // particle of sorted rank r. Every output position is computed independently.
+// Moved particles with index < i (0 <= i <= n) from the bitmask and per-word prefix.
+__device__ __forceinline__ uint32_t moved_before(const uint32_t* __restrict__ bits, uint32_t W,
+                                                 uint32_t i) {
+    const uint32_t w = i >> 5;
+    if (w >= W) return bits[W + W];
+    return bits[W + w] + __popc(bits[w] & ((1u << (i & 31u)) - 1u));
+}
+
 __global__ void __launch_bounds__(256)
-    k_merge(uint32_t n, const uint32_t* __restrict__ pkeys, const uint32_t* __restrict__ mprefix,
+    k_merge(uint32_t n, const uint32_t* __restrict__ pkeys, const uint32_t* __restrict__ bits,
             const uint32_t* __restrict__ mcount, const uint32_t* __restrict__ mk,
             const uint32_t* __restrict__ mi, uint32_t* __restrict__ out_keys,
             uint32_t* __restrict__ out_perm) {
     const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t m = min(*mcount, n);
+    const uint32_t W = (n + 31u) >> 5;
     uint32_t key, idx, pos;
     if (t < n) {
         idx = (uint32_t)t;
-        const uint32_t before = mprefix[idx];
-        if (mprefix[idx + 1u] != before) return;  // moved: placed by its sorted rank
+        const uint32_t word = bits[idx >> 5];
+        if ((word >> (idx & 31u)) & 1u) return;  // moved: placed by its sorted rank
+        const uint32_t before = bits[W + (idx >> 5)] + __popc(word & ((1u << (idx & 31u)) - 1u));
         key = pkeys[idx];
         uint32_t lo = 0u, hi = m;  // moved particles ordered before (key, idx)
         while (lo < hi) {
@@ -1071,7 +1087,8 @@ __global__ void __launch_bounds__(256)
         // the equal-key range [L, R).
         const uint32_t lb = lower_bound_u32(pkeys, n, key), ub = upper_bound_u32(pkeys, n, key);
         const uint32_t e = idx > lb ? min(idx, ub) : lb;
-        pos = r + (lb - mprefix[lb]) + ((e - lb) - (mprefix[e] - mprefix[lb]));
+        const uint32_t mlb = moved_before(bits, W, lb);
+        pos = r + (lb - mlb) + ((e - lb) - (moved_before(bits, W, e) - mlb));
     } else {
         return;
     }
@@ -1156,26 +1173,26 @@ cudaError_t launch_keys(const StepLaunch& L, const float4* pos, uint32_t* keys,
 }
 
 cudaError_t launch_keys_delta(const StepLaunch& L, const float4* pos, const uint32_t* pkeys,
-                              uint32_t* mkeys, uint32_t* midx, uint32_t* mprefix,
+                              uint32_t* mkeys, uint32_t* midx, uint32_t* bits,
                               const SortConfig& sc, const SortScratch& scr, cudaStream_t s) {
     if (L.total == 0) return cudaSuccess;
     if (L.n_scenes > 1)
-        k_keys_delta<true><<<sc.delta_blocks, 256, 0, s>>>(L, pos, pkeys, mkeys, midx, mprefix,
+        k_keys_delta<true><<<sc.delta_blocks, 256, 0, s>>>(L, pos, pkeys, mkeys, midx, bits,
                                                           sc.passes, sc.digit_bits, scr.ghist,
                                                           scr.dcounter, scr.dstatus, scr.mcount, scr.err);
     else
-        k_keys_delta<false><<<sc.delta_blocks, 256, 0, s>>>(L, pos, pkeys, mkeys, midx, mprefix,
+        k_keys_delta<false><<<sc.delta_blocks, 256, 0, s>>>(L, pos, pkeys, mkeys, midx, bits,
                                                            sc.passes, sc.digit_bits, scr.ghist,
                                                            scr.dcounter, scr.dstatus, scr.mcount, scr.err);
     return cudaGetLastError();
 }
 
-cudaError_t launch_merge(uint32_t n, const uint32_t* pkeys, const uint32_t* mprefix,
+cudaError_t launch_merge(uint32_t n, const uint32_t* pkeys, const uint32_t* bits,
                          const uint32_t* mcount, const uint32_t* mk, const uint32_t* mi,
                          uint32_t* out_keys, uint32_t* out_perm, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
     const uint64_t threads = 2ull * n;
-    k_merge<<<(unsigned)((threads + 255u) / 256u), 256, 0, s>>>(n, pkeys, mprefix, mcount, mk, mi,
+    k_merge<<<(unsigned)((threads + 255u) / 256u), 256, 0, s>>>(n, pkeys, bits, mcount, mk, mi,
                                                                  out_keys, out_perm);
     return cudaGetLastError();
 }
