@@ -124,10 +124,6 @@ struct KernelConfig {
 };
 size_t sort_scratch_words(const SortConfig& c);
 
-// keys[i] = off + HashCell3D(floor(pos[i] / h)) % n of i's scene, and the per-pass digit
-// histograms.
-cudaError_t launch_keys(const StepLaunch& L, const float4* pos, uint32_t* keys,
-                        const SortConfig& sc, uint32_t* ghist, cudaStream_t s);
 // Per-pass digit histograms of caller-provided keys.
 cudaError_t launch_digit_hist(const uint32_t* keys, uint32_t n, const SortConfig& sc,
                               uint32_t* ghist, cudaStream_t s);

@@ -220,30 +220,6 @@ __device__ __forceinline__ const SceneParams& scene_params(const StepLaunch& L, 
 
 // ---------------------------------------------------------------- kernels
 
-template <bool kBatch>
-__global__ void __launch_bounds__(256) k_keys(StepLaunch L, const float4* __restrict__ pos,
-                                              uint32_t* __restrict__ keys, int passes,
-                                              int digit_bits, uint32_t* __restrict__ ghist) {
-    __shared__ uint32_t s_h[kMaxSortPasses * kMaxSortBins];
-    const int bins = 1 << digit_bits;
-    const uint32_t mask = (uint32_t)bins - 1u;
-    for (int e = threadIdx.x; e < passes * bins; e += blockDim.x) s_h[e] = 0u;
-    __syncthreads();
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < L.total;
-         i += gridDim.x * blockDim.x) {
-        const SceneParams& p = scene_params<kBatch>(L, i);
-        const float4 x = pos[i];
-        const uint32_t key = p.off + key_mod(hash_cell(cell_coord(x.x, p.h), cell_coord(x.y, p.h),
-                                                       cell_coord(x.z, p.h)),
-                                             p.mod_magic, p.n);
-        keys[i] = key;
-        for (int ps = 0; ps < passes; ps++)
-            atomicAdd(&s_h[ps * bins + ((key >> (ps * digit_bits)) & mask)], 1u);
-    }
-    __syncthreads();
-    for (int e = threadIdx.x; e < passes * bins; e += blockDim.x)
-        if (s_h[e]) atomicAdd(&ghist[e], s_h[e]);
-}
 
 // Per-pass digit histograms of caller-provided keys (the histogram half of k_keys).
 __global__ void __launch_bounds__(256) k_digit_hist(const uint32_t* __restrict__ keys, uint32_t n,
@@ -1160,17 +1136,6 @@ size_t sort_scratch_words(const SortConfig& c) {
            2u + (size_t)c.delta_blocks;
 }
 
-cudaError_t launch_keys(const StepLaunch& L, const float4* pos, uint32_t* keys,
-                        const SortConfig& sc, uint32_t* ghist, cudaStream_t s) {
-    if (L.total == 0) return cudaSuccess;
-    uint32_t blocks = (L.total + 255u) / 256u;
-    if (blocks > 152u * 8u) blocks = 152u * 8u;
-    if (L.n_scenes > 1)
-        k_keys<true><<<blocks, 256, 0, s>>>(L, pos, keys, sc.passes, sc.digit_bits, ghist);
-    else
-        k_keys<false><<<blocks, 256, 0, s>>>(L, pos, keys, sc.passes, sc.digit_bits, ghist);
-    return cudaGetLastError();
-}
 
 cudaError_t launch_keys_delta(const StepLaunch& L, const float4* pos, const uint32_t* pkeys,
                               uint32_t* mkeys, uint32_t* midx, uint32_t* bits,
