@@ -313,3 +313,31 @@ def test_negative_cells_and_hash_block_boundaries():
     o = oracle_for(w, m)
     for _ in range(2):
         compare_step(m, o, "negative_cells")
+
+
+def test_incremental_sort_when_no_particle_changes_cell():
+    """Zero gravity and velocity, particles held at rest in a lattice far from walls: after the
+    first substep no key changes, the moved set is empty and the order must stay the stable sort."""
+    w = W.dam_break(dims=(20, 20, 20), spacing=0.02, map_res=0, seed=3)
+    w.sim = replace(w.sim, gravity=(0.0, 0.0, 0.0))
+    w.pos = (w.pos + np.float32(0.1)).astype(np.float32)
+    w.wcsph = replace(w.wcsph, stiffness=0.0, viscosity_strenght=0.0)
+    m = W.build_model(w)
+    o = oracle_for(w, m)
+    for k in range(3):
+        compare_step(m, o, f"no_moves_{k}", check_fields=False)
+
+
+def test_incremental_sort_when_every_particle_changes_cell():
+    """Velocities of about two cells per substep in random directions: nearly every key changes
+    each substep, so the moved set is almost everything (and the merge has little to merge)."""
+    w = W.dam_break(dims=(24, 24, 24), spacing=0.02, map_res=0, seed=8)
+    w.sph = replace(w.sph, bbox_size=(4.0, 4.0, 4.0), bbox_pos=(-2.0, -2.0, -2.0))
+    h, dt = float(w.sim.smooth_radius), float(w.sph.fixed_dt)
+    rng = np.random.default_rng(9)
+    w.vel = (rng.standard_normal(w.pos.shape) * (2.0 * h / dt)).astype(np.float32)
+    w.wcsph = replace(w.wcsph, stiffness=0.0, viscosity_strenght=0.0)
+    m = W.build_model(w)
+    o = oracle_for(w, m)
+    for k in range(3):
+        compare_step(m, o, f"all_move_{k}", check_fields=False)
