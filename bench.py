@@ -156,9 +156,9 @@ def oracle_for_workload(w, model=None):
 def time_cpu(w, model=None, budget_s=12.0, max_steps=200, threads=None):
     from oracle import binding as ob
 
+    o = oracle_for_workload(w, model)  # boundary grids built with every host thread
     if threads:
         ob.set_threads(threads)
-    o = oracle_for_workload(w, model)
     o.substeps(1)  # warm-up
     steps, t0 = 0, time.perf_counter()
     while steps < max_steps:
@@ -405,6 +405,30 @@ def time_next_rows(args, stream, torch, model, rank):
     return out
 
 
+def time_small(args, stream, torch):
+    """The 32,768-particle dam break (32^3 lattice at 0.02, h = 0.04, 64^3 box-wall volume map,
+    dt = 2e-4): device-timed graphed substeps, and the oracle on one host core for comparison."""
+    from vkfluidsim_gb300 import workloads as W
+
+    w = W.dam_break_32k()
+    m = W.build_model(w)
+    m.set_stream(stream.cuda_stream)
+    for _ in range(args.warmup):
+        m.substeps(1)
+    steps = max(args.steps, 50)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    m.substeps(steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    out = {"workload": w.name, "particles": w.n, "steps": steps, "ms_per_step": ms,
+           "value": w.n / (ms * 1e-3)}
+    del m
+    return out
+
+
 def run_gpu(args):
     import torch
 
@@ -504,9 +528,20 @@ def run_gpu(args):
     stress = time_stress(args, stream, torch) if args.stress else None
     next_rows = time_next_rows(args, stream, torch, m, rank) if args.next_rows else None
 
+    small = time_small(args, stream, torch) if args.small else None
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
+        from oracle import binding as ob
+
+        all_threads = ob.get_threads()
         cpu = time_cpu(w, m, budget_s=args.cpu_budget)
+        one = time_cpu(w, m, budget_s=max(2.0, args.cpu_budget / 3), max_steps=3, threads=1)
+        cpu["single_core"] = {k: one[k] for k in ("value", "cores", "sample")}
+        if small:
+            s1 = time_cpu(W.dam_break_32k(), None, budget_s=max(2.0, args.cpu_budget / 3), threads=1)
+            small["cpu_single_core"] = {k: s1[k] for k in ("value", "cores", "sample")}
+        ob.set_threads(all_threads)
 
     if rank == 0:
         line = {
@@ -540,6 +575,8 @@ def run_gpu(args):
             line["stress"] = stress
         if next_rows:
             line["next_rows"] = next_rows
+        if small:
+            line["small"] = small
         if cpu:
             line["cpu_baseline"] = cpu
         print(json.dumps(line), flush=True)
@@ -562,6 +599,7 @@ def main():
     ap.add_argument("--stress", type=int, default=1)
     ap.add_argument("--autotune", type=int, default=1)
     ap.add_argument("--next-rows", type=int, default=1)
+    ap.add_argument("--small", type=int, default=1)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
