@@ -563,7 +563,8 @@ def run_gpu(args):
                               "achieved_gbs": B_STEP * n / (ms_per_step * 1e-3) / 1e9,
                               "frac": B_STEP * n / (ms_per_step * 1e-3) / 1e9 / hbm},
             "phase_ms": prof,
-            "gpu_launches": (4 + passes) * args.steps,
+            # keys+delta, `passes` onesweep passes, merge, cells+reorder, density, force.
+            "gpu_launches": (5 + passes) * args.steps,
             "clocks": clk.summary(),
             "wall_s_timed_region": t_wall,
         }
