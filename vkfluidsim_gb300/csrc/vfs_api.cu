@@ -46,34 +46,79 @@ int fail(int code, const std::string& msg) {
 
 namespace {
 
-__global__ void k_expand_state(uint32_t offset, uint32_t count, const float* __restrict__ pos3,
-                               const float* __restrict__ vel3, float4* __restrict__ pos,
-                               float4* __restrict__ vel, float4* __restrict__ aux) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= count) return;
-    const uint32_t d = offset + i;
-    pos[d] = make_float4(pos3[3 * i], pos3[3 * i + 1], pos3[3 * i + 2], __uint_as_float(d));
-    vel[d] = make_float4(vel3[3 * i], vel3[3 * i + 1], vel3[3 * i + 2], 0.0f);
+constexpr uint32_t kIoBlock = 256;
+
+// SetParticleState's layout conversion: packed float3 records (host memory mapped into the
+// device's address space, or a device staging copy) to the float4 state. A block moves its
+// 256 records through shared memory, so every warp reads 128 contiguous bytes.
+__global__ void __launch_bounds__(kIoBlock)
+    k_expand_state(uint32_t offset, uint32_t count, const float* __restrict__ pos3,
+                   const float* __restrict__ vel3, float4* __restrict__ pos,
+                   float4* __restrict__ vel, float4* __restrict__ aux) {
+    __shared__ float s_p[3 * kIoBlock], s_v[3 * kIoBlock];
+    const uint32_t base = blockIdx.x * kIoBlock, t = threadIdx.x;
+    const uint32_t m = min(kIoBlock, count - base);
+    const size_t b3 = 3 * (size_t)base;
+    for (uint32_t k = t; k < 3 * m; k += kIoBlock) {
+        s_p[k] = pos3[b3 + k];
+        s_v[k] = vel3[b3 + k];
+    }
+    __syncthreads();
+    if (t >= m) return;
+    const uint32_t d = offset + base + t;
+    pos[d] = make_float4(s_p[3 * t], s_p[3 * t + 1], s_p[3 * t + 2], __uint_as_float(d));
+    vel[d] = make_float4(s_v[3 * t], s_v[3 * t + 1], s_v[3 * t + 2], 0.0f);
     aux[d].z = 0.0f;  // SetParticleState zeroes the densities it covers (model.cpp:146)
 }
 
-// Packs particles [start, start + n) into float3 / float arrays; ids become scene-local.
-__global__ void k_compact_state(uint32_t n, uint32_t start, const float4* __restrict__ pos,
-                                const float4* __restrict__ vel, const float4* __restrict__ aux,
-                                float* __restrict__ pos3, float* __restrict__ vel3,
-                                float* __restrict__ dens, uint32_t* __restrict__ ids) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const float4 p = pos[start + i];
-    const float4 v = vel[start + i];
-    pos3[3 * i] = p.x;
-    pos3[3 * i + 1] = p.y;
-    pos3[3 * i + 2] = p.z;
-    vel3[3 * i] = v.x;
-    vel3[3 * i + 1] = v.y;
-    vel3[3 * i + 2] = v.z;
-    dens[i] = aux[start + i].z;
-    ids[i] = __float_as_uint(p.w) - start;
+// Packs particles [start, start + n) into float3 / float arrays (any of them may be null);
+// ids become scene-local. The float3 arrays are written through shared memory, 128 contiguous
+// bytes per warp store, so host-mapped outputs receive whole lines.
+__global__ void __launch_bounds__(kIoBlock)
+    k_compact_state(uint32_t n, uint32_t start, const float4* __restrict__ pos,
+                    const float4* __restrict__ vel, const float4* __restrict__ aux,
+                    float* __restrict__ pos3, float* __restrict__ vel3,
+                    float* __restrict__ dens, uint32_t* __restrict__ ids) {
+    __shared__ float s_p[3 * kIoBlock], s_v[3 * kIoBlock];
+    const uint32_t base = blockIdx.x * kIoBlock, t = threadIdx.x;
+    const uint32_t m = min(kIoBlock, n - base);
+    if (t < m) {
+        const uint32_t i = start + base + t;
+        const float4 p = pos[i];
+        const float4 v = vel[i];
+        s_p[3 * t] = p.x;
+        s_p[3 * t + 1] = p.y;
+        s_p[3 * t + 2] = p.z;
+        s_v[3 * t] = v.x;
+        s_v[3 * t + 1] = v.y;
+        s_v[3 * t + 2] = v.z;
+        if (dens) dens[base + t] = aux[i].z;
+        if (ids) ids[base + t] = __float_as_uint(p.w) - start;
+    }
+    __syncthreads();
+    const size_t b3 = 3 * (size_t)base;
+    for (uint32_t k = t; k < 3 * m; k += kIoBlock) {
+        if (pos3) pos3[b3 + k] = s_p[k];
+        if (vel3) vel3[b3 + k] = s_v[k];
+    }
+}
+
+// The address under which this device's kernels reach host buffer p: page-locked host memory
+// (cudaHostAlloc / cudaHostRegister, mapped under unified addressing) or device and managed
+// memory of this device. Null for pageable memory, which goes through a staging copy.
+void* device_alias(const void* p) {
+    if (!p) return nullptr;
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    int dev = -1;
+    cudaGetDevice(&dev);
+    if (a.type == cudaMemoryTypeHost) return a.devicePointer;
+    if ((a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged) && a.device == dev)
+        return a.devicePointer;
+    return nullptr;
 }
 
 // Scene id of every particle of a batched model.
@@ -522,11 +567,20 @@ int Model::set_state(uint32_t scene, const float* pos3, const float* vel3, uint3
         return fail(VFS_ERR_CAPACITY, "offset + count exceeds the scene's particle count");
     if (cnt == 0) return VFS_OK;
     if (!pos3 || !vel3) return fail(VFS_ERR_INVALID_ARGUMENT, "pos and vel must not be NULL");
-    float* sp = stage;
-    float* sv = stage + 3 * (size_t)n;
-    VFS_CUDA_TRY(cudaMemcpyAsync(sp, pos3, cnt * 12, cudaMemcpyHostToDevice, stream));
-    VFS_CUDA_TRY(cudaMemcpyAsync(sv, vel3, cnt * 12, cudaMemcpyHostToDevice, stream));
-    k_expand_state<<<(unsigned)((cnt + 255) / 256), 256, 0, stream>>>(
+    // Page-locked inputs are read by the conversion kernel itself (over NVLink-C2C on GB300);
+    // pageable ones are copied into the staging buffer first.
+    const float* sp = static_cast<const float*>(device_alias(pos3));
+    const float* sv = static_cast<const float*>(device_alias(vel3));
+    if (!sp) {
+        VFS_CUDA_TRY(cudaMemcpyAsync(stage, pos3, cnt * 12, cudaMemcpyHostToDevice, stream));
+        sp = stage;
+    }
+    if (!sv) {
+        float* st = stage + 3 * (size_t)n;
+        VFS_CUDA_TRY(cudaMemcpyAsync(st, vel3, cnt * 12, cudaMemcpyHostToDevice, stream));
+        sv = st;
+    }
+    k_expand_state<<<(unsigned)((cnt + kIoBlock - 1) / kIoBlock), kIoBlock, 0, stream>>>(
         sh.off + offset, (uint32_t)cnt, sp, sv, pos[cur], vel[cur], aux);
     VFS_CUDA_TRY(cudaGetLastError());
     VFS_CUDA_TRY(cudaStreamSynchronize(stream));
@@ -537,17 +591,23 @@ int Model::get_state(uint32_t scene, float* pos3, float* vel3, float* dens, uint
     if (scene >= scenes.size()) return fail(VFS_ERR_INVALID_ARGUMENT, "scene index out of range");
     const SceneHost& sh = scenes[scene];
     if (sh.n == 0) return VFS_OK;
-    float* sp = stage;
-    float* sv = stage + 3 * (size_t)n;
-    float* sd = stage + 6 * (size_t)n;
-    uint32_t* si = reinterpret_cast<uint32_t*>(stage + 7 * (size_t)n);
-    k_compact_state<<<(sh.n + 255) / 256, 256, 0, stream>>>(sh.n, sh.off, pos[cur], vel[cur], aux,
-                                                           sp, sv, sd, si);
+    // Page-locked outputs are written by the packing kernel itself; the others through staging.
+    float* dp = static_cast<float*>(device_alias(pos3));
+    float* dv = static_cast<float*>(device_alias(vel3));
+    float* dd = static_cast<float*>(device_alias(dens));
+    uint32_t* di = static_cast<uint32_t*>(device_alias(ids));
+    float* sp = pos3 && !dp ? stage : nullptr;
+    float* sv = vel3 && !dv ? stage + 3 * (size_t)n : nullptr;
+    float* sd = dens && !dd ? stage + 6 * (size_t)n : nullptr;
+    uint32_t* si = ids && !di ? reinterpret_cast<uint32_t*>(stage + 7 * (size_t)n) : nullptr;
+    k_compact_state<<<(sh.n + kIoBlock - 1) / kIoBlock, kIoBlock, 0, stream>>>(
+        sh.n, sh.off, pos[cur], vel[cur], aux, dp ? dp : sp, dv ? dv : sv, dd ? dd : sd,
+        di ? di : si);
     VFS_CUDA_TRY(cudaGetLastError());
-    if (pos3) VFS_CUDA_TRY(cudaMemcpyAsync(pos3, sp, (size_t)sh.n * 12, cudaMemcpyDeviceToHost, stream));
-    if (vel3) VFS_CUDA_TRY(cudaMemcpyAsync(vel3, sv, (size_t)sh.n * 12, cudaMemcpyDeviceToHost, stream));
-    if (dens) VFS_CUDA_TRY(cudaMemcpyAsync(dens, sd, (size_t)sh.n * 4, cudaMemcpyDeviceToHost, stream));
-    if (ids) VFS_CUDA_TRY(cudaMemcpyAsync(ids, si, (size_t)sh.n * 4, cudaMemcpyDeviceToHost, stream));
+    if (sp) VFS_CUDA_TRY(cudaMemcpyAsync(pos3, sp, (size_t)sh.n * 12, cudaMemcpyDeviceToHost, stream));
+    if (sv) VFS_CUDA_TRY(cudaMemcpyAsync(vel3, sv, (size_t)sh.n * 12, cudaMemcpyDeviceToHost, stream));
+    if (sd) VFS_CUDA_TRY(cudaMemcpyAsync(dens, sd, (size_t)sh.n * 4, cudaMemcpyDeviceToHost, stream));
+    if (si) VFS_CUDA_TRY(cudaMemcpyAsync(ids, si, (size_t)sh.n * 4, cudaMemcpyDeviceToHost, stream));
     return check_device();
 }
 
