@@ -691,41 +691,38 @@ struct ForceAcc {
 };
 
 // Pressure and viscosity contributions of one in-range neighbour (PressureAccel slang:234-249,
-// ViscousAccel slang:301-318).
-// Written with explicit round-to-nearest intrinsics so that no fusion is left to the compiler:
-// every launch shape of the force pass then gives bit-identical results.
+// ViscousAccel slang:301-318) with the constant factors taken out of the sums. With
+// dW = grad_over_h * c(q) (c = -(1-q)^2 above q = 1/2, q (3q - 2) below, 0 outside the support or
+// at r <= 1e-9) and u = c(q) / r, the reference's terms are
+//   pressure:   mass * (pd_i + pd_j) * dW * x_ij / r  = (mass * grad_over_h) * [(pd_i + pd_j) u x_ij]
+//   viscosity:  mr_j (v_ij . x_ij) dW x_ij / r / (r^2 + 0.01 h^2) = grad_over_h * [mr_j (v_ij . x_ij) u x_ij / (r^2 + eps)]
+// and only the bracketed parts are summed here; k_force applies the factors once per particle.
+// Every operation is an explicit round-to-nearest intrinsic, so no fusion is left to the
+// compiler and every launch shape of the force pass gives bit-identical results.
 __device__ __forceinline__ void force_term(const SceneParams& p, const float4& xi, const float4& vi,
                                            float pdi, const float4& xj, const float2& aj,
                                            const float4& vj, ForceAcc& f) {
     const float xx = __fsub_rn(xi.x, xj.x), xy = __fsub_rn(xi.y, xj.y), xz = __fsub_rn(xi.z, xj.z);
     const float r2 = __fmaf_rn(xz, xz, __fmaf_rn(xy, xy, __fmul_rn(xx, xx)));
-    const bool pos_r = r2 > 0.0f;
-    const float ir = pos_r ? rsqrtf(r2) : 0.0f;
+    const float ir = rsqrtf(fmaxf(r2, 1e-30f));  // finite at r2 = 0, where u is 0 below
     const float r = __fmul_rn(r2, ir);
-    const float nx = pos_r ? __fmul_rn(xx, ir) : 0.0f;
-    const float ny = pos_r ? __fmul_rn(xy, ir) : 1.0f;
-    const float nz = pos_r ? __fmul_rn(xz, ir) : 0.0f;
     const float q = __fmul_rn(r, p.inv_h);
-    float gw = 0.0f;
-    if ((r > 1e-9f) && (q <= 1.0f)) {
-        if (q > 0.5f) {
-            const float t = __fsub_rn(1.0f, q);
-            gw = __fmul_rn(-p.grad_over_h, __fmul_rn(t, t));
-        } else {
-            gw = __fmul_rn(__fmul_rn(p.grad_over_h, q), __fmaf_rn(3.0f, q, -2.0f));
-        }
-    }
-    const float s = __fmul_rn(__fmul_rn(p.mass, __fadd_rn(pdi, aj.x)), gw);
-    f.Px = __fmaf_rn(s, nx, f.Px);
-    f.Py = __fmaf_rn(s, ny, f.Py);
-    f.Pz = __fmaf_rn(s, nz, f.Pz);
+    const float t = __fsub_rn(1.0f, q);
+    const float c_out = -__fmul_rn(t, t);
+    const float c_in = __fmul_rn(q, __fmaf_rn(3.0f, q, -2.0f));
+    const float c = q > 0.5f ? c_out : c_in;
+    const float u = (r > 1e-9f && q <= 1.0f) ? __fmul_rn(c, ir) : 0.0f;
+    const float sp = __fmul_rn(__fadd_rn(pdi, aj.x), u);
+    f.Px = __fmaf_rn(sp, xx, f.Px);
+    f.Py = __fmaf_rn(sp, xy, f.Py);
+    f.Pz = __fmaf_rn(sp, xz, f.Pz);
     const float dv = __fmaf_rn(__fsub_rn(vi.z, vj.z), xz,
                                __fmaf_rn(__fsub_rn(vi.y, vj.y), xy, __fmul_rn(__fsub_rn(vi.x, vj.x), xx)));
-    const float tv = __fmul_rn(aj.y, dv);
     const float iden = __fdividef(1.0f, __fadd_rn(r2, p.visc_eps));
-    f.Vx = __fmaf_rn(__fmul_rn(tv, __fmul_rn(nx, gw)), iden, f.Vx);
-    f.Vy = __fmaf_rn(__fmul_rn(tv, __fmul_rn(ny, gw)), iden, f.Vy);
-    f.Vz = __fmaf_rn(__fmul_rn(tv, __fmul_rn(nz, gw)), iden, f.Vz);
+    const float sv = __fmul_rn(__fmul_rn(__fmul_rn(aj.y, dv), u), iden);
+    f.Vx = __fmaf_rn(sv, xx, f.Vx);
+    f.Vy = __fmaf_rn(sv, xy, f.Vy);
+    f.Vz = __fmaf_rn(sv, xz, f.Vz);
 }
 
 // A 32-byte force record in one 256-bit load (sm_100+; rec + 2j is 32-byte aligned because the
@@ -820,6 +817,11 @@ __global__ void __launch_bounds__(kNbrBlock, kMinBlocks)
         });
         force_drain<kNbrBlock>(p, rec, s_j, tid, cnt, xi, vi, pdi, f);
     }
+    // The factors force_term leaves out of the sums.
+    const float cp = p.mass * p.grad_over_h, cv = p.visc_scale * p.grad_over_h;
+    f.Px *= cp;
+    f.Py *= cp;
+    f.Pz *= cp;
     const float4 bi = __ldg(bnd + i);
     const float sb = (pdi + ai.w) * p.rho0;
     f.Px += sb * bi.x;
@@ -827,9 +829,9 @@ __global__ void __launch_bounds__(kNbrBlock, kMinBlocks)
     f.Pz += sb * bi.z;
 
     float ax = p.gx + -f.Px, ay = p.gy + -f.Py, az = p.gz + -f.Pz;
-    ax += p.visc_scale * f.Vx;
-    ay += p.visc_scale * f.Vy;
-    az += p.visc_scale * f.Vz;
+    ax += cv * f.Vx;
+    ay += cv * f.Vy;
+    az += cv * f.Vz;
     // WallAcceleration, wcsph_with_boundary_model.slang:336-347.
     const float dx = fminf(xi.x - p.lo[0], 0.0f) - fminf(p.hi[0] - xi.x, 0.0f);
     const float dyw = fminf(xi.y - p.lo[1], 0.0f) - fminf(p.hi[1] - xi.y, 0.0f);
