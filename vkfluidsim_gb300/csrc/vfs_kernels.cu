@@ -635,18 +635,14 @@ __global__ void __launch_bounds__(kNbrBlock, kMinBlocks)
             const float dx = __fsub_rn(xj.x, xi.x), dy = __fsub_rn(xj.y, xi.y), dz = __fsub_rn(xj.z, xi.z);
             const float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
             const float r = r2 > 0.0f ? __fmul_rn(r2, rsqrtf(r2)) : 0.0f;
+            // W(q) / sigma, branch-free: 2 (1-q)^3 above q = 1/2, 6q^3 - 6q^2 + 1 below, 0 past 1.
             const float q = __fmul_rn(r, p.inv_h);
-            float w = 0.0f;
-            if (q <= 1.0f) {
-                if (q > 0.5f) {
-                    const float t = __fsub_rn(1.0f, q);
-                    w = __fmul_rn(__fmul_rn(p.cubic, 2.0f), __fmul_rn(__fmul_rn(t, t), t));
-                } else {
-                    const float q2 = __fmul_rn(q, q);
-                    w = __fmul_rn(p.cubic, __fmaf_rn(6.0f, __fmul_rn(q2, q), __fmaf_rn(-6.0f, q2, 1.0f)));
-                }
-            }
-            rho = __fmaf_rn(p.mass, w, rho);
+            const float t = __fsub_rn(1.0f, q);
+            const float w_out = __fmul_rn(__fmul_rn(__fmul_rn(t, t), t), 2.0f);
+            const float q2 = __fmul_rn(q, q);
+            const float w_in = __fmaf_rn(6.0f, __fmul_rn(q2, q), __fmaf_rn(-6.0f, q2, 1.0f));
+            const float w = q <= 1.0f ? (q > 0.5f ? w_out : w_in) : 0.0f;
+            rho = __fadd_rn(rho, w);
             if (j != i) {
                 if (listed < p.nbr_cap) {
                     *nbr_out = j;
@@ -673,7 +669,7 @@ __global__ void __launch_bounds__(kNbrBlock, kMinBlocks)
     nbr_count[i] = nbr_word(listed, cx, cy, cz, distinct);
     float bd, bgx, bgy, bgz;
     boundary_terms(p, xi.x, xi.y, xi.z, bd, bgx, bgy, bgz);
-    rho += p.rho0 * bd;
+    rho = p.mass * p.cubic * rho + p.rho0 * bd;  // the factor the drain leaves out of the sum
     const float pr = p.stiffness * (powf(fmaxf(rho, p.rho0) / p.rho0, p.expoent) - 1.0f);
     const float pd = rho > 0.0f ? pr / (rho * rho) : 0.0f;
     const float mr = p.mass / fmaxf(rho, 1e-6f);
