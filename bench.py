@@ -397,6 +397,32 @@ def time_next_rows(args, stream, torch, model, rank):
     t0 = time.perf_counter()
     model.render_particles(mv, pj, 1920, 1080, quad_side=0.01)
     out["render_1920x1080_ms"] = 1e3 * (time.perf_counter() - t0)
+    # The density field of the scene on 256 x 128 x 128 nodes over its 2 x 1 x 1 m box and its
+    # raymarch (raymarch.slang, 0.01 m steps) at 1920 x 1080, both into device buffers.
+    import ctypes as C
+
+    from vkfluidsim_gb300._abi import check
+
+    lo, hi = np.zeros(3, np.float32), np.array([2.0, 1.0, 1.0], np.float32)
+    res = np.array([256, 128, 128], np.int32)
+    grid = torch.empty((128, 128, 256), dtype=torch.float32, device="cuda")
+    img = torch.zeros((1080, 1920, 4), dtype=torch.float32, device="cuda")
+    tp = lambda t_: C.cast(C.c_void_p(t_.data_ptr()), C.POINTER(C.c_float))  # noqa: E731
+    fp = lambda a: a.ctypes.data_as(C.POINTER(C.c_float))  # noqa: E731
+    ip = res.ctypes.data_as(C.POINTER(C.c_int32))
+    lib = model._lib
+    for k in range(2):  # the first call warms up
+        t0 = time.perf_counter()
+        check(lib.vfs_model_density_grid(model._h, fp(lo), fp(hi), ip, tp(grid)))
+        out["density_grid_256x128x128_ms"] = 1e3 * (time.perf_counter() - t0)
+    grid /= 1000.0
+    torch.cuda.synchronize()
+    center, half = (lo + hi) / 2, (hi - lo) / 2
+    for k in range(2):
+        t0 = time.perf_counter()
+        check(lib.vfs_render_density_raymarch(tp(grid), ip, fp(center), fp(half), fp(mv), fp(pj),
+                                              1920, 1080, 0.01, 1000, 5.0, 2.0, tp(img)))
+        out["raymarch_1920x1080_ms"] = 1e3 * (time.perf_counter() - t0)
     with tempfile.TemporaryDirectory() as d:
         t0 = time.perf_counter()
         model.export_state(f"{d}/snap")

@@ -233,6 +233,31 @@ int vfs_model_render_particles(vfs_model* m, const float* model_view, const floa
                                int32_t width, int32_t height, float quad_side, float depth_radius,
                                float v_max, uint8_t* rgba, float* depth);
 
+/* ---- density field and density raymarch (assets/shaders/draw/raymarch.slang as drawn by
+ * DensityRaymarchDrawPipeline::Draw, src/pipelines/raymarch_pipeline.cpp:62-115; an extension
+ * for the field: the reference raymarches a precomputed 3D grid) ----
+ * vfs_model_density_grid: SPH density sum_j m W(|x - x_j|) of the current particles at the nodes
+ * of a regular grid over [lo, hi] (node (i, j, k) at lo + (i, j, k) (hi - lo) / (res - 1); res[a]
+ * = 1 puts one node at lo[a]), stored x fastest: grid[(k res[1] + j) res[0] + i]. grid: device,
+ * page-locked or pageable memory, res[0] res[1] res[2] floats. Float atomics: the sums' last
+ * bits vary from run to run. */
+int vfs_model_density_grid(vfs_model* m, const float* lo, const float* hi, const int32_t* res,
+                           float* grid);
+/* Raymarches the scalar field (res[0] x res[1] x res[2] floats, x fastest, host or device memory)
+ * occupying the box center +- half_extent, the reference placing it at 0 +- field_size, and
+ * alpha-blends the result over rgba (width * height float4 RGBA, row 0 at NDC y = -1, in/out,
+ * host or device memory). Per pixel: start on the box face the camera sees first (the exit face
+ * when the camera is inside), then at most n_steps steps of `step` world units while inside the
+ * box, adding step * colormap(d * color_scale) * d * emission, colormap = IDL Mac style with
+ * alpha 1 and d the trilinear, wrap-around sample of the field (texel centres at (i + 0.5) / n).
+ * The sum is clamped to [0, 1] and blended: rgb = s.rgb s.a + dst.rgb (1 - s.a),
+ * a = s.a + dst.a (1 - s.a). Reference values: step 0.05, n_steps 1000, color_scale 5,
+ * emission 200. view, proj: column-major 4x4 (glm layout). */
+int vfs_render_density_raymarch(const float* field, const int32_t* res, const float* center,
+                                const float* half_extent, const float* view, const float* proj,
+                                int32_t width, int32_t height, float step, int32_t n_steps,
+                                float color_scale, float emission, float* rgba);
+
 /* ---- autotuner (an extension: the reference's dispatch sizes are fixed in its shaders'
  * numthreads, e.g. assets/shaders/simulation/wcsph_with_boundary_model.slang:92) ----
  * Launch shapes of one substep. None changes any result: the sort is stable for every digit
@@ -301,6 +326,8 @@ int vfs_batch_record(vfs_batch* b, int32_t substeps, int32_t every, const char* 
 int vfs_batch_render_particles(vfs_batch* b, int32_t scene, const float* model_view,
                                const float* proj, int32_t width, int32_t height, float quad_side,
                                float depth_radius, float v_max, uint8_t* rgba, float* depth);
+int vfs_batch_density_grid(vfs_batch* b, int32_t scene, const float* lo, const float* hi,
+                           const int32_t* res, float* grid);
 int vfs_batch_autotune(vfs_batch* b, int32_t repeats, int32_t use_cache, vfs_tune_config* chosen);
 int vfs_batch_set_tune_config(vfs_batch* b, const vfs_tune_config* c);
 int vfs_batch_get_tune_config(vfs_batch* b, vfs_tune_config* c);

@@ -7,12 +7,14 @@ from ._abi import LIB_PATH, VfsError, load_library, SHAPE_SPHERE, SHAPE_BOX, SHA
 from .model import (AnalyticObject, Batch, MeshObject, mesh_signed_distance, SimulationParameters, SPHParameters, WCSPHParameters,
                     WCSPHWithBoundaryModel, generate_fourier_velocity, generate_lattice,
                     generate_uniform_blob, load_scene, look_at, perspective, read_state,
-                    tune_cache_clear, tune_cache_load, tune_cache_save, write_ppm)
+                    render_density_raymarch, to_rgba8, tune_cache_clear, tune_cache_load,
+                    tune_cache_save, write_ppm)
 
 __all__ = [
     "LIB_PATH", "VfsError", "load_library", "SHAPE_SPHERE", "SHAPE_BOX", "SHAPE_CONTAINER",
     "AnalyticObject", "Batch", "MeshObject", "mesh_signed_distance", "SimulationParameters", "SPHParameters", "WCSPHParameters",
     "WCSPHWithBoundaryModel", "generate_fourier_velocity", "generate_lattice",
     "generate_uniform_blob", "load_scene", "look_at", "perspective", "read_state",
-    "tune_cache_clear", "tune_cache_load", "tune_cache_save", "write_ppm",
+    "render_density_raymarch", "to_rgba8", "tune_cache_clear", "tune_cache_load",
+    "tune_cache_save", "write_ppm",
 ]

@@ -177,6 +177,11 @@ SIGNATURES = {
     "vfs_batch_render_particles": (_I, [_P, C.c_int32, C.POINTER(C.c_float), C.POINTER(C.c_float),
                                         C.c_int32, C.c_int32, C.c_float, C.c_float, C.c_float,
                                         C.POINTER(C.c_uint8), C.POINTER(C.c_float)]),
+    "vfs_model_density_grid": (_I, [_P, _F, _F, C.POINTER(C.c_int32), _F]),
+    "vfs_batch_density_grid": (_I, [_P, C.c_int32, _F, _F, C.POINTER(C.c_int32), _F]),
+    "vfs_render_density_raymarch": (_I, [_F, C.POINTER(C.c_int32), _F, _F, _F, _F, C.c_int32,
+                                         C.c_int32, C.c_float, C.c_int32, C.c_float, C.c_float,
+                                         _F]),
     "vfs_model_import_state": (_I, [_P, C.c_char_p]),
     "vfs_model_record": (_I, [_P, C.c_int32, C.c_int32, C.c_char_p]),
     "vfs_batch_export_state": (_I, [_P, C.c_int32, C.c_char_p]),

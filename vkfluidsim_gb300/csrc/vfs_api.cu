@@ -103,23 +103,6 @@ __global__ void __launch_bounds__(kIoBlock)
     }
 }
 
-// The address under which this device's kernels reach host buffer p: page-locked host memory
-// (cudaHostAlloc / cudaHostRegister, mapped under unified addressing) or device and managed
-// memory of this device. Null for pageable memory, which goes through a staging copy.
-void* device_alias(const void* p) {
-    if (!p) return nullptr;
-    cudaPointerAttributes a{};
-    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
-        cudaGetLastError();
-        return nullptr;
-    }
-    int dev = -1;
-    cudaGetDevice(&dev);
-    if (a.type == cudaMemoryTypeHost) return a.devicePointer;
-    if ((a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged) && a.device == dev)
-        return a.devicePointer;
-    return nullptr;
-}
 
 // Scene id of every particle of a batched model.
 __global__ void k_fill_scene_of(const uint32_t* __restrict__ scene_off, uint32_t n_scenes,
@@ -555,6 +538,24 @@ int create_model(const std::vector<SceneHost>& scenes, Model** out) {
     }
     *out = m;
     return VFS_OK;
+}
+
+// The address under which this device's kernels reach host buffer p: page-locked host memory
+// (cudaHostAlloc / cudaHostRegister, mapped under unified addressing) or device and managed
+// memory of this device. Null for pageable memory, which goes through a staging copy.
+void* device_alias(const void* p) {
+    if (!p) return nullptr;
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    int dev = -1;
+    cudaGetDevice(&dev);
+    if (a.type == cudaMemoryTypeHost) return a.devicePointer;
+    if ((a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged) && a.device == dev)
+        return a.devicePointer;
+    return nullptr;
 }
 
 int Model::set_state(uint32_t scene, const float* pos3, const float* vel3, uint32_t offset,

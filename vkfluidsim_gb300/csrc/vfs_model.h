@@ -117,6 +117,9 @@ int create_model(const std::vector<SceneHost>& scenes, Model** out);
 
 // Runs `count` substeps with events between the passes; phase_ms[6] = mean ms of keys, sort,
 // cells+reorder, density, force, clear.
+// The address under which this device's kernels reach buffer p: page-locked host memory, or
+// device and managed memory of this device; null for pageable host memory.
+void* device_alias(const void* p);
 int profile_phases(Model& m, int32_t count, float* phase_ms);
 int set_sort_config(Model& m, int32_t digit_bits, int32_t tile_items);
 int set_neighbor_capacity(Model& m, int32_t slots);

@@ -220,6 +220,44 @@ def _render(lib_fn, args, width, height, quad_side, depth_radius, v_max, with_de
     return (img, dep) if with_depth else img
 
 
+def _density_grid(lib_fn, args, lo, hi, res) -> np.ndarray:
+    lo = _f32(lo, (3,))
+    hi = _f32(hi, (3,))
+    r = np.ascontiguousarray(np.asarray(res, dtype=np.int32).reshape(3))
+    grid = np.empty((int(r[2]), int(r[1]), int(r[0])), np.float32)
+    check(lib_fn(*args, _fp(lo), _fp(hi), r.ctypes.data_as(C.POINTER(C.c_int32)), _fp(grid)))
+    return grid
+
+
+def render_density_raymarch(field, center, half_extent, view, proj, width: int, height: int,
+                            step: float = 0.05, n_steps: int = 1000, color_scale: float = 5.0,
+                            emission: float = 200.0, background=None) -> np.ndarray:
+    """The reference's density raymarch (raymarch.slang) of a scalar field of shape
+    (nz, ny, nx) occupying center +- half_extent, alpha-blended over `background` (an
+    (height, width, 4) float RGBA image, transparent black by default). Returns the float image
+    (row 0 at NDC y = -1); `to_rgba8` quantises it as the reference's 8-bit draw image does."""
+    f = np.ascontiguousarray(field, dtype=np.float32)
+    if f.ndim != 3:
+        raise ValueError("field must have shape (nz, ny, nx)")
+    res = np.array([f.shape[2], f.shape[1], f.shape[0]], np.int32)
+    img = np.zeros((height, width, 4), np.float32)
+    if background is not None:
+        img[...] = np.asarray(background, np.float32)
+    c = _f32(center, (3,))
+    he = _f32(half_extent, (3,))
+    v = np.ascontiguousarray(view, np.float32)
+    pj = np.ascontiguousarray(proj, np.float32)
+    check(load_library().vfs_render_density_raymarch(
+        _fp(f), res.ctypes.data_as(C.POINTER(C.c_int32)), _fp(c), _fp(he), _fp(v), _fp(pj), width,
+        height, step, n_steps, color_scale, emission, _fp(img)))
+    return img
+
+
+def to_rgba8(img) -> np.ndarray:
+    """Float RGBA in [0, 1] to uint8, rounding to nearest (a UNORM attachment's conversion)."""
+    return np.clip(np.rint(np.asarray(img, np.float32) * 255.0), 0, 255).astype(np.uint8)
+
+
 def tune_dict(c) -> dict:
     return {k: int(getattr(c, k)) for k, _ in _abi.TuneConfig._fields_}
 
@@ -435,6 +473,12 @@ class WCSPHWithBoundaryModel:
         return _render(self._lib.vfs_model_render_particles, (self._h, model_view, proj), width,
                        height, quad_side, depth_radius, v_max, with_depth)
 
+    def density_grid(self, lo, hi, res) -> np.ndarray:
+        """SPH density of the current particles at the nodes of a regular grid over [lo, hi]
+        (vfs_model_density_grid): shape (res_z, res_y, res_x), node (i, j, k) at
+        lo + (i, j, k) (hi - lo) / (res - 1)."""
+        return _density_grid(self._lib.vfs_model_density_grid, (self._h,), lo, hi, res)
+
     def autotune(self, repeats: int = 3, use_cache: bool = True) -> dict:
         """Runs the autotuner (vfs_model_autotune) and returns the chosen launch shapes."""
         c = _abi.TuneConfig()
@@ -638,6 +682,9 @@ class Batch:
                          with_depth: bool = False):
         return _render(self._lib.vfs_batch_render_particles, (self._h, scene, model_view, proj),
                        width, height, quad_side, depth_radius, v_max, with_depth)
+
+    def density_grid(self, scene: int, lo, hi, res) -> np.ndarray:
+        return _density_grid(self._lib.vfs_batch_density_grid, (self._h, scene), lo, hi, res)
 
     def autotune(self, repeats: int = 3, use_cache: bool = True) -> dict:
         """Runs the autotuner (vfs_batch_autotune) and returns the chosen launch shapes."""
