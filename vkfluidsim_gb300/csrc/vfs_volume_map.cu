@@ -38,20 +38,6 @@ __device__ __forceinline__ double shape_sdf(int shape, const double* prm, double
     return shape == 1 ? box : -box;
 }
 
-// CubicSplineKernel::W in double (src/util/kernel.cpp:22-38).
-__device__ __forceinline__ double kernel_w(double r, double radius, double factor) {
-    const double q = r / radius;
-    if (q <= 1.0) {
-        if (q <= 0.5) {
-            const double q2 = dm(q, q), q3 = dm(q2, q);
-            return dm(factor, da(ds(dm(6.0, q3), dm(6.0, q2)), 1.0));
-        }
-        return dm(factor, dm(2.0, pow(ds(1.0, q), 3.0)));
-    }
-    return 0.0;
-}
-
-
 // ---------------------------------------------------------------- triangle meshes
 
 enum : int { kEntV0 = 0, kEntV1, kEntV2, kEntE01, kEntE12, kEntE02, kEntF };
