@@ -742,16 +742,6 @@ __device__ __forceinline__ void force_term_rec(const SceneParams& p, const float
     force_term(p, xi, vi, pdi, r0, make_float2(r0.w, r1.w), r1, f);
 }
 
-// Phase B of the force pass over the first cnt listed neighbours.
-template <int kNbrBlock>
-__device__ __forceinline__ void force_drain(const SceneParams& p, const float4* __restrict__ rec,
-                                            const uint32_t* s_j, int tid, int cnt,
-                                            const float4& xi, const float4& vi, float pdi,
-                                            ForceAcc& f) {
-#pragma unroll 2
-    for (int k = 0; k < cnt; k++) force_term_rec(p, xi, vi, pdi, rec, s_j[k * kNbrBlock + tid], f);
-}
-
 // CalculatePressureAccel + CalculateViscousAccel + UpdatePositions
 // (wcsph_with_boundary_model.slang:205-360), fused: both sums are accumulated separately in the
 // reference's visiting order, then a = ((g - P) + V) + wall, v += a dt, x += v dt.
@@ -763,11 +753,9 @@ __global__ void __launch_bounds__(kNbrBlock, kMinBlocks)
             const uint32_t* __restrict__ scan, const uint32_t* __restrict__ nbr,
             const uint32_t* __restrict__ nbr_count, float4* __restrict__ pos_out,
             float4* __restrict__ vel_out, float4* __restrict__ acc_out) {
-    __shared__ uint32_t s_j[kListCap * kNbrBlock];
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= L.total) return;
     const SceneParams& p = scene_params<kBatch>(L, i);
-    const int tid = threadIdx.x;
     const float4 xi = __ldg(pos + i);
     const float4 vi = __ldg(vel + i);
     const float4 ai = __ldg(aux + i);
@@ -794,24 +782,16 @@ __global__ void __launch_bounds__(kNbrBlock, kMinBlocks)
 #pragma unroll 1
         for (; k < listed; k++, nl += stride) force_term_rec(p, xi, vi, pdi, rec, __ldg(nl), f);
     } else {
-        // Overflowed list (very dense neighbourhood): walk the candidates again.
+        // Overflowed list (very dense neighbourhood): walk the candidates again and add every
+        // in-range one as it comes, in the same order. This path needs no shared memory, so
+        // the pass keeps the whole on-chip memory as L1 for its record gathers.
         const uint32_t cx = cell_coord(xi.x, p.h), cy = cell_coord(xi.y, p.h),
                        cz = cell_coord(xi.z, p.h);
-        int cnt = 0;
         for_each_candidate(p, scan, pos, xi, cx, cy, cz, [&](uint32_t j, const float4& xj) {
             const float xx = xi.x - xj.x, xy = xi.y - xj.y, xz = xi.z - xj.z;
             const float r2 = xx * xx + xy * xy + xz * xz;
-            if (r2 <= p.h2 && j != i) {
-                s_j[cnt * kNbrBlock + tid] = j;
-                cnt++;
-            }
-        }, [&]() {
-            if (cnt > kDrainAt) {
-                force_drain<kNbrBlock>(p, rec, s_j, tid, cnt, xi, vi, pdi, f);
-                cnt = 0;
-            }
-        });
-        force_drain<kNbrBlock>(p, rec, s_j, tid, cnt, xi, vi, pdi, f);
+            if (r2 <= p.h2 && j != i) force_term_rec(p, xi, vi, pdi, rec, j, f);
+        }, [&]() {});
     }
     // The factors force_term leaves out of the sums.
     const float cp = p.mass * p.grad_over_h, cv = p.visc_scale * p.grad_over_h;
