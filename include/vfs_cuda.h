@@ -269,6 +269,8 @@ typedef struct vfs_tune_config {
     int32_t nbr_block;       /* neighbour passes: threads per block ... */
     int32_t nbr_min_blocks;  /* ... and minimum resident blocks per SM: 128x6, 128x8, 96x8, 64x12 */
     int32_t cell_block;      /* keys per block of the cell-range / reorder kernel: 128, 256, 512 */
+    int32_t force_block;     /* force pass: threads per block and minimum resident blocks per */
+    int32_t force_min_blocks;/* SM, the same four shapes; 0, 0 = the neighbour passes' shape */
 } vfs_tune_config;
 /* Times every candidate of each stage (sort, neighbour passes, cell ranges) for `repeats`
  * substeps from the model's current state, keeps the fastest, and restores the state (the

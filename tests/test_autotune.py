@@ -12,16 +12,20 @@ from vkfluidsim_gb300 import workloads as W
 def test_tune_cache_file_round_trip(tmp_path):
     vfs.tune_cache_clear()
     f = tmp_path / "tune.txt"
-    f.write_text("# header\nsm103_152sms_n32768_s1_00000000000000aa 7 12 96 8 512\n")
+    # A full line, and a line without the force shape (which then follows the neighbour shape).
+    f.write_text("# header\nsm103_152sms_n32768_s1_00000000000000aa 7 12 96 8 512 128 8\n"
+                 "sm103_152sms_n65536_s1_00000000000000bb 8 16 64 12 256\n")
     vfs.tune_cache_load(str(f))
     out = tmp_path / "out.txt"
     vfs.tune_cache_save(str(out))
     lines = [ln for ln in out.read_text().splitlines() if not ln.startswith("#")]
-    assert lines == ["sm103_152sms_n32768_s1_00000000000000aa 7 12 96 8 512"]
+    assert lines == ["sm103_152sms_n32768_s1_00000000000000aa 7 12 96 8 512 128 8",
+                     "sm103_152sms_n65536_s1_00000000000000bb 8 16 64 12 256 64 12"]
     vfs.tune_cache_clear()
 
 
-@pytest.mark.parametrize("bad", ["key 7 12 100 3 512\n", "key 9 12 128 6 256\n", "key 7\n"])
+@pytest.mark.parametrize("bad", ["key 7 12 100 3 512\n", "key 9 12 128 6 256\n", "key 7\n",
+                                 "key 7 12 128 6 256 100 3\n", "key 7 12 128 6 256 128\n"])
 def test_tune_cache_rejects_bad_lines(tmp_path, bad):
     f = tmp_path / "bad.txt"
     f.write_text(bad)
@@ -76,7 +80,8 @@ def test_every_launch_shape_gives_the_same_step(shape, cell_block):
     ref.substeps(3)
     m = W.build_model(w)
     m.set_tune_config(nbr_block=shape[0], nbr_min_blocks=shape[1], cell_block=cell_block,
-                      sort_digit_bits=6, sort_tile_items=8)
+                      sort_digit_bits=6, sort_tile_items=8, force_block=shape[0],
+                      force_min_blocks=shape[1])
     m.substeps(3)
     x0, v0 = _state(ref)
     x1, v1 = _state(m)
@@ -84,10 +89,30 @@ def test_every_launch_shape_gives_the_same_step(shape, cell_block):
 
 
 @pytest.mark.gpu
+def test_force_shape_apart_from_density_shape():
+    w = W.dam_break(dims=(24, 24, 24), map_res=24, seed=6)
+    ref = W.build_model(w)
+    ref.substeps(3)
+    m = W.build_model(w)
+    m.set_tune_config(nbr_block=64, nbr_min_blocks=12, force_block=128, force_min_blocks=6)
+    assert m.get_tune_config()["force_block"] == 128
+    m.substeps(3)
+    x0, v0 = _state(ref)
+    x1, v1 = _state(m)
+    assert np.array_equal(x0, x1) and np.array_equal(v0, v1)
+    # 0 x 0 selects the neighbour passes' shape.
+    m.set_tune_config(nbr_block=64, nbr_min_blocks=12, force_block=0, force_min_blocks=0)
+    cfg = m.get_tune_config()
+    assert (cfg["force_block"], cfg["force_min_blocks"]) == (64, 12)
+
+
+@pytest.mark.gpu
 def test_invalid_tune_config_is_rejected():
     m = W.build_model(W.dam_break(dims=(8, 8, 8), map_res=0))
     with pytest.raises(vfs.VfsError):
-        m.set_tune_config(nbr_block=96)
+        m.set_tune_config(nbr_block=100)
+    with pytest.raises(vfs.VfsError):
+        m.set_tune_config(force_block=100)
     with pytest.raises(vfs.VfsError):
         m.set_tune_config(cell_block=1000)
 

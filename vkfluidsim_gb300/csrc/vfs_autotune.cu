@@ -48,6 +48,8 @@ vfs_tune_config current(const Model& m) {
     c.nbr_block = kShapes[m.kc.nbr_shape].threads;
     c.nbr_min_blocks = kShapes[m.kc.nbr_shape].min_blocks;
     c.cell_block = m.kc.cell_block;
+    c.force_block = kShapes[m.kc.force_shape].threads;
+    c.force_min_blocks = kShapes[m.kc.force_shape].min_blocks;
     return c;
 }
 
@@ -87,6 +89,12 @@ int apply_tune_config(Model& m, const vfs_tune_config& c) {
     if (shape < 0)
         return fail(VFS_ERR_INVALID_ARGUMENT,
                     "neighbour block shape must be 128x6, 128x8, 96x8 or 64x12 (threads x blocks/SM)");
+    const int fshape = c.force_block == 0 && c.force_min_blocks == 0
+                           ? shape
+                           : shape_of(c.force_block, c.force_min_blocks);
+    if (fshape < 0)
+        return fail(VFS_ERR_INVALID_ARGUMENT,
+                    "force block shape must be 128x6, 128x8, 96x8 or 64x12, or 0x0 for the neighbour shape");
     if (c.cell_block != 128 && c.cell_block != 256 && c.cell_block != 512)
         return fail(VFS_ERR_INVALID_ARGUMENT, "cell_block must be 128, 256 or 512");
     if (c.sort_digit_bits != m.digit_bits || c.sort_tile_items != m.tile_items) {
@@ -95,6 +103,7 @@ int apply_tune_config(Model& m, const vfs_tune_config& c) {
     }
     VFS_TUNE_TRY(cudaStreamSynchronize(m.stream));
     m.kc.nbr_shape = shape;
+    m.kc.force_shape = fshape;
     m.kc.cell_block = c.cell_block;
     m.invalidate_graph();
     return VFS_OK;
@@ -164,18 +173,24 @@ int autotune(Model& m, int repeats, bool use_cache, vfs_tune_config* chosen) {
                 }
             }
     }
-    // Stage 2: neighbour-pass block shape (density + force).
+    // Stage 2: block shapes of the density and force passes (independent kernels, one sweep).
     if (rc == VFS_OK) {
-        float best_t = 1e30f;
+        float best_d = 1e30f, best_f = 1e30f;
         vfs_tune_config c = best;
         for (int k = 0; k < kNumNbrShapes && rc == VFS_OK; k++) {
-            c.nbr_block = kShapes[k].threads;
-            c.nbr_min_blocks = kShapes[k].min_blocks;
+            c.nbr_block = c.force_block = kShapes[k].threads;
+            c.nbr_min_blocks = c.force_min_blocks = kShapes[k].min_blocks;
             measure(c, ph);
-            if (rc == VFS_OK && ph[3] + ph[4] < best_t) {
-                best_t = ph[3] + ph[4];
+            if (rc) break;
+            if (ph[3] < best_d) {
+                best_d = ph[3];
                 best.nbr_block = c.nbr_block;
                 best.nbr_min_blocks = c.nbr_min_blocks;
+            }
+            if (ph[4] < best_f) {
+                best_f = ph[4];
+                best.force_block = c.force_block;
+                best.force_min_blocks = c.force_min_blocks;
             }
         }
     }
@@ -215,11 +230,12 @@ int tune_cache_save(const char* path) {
     std::lock_guard<std::mutex> lk(g_cache_mu);
     FILE* f = std::fopen(path, "w");
     if (!f) return fail(VFS_ERR_IO, std::string("cannot write ") + path);
-    std::fprintf(f, "# vkfluidsim_gb300 tune cache: key digit_bits tile_items nbr_block nbr_min_blocks cell_block\n");
+    std::fprintf(f, "# vkfluidsim_gb300 tune cache: key digit_bits tile_items nbr_block nbr_min_blocks "
+                    "cell_block force_block force_min_blocks\n");
     for (const auto& kv : g_cache)
-        std::fprintf(f, "%s %d %d %d %d %d\n", kv.first.c_str(), kv.second.sort_digit_bits,
+        std::fprintf(f, "%s %d %d %d %d %d %d %d\n", kv.first.c_str(), kv.second.sort_digit_bits,
                      kv.second.sort_tile_items, kv.second.nbr_block, kv.second.nbr_min_blocks,
-                     kv.second.cell_block);
+                     kv.second.cell_block, kv.second.force_block, kv.second.force_min_blocks);
     const bool ok = std::fclose(f) == 0;
     return ok ? VFS_OK : fail(VFS_ERR_IO, std::string("cannot write ") + path);
 }
@@ -235,9 +251,16 @@ int tune_cache_load(const char* path) {
         if (line[0] == '#' || line[0] == '\n') continue;
         char key[256];
         vfs_tune_config c{};
-        if (std::sscanf(line, "%255s %d %d %d %d %d", key, &c.sort_digit_bits, &c.sort_tile_items,
-                        &c.nbr_block, &c.nbr_min_blocks, &c.cell_block) != 6 ||
-            shape_of(c.nbr_block, c.nbr_min_blocks) < 0 || c.sort_digit_bits < 4 ||
+        // Lines of 6 values (no force shape) take the neighbour shape for the force pass.
+        const int got = std::sscanf(line, "%255s %d %d %d %d %d %d %d", key, &c.sort_digit_bits,
+                                    &c.sort_tile_items, &c.nbr_block, &c.nbr_min_blocks,
+                                    &c.cell_block, &c.force_block, &c.force_min_blocks);
+        if (got == 6) {
+            c.force_block = c.nbr_block;
+            c.force_min_blocks = c.nbr_min_blocks;
+        }
+        if ((got != 6 && got != 8) || shape_of(c.nbr_block, c.nbr_min_blocks) < 0 ||
+            shape_of(c.force_block, c.force_min_blocks) < 0 || c.sort_digit_bits < 4 ||
             c.sort_digit_bits > 8) {
             rc = fail(VFS_ERR_PARSE, std::string("bad tune cache line in ") + path);
             break;

@@ -119,7 +119,8 @@ SortConfig make_sort_config(uint32_t n, int digit_bits, int tile_items, int key_
 enum NbrShape : int { kNbr128x6 = 0, kNbr128x8 = 1, kNbr96x8 = 2, kNbr64x12 = 3, kNumNbrShapes = 4 };
 // Launch shapes chosen per model (by default or by the autotuner); none changes any result.
 struct KernelConfig {
-    int nbr_shape = kNbr128x6;
+    int nbr_shape = kNbr96x8;     // density pass (and the adjoint's recomputed forward)
+    int force_shape = kNbr128x8;  // force pass (no shared memory: it takes the larger blocks)
     int cell_block = 256;  // keys per block of the cell-range / reorder kernel: 128, 256 or 512
 };
 size_t sort_scratch_words(const SortConfig& c);

@@ -1242,7 +1242,7 @@ cudaError_t launch_force(const StepLaunch& L, const float4* pos, const float4* v
                          const uint32_t* nbr, const uint32_t* nbr_count, float4* pos_out,
                          float4* vel_out, float4* acc_out, const KernelConfig& kc, cudaStream_t s) {
     if (L.total == 0) return cudaSuccess;
-    switch (kc.nbr_shape) {
+    switch (kc.force_shape) {
         case kNbr128x8:
             force_shape<128, 8>(L, pos, vel, aux, rec, bnd, cell_scan, nbr, nbr_count, pos_out, vel_out, acc_out, s);
             break;
