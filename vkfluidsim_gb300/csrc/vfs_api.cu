@@ -361,7 +361,8 @@ int Model::enqueue_substep(cudaEvent_t* ev) {
     sperm = sp_buf;
     if (ev) VFS_CUDA_TRY(cudaEventRecord(ev[3], s));
     VFS_CUDA_TRY(launch_cells_reorder(n, skeys, sperm, cell_scan, pos[c], vel[c], pos[o], vel[o],
-                                      scratch, (uint32_t)sort_scratch_words(sc), pkeys, kc, s));
+                                      scratch, (uint32_t)sort_scratch_words(sc), pkeys, cell_guess,
+                                      kc, s));
     if (ev) VFS_CUDA_TRY(cudaEventRecord(ev[4], s));
     VFS_CUDA_TRY(launch_density(launch, pos[o], vel[o], rec, cell_scan, aux, bnd, nbr, nbr_count, kc, s));
     if (ev) VFS_CUDA_TRY(cudaEventRecord(ev[5], s));
@@ -433,6 +434,7 @@ Model::~Model() {
     cudaFree(sp_buf);
     cudaFree(pkeys);
     cudaFree(moved);
+    cudaFree(cell_guess);
     cudaFree(bnd);
     cudaFree(acc);
     cudaFree(stage);
@@ -478,6 +480,8 @@ int Model::init() {
     VFS_CUDA_TRY(cudaMalloc(&pkeys, N * 4));
     VFS_CUDA_TRY(cudaMemset(pkeys, 0xFF, N * 4));  // sorted, and no key equals it: all moved
     VFS_CUDA_TRY(cudaMalloc(&moved, (2 * ((N + 31) / 32) + 1) * 4));
+    VFS_CUDA_TRY(cudaMalloc(&cell_guess, (N / 128 + 2) * 4));
+    VFS_CUDA_TRY(cudaMemset(cell_guess, 0, (N / 128 + 2) * 4));
     VFS_CUDA_TRY(cudaMalloc(&aux, N * sizeof(float4)));
     VFS_CUDA_TRY(cudaMalloc(&rec, 2 * N * sizeof(float4)));
     VFS_CUDA_TRY(cudaMalloc(&bnd, N * sizeof(float4)));

@@ -148,12 +148,14 @@ cudaError_t launch_sort(uint32_t n, const SortConfig& sc, const SortScratch& scr
                         bool vals_given = false, const uint32_t* n_dev = nullptr);
 // cell_scan[k] = first sorted index with key >= k (k in [0, n]); gathers pos/vel by perm; zeroes
 // zero[0, zero_words) (the sort scratch, for the next substep); copies skeys to pkeys_out (the next
-// substep's previous sorted keys) when pkeys_out is not NULL.
+// substep's previous sorted keys) when pkeys_out is not NULL. guess (n / 128 + 2 words, any
+// contents) keeps each block's bound of the sorted keys as the next call's starting point; NULL
+// searches from scratch.
 cudaError_t launch_cells_reorder(uint32_t n, const uint32_t* skeys, const uint32_t* perm,
                                  uint32_t* cell_scan, const float4* pos_in, const float4* vel_in,
                                  float4* pos_out, float4* vel_out, uint32_t* zero,
-                                 uint32_t zero_words, uint32_t* pkeys_out, const KernelConfig& kc,
-                                 cudaStream_t s);
+                                 uint32_t zero_words, uint32_t* pkeys_out, uint32_t* guess,
+                                 const KernelConfig& kc, cudaStream_t s);
 // Failure-detection self-test of the sort's bounded look-back wait (d_work: 96 words).
 cudaError_t launch_lookback_selftest(bool published, uint32_t spin_limit, uint32_t* d_work,
                                      uint32_t* err, cudaStream_t s);
