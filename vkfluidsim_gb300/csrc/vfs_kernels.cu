@@ -98,28 +98,53 @@ __device__ __forceinline__ void grid_axis(uint32_t n, float u, uint32_t& cell, f
     chi = fsb(fm(2.0f, fsb(x, f)), 1.0f);
 }
 
-// SampleGrid, wcsph_with_boundary_model.slang:51-66.
-__device__ __forceinline__ float sample_grid(const float* __restrict__ g, const uint32_t* n,
-                                             float u, float v, float w) {
-    uint32_t cx, cy, cz;
-    float ax, ay, az;
-    grid_axis(n[0], u, cx, ax);
-    grid_axis(n[1], v, cy, ay);
-    grid_axis(n[2], w, cz, az);
-    const size_t sx = 1, sy = n[0], sz = (size_t)n[0] * n[1];
-    const size_t b = cx + sy * cy + sz * cz;
-    // Corner order of the shader's offsets[8]: (0,0,0) (0,1,0) (0,0,1) (0,1,1) (1,0,0) ...
+// A point of a grid in SampleGrid's terms: per axis the clamped cell and chi = 2 frac - 1.
+struct GridPoint {
+    uint32_t cell[3];
+    float chi[3];
+};
+
+// Index of a point's base corner (its cell's lowest corner) in the grid array.
+__device__ __forceinline__ size_t grid_base(const uint32_t* n, const GridPoint& g) {
+    return g.cell[0] + (size_t)n[0] * g.cell[1] + (size_t)n[0] * n[1] * g.cell[2];
+}
+
+// The 8 corner values of a point's cell, in the shader's offsets[8] order:
+// (0,0,0) (0,1,0) (0,0,1) (0,1,1) (1,0,0) ...
+__device__ __forceinline__ void grid_corners(const float* __restrict__ g, const uint32_t* n,
+                                             const GridPoint& p, float c[8]) {
+    const size_t b = grid_base(n, p), sy = n[0], sz = (size_t)n[0] * n[1];
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+        const int ox = i >> 2, oy = i & 1, oz = (i >> 1) & 1;
+        c[i] = __ldg(g + b + ox + oy * sy + oz * sz);
+    }
+}
+
+// SampleGrid's weighted sum over the corner values (wcsph_with_boundary_model.slang:51-66).
+__device__ __forceinline__ float grid_interp(const float c[8], const GridPoint& p) {
     float val = 0.0f;
 #pragma unroll
     for (int i = 0; i < 8; i++) {
         const int ox = i >> 2, oy = i & 1, oz = (i >> 1) & 1;
-        const float fx = fa(1.0f, fm(ox ? 1.0f : -1.0f, ax));
-        const float fy = fa(1.0f, fm(oy ? 1.0f : -1.0f, ay));
-        const float fz = fa(1.0f, fm(oz ? 1.0f : -1.0f, az));
-        const float gval = __ldg(g + b + ox * sx + oy * sy + oz * sz);
-        val = fa(val, fm(gval, fm(fm(fx, fy), fz)));
+        const float fx = fa(1.0f, fm(ox ? 1.0f : -1.0f, p.chi[0]));
+        const float fy = fa(1.0f, fm(oy ? 1.0f : -1.0f, p.chi[1]));
+        const float fz = fa(1.0f, fm(oz ? 1.0f : -1.0f, p.chi[2]));
+        val = fa(val, fm(c[i], fm(fm(fx, fy), fz)));
     }
     return fdv(val, 8.0f);
+}
+
+// SampleGrid at normalised coordinates (u, v, w).
+__device__ __forceinline__ float sample_grid(const float* __restrict__ g, const uint32_t* n,
+                                             float u, float v, float w) {
+    GridPoint p;
+    grid_axis(n[0], u, p.cell[0], p.chi[0]);
+    grid_axis(n[1], v, p.cell[1], p.chi[1]);
+    grid_axis(n[2], w, p.cell[2], p.chi[2]);
+    float c[8];
+    grid_corners(g, n, p, c);
+    return grid_interp(c, p);
 }
 
 __device__ __forceinline__ void to_uvw(const DevObject& o, float x, float y, float z, float& u,
@@ -151,32 +176,42 @@ __device__ __forceinline__ void boundary_terms(const SceneParams& p, float px, f
         if (outside) continue;
         float u, v, w;
         to_uvw(o, lx, ly, lz, u, v, w);
-        const float dist = sample_grid(o.sdf, o.res, u, v, w);
+        GridPoint g0;
+        grid_axis(o.res[0], u, g0.cell[0], g0.chi[0]);
+        grid_axis(o.res[1], v, g0.cell[1], g0.chi[1]);
+        grid_axis(o.res[2], w, g0.cell[2], g0.chi[2]);
+        float c0[8];
+        grid_corners(o.sdf, o.res, g0, c0);
+        const float dist = grid_interp(c0, g0);
         if (!(dist >= 0.0f && dist < p.h)) continue;
         const float volume = sample_grid(o.vm, o.res, u, v, w);
         if (!(volume > 0.0f)) continue;
-        // GradientVector (slang:68-85): central differences of the SDF at +-0.1 h.
+        // GradientVector (slang:68-85): central differences of the SDF at +-0.1 h. A sample
+        // moved along one axis shares the other two axes' coordinates with the centre (the same
+        // operations on the same inputs), and the centre's corner values while it stays in the
+        // centre's cell; the sums are formed exactly as SampleGrid forms them.
         const float e = p.grad_eps;
-        float gx, gy, gz;
-        {
-            float a0, a1, a2;
-            to_uvw(o, fa(lx, e), ly, lz, a0, a1, a2);
-            const float v1x = sample_grid(o.sdf, o.res, a0, a1, a2);
-            to_uvw(o, fsb(lx, e), ly, lz, a0, a1, a2);
-            const float v0x = sample_grid(o.sdf, o.res, a0, a1, a2);
-            to_uvw(o, lx, fa(ly, e), lz, a0, a1, a2);
-            const float v1y = sample_grid(o.sdf, o.res, a0, a1, a2);
-            to_uvw(o, lx, fsb(ly, e), lz, a0, a1, a2);
-            const float v0y = sample_grid(o.sdf, o.res, a0, a1, a2);
-            to_uvw(o, lx, ly, fa(lz, e), a0, a1, a2);
-            const float v1z = sample_grid(o.sdf, o.res, a0, a1, a2);
-            to_uvw(o, lx, ly, fsb(lz, e), a0, a1, a2);
-            const float v0z = sample_grid(o.sdf, o.res, a0, a1, a2);
-            const float den = fm(2.0f, e);
-            gx = fdv(fsb(v1x, v0x), den);
-            gy = fdv(fsb(v1y, v0y), den);
-            gz = fdv(fsb(v1z, v0z), den);
+        const float lc[3] = {lx, ly, lz};
+        float grad[3];
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+            float s2[2];
+#pragma unroll
+            for (int sgn = 0; sgn < 2; sgn++) {
+                const float la = sgn == 0 ? fa(lc[a], e) : fsb(lc[a], e);
+                GridPoint g = g0;
+                grid_axis(o.res[a], fdv(fsb(la, o.box_pos[a]), o.box_size[a]), g.cell[a], g.chi[a]);
+                if (g.cell[a] == g0.cell[a]) {
+                    s2[sgn] = grid_interp(c0, g);
+                } else {
+                    float c[8];
+                    grid_corners(o.sdf, o.res, g, c);
+                    s2[sgn] = grid_interp(c, g);
+                }
+            }
+            grad[a] = fdv(fsb(s2[0], s2[1]), fm(2.0f, e));
         }
+        const float gx = grad[0], gy = grad[1], gz = grad[2];
         const float modn = __fsqrt_rn(fa(fa(fm(gx, gx), fm(gy, gy)), fm(gz, gz)));
         if (!(modn > 1e-9f)) continue;
         float nx = mat_row(o.R, 0, gx, gy, gz);
@@ -945,6 +980,17 @@ __global__ void __launch_bounds__(256)
     const uint32_t base = tile * kDeltaTile + (uint32_t)tid;
     uint32_t key[kDeltaItems];
     uint32_t ball[kDeltaItems];
+    // All of the thread's loads first (positions and previous keys), then the key arithmetic.
+    float4 xs[kDeltaItems];
+    uint32_t pks[kDeltaItems];
+#pragma unroll
+    for (int k = 0; k < kDeltaItems; k++) {
+        const uint32_t i = base + (uint32_t)k * 256u;
+        if (i < L.total) {
+            xs[k] = __ldg(pos + i);
+            pks[k] = __ldg(pkeys + i);
+        }
+    }
 #pragma unroll
     for (int k = 0; k < kDeltaItems; k++) {
         const uint32_t i = base + (uint32_t)k * 256u;
@@ -952,11 +998,11 @@ __global__ void __launch_bounds__(256)
         key[k] = 0u;
         if (i < L.total) {
             const SceneParams& p = scene_params<kBatch>(L, i);
-            const float4 x = pos[i];
+            const float4 x = xs[k];
             key[k] = p.off + key_mod(hash_cell(cell_coord(x.x, p.h), cell_coord(x.y, p.h),
                                                cell_coord(x.z, p.h)),
                                      p.mod_magic, p.n);
-            moved = key[k] != pkeys[i];
+            moved = key[k] != pks[k];
             if (moved)
                 for (int ps = 0; ps < passes; ps++)
                     atomicAdd(&s_h[ps * bins + ((key[k] >> (ps * digit_bits)) & mask)], 1u);
