@@ -321,7 +321,9 @@ void Model::invalidate_graph() {
 int Model::alloc_sort_scratch() {
     sc = make_sort_config(n, digit_bits, tile_items);
     const size_t words = sort_scratch_words(sc);
-    if (words > scratch_words) {
+    // Sized exactly for the configuration (a fresh buffer on every change), so every
+    // configuration lays its regions out the same way whatever ran before it.
+    if (words != scratch_words) {
         if (scratch) cudaFree(scratch);
         scratch = nullptr;
         VFS_CUDA_TRY(cudaMalloc(&scratch, words * sizeof(uint32_t)));
