@@ -302,6 +302,8 @@ def time_stress(args, stream, torch):
     m = W.build_model(w)
     m.set_stream(stream.cuda_stream)
     m.set_neighbor_capacity(STRESS_NBR_SLOTS)  # the blob's ~900 neighbours fit the lists
+    # Launch shapes for this state (the autotuner restores the state before every candidate).
+    tuned = m.autotune(repeats=1, use_cache=False) if args.autotune else m.get_tune_config()
     reps = max(3, min(args.steps, 10))
     for _ in range(args.warmup):
         m.set_particle_state(w.pos, w.vel)
@@ -328,6 +330,7 @@ def time_stress(args, stream, torch):
     frac = {k: B_PHASE[k] * n / (phase[k] * 1e-3) / 1e9 / hbm for k in ("density", "force") if k in phase}
     del m
     return {"workload": w.name, "particles": n, "repeats": reps, "neighbor_slots": STRESS_NBR_SLOTS,
+            "launch_shapes": tuned,
             "ms_per_step": float(np.median(ms)), "value": n / (float(np.median(ms)) * 1e-3),
             "phase_ms": phase,
             "sort": {"digit_bits": digits, "passes": passes,
