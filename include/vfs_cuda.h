@@ -193,8 +193,9 @@ int vfs_model_use_graph(vfs_model* m, int32_t enable);
 /* Waits for the stream and reads the device error word; VFS_ERR_DEVICE_CHECK if set. */
 int vfs_model_synchronize(vfs_model* m);
 /* count substeps without graphs, with events between passes; phase_ms[6] receives the mean
- * milliseconds per substep of: key+histogram, radix sort, cell ranges+reorder, density,
- * force+integrate, scratch clear. */
+ * milliseconds per substep of: keys+moved flags, radix sort+merge, cell ranges+reorder, density,
+ * force+integrate, and a sixth slot with nothing enqueued between its events (the event overhead
+ * alone: the sort scratch is cleared by the cell pass). */
 int vfs_model_profile_substeps(vfs_model* m, int32_t count, float* phase_ms);
 /* Sort tuning: digit width in bits (4..8) and items per thread of a onesweep tile (8, 12, 16). */
 int vfs_model_set_sort_config(vfs_model* m, int32_t digit_bits, int32_t tile_items);

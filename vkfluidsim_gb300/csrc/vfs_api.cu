@@ -3,9 +3,10 @@
 // of the compute primitives they drive (src/compute/spatial_hash.cpp, sort.cpp).
 //
 // The reference records 20 dispatches and 2 buffer copies per substep, each behind a full
-// compute barrier. Here one substep is five kernels plus one memset on one stream
-// (keys+histogram, 2-4 onesweep passes, cells+reorder, density, force), captured once as a CUDA
-// graph and replayed. State ping-pongs between two float4 buffer pairs: the reorder writes the
+// compute barrier. Here one substep is keys+moved flags, 2-4 onesweep passes over the particles
+// whose cell changed, merge, cells+reorder, density and force on one stream, with no memset
+// (the cell pass clears the sort scratch for the next substep), captured once as a CUDA graph and
+// replayed. State ping-pongs between two float4 buffer pairs: the reorder writes the
 // sorted copy into the spare pair and the force pass writes the integrated state back into the
 // original pair, so the substep is graph-stable.
 //
@@ -902,7 +903,8 @@ int profile_phases(Model& m, int32_t count, float* phase_ms) {
     if (m.n == 0) return VFS_OK;
     cudaEvent_t ev[7];
     for (int k = 0; k < 7; k++) VFS_CUDA_TRY(cudaEventCreate(&ev[k]));
-    // Event pairs in enqueue order: clear, keys, sort, cells+reorder, density, force.
+    // Event pairs in enqueue order: an empty pair (event overhead), keys, sort, cells+reorder,
+    // density, force.
     double acc_ms[6] = {0, 0, 0, 0, 0, 0};
     int rc = VFS_OK;
     for (int it = 0; it < count && rc == VFS_OK; it++) {
