@@ -707,6 +707,10 @@ __global__ void __launch_bounds__(kNbrBlock, kMinBlocks)
     uint32_t s_end = tid;  // shared-memory word one past the last kept candidate (stride kNbrBlock)
     uint32_t listed = 0;
     uint32_t* nbr_out = nbr + i;  // slot `listed` of particle i's list
+    // Scene constants used per candidate, in registers (a batched launch reads its scene's
+    // parameters from a device table).
+    const float s_inv_h = p.inv_h;
+    const uint32_t s_nbr_cap = p.nbr_cap;
     auto drain = [&]() {
 #pragma unroll 2
         for (uint32_t o = tid; o < s_end; o += kNbrBlock) {
@@ -717,7 +721,7 @@ __global__ void __launch_bounds__(kNbrBlock, kMinBlocks)
             const float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
             const float r = r2 > 0.0f ? __fmul_rn(r2, rsqrtf(r2)) : 0.0f;
             // W(q) / sigma, branch-free: 2 (1-q)^3 above q = 1/2, 6q^3 - 6q^2 + 1 below, 0 past 1.
-            const float q = __fmul_rn(r, p.inv_h);
+            const float q = __fmul_rn(r, s_inv_h);
             const float t = __fsub_rn(1.0f, q);
             const float w_out = __fmul_rn(__fmul_rn(__fmul_rn(t, t), t), 2.0f);
             const float q2 = __fmul_rn(q, q);
@@ -725,7 +729,7 @@ __global__ void __launch_bounds__(kNbrBlock, kMinBlocks)
             const float w = q <= 1.0f ? (q > 0.5f ? w_out : w_in) : 0.0f;
             rho = __fadd_rn(rho, w);
             if (j != i) {
-                if (listed < p.nbr_cap) {
+                if (listed < s_nbr_cap) {
                     *nbr_out = j;
                     nbr_out += L.total;
                 }
@@ -738,11 +742,12 @@ __global__ void __launch_bounds__(kNbrBlock, kMinBlocks)
     // range (the next one overwrites it otherwise). Lists are drained above kDrainAt, so the slot
     // index stays below kListCap.
     const bool distinct = distinct_keys(p, cx, cy, cz);
+    const float h2 = p.h2;
     for_each_candidate(p, scan, pos, xi, cx, cy, cz, [&](uint32_t j, const float4& xj) {
         const float dx = xj.x - xi.x, dy = xj.y - xi.y, dz = xj.z - xi.z;
         const float r2 = dx * dx + dy * dy + dz * dz;
         s_j[s_end] = j;
-        s_end += r2 <= p.h2 ? kNbrBlock : 0u;
+        s_end += r2 <= h2 ? kNbrBlock : 0u;
     }, [&]() {
         if (s_end > tid + kDrainAt * kNbrBlock) drain();
     });
