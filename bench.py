@@ -14,6 +14,9 @@ density, pressure + viscosity + integration).
   against the measured HBM copy bandwidth.
 * ``cpu_baseline`` the oracle (the project's restatement of the reference's shader math) on the
   host's cores, on a bounded sample of the same workload.
+* ``full_run`` the configured 1000-substep run timed end to end from the initial state (the run
+  blows up near substep 250 with the configured parameters, in the oracle as on the GPU; its
+  per-segment times show what that does to the cost).
 
 ``--impl reference`` times that CPU restatement alone, on every host thread (the reference's own
 Vulkan pipeline has no runnable form here: no Vulkan stack or software renderer exists).
@@ -434,6 +437,44 @@ def time_next_rows(args, stream, torch, model, rank):
     return out
 
 
+def time_full_run(args, stream, torch):
+    """The configured obstacle_1m run end to end: 1000 graphed substeps from the initial state,
+    timed with CUDA events around the whole run (no L2 flush: one continuous simulation). The
+    configured run does not stay physical (the column starts below rest density, free-falls and
+    is blown apart by the impact near substep 250, in the CPU oracle as on the GPU), so the peak
+    speed is reported beside the time."""
+    from vkfluidsim_gb300 import workloads as W
+
+    w = W.obstacle_1m()
+    m = W.build_model(w)
+    m.set_stream(stream.cuda_stream)
+    tuned = m.autotune(repeats=3) if args.autotune else m.get_tune_config()
+    m.set_particle_state(w.pos, w.vel)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    marks = {}
+    e0.record(stream)
+    done = 0
+    for chunk in (250, 250, 500):
+        m.substeps(chunk)
+        done += chunk
+        ev = torch.cuda.Event(enable_timing=True)
+        ev.record(stream)
+        marks[done] = ev
+    e1.record(stream)
+    torch.cuda.synchronize()
+    total = e0.elapsed_time(e1)
+    v = np.linalg.norm(m.copy_data_buffers()["velocities"], axis=1)
+    seg, prev = {}, e0
+    for k, ev in marks.items():
+        seg[f"to_{k}"] = prev.elapsed_time(ev) / (250 if k <= 500 else 500)
+        prev = ev
+    return {"workload": w.name, "particles": w.n, "substeps": done, "ms_total": total,
+            "ms_per_substep": total / done, "value": w.n * done / (total * 1e-3),
+            "ms_per_substep_by_segment": seg, "final_max_speed_m_s": float(v.max()),
+            "launch_shapes": tuned}
+
+
 def time_small(args, stream, torch):
     """The 32,768-particle dam break (32^3 lattice at 0.02, h = 0.04, 64^3 box-wall volume map,
     dt = 2e-4): device-timed graphed substeps, and the oracle on one host core for comparison."""
@@ -558,6 +599,7 @@ def run_gpu(args):
     next_rows = time_next_rows(args, stream, torch, m, rank) if args.next_rows else None
 
     small = time_small(args, stream, torch) if args.small else None
+    full_run = time_full_run(args, stream, torch) if args.full_run else None
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -607,6 +649,8 @@ def run_gpu(args):
             line["next_rows"] = next_rows
         if small:
             line["small"] = small
+        if full_run:
+            line["full_run"] = full_run
         if cpu:
             line["cpu_baseline"] = cpu
         print(json.dumps(line), flush=True)
@@ -630,6 +674,7 @@ def main():
     ap.add_argument("--autotune", type=int, default=1)
     ap.add_argument("--next-rows", type=int, default=1)
     ap.add_argument("--small", type=int, default=1)
+    ap.add_argument("--full-run", type=int, default=1)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
