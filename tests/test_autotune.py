@@ -51,9 +51,12 @@ def _state(m):
 
 
 @pytest.mark.gpu
+# The models below have 110,592 particles: large enough for one lane per particle in the density
+# pass, where its launch shapes apply (smaller models run it three lanes per particle with one
+# fixed shape).
 def test_autotuned_model_is_bit_identical_to_default():
     vfs.tune_cache_clear()
-    w = W.dam_break(dims=(32, 32, 32), map_res=32, seed=2)
+    w = W.dam_break(dims=(48, 48, 48), map_res=32, seed=2)
     ref = W.build_model(w)
     ref.substeps(4)
     m = W.build_model(w)
@@ -75,7 +78,7 @@ def test_autotuned_model_is_bit_identical_to_default():
 @pytest.mark.parametrize("shape", [(128, 6), (128, 8), (96, 8), (64, 12)])
 @pytest.mark.parametrize("cell_block", [128, 512])
 def test_every_launch_shape_gives_the_same_step(shape, cell_block):
-    w = W.dam_break(dims=(24, 24, 24), map_res=24, seed=5)
+    w = W.dam_break(dims=(48, 48, 48), map_res=24, seed=5)
     ref = W.build_model(w)
     ref.substeps(3)
     m = W.build_model(w)
@@ -90,7 +93,7 @@ def test_every_launch_shape_gives_the_same_step(shape, cell_block):
 
 @pytest.mark.gpu
 def test_force_shape_apart_from_density_shape():
-    w = W.dam_break(dims=(24, 24, 24), map_res=24, seed=6)
+    w = W.dam_break(dims=(48, 48, 48), map_res=24, seed=6)
     ref = W.build_model(w)
     ref.substeps(3)
     m = W.build_model(w)

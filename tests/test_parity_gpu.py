@@ -268,12 +268,14 @@ def test_partial_state_update_and_profile():
         m.set_particle_state(newp, newp, offset=w.n - 10, count=100)
 
 
-def test_dense_cluster_overflows_the_neighbour_list():
+# 24,000 particles run the density pass three lanes per particle, 64,000 one lane.
+@pytest.mark.parametrize("n_uniform", [20000, 60000])
+def test_dense_cluster_overflows_the_neighbour_list(n_uniform):
     """A tight Gaussian cluster gives hundreds of neighbours per particle, more than the
     neighbour-list capacity: the force pass must fall back to its own candidate walk."""
-    w = W.stress_4m(n_uniform=20000, n_blob=4000, map_res=0)
+    w = W.stress_4m(n_uniform=n_uniform, n_blob=4000, map_res=0)
     blob = vfs.generate_uniform_blob(0, (0, 0, 0), (1, 1, 1), 4000, (2.0, 1.0, 1.0), 0.008, 77)
-    w.pos[20000:] = blob
+    w.pos[n_uniform:] = blob
     m = W.build_model(w)
     o = oracle_for(w, m)
     compare_step(m, o, "dense_cluster")
@@ -281,12 +283,13 @@ def test_dense_cluster_overflows_the_neighbour_list():
     assert g["densities"].max() > 50 * np.median(g["densities"])
 
 
-def test_neighbour_capacity_changes_no_result():
+@pytest.mark.parametrize("n_uniform", [20000, 60000])
+def test_neighbour_capacity_changes_no_result(n_uniform):
     """The same dense cluster with 2048 list slots (no list overflows, so the force pass uses the
     lists) and with 128 (most blob particles fall back to the walk): bit-identical steps."""
-    w = W.stress_4m(n_uniform=20000, n_blob=4000, map_res=0)
+    w = W.stress_4m(n_uniform=n_uniform, n_blob=4000, map_res=0)
     blob = vfs.generate_uniform_blob(0, (0, 0, 0), (1, 1, 1), 4000, (2.0, 1.0, 1.0), 0.008, 77)
-    w.pos[20000:] = blob
+    w.pos[n_uniform:] = blob
     a = W.build_model(w)
     b = W.build_model(w)
     assert a.neighbor_capacity == 128

@@ -159,6 +159,10 @@ cudaError_t launch_cells_reorder(uint32_t n, const uint32_t* skeys, const uint32
 // Failure-detection self-test of the sort's bounded look-back wait (d_work: 96 words).
 cudaError_t launch_lookback_selftest(bool published, uint32_t spin_limit, uint32_t* d_work,
                                      uint32_t* err, cudaStream_t s);
+// True when the density pass runs three lanes per particle: the model is small enough that one
+// lane per particle would leave the GPU waiting on each thread's chain of loads (3 N threads
+// still fit one wave at 768 threads per SM). The density pass's launch shape does not apply then.
+bool planes_mode(uint32_t total);
 // Boundary volume + density + EOS epilogue; writes each particle's neighbour list.
 // Also writes rec[2i], rec[2i+1] = (x, y, z, p/rho^2), (v, m/max(rho, 1e-6)) for the force pass.
 cudaError_t launch_density(const StepLaunch& L, const float4* pos, const float4* vel, float4* rec,

@@ -20,6 +20,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
+
 #include "vfs_internal.h"
 
 namespace vfs {
@@ -615,13 +617,15 @@ __device__ __forceinline__ bool distinct_keys(const SceneParams& p, uint32_t cx,
 // Walks the candidates of the 27 neighbour buckets of cell (cx, cy, cz) in the reference's order
 // and calls visit(j, q) for each, with q = pos[j]; four positions are fetched per iteration and
 // batch_end() runs after each group of at most four (where a full list is drained).
+// Rows t_begin..t_end-1 only, when given (t = (dy + 1) + 3 (dz + 1)).
 template <typename Visit, typename BatchEnd>
 __device__ __forceinline__ void for_each_candidate(const SceneParams& p,
                                                    const uint32_t* __restrict__ scan,
                                                    const float4* __restrict__ pos,
                                                    const float4& xi, uint32_t cx, uint32_t cy,
                                                    uint32_t cz, Visit&& visit,
-                                                   BatchEnd&& batch_end) {
+                                                   BatchEnd&& batch_end, int t_begin = 0,
+                                                   int t_end = 9) {
     const bool interior = distinct_keys(p, cx, cy, cz);
     const float lim = interior ? kPruneLimit : 1e30f;
     const float fx = fmaf(-(float)(int)cx, p.h, xi.x) * p.inv_h;
@@ -629,7 +633,7 @@ __device__ __forceinline__ void for_each_candidate(const SceneParams& p,
     const float fz = fmaf(-(float)(int)cz, p.h, xi.z) * p.inv_h;
     const float dxl = face_dist2(0xFFFFFFFFu, fx), dxr = face_dist2(1u, fx);
 #pragma unroll 1
-    for (int t = 0; t < 9; t++) {
+    for (int t = t_begin; t < t_end; t++) {
         const uint32_t dy = (uint32_t)(t % 3) - 1u, dz = (uint32_t)(t / 3) - 1u;
         const float dyz = face_dist2(dy, fy) + face_dist2(dz, fz);
         if (dyz > lim) continue;
@@ -768,6 +772,115 @@ __global__ void __launch_bounds__(kNbrBlock, kMinBlocks)
     bnd[i] = make_float4(bgx, bgy, bgz, bd);
 }
 
+// W(|x_j - x_i|) / sigma with the density drain's explicitly rounded arithmetic.
+__device__ __forceinline__ float w_over_sigma(const float4& xi, const float4& xj, float inv_h) {
+    const float dx = __fsub_rn(xj.x, xi.x), dy = __fsub_rn(xj.y, xi.y), dz = __fsub_rn(xj.z, xi.z);
+    const float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+    const float r = r2 > 0.0f ? __fmul_rn(r2, rsqrtf(r2)) : 0.0f;
+    const float q = __fmul_rn(r, inv_h);
+    const float t = __fsub_rn(1.0f, q);
+    const float w_out = __fmul_rn(__fmul_rn(__fmul_rn(t, t), t), 2.0f);
+    const float q2 = __fmul_rn(q, q);
+    const float w_in = __fmaf_rn(6.0f, __fmul_rn(q2, q), __fmaf_rn(-6.0f, q2, 1.0f));
+    return q <= 1.0f ? (q > 0.5f ? w_out : w_in) : 0.0f;
+}
+
+// Small models, where three lanes per particle still fit one wave of the GPU and one lane per
+// particle would leave the SMs waiting on each thread's chain of candidate loads: the density pass
+// with the 27-cell walk split over three lanes of one warp, lane r walking the rows of the z-plane
+// dz = r - 1 (rows 3r..3r+2). Each lane sums its plane in visiting order and the particle's density
+// is (plane 0 + plane 1) + plane 2, whatever the list capacity. The neighbour list is the planes'
+// entries one after the other, the reference's visiting order as in k_density, so the force pass
+// is the same in both modes. A plane whose shared list fills mid-walk keeps summing but its
+// entries are not listed (the list length is then reported above the capacity, and the force
+// pass walks the candidates again).
+constexpr int kPlaneBlock = 96;  // 3 warps x 10 particles x 3 lanes (2 lanes of each warp idle)
+
+template <bool kBatch>
+__global__ void __launch_bounds__(kPlaneBlock)
+    k_density_planes(StepLaunch L, const float4* __restrict__ pos, const float4* __restrict__ vel,
+                     float4* __restrict__ rec, const uint32_t* __restrict__ scan,
+                     float4* __restrict__ aux, float4* __restrict__ bnd,
+                     uint32_t* __restrict__ nbr, uint32_t* __restrict__ nbr_count) {
+    __shared__ uint32_t s_j[kListCap * kPlaneBlock];
+    const uint32_t tid = threadIdx.x;
+    const uint32_t lane = tid & 31u, pw = lane / 3u, pl = lane - 3u * pw;
+    const uint32_t lead = lane - pl;
+    const uint32_t i = (blockIdx.x * (kPlaneBlock / 32u) + (tid >> 5)) * 10u + pw;
+    const bool active = lane < 30u && i < L.total;
+    float rho = 0.0f;
+    uint32_t n_pl = 0u;  // this plane's entries other than the particle itself
+    bool lost = false;   // entries summed mid-walk and not kept for the list
+    uint32_t s_end = tid;
+    float4 xi = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    if (active) {
+        const SceneParams& p = scene_params<kBatch>(L, i);
+        xi = __ldg(pos + i);
+        const uint32_t cx = cell_coord(xi.x, p.h), cy = cell_coord(xi.y, p.h),
+                       cz = cell_coord(xi.z, p.h);
+        const float s_inv_h = p.inv_h, h2 = p.h2;
+        auto sum_list = [&]() {
+#pragma unroll 2
+            for (uint32_t o = tid; o < s_end; o += kPlaneBlock) {
+                const uint32_t j = s_j[o];
+                rho = __fadd_rn(rho, w_over_sigma(xi, __ldg(pos + j), s_inv_h));
+                n_pl += j != i ? 1u : 0u;
+            }
+        };
+        for_each_candidate(p, scan, pos, xi, cx, cy, cz, [&](uint32_t j, const float4& xj) {
+            const float dx = xj.x - xi.x, dy = xj.y - xi.y, dz = xj.z - xi.z;
+            const float r2 = dx * dx + dy * dy + dz * dz;
+            s_j[s_end] = j;
+            s_end += r2 <= h2 ? kPlaneBlock : 0u;
+        }, [&]() {
+            if (s_end > tid + kDrainAt * kPlaneBlock) {
+                sum_list();
+                lost = true;
+                s_end = tid;
+            }
+        }, 3 * (int)pl, 3 * (int)pl + 3);
+        sum_list();
+    }
+    // The three planes of a particle meet in its lead lane (lanes 30 and 31 exchange nothing
+    // that is used).
+    const uint32_t n0 = __shfl_sync(0xffffffffu, n_pl, lead);
+    const uint32_t n1 = __shfl_sync(0xffffffffu, n_pl, lead + 1u);
+    const uint32_t n2 = __shfl_sync(0xffffffffu, n_pl, lead + 2u);
+    const float rho1 = __shfl_sync(0xffffffffu, rho, lead + 1u);
+    const float rho2 = __shfl_sync(0xffffffffu, rho, lead + 2u);
+    const uint32_t lost_bits = __ballot_sync(0xffffffffu, lost);
+    if (!active) return;
+    const SceneParams& p = scene_params<kBatch>(L, i);
+    const bool any_lost = ((lost_bits >> lead) & 7u) != 0u;
+    const uint32_t total = n0 + n1 + n2;
+    if (!any_lost) {
+        uint32_t k = (pl >= 1u ? n0 : 0u) + (pl >= 2u ? n1 : 0u);
+        for (uint32_t o = tid; o < s_end; o += kPlaneBlock) {
+            const uint32_t j = s_j[o];
+            if (j == i) continue;
+            if (k < p.nbr_cap) nbr[(size_t)k * L.total + i] = j;
+            k++;
+        }
+    }
+    if (pl != 0u) return;
+    const uint32_t cx = cell_coord(xi.x, p.h), cy = cell_coord(xi.y, p.h), cz = cell_coord(xi.z, p.h);
+    const uint32_t listed = any_lost ? max(total, p.nbr_cap + 1u) : total;
+    nbr_count[i] = nbr_word(listed, cx, cy, cz, distinct_keys(p, cx, cy, cz));
+    float bd, bgx, bgy, bgz;
+    boundary_terms(p, xi.x, xi.y, xi.z, bd, bgx, bgy, bgz);
+    rho = __fadd_rn(__fadd_rn(rho, rho1), rho2);
+    rho = p.mass * p.cubic * rho + p.rho0 * bd;
+    const float pr = p.stiffness * (powf(fmaxf(rho, p.rho0) / p.rho0, p.expoent) - 1.0f);
+    const float pd = rho > 0.0f ? pr / (rho * rho) : 0.0f;
+    const float mr = p.mass / fmaxf(rho, 1e-6f);
+    const float pb = rho > 0.0f ? pr / (p.rho0 * p.rho0) : 0.0f;
+    aux[i] = make_float4(pd, mr, rho, pb);
+    const float4 vi = __ldg(vel + i);
+    rec[2 * (size_t)i] = make_float4(xi.x, xi.y, xi.z, pd);
+    rec[2 * (size_t)i + 1] = make_float4(vi.x, vi.y, vi.z, mr);
+    bnd[i] = make_float4(bgx, bgy, bgz, bd);
+}
+
 struct ForceAcc {
     float Px, Py, Pz, Vx, Vy, Vz;
 };
@@ -828,6 +941,46 @@ __device__ __forceinline__ void force_term_rec(const SceneParams& p, const float
     force_term(p, xi, vi, pdi, r0, make_float2(r0.w, r1.w), r1, f);
 }
 
+// The rest of CalculatePressureAccel + CalculateViscousAccel + UpdatePositions for particle i
+// once its sums are complete: the constant factors, the boundary term, gravity, the wall, and
+// symplectic Euler.
+__device__ __forceinline__ void force_finish(const SceneParams& p, uint32_t i, const float4& xi,
+                                             const float4& vi, const float4& ai, ForceAcc f,
+                                             const float4* __restrict__ bnd,
+                                             float4* __restrict__ pos_out,
+                                             float4* __restrict__ vel_out,
+                                             float4* __restrict__ acc_out) {
+    const float pdi = ai.x;
+    // The factors force_term leaves out of the sums.
+    const float cp = p.mass * p.grad_over_h, cv = p.visc_scale * p.grad_over_h;
+    f.Px *= cp;
+    f.Py *= cp;
+    f.Pz *= cp;
+    const float4 bi = __ldg(bnd + i);
+    const float sb = (pdi + ai.w) * p.rho0;
+    f.Px += sb * bi.x;
+    f.Py += sb * bi.y;
+    f.Pz += sb * bi.z;
+
+    float ax = p.gx + -f.Px, ay = p.gy + -f.Py, az = p.gz + -f.Pz;
+    ax += cv * f.Vx;
+    ay += cv * f.Vy;
+    az += cv * f.Vz;
+    // WallAcceleration, wcsph_with_boundary_model.slang:336-347.
+    const float dx = fminf(xi.x - p.lo[0], 0.0f) - fminf(p.hi[0] - xi.x, 0.0f);
+    const float dyw = fminf(xi.y - p.lo[1], 0.0f) - fminf(p.hi[1] - xi.y, 0.0f);
+    const float dzw = fminf(xi.z - p.lo[2], 0.0f) - fminf(p.hi[2] - xi.z, 0.0f);
+    if (fabsf(dx) > 1e-9f || fabsf(dyw) > 1e-9f || fabsf(dzw) > 1e-9f) {
+        ax += -p.wall_k * dx;
+        ay += -p.wall_k * dyw;
+        az += -p.wall_k * dzw;
+    }
+    if (acc_out) acc_out[i] = make_float4(ax, ay, az, 0.0f);
+    const float nvx = vi.x + ax * p.dt, nvy = vi.y + ay * p.dt, nvz = vi.z + az * p.dt;
+    vel_out[i] = make_float4(nvx, nvy, nvz, 0.0f);
+    pos_out[i] = make_float4(xi.x + nvx * p.dt, xi.y + nvy * p.dt, xi.z + nvz * p.dt, xi.w);
+}
+
 // CalculatePressureAccel + CalculateViscousAccel + UpdatePositions
 // (wcsph_with_boundary_model.slang:205-360), fused: both sums are accumulated separately in the
 // reference's visiting order, then a = ((g - P) + V) + wall, v += a dt, x += v dt.
@@ -879,34 +1032,7 @@ __global__ void __launch_bounds__(kNbrBlock, kMinBlocks)
             if (r2 <= p.h2 && j != i) force_term_rec(p, xi, vi, pdi, rec, j, f);
         }, [&]() {});
     }
-    // The factors force_term leaves out of the sums.
-    const float cp = p.mass * p.grad_over_h, cv = p.visc_scale * p.grad_over_h;
-    f.Px *= cp;
-    f.Py *= cp;
-    f.Pz *= cp;
-    const float4 bi = __ldg(bnd + i);
-    const float sb = (pdi + ai.w) * p.rho0;
-    f.Px += sb * bi.x;
-    f.Py += sb * bi.y;
-    f.Pz += sb * bi.z;
-
-    float ax = p.gx + -f.Px, ay = p.gy + -f.Py, az = p.gz + -f.Pz;
-    ax += cv * f.Vx;
-    ay += cv * f.Vy;
-    az += cv * f.Vz;
-    // WallAcceleration, wcsph_with_boundary_model.slang:336-347.
-    const float dx = fminf(xi.x - p.lo[0], 0.0f) - fminf(p.hi[0] - xi.x, 0.0f);
-    const float dyw = fminf(xi.y - p.lo[1], 0.0f) - fminf(p.hi[1] - xi.y, 0.0f);
-    const float dzw = fminf(xi.z - p.lo[2], 0.0f) - fminf(p.hi[2] - xi.z, 0.0f);
-    if (fabsf(dx) > 1e-9f || fabsf(dyw) > 1e-9f || fabsf(dzw) > 1e-9f) {
-        ax += -p.wall_k * dx;
-        ay += -p.wall_k * dyw;
-        az += -p.wall_k * dzw;
-    }
-    if (acc_out) acc_out[i] = make_float4(ax, ay, az, 0.0f);
-    const float nvx = vi.x + ax * p.dt, nvy = vi.y + ay * p.dt, nvz = vi.z + az * p.dt;
-    vel_out[i] = make_float4(nvx, nvy, nvz, 0.0f);
-    pos_out[i] = make_float4(xi.x + nvx * p.dt, xi.y + nvy * p.dt, xi.z + nvz * p.dt, xi.w);
+    force_finish(p, i, xi, vi, ai, f, bnd, pos_out, vel_out, acc_out);
 }
 
 // ---------------------------------------------------------------- incremental sort
@@ -1321,10 +1447,32 @@ void force_shape(const StepLaunch& L, const float4* pos, const float4* vel, cons
                                                   pos_out, vel_out, acc_out);
 }
 
+bool planes_mode(uint32_t total) {
+    static std::atomic<int> sms[16];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 16) return false;
+    int n = sms[dev].load(std::memory_order_relaxed);
+    if (n == 0) {
+        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return false;
+        sms[dev].store(n, std::memory_order_relaxed);
+    }
+    return (uint64_t)total * 3u <= (uint64_t)n * 768u;
+}
+
 cudaError_t launch_density(const StepLaunch& L, const float4* pos, const float4* vel, float4* rec,
                            const uint32_t* cell_scan, float4* aux, float4* bnd, uint32_t* nbr,
                            uint32_t* nbr_count, const KernelConfig& kc, cudaStream_t s) {
     if (L.total == 0) return cudaSuccess;
+    if (planes_mode(L.total)) {
+        const uint32_t blocks = (L.total + 29u) / 30u;
+        if (L.n_scenes > 1)
+            k_density_planes<true><<<blocks, kPlaneBlock, 0, s>>>(L, pos, vel, rec, cell_scan, aux, bnd,
+                                                                  nbr, nbr_count);
+        else
+            k_density_planes<false><<<blocks, kPlaneBlock, 0, s>>>(L, pos, vel, rec, cell_scan, aux, bnd,
+                                                                   nbr, nbr_count);
+        return cudaGetLastError();
+    }
     switch (kc.nbr_shape) {
         case kNbr128x8: density_shape<128, 8>(L, pos, vel, rec, cell_scan, aux, bnd, nbr, nbr_count, s); break;
         case kNbr96x8: density_shape<96, 8>(L, pos, vel, rec, cell_scan, aux, bnd, nbr, nbr_count, s); break;

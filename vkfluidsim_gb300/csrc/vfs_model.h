@@ -59,8 +59,8 @@ struct Model {
     uint32_t* sk_buf = nullptr;   // merge output: sorted keys
     uint32_t* sp_buf = nullptr;   // merge output: sorted_indices
     uint32_t* pkeys = nullptr;    // previous substep's sorted keys (all ones in a fresh model)
-    uint32_t* moved = nullptr;
-    uint32_t* cell_guess = nullptr;  // per cell block: its bound in the sorted keys last substep    // 2 ceil(n/32) + 1 words: moved bitmask, moved count before each word
+    uint32_t* moved = nullptr;       // 2 ceil(n/32) + 1 words: moved bitmask, moved count before each word
+    uint32_t* cell_guess = nullptr;  // per cell block: its bound in the sorted keys last substep
     uint32_t* cell_scan = nullptr;
     float4* aux = nullptr;
     float4* rec = nullptr;  // 2 float4 per particle: the force pass's neighbour records
