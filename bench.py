@@ -57,7 +57,42 @@ def peaks():
     return 6800.0, "fallback"
 
 
+class _Nvml:
+    """Read-only NVML queries through ctypes (the driver's libnvidia-ml): SM clock, its maximum
+    and the active clock-event reasons of one device. None when the library is unavailable."""
+
+    # nvmlClocksEventReason* bits (nvml.h).
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown",
+               0x40: "hw_thermal_slowdown", 0x80: "hw_power_brake_slowdown"}
+
+    def __init__(self, index: int):
+        import ctypes as C
+
+        lib = C.CDLL("libnvidia-ml.so.1")
+        if lib.nvmlInit_v2() != 0:
+            raise OSError("nvmlInit failed")
+        self.C, self.lib = C, lib
+        self.h = C.c_void_p()
+        if lib.nvmlDeviceGetHandleByIndex_v2(C.c_uint(index), C.byref(self.h)) != 0:
+            raise OSError("no NVML device")
+        mx = C.c_uint()
+        lib.nvmlDeviceGetMaxClockInfo(self.h, C.c_int(1), C.byref(mx))  # NVML_CLOCK_SM
+        self.max_mhz = float(mx.value)
+        self.reasons_fn = getattr(lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            getattr(lib, "nvmlDeviceGetCurrentClocksThrottleReasons")
+
+    def sample(self):
+        C = self.C
+        clk, bits = C.c_uint(), C.c_ulonglong()
+        self.lib.nvmlDeviceGetClockInfo(self.h, C.c_int(1), C.byref(clk))
+        self.reasons_fn(self.h, C.byref(bits))
+        return float(clk.value), int(bits.value)
+
+
 class ClockSampler:
+    """SM clock and clock-event reasons during a timed region: NVML polled every ~2 ms from a
+    thread (the timed regions last milliseconds), else nvidia-smi at its 200 ms period."""
+
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
@@ -65,8 +100,31 @@ class ClockSampler:
     def __init__(self, index: int):
         self.index = index
         self.proc = None
+        self.nvml = None
+        self.samples = []
+        self.out = ""
+
+    def _poll(self):
+        while not self._stop.is_set():
+            try:
+                self.samples.append(self.nvml.sample())
+            except Exception:
+                return
+            self._stop.wait(0.002)
 
     def __enter__(self):
+        try:
+            self.nvml = _Nvml(self.index)
+        except Exception:
+            self.nvml = None
+        if self.nvml is not None:
+            import threading
+
+            self._stop = threading.Event()
+            self.samples.append(self.nvml.sample())
+            self._thread = threading.Thread(target=self._poll, daemon=True)
+            self._thread.start()
+            return self
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
@@ -77,6 +135,11 @@ class ClockSampler:
         return self
 
     def __exit__(self, *exc):
+        if self.nvml is not None:
+            self._stop.set()
+            self._thread.join(timeout=5)
+            self.samples.append(self.nvml.sample())
+            return
         if self.proc:
             self.proc.terminate()
             try:
@@ -84,10 +147,17 @@ class ClockSampler:
             except subprocess.TimeoutExpired:
                 self.proc.kill()
                 self.out = ""
-        else:
-            self.out = ""
 
     def summary(self):
+        if self.nvml is not None:
+            reasons = set()
+            for _, bits in self.samples:
+                for bit, name in _Nvml.REASONS.items():
+                    if bits & bit:
+                        reasons.add(name)
+            sm = [c for c, _ in self.samples]
+            return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": self.nvml.max_mhz,
+                    "reasons": sorted(reasons), "samples": len(sm), "source": "nvml"}
         sm, mx, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for line in (self.out or "").splitlines():
@@ -103,7 +173,7 @@ class ClockSampler:
                 if v.lower() == "active":
                     reasons.add(n)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
-                "reasons": sorted(reasons), "samples": len(sm)}
+                "reasons": sorted(reasons), "samples": len(sm), "source": "nvidia-smi"}
 
 
 def dist_env():
