@@ -206,6 +206,30 @@ def test_full_size_one_million_particles():
     compare_step(m, o, "obstacle_1m")
 
 
+@pytest.mark.parametrize("slots", [128, 1536])
+def test_full_size_stress_workload(slots):
+    """The stress workload at full size: 4,194,304 uniform particles in a 4 x 2 x 2 box plus a
+    419,430-particle Gaussian blob (sigma 0.1, ~900 neighbours per particle), h = 0.02, 128^3
+    container map. With 128 list slots the blob's lists overflow and the force pass walks the
+    candidates; with 1,536 (the measured configuration) every list fits."""
+    w = W.stress_4m()
+    assert w.n == 4_613_734
+    m = W.build_model(w)
+    m.set_neighbor_capacity(slots)
+    m.substeps(1)
+    keys, perm, offs = m.get_neighbor_arrays()
+    expected = np_keys(w.pos, w.sim.smooth_radius, w.n)
+    assert np.array_equal(np.sort(perm), np.arange(w.n, dtype=np.uint32))
+    assert np.array_equal(keys, expected[perm])
+    same = keys[1:] == keys[:-1]
+    assert np.all(np.diff(keys.astype(np.int64)) >= 0) and np.all(perm[1:][same] > perm[:-1][same])
+    s = m.copy_data_buffers()
+    o = oracle_for(w, m, pos=s["positions"], vel=s["velocities"], ids=m.get_ids())
+    compare_step(m, o, f"stress_4m_{slots}_slots")
+    g = m.copy_data_buffers()
+    assert g["densities"].max() > 10 * np.median(g["densities"])
+
+
 def test_volume_map_generation_matches_oracle():
     from oracle import binding as ob
 
