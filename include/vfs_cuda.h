@@ -207,7 +207,10 @@ int vfs_model_get_sort_config(const vfs_model* m, int32_t* digit_bits, int32_t* 
  * not depend on the capacity. The getter returns -1 for a NULL handle. */
 int vfs_model_set_neighbor_capacity(vfs_model* m, int32_t slots);
 int32_t vfs_model_get_neighbor_capacity(const vfs_model* m);
-/* Device pointers of the current state: float4 (x, y, z, id bits) and (vx, vy, vz, 0). */
+/* Device pointers of the current state: float4 (x, y, z, id bits) and (vx, vy, vz, 0). They stay
+ * valid for the model's lifetime. Positions and velocities written through them (ordered with
+ * the model's stream) are what the next substep steps: every substep recomputes each particle's
+ * key from its position, as UpdateSpatialHash does. */
 int vfs_model_device_state(vfs_model* m, void** pos4, void** vel4);
 
 /* ---- headless state export (the "record particle positions" roadmap item, README.md:30, in
