@@ -176,6 +176,29 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm), "source": "nvidia-smi"}
 
 
+def issue_roofline(inst_pp, phase_ms, n, device, clocks):
+    """The neighbour passes against the instruction-issue roofline: warp instructions per launch
+    (per particle from one ncu capture of this workload, smsp__inst_executed.sum, times N) over the
+    pass's event-timed duration, against one warp instruction per cycle on each of an SM's four
+    schedulers at the SM clock sampled during the timed region."""
+    import torch
+
+    sms = torch.cuda.get_device_properties(device).multi_processor_count
+    mhz = clocks.get("sm_mhz") or clocks.get("sm_max_mhz")
+    if not inst_pp or not mhz:
+        return None
+    peak = sms * 4 * mhz * 1e6
+    out = {"unit": "G warp-instructions/s", "peak": peak / 1e9, "sms": sms, "sm_mhz": mhz,
+           "source": "profiles/ncu_traffic.json warp_instructions_per_particle"}
+    for k in ("density", "force"):
+        if k in inst_pp and k in phase_ms:
+            inst = inst_pp[k] * n
+            achieved = inst / (phase_ms[k] * 1e-3)
+            out[k] = {"warp_instructions_per_launch": inst, "achieved": achieved / 1e9,
+                      "frac": achieved / peak}
+    return out
+
+
 def dist_env():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -625,12 +648,14 @@ def run_gpu(args):
     hbm, peak_kind = peaks()
     achieved = B_PHASE[dom] * n / (kernel_phases[dom] * 1e-3) / 1e9
     traffic = None
+    inst_pp = {}
     tfile = ROOT / "profiles" / "ncu_traffic.json"
     if tfile.exists():
         t = json.loads(tfile.read_text())
         per = t.get("bytes_per_particle", {}).get(dom)
         if per is not None:
             traffic = per * n
+        inst_pp = t.get("warp_instructions_per_particle", {})
 
     # ---- e2e through the C ABI with pinned host buffers.
     s0 = m.copy_data_buffers()
@@ -700,6 +725,7 @@ def run_gpu(args):
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm,
                          "unit": "GB/s", "frac": achieved / hbm, "peak_kind": peak_kind,
                          "algorithmic_bytes_per_launch": B_PHASE[dom] * n, "traffic": traffic},
+            "issue_roofline": issue_roofline(inst_pp, kernel_phases, n, local, clk.summary()),
             "step_roofline": {"bytes_per_particle_step": B_STEP,
                               "achieved_gbs": B_STEP * n / (ms_per_step * 1e-3) / 1e9,
                               "frac": B_STEP * n / (ms_per_step * 1e-3) / 1e9 / hbm},
