@@ -207,6 +207,20 @@ int vfs_model_get_sort_config(const vfs_model* m, int32_t* digit_bits, int32_t* 
  * not depend on the capacity. The getter returns -1 for a NULL handle. */
 int vfs_model_set_neighbor_capacity(vfs_model* m, int32_t slots);
 int32_t vfs_model_get_neighbor_capacity(const vfs_model* m);
+/* Candidate lists with a skin (Verlet lists). At a build, each particle lists the particles within
+ * h (1 + skin); until some particle of the scene has moved more than h skin / 2 since then
+ * (checked every substep from the current positions, so state set by any route is seen), a
+ * particle whose list was built from 125 distinct cell keys (its 5x5x5 block in one hash block)
+ * sums the list instead of walking the 27 buckets of CalculateDensities
+ * (wcsph_with_boundary_model.slang:153-197). The in-range sets are the reference's; the sums follow
+ * the visiting order of the last build. skin in [0, 0.5], default 0.1; 0 walks the buckets every
+ * substep. Models of up to ~39,000 particles (three lanes per particle in the density pass) and
+ * models whose lists do not fit in device memory (288 bytes per particle) have no lists; the
+ * getter then reports 0. */
+int vfs_model_set_skin(vfs_model* m, float skin);
+int vfs_model_get_skin(const vfs_model* m, float* skin);
+/* Number of list builds so far (synchronises the handle's stream). */
+int vfs_model_get_skin_builds(vfs_model* m, uint32_t* builds);
 /* Device pointers of the current state: float4 (x, y, z, id bits) and (vx, vy, vz, 0). They stay
  * valid for the model's lifetime. Positions and velocities written through them (ordered with
  * the model's stream) are what the next substep steps: every substep recomputes each particle's
@@ -325,6 +339,9 @@ int vfs_batch_synchronize(vfs_batch* b);
 int vfs_batch_profile_substeps(vfs_batch* b, int32_t count, float* phase_ms);
 int vfs_batch_set_sort_config(vfs_batch* b, int32_t digit_bits, int32_t tile_items);
 int vfs_batch_set_neighbor_capacity(vfs_batch* b, int32_t slots);
+int vfs_batch_set_skin(vfs_batch* b, float skin);
+int vfs_batch_get_skin(const vfs_batch* b, float* skin);
+int vfs_batch_get_skin_builds(vfs_batch* b, uint32_t scene, uint32_t* builds);
 int vfs_batch_export_state(vfs_batch* b, int32_t scene, const char* path_prefix);
 int vfs_batch_import_state(vfs_batch* b, int32_t scene, const char* path_prefix);
 /* As vfs_model_record; the snapshots are `<prefix>_s<scene>_f<frame>`. */

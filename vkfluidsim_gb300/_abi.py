@@ -158,6 +158,12 @@ SIGNATURES = {
     "vfs_batch_set_sort_config": (_I, [_P, C.c_int32, C.c_int32]),
     "vfs_batch_set_neighbor_capacity": (_I, [_P, C.c_int32]),
     "vfs_model_set_neighbor_capacity": (_I, [_P, C.c_int32]),
+    "vfs_model_set_skin": (_I, [_P, C.c_float]),
+    "vfs_model_get_skin": (_I, [_P, C.POINTER(C.c_float)]),
+    "vfs_batch_set_skin": (_I, [_P, C.c_float]),
+    "vfs_batch_get_skin": (_I, [_P, C.POINTER(C.c_float)]),
+    "vfs_model_get_skin_builds": (_I, [_P, C.POINTER(C.c_uint32)]),
+    "vfs_batch_get_skin_builds": (_I, [_P, C.c_uint32, C.POINTER(C.c_uint32)]),
     "vfs_model_get_neighbor_capacity": (C.c_int32, [_P]),
     "vfs_batch_autotune": (_I, [_P, C.c_int32, C.c_int32, C.POINTER(TuneConfig)]),
     "vfs_batch_set_tune_config": (_I, [_P, C.POINTER(TuneConfig)]),

@@ -257,6 +257,7 @@ static void derive_scene_params(const SceneHost& sh, SceneParams& p) {
     p.bnd_eighth = 0.125f * r;
     p.bnd_half = 0.5f * r;
     p.nbr_cap = kNbrCap;
+    p.skin_r2 = p.skin_half2 = p.skin_lim = 0.0f;  // set by refresh_params when lists are on
     p.n_objects = (uint32_t)sh.objects.size();
     p.objects = nullptr;
 }
@@ -279,6 +280,12 @@ int Model::refresh_params() {
     for (SceneHost& sh : scenes) {
         derive_scene_params(sh, sh.params);
         sh.params.nbr_cap = nbr_cap;
+        if (skin.list && skin_fraction > 0.0f) {
+            const float r = sh.params.h * (1.0f + skin_fraction), half = 0.5f * sh.params.h * skin_fraction;
+            sh.params.skin_r2 = r * r;
+            sh.params.skin_half2 = half * half;
+            sh.params.skin_lim = (1.0f + skin_fraction) * (1.0f + skin_fraction) * 1.002f;
+        }
         for (const ObjectStore& o : sh.objects) {
             DevObject d{};
             to_dev_object(o, d);
@@ -311,7 +318,7 @@ int Model::refresh_params() {
     launch.scene_of = d_scene_of;
     launch.one = scenes.empty() ? SceneParams{} : scenes[0].params;
     invalidate_graph();
-    return VFS_OK;
+    return invalidate_skin();  // h or the skin may have changed
 }
 
 void Model::invalidate_graph() {
@@ -354,6 +361,7 @@ int Model::enqueue_substep(cudaEvent_t* ev) {
     if (ev) VFS_CUDA_TRY(cudaEventRecord(ev[1], s));
     // Incremental stable sort: keys + the particles whose key changed (compacted into keys/vals),
     // a sort of those alone (count on the device), a merge with the rest.
+    const SkinLists sk = active_skin();
     VFS_CUDA_TRY(launch_keys_delta(launch, pos[c], pkeys, keys, vals, moved, sc, sort_scratch, s));
     if (ev) VFS_CUDA_TRY(cudaEventRecord(ev[2], s));
     uint32_t *mk = nullptr, *mi = nullptr;
@@ -363,14 +371,14 @@ int Model::enqueue_substep(cudaEvent_t* ev) {
     skeys = sk_buf;
     sperm = sp_buf;
     if (ev) VFS_CUDA_TRY(cudaEventRecord(ev[3], s));
-    VFS_CUDA_TRY(launch_cells_reorder(n, skeys, sperm, cell_scan, pos[c], vel[c], pos[o], vel[o],
+    VFS_CUDA_TRY(launch_cells_reorder(launch, n, skeys, sperm, cell_scan, pos[c], vel[c], pos[o], vel[o],
                                       scratch, (uint32_t)sort_scratch_words(sc), pkeys, cell_guess,
-                                      kc, s));
+                                      sk, kc, s));
     if (ev) VFS_CUDA_TRY(cudaEventRecord(ev[4], s));
-    VFS_CUDA_TRY(launch_density(launch, pos[o], vel[o], rec, cell_scan, aux, bnd, nbr, nbr_count, kc, s));
+    VFS_CUDA_TRY(launch_density(launch, pos[o], vel[o], rec, cell_scan, aux, bnd, nbr, nbr_count, sk, kc, s));
     if (ev) VFS_CUDA_TRY(cudaEventRecord(ev[5], s));
     VFS_CUDA_TRY(launch_force(launch, pos[o], vel[o], aux, rec, bnd, cell_scan, nbr, nbr_count, pos[c],
-                              vel[c], record ? acc : nullptr, kc, s));
+                              vel[c], record ? acc : nullptr, sk, kc, s));
     if (ev) VFS_CUDA_TRY(cudaEventRecord(ev[6], s));
     return VFS_OK;
 }
@@ -443,6 +451,15 @@ Model::~Model() {
     cudaFree(stage);
     cudaFree(nbr);
     cudaFree(nbr_count);
+    cudaFree(skin.list);
+    cudaFree(skin.count);
+    cudaFree(skin.x_build);
+    cudaFree(skin.b_of_id);
+    cudaFree(skin.cur);
+    cudaFree(skin.stale);
+    cudaFree(skin.ctl);
+    cudaFree(skin.queue);
+    cudaFree(skin.queue_n);
     cudaFree(scratch);
     cudaFree(err);
     if (err_host) cudaFreeHost(err_host);
@@ -531,7 +548,67 @@ int Model::init() {
         init[i] = make_float4(0.f, 0.f, 0.f, f);
     }
     VFS_CUDA_TRY(cudaMemcpy(pos[cur], init.data(), N * sizeof(float4), cudaMemcpyHostToDevice));
+    rc = alloc_skin();
+    if (rc) return rc;
     return refresh_params();
+}
+
+// Candidate lists with a skin, 288 bytes per particle. Three-lane (small) models do not use them,
+// and a model too large for them on this device runs without (every particle walks its buckets).
+int Model::alloc_skin() {
+    if (n == 0 || planes_mode(n)) return VFS_OK;
+    const size_t N = n;
+    SkinLists s{};
+    s.cap = kSkinCap;
+    if (cudaMalloc(&s.list, N * s.cap * sizeof(uint32_t)) != cudaSuccess ||
+        cudaMalloc(&s.count, N * sizeof(uint32_t)) != cudaSuccess ||
+        cudaMalloc(&s.x_build, N * sizeof(float4)) != cudaSuccess ||
+        cudaMalloc(&s.b_of_id, N * sizeof(uint32_t)) != cudaSuccess ||
+        cudaMalloc(&s.cur, N * sizeof(uint32_t)) != cudaSuccess ||
+        cudaMalloc(&s.stale, scenes.size() * sizeof(uint32_t)) != cudaSuccess ||
+        cudaMalloc(&s.ctl, scenes.size() * kSkinCtl * sizeof(uint32_t)) != cudaSuccess ||
+        cudaMalloc(&s.queue, N * sizeof(uint32_t)) != cudaSuccess ||
+        cudaMalloc(&s.queue_n, sizeof(uint32_t)) != cudaSuccess) {
+        cudaGetLastError();  // out of memory is not sticky: clear it and go on without lists
+        cudaFree(s.list);
+        cudaFree(s.count);
+        cudaFree(s.x_build);
+        cudaFree(s.b_of_id);
+        cudaFree(s.cur);
+        cudaFree(s.stale);
+        cudaFree(s.ctl);
+        cudaFree(s.queue);
+        cudaFree(s.queue_n);
+        return VFS_OK;
+    }
+    VFS_CUDA_TRY(cudaMemset(s.count, 0, N * sizeof(uint32_t)));
+    VFS_CUDA_TRY(cudaMemset(s.b_of_id, 0, N * sizeof(uint32_t)));  // any index below n until a build
+    VFS_CUDA_TRY(cudaMemset(s.stale, 0, scenes.size() * sizeof(uint32_t)));
+    VFS_CUDA_TRY(cudaMemset(s.queue_n, 0, sizeof(uint32_t)));
+    skin = s;
+    return invalidate_skin();
+}
+
+// Every list is rebuilt by the next substep: the build positions are set far away (3.4e38), so
+// every scene's displacement check fails, and the build policy starts over (builds counted from
+// zero, no wait).
+int Model::invalidate_skin() {
+    if (!skin.x_build) return VFS_OK;
+    VFS_CUDA_TRY(cudaMemsetAsync(skin.x_build, 0x7F, (size_t)n * sizeof(float4), stream));
+    std::vector<uint32_t> ctl(scenes.size() * kSkinCtl, 0u);
+    for (size_t s = 0; s < scenes.size(); s++) {
+        ctl[s * kSkinCtl + kCtlAllow] = 1u;
+        ctl[s * kSkinCtl + kCtlWait] = 1u;
+    }
+    VFS_CUDA_TRY(cudaMemcpyAsync(skin.ctl, ctl.data(), ctl.size() * sizeof(uint32_t),
+                                 cudaMemcpyHostToDevice, stream));
+    VFS_CUDA_TRY(cudaStreamSynchronize(stream));  // ctl is a local
+    return VFS_OK;
+}
+
+// The lists the passes use: none when switched off.
+SkinLists Model::active_skin() const {
+    return skin_fraction > 0.0f ? skin : SkinLists{};
 }
 
 int create_model(const std::vector<SceneHost>& scenes, Model** out) {
@@ -966,6 +1043,25 @@ int set_neighbor_capacity(Model& m, int32_t slots) {
     return m.refresh_params();
 }
 
+int set_skin(Model& m, float skin) {
+    if (!(skin >= 0.0f && skin <= 0.5f)) return fail(VFS_ERR_INVALID_ARGUMENT, "skin must be in [0, 0.5]");
+    m.skin_fraction = skin;
+    return m.refresh_params();  // new constants and graph; every list is rebuilt
+}
+
+float get_skin(const Model& m) { return m.skin.list ? m.skin_fraction : 0.0f; }
+
+int get_skin_builds(Model& m, uint32_t scene, uint32_t* builds) {
+    if (scene >= m.scenes.size()) return fail(VFS_ERR_INVALID_ARGUMENT, "scene index out of range");
+    *builds = 0;
+    if (!m.skin.ctl) return VFS_OK;
+    VFS_CUDA_TRY(cudaMemcpyAsync(m.err_host, m.skin.ctl + scene * kSkinCtl + kCtlBuilds, sizeof(uint32_t),
+                                 cudaMemcpyDeviceToHost, m.stream));
+    VFS_CUDA_TRY(cudaStreamSynchronize(m.stream));
+    *builds = *m.err_host;
+    return VFS_OK;
+}
+
 int set_sort_config(Model& m, int32_t digit_bits, int32_t tile_items) {
     if (digit_bits < 4 || digit_bits > 8) return fail(VFS_ERR_INVALID_ARGUMENT, "digit_bits must be in [4, 8]");
     if (tile_items != 8 && tile_items != 12 && tile_items != 16)
@@ -1239,6 +1335,23 @@ int vfs_model_set_neighbor_capacity(vfs_model* h, int32_t slots) {
     return vfs::set_neighbor_capacity(m, slots);
 }
 
+int vfs_model_set_skin(vfs_model* h, float skin) {
+    VFS_HANDLE(h);
+    return vfs::set_skin(m, skin);
+}
+
+int vfs_model_get_skin_builds(vfs_model* h, uint32_t* builds) {
+    VFS_HANDLE(h);
+    if (!builds) return vfs::fail(VFS_ERR_INVALID_ARGUMENT, "NULL output");
+    return vfs::get_skin_builds(m, 0, builds);
+}
+
+int vfs_model_get_skin(const vfs_model* h, float* skin) {
+    if (!h || !h->m || !skin) return vfs::fail(VFS_ERR_INVALID_ARGUMENT, "NULL handle or output");
+    *skin = vfs::get_skin(*h->m);
+    return VFS_OK;
+}
+
 int32_t vfs_model_get_neighbor_capacity(const vfs_model* h) {
     return (h && h->m) ? (int32_t)h->m->nbr_cap : -1;
 }
@@ -1400,6 +1513,23 @@ int vfs_batch_profile_substeps(vfs_batch* h, int32_t count, float* phase_ms) {
 int vfs_batch_set_neighbor_capacity(vfs_batch* h, int32_t slots) {
     VFS_HANDLE(h);
     return vfs::set_neighbor_capacity(m, slots);
+}
+
+int vfs_batch_set_skin(vfs_batch* h, float skin) {
+    VFS_HANDLE(h);
+    return vfs::set_skin(m, skin);
+}
+
+int vfs_batch_get_skin_builds(vfs_batch* h, uint32_t scene, uint32_t* builds) {
+    VFS_HANDLE(h);
+    if (!builds) return vfs::fail(VFS_ERR_INVALID_ARGUMENT, "NULL output");
+    return vfs::get_skin_builds(m, scene, builds);
+}
+
+int vfs_batch_get_skin(const vfs_batch* h, float* skin) {
+    if (!h || !h->m || !skin) return vfs::fail(VFS_ERR_INVALID_ARGUMENT, "NULL handle or output");
+    *skin = vfs::get_skin(*h->m);
+    return VFS_OK;
 }
 
 int vfs_batch_set_sort_config(vfs_batch* h, int32_t digit_bits, int32_t tile_items) {

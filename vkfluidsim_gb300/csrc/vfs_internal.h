@@ -75,6 +75,9 @@ struct SceneParams {
     float bnd_eighth;   // 0.125 h
     float bnd_half;     // 0.5 h
     uint32_t nbr_cap;   // neighbour-list slots per particle
+    float skin_r2;      // (h (1 + skin))^2: radius of the candidate lists (0: no lists)
+    float skin_half2;   // (h skin / 2)^2: displacement since the last build that forces a rebuild
+    float skin_lim;     // (1 + skin)^2 x 1.002: cell pruning limit of the list build, in h^2
     uint32_t n_objects;
     const DevObject* objects;  // device array of n_objects
 };
@@ -117,6 +120,40 @@ SortConfig make_sort_config(uint32_t n, int digit_bits, int tile_items, int key_
 
 // Launch shapes of the neighbour passes: threads per block x minimum resident blocks per SM.
 enum NbrShape : int { kNbr128x6 = 0, kNbr128x8 = 1, kNbr96x8 = 2, kNbr64x12 = 3, kNumNbrShapes = 4 };
+// Candidate lists with a skin (Verlet lists). A build, in a density pass, lists for every particle
+// the particles within h (1 + skin), in the reference's visiting order, under the particles' sorted
+// indices of that substep (their build indices), and keeps each particle's position. Until some
+// particle of the scene has moved more than h skin / 2 since then, every pair within h is in the
+// lists, and a particle whose list is usable sums it instead of walking the 27 buckets (same
+// in-range set, multiplicity one). The cell pass keeps `cur`, the current sorted index of every
+// build index, checks every displacement against `x_build` and marks the scene stale; in a stale
+// scene every particle walks, and the lists are rebuilt when the scene's build policy allows it.
+// The force pass runs the policy: lists that went stale within kSkinMinLife substeps of their build
+// double the substeps the scene waits before its next build (up to kSkinMaxWait), longer-lived ones
+// reset the wait to one, so a fast flow walks instead of rebuilding every substep.
+struct SkinLists {
+    uint32_t* list = nullptr;     // slot-major: list[k * total + b] = build index of candidate k of b
+    uint32_t* count = nullptr;    // per build index: list length, kSkinUsable when it can be summed
+    float4* x_build = nullptr;    // per build index: position at the last build
+    uint32_t* b_of_id = nullptr;  // per id: build index
+    uint32_t* cur = nullptr;      // per build index: current sorted index (written by the cell pass)
+    uint32_t* stale = nullptr;    // per scene: nonzero when some particle moved past h skin / 2
+    uint32_t* ctl = nullptr;      // per scene, kSkinCtl words: the build policy's state (kCtl*)
+    uint32_t* queue = nullptr;    // the particles the density pass walks this substep
+    uint32_t* queue_n = nullptr;  // their number (cleared by the force pass)
+    uint32_t cap = 0;             // slots per particle
+};
+constexpr uint32_t kSkinUsable = 1u << 31;
+constexpr uint32_t kSkinCtl = 8;       // words of policy state per scene:
+constexpr uint32_t kCtlAllow = 0;      //   a stale scene may rebuild this substep
+constexpr uint32_t kCtlAge = 1;        //   substeps since the last build
+constexpr uint32_t kCtlWait = 2;       //   substeps to wait after a build before the next
+constexpr uint32_t kCtlBuilds = 3;     //   builds so far
+constexpr uint32_t kCtlFresh = 4;      //   the lists of the last build have not gone stale yet
+constexpr uint32_t kSkinMinLife = 4;
+constexpr uint32_t kSkinMaxWait = 64;
+constexpr uint32_t kSkinCap = 64;
+
 // Launch shapes chosen per model (by default or by the autotuner); none changes any result.
 struct KernelConfig {
     int nbr_shape = kNbr96x8;     // density pass (and the adjoint's recomputed forward)
@@ -150,12 +187,14 @@ cudaError_t launch_sort(uint32_t n, const SortConfig& sc, const SortScratch& scr
 // zero[0, zero_words) (the sort scratch, for the next substep); copies skeys to pkeys_out (the next
 // substep's previous sorted keys) when pkeys_out is not NULL. guess (n / 128 + 2 words, any
 // contents) keeps each block's bound of the sorted keys as the next call's starting point; NULL
-// searches from scratch.
-cudaError_t launch_cells_reorder(uint32_t n, const uint32_t* skeys, const uint32_t* perm,
+// searches from scratch. With skin lists (sk.cur set), also sk.cur[sk.b_of_id[id]] = sorted index
+// for the ids in x.w, and flags every scene of L with a particle that moved more than h skin / 2
+// since its list build.
+cudaError_t launch_cells_reorder(const StepLaunch& L, uint32_t n, const uint32_t* skeys, const uint32_t* perm,
                                  uint32_t* cell_scan, const float4* pos_in, const float4* vel_in,
                                  float4* pos_out, float4* vel_out, uint32_t* zero,
                                  uint32_t zero_words, uint32_t* pkeys_out, uint32_t* guess,
-                                 const KernelConfig& kc, cudaStream_t s);
+                                 const SkinLists& sk, const KernelConfig& kc, cudaStream_t s);
 // Failure-detection self-test of the sort's bounded look-back wait (d_work: 96 words).
 cudaError_t launch_lookback_selftest(bool published, uint32_t spin_limit, uint32_t* d_work,
                                      uint32_t* err, cudaStream_t s);
@@ -165,14 +204,18 @@ cudaError_t launch_lookback_selftest(bool published, uint32_t spin_limit, uint32
 bool planes_mode(uint32_t total);
 // Boundary volume + density + EOS epilogue; writes each particle's neighbour list.
 // Also writes rec[2i], rec[2i+1] = (x, y, z, p/rho^2), (v, m/max(rho, 1e-6)) for the force pass.
+// With skin lists (sk.list set): sums the lists where they are usable and rebuilds flagged scenes.
 cudaError_t launch_density(const StepLaunch& L, const float4* pos, const float4* vel, float4* rec,
                            const uint32_t* cell_scan, float4* aux, float4* bnd, uint32_t* nbr,
-                           uint32_t* nbr_count, const KernelConfig& kc, cudaStream_t s);
-// Pressure + viscosity + wall + symplectic Euler over the density pass's neighbour lists.
+                           uint32_t* nbr_count, const SkinLists& sk, const KernelConfig& kc,
+                           cudaStream_t s);
+// Pressure + viscosity + wall + symplectic Euler over the density pass's neighbour lists; runs the
+// skin lists' build policy and clears their flags (when sk.stale is set).
 cudaError_t launch_force(const StepLaunch& L, const float4* pos, const float4* vel,
                          const float4* aux, const float4* rec, const float4* bnd, const uint32_t* cell_scan,
                          const uint32_t* nbr, const uint32_t* nbr_count, float4* pos_out,
-                         float4* vel_out, float4* acc_out, const KernelConfig& kc, cudaStream_t s);
+                         float4* vel_out, float4* acc_out, const SkinLists& sk,
+                         const KernelConfig& kc, cudaStream_t s);
 // Stable in-place sort of (keys, items) with caller-provided temporaries (n words each) and
 // sort scratch (sort_scratch_words(sc) + 1 words, zeroed here); items become the permutation.
 int enqueue_sort_pairs(uint32_t* items, uint32_t* keys, uint32_t n, const SortConfig& sc,

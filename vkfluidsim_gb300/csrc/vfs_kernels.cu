@@ -20,6 +20,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <algorithm>
 #include <atomic>
 
 #include "vfs_internal.h"
@@ -518,12 +519,14 @@ __device__ __forceinline__ uint32_t lower_bound_near(const uint32_t* __restrict_
 
 template <uint32_t kCellBlock>
 __global__ void __launch_bounds__(kCellBlock)
-    k_cells_reorder(uint32_t n, const uint32_t* __restrict__ skeys,
+    k_cells_reorder(StepLaunch L, uint32_t n, const uint32_t* __restrict__ skeys,
                     const uint32_t* __restrict__ perm, uint32_t* __restrict__ scan,
                     const float4* __restrict__ pos_in, const float4* __restrict__ vel_in,
                     float4* __restrict__ pos_out, float4* __restrict__ vel_out,
                     uint32_t* __restrict__ zero, uint32_t zero_words,
-                    uint32_t* __restrict__ pkeys_out, uint32_t* guess) {
+                    uint32_t* __restrict__ pkeys_out, uint32_t* guess,
+                    const uint32_t* __restrict__ b_of_id, uint32_t* __restrict__ cur,
+                    const float4* __restrict__ x_build, uint32_t* __restrict__ stale) {
     __shared__ uint32_t s_lo, s_hi;
     // The sort is done with its scratch (histograms, tile counters, look-back status): clear it
     // for the next substep here instead of in a separate memset.
@@ -547,8 +550,24 @@ __global__ void __launch_bounds__(kCellBlock)
     if (i < n) {
         uint32_t src = perm[i];
         if (src >= n) src = i;  // only after a reported sort failure
-        pos_out[i] = __ldg(pos_in + src);
+        const float4 x = __ldg(pos_in + src);
+        pos_out[i] = x;
         vel_out[i] = __ldg(vel_in + src);
+        if (cur) {
+            // Skin lists: where the particle's build index sits now, and its displacement since
+            // the build.
+            const uint32_t id = __float_as_uint(x.w);
+            const uint32_t bi = id < n ? __ldg(b_of_id + id) : n;
+            if (bi < n) {
+                cur[bi] = i;
+                const float4 b = __ldg(x_build + bi);
+                const float dx = x.x - b.x, dy = x.y - b.y, dz = x.z - b.z;
+                const uint32_t sc = L.n_scenes > 1 ? (uint32_t)__ldg(L.scene_of + i) : 0u;
+                const float lim = L.n_scenes > 1 ? L.scenes[sc].skin_half2 : L.one.skin_half2;
+                if (!(dx * dx + dy * dy + dz * dz <= lim) && ld_volatile(stale + sc) == 0u)
+                    atomicOr(stale + sc, 1u);
+            }
+        }
         if (pkeys_out) pkeys_out[i] = skeys[i];
     }
     __syncthreads();
@@ -687,79 +706,173 @@ __device__ __forceinline__ void for_each_candidate(const SceneParams& p,
     }
 }
 
-// CalculateBoundaryVolume + CalculateDensities + the per-particle part of PressureFromDensityEOS
-// (wcsph_with_boundary_model.slang:102-203). Besides the density products it writes particle i's
-// neighbour list: every in-range j except i itself, in visiting order, slot-major
-// (nbr[s * n + i], so a warp's lanes store and later load consecutive words), and its length in
-// nbr_count[i] (a length above nbr_cap means the list overflowed and was truncated). Positions
-// do not change before the force pass, so that list is exactly the force pass's neighbour set.
-template <bool kBatch, int kNbrBlock, int kMinBlocks>
-__global__ void __launch_bounds__(kNbrBlock, kMinBlocks)
-    k_density(StepLaunch L, const float4* __restrict__ pos, const float4* __restrict__ vel,
-              float4* __restrict__ rec, const uint32_t* __restrict__ scan,
-              float4* __restrict__ aux, float4* __restrict__ bnd, uint32_t* __restrict__ nbr,
-              uint32_t* __restrict__ nbr_count) {
-    __shared__ uint32_t s_j[kListCap * kNbrBlock];
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= L.total) return;
-    const SceneParams& p = scene_params<kBatch>(L, i);
-    const int tid = threadIdx.x;
-    const float4 xi = __ldg(pos + i);
-    const uint32_t cx = cell_coord(xi.x, p.h), cy = cell_coord(xi.y, p.h),
-                   cz = cell_coord(xi.z, p.h);
-    float rho = 0.0f;
-    uint32_t s_end = tid;  // shared-memory word one past the last kept candidate (stride kNbrBlock)
-    uint32_t listed = 0;
-    uint32_t* nbr_out = nbr + i;  // slot `listed` of particle i's list
-    // Scene constants used per candidate, in registers (a batched launch reads its scene's
-    // parameters from a device table).
-    const float s_inv_h = p.inv_h;
-    const uint32_t s_nbr_cap = p.nbr_cap;
-    auto drain = [&]() {
-#pragma unroll 2
-        for (uint32_t o = tid; o < s_end; o += kNbrBlock) {
-            const uint32_t j = s_j[o];
+// |x_j - x_i|^2 as the density pass's in-range tests evaluate it, explicitly rounded so that the
+// bucket walk and the skin lists decide every pair the same way.
+__device__ __forceinline__ float in_range2(const float4& xi, const float4& xj) {
+    const float dx = __fsub_rn(xj.x, xi.x), dy = __fsub_rn(xj.y, xi.y), dz = __fsub_rn(xj.z, xi.z);
+    return __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+}
+
+// Along one axis, how many of the cells c-2..c+2 share the 50-cell hash block of c-2 (5 when all
+// do). Five consecutive cells span at most two blocks: the short block before the 2^32 wrap of
+// cell + 25 is 46 cells long.
+__device__ __forceinline__ int first_block_cells(uint32_t c) {
+    const uint32_t b0 = (c - 2u + 25u) / 50u;
+    int n = 1;
+#pragma unroll
+    for (int t = 1; t < 5; t++) n += (c - 2u + (uint32_t)t + 25u) / 50u == b0 ? 1 : 0;
+    return n;
+}
+
+// True when the 125 cells around (cx, cy, cz) provably have distinct keys, so that a walk of their
+// buckets meets every particle once. The block splits into at most eight boxes, one per hash
+// block it touches; inside a box the hashes are hmin + lx + 50 ly + 2500 lz, so its keys lie in the
+// circular interval [hmin mod n, hmin mod n + span] (span <= 10204) and are distinct when
+// n > 10204 and the box's hashes do not wrap 2^32. Boxes whose intervals are disjoint modulo n
+// share no key.
+__device__ __forceinline__ bool skin_keys_distinct(const SceneParams& p, uint32_t cx, uint32_t cy,
+                                                   uint32_t cz) {
+    if (p.n <= 10204u) return false;
+    const int fx = first_block_cells(cx), fy = first_block_cells(cy), fz = first_block_cells(cz);
+    uint32_t k[8], span[8];
+    int boxes = 0;
+#pragma unroll 1
+    for (int bz = 0; bz < (fz < 5 ? 2 : 1); bz++)
+#pragma unroll 1
+        for (int by = 0; by < (fy < 5 ? 2 : 1); by++)
+#pragma unroll 1
+            for (int bx = 0; bx < (fx < 5 ? 2 : 1); bx++) {
+                const uint32_t x0 = bx ? fx : 0, x1 = bx ? 4 : fx - 1;
+                const uint32_t y0 = by ? fy : 0, y1 = by ? 4 : fy - 1;
+                const uint32_t z0 = bz ? fz : 0, z1 = bz ? 4 : fz - 1;
+                const uint32_t lo = hash_cell(cx - 2u + x0, cy - 2u + y0, cz - 2u + z0);
+                const uint32_t hi = hash_cell(cx - 2u + x1, cy - 2u + y1, cz - 2u + z1);
+                if (hi < lo) return false;
+                k[boxes] = key_mod(lo, p.mod_magic, p.n);
+                span[boxes] = hi - lo;
+                boxes++;
+            }
+#pragma unroll 1
+    for (int a = 1; a < boxes; a++)
+#pragma unroll 1
+        for (int b = 0; b < a; b++) {
+            const uint32_t ab = k[b] >= k[a] ? k[b] - k[a] : k[b] + (p.n - k[a]);  // (k_b - k_a) mod n
+            const uint32_t ba = k[a] >= k[b] ? k[a] - k[b] : k[a] + (p.n - k[b]);
+            if (ab <= span[a] || ba <= span[b]) return false;
+        }
+    return true;
+}
+
+// Squared distance, in h^2, from a particle at fraction f of its cell to the slab of cells at
+// offset d in [-2, 2] along one axis.
+__device__ __forceinline__ float slab_dist2(int d, float f) {
+    const float l = d < 0 ? f + (float)(-d - 1) : (d > 0 ? (float)d - f : 0.0f);
+    const float c = fmaxf(l, 0.0f);
+    return c * c;
+}
+
+// The list build of a particle whose 125 keys are distinct: the sorted indices (this substep's,
+// which become the build indices) of every particle within h (1 + skin), stored slot-major from
+// `out`, from the 5x5x5 cells around (cx, cy, cz) whose boxes lie within that radius: planes dz and
+// rows dy in increasing order, the cells of a row in increasing x as runs of consecutive keys (a
+// run ends at a hash-block boundary; a run whose keys pass n - 1 continues at key 0) - the
+// reference's visiting order restricted to its 27 cells. Returns the number found (ids past
+// `cap` are not stored).
+__device__ __forceinline__ uint32_t skin_walk(const SceneParams& p, const uint32_t* __restrict__ scan,
+                                              const float4* __restrict__ pos, const float4& xi,
+                                              uint32_t cx, uint32_t cy, uint32_t cz,
+                                              uint32_t* __restrict__ out, size_t stride,
+                                              uint32_t cap) {
+    const float fx = fmaf(-(float)(int)cx, p.h, xi.x) * p.inv_h;
+    const float fy = fmaf(-(float)(int)cy, p.h, xi.y) * p.inv_h;
+    const float fz = fmaf(-(float)(int)cz, p.h, xi.z) * p.inv_h;
+    const float lim = p.skin_lim;
+    const uint32_t* sc = scan + p.off;
+    uint32_t c = 0;
+    auto walk = [&](uint32_t b, uint32_t e) {
+#pragma unroll 1
+        for (uint32_t j = b; j < e; j++) {
             const float4 xj = __ldg(pos + j);
-            // Explicit rounding: the same sums for every launch shape.
-            const float dx = __fsub_rn(xj.x, xi.x), dy = __fsub_rn(xj.y, xi.y), dz = __fsub_rn(xj.z, xi.z);
-            const float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
-            const float r = r2 > 0.0f ? __fmul_rn(r2, rsqrtf(r2)) : 0.0f;
-            // W(q) / sigma, branch-free: 2 (1-q)^3 above q = 1/2, 6q^3 - 6q^2 + 1 below, 0 past 1.
-            const float q = __fmul_rn(r, s_inv_h);
-            const float t = __fsub_rn(1.0f, q);
-            const float w_out = __fmul_rn(__fmul_rn(__fmul_rn(t, t), t), 2.0f);
-            const float q2 = __fmul_rn(q, q);
-            const float w_in = __fmaf_rn(6.0f, __fmul_rn(q2, q), __fmaf_rn(-6.0f, q2, 1.0f));
-            const float w = q <= 1.0f ? (q > 0.5f ? w_out : w_in) : 0.0f;
-            rho = __fadd_rn(rho, w);
-            if (j != i) {
-                if (listed < s_nbr_cap) {
-                    *nbr_out = j;
-                    nbr_out += L.total;
-                }
-                listed++;
+            if (in_range2(xi, xj) <= p.skin_r2) {
+                if (c < cap) out[c * stride] = j;
+                c++;
             }
         }
-        s_end = tid;
     };
-    // Branch-free append: every candidate is stored at the list's end and kept only when in
-    // range (the next one overwrites it otherwise). Lists are drained above kDrainAt, so the slot
-    // index stays below kListCap.
-    const bool distinct = distinct_keys(p, cx, cy, cz);
-    const float h2 = p.h2;
-    for_each_candidate(p, scan, pos, xi, cx, cy, cz, [&](uint32_t j, const float4& xj) {
-        const float dx = xj.x - xi.x, dy = xj.y - xi.y, dz = xj.z - xi.z;
-        const float r2 = dx * dx + dy * dy + dz * dz;
-        s_j[s_end] = j;
-        s_end += r2 <= h2 ? kNbrBlock : 0u;
-    }, [&]() {
-        if (s_end > tid + kDrainAt * kNbrBlock) drain();
-    });
-    drain();
-    nbr_count[i] = nbr_word(listed, cx, cy, cz, distinct);
+#pragma unroll 1
+    for (int dz = -2; dz <= 2; dz++) {
+        const float sz = slab_dist2(dz, fz);
+        if (sz > lim) continue;
+#pragma unroll 1
+        for (int dy = -2; dy <= 2; dy++) {
+            const float syz = sz + slab_dist2(dy, fy);
+            if (syz > lim) continue;
+            int xl = -2, xr = 2;  // cell 0 is always within the limit here
+            while (xl < 0 && syz + slab_dist2(xl, fx) > lim) xl++;
+            while (xr > 0 && syz + slab_dist2(xr, fx) > lim) xr--;
+            const uint32_t ry = cy + (uint32_t)dy, rz = cz + (uint32_t)dz;
+#pragma unroll 1
+            for (int x = xl; x <= xr;) {
+                const uint32_t bx = (cx + (uint32_t)x + 25u) / 50u;
+                int xe = x;
+                while (xe < xr && (cx + (uint32_t)(xe + 1) + 25u) / 50u == bx) xe++;
+                const uint32_t k0 = key_mod(hash_cell(cx + (uint32_t)x, ry, rz), p.mod_magic, p.n);
+                const uint32_t len = (uint32_t)(xe - x + 1);
+                if (k0 + len <= p.n) {
+                    walk(__ldg(sc + k0), __ldg(sc + k0 + len));
+                } else {
+                    walk(__ldg(sc + k0), __ldg(sc + p.n));
+                    walk(__ldg(sc), __ldg(sc + (k0 + len - p.n)));
+                }
+                x = xe + 1;
+            }
+        }
+    }
+    return c;
+}
+
+// Particle i's density sum and neighbour list as the density pass builds them: add() takes one
+// in-range neighbour, adds its W / sigma (explicitly rounded, so every launch shape and both the
+// bucket walk and the skin lists give the same sums) and appends j to the list unless j == i.
+struct DensitySum {
+    float rho = 0.0f;
+    uint32_t listed = 0;
+    uint32_t* out;  // slot `listed` of i's list (slot-major, stride = particles)
+    __device__ __forceinline__ void add(uint32_t i, const float4& xi, uint32_t j, const float4& xj,
+                                        float inv_h, uint32_t cap, uint32_t stride) {
+        const float dx = __fsub_rn(xj.x, xi.x), dy = __fsub_rn(xj.y, xi.y), dz = __fsub_rn(xj.z, xi.z);
+        const float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+        const float r = r2 > 0.0f ? __fmul_rn(r2, rsqrtf(r2)) : 0.0f;
+        // W(q) / sigma, branch-free: 2 (1-q)^3 above q = 1/2, 6q^3 - 6q^2 + 1 below, 0 past 1.
+        const float q = __fmul_rn(r, inv_h);
+        const float t = __fsub_rn(1.0f, q);
+        const float w_out = __fmul_rn(__fmul_rn(__fmul_rn(t, t), t), 2.0f);
+        const float q2 = __fmul_rn(q, q);
+        const float w_in = __fmaf_rn(6.0f, __fmul_rn(q2, q), __fmaf_rn(-6.0f, q2, 1.0f));
+        const float w = q <= 1.0f ? (q > 0.5f ? w_out : w_in) : 0.0f;
+        rho = __fadd_rn(rho, w);
+        if (j != i) {
+            if (listed < cap) {
+                *out = j;
+                out += stride;
+            }
+            listed++;
+        }
+    }
+};
+
+// The per-particle end of the density pass: list length word, boundary terms, density, Tait EOS
+// and the force pass's record of i.
+__device__ __forceinline__ void density_finish(const SceneParams& p, uint32_t i, const float4& xi,
+                                               const float4* __restrict__ vel, uint32_t cx,
+                                               uint32_t cy, uint32_t cz, bool distinct,
+                                               const DensitySum& d, float4* __restrict__ rec,
+                                               float4* __restrict__ aux, float4* __restrict__ bnd,
+                                               uint32_t* __restrict__ nbr_count) {
+    nbr_count[i] = nbr_word(d.listed, cx, cy, cz, distinct);
     float bd, bgx, bgy, bgz;
     boundary_terms(p, xi.x, xi.y, xi.z, bd, bgx, bgy, bgz);
-    rho = p.mass * p.cubic * rho + p.rho0 * bd;  // the factor the drain leaves out of the sum
+    const float rho = p.mass * p.cubic * d.rho + p.rho0 * bd;  // the factor the sum leaves out
     const float pr = p.stiffness * (powf(fmaxf(rho, p.rho0) / p.rho0, p.expoent) - 1.0f);
     const float pd = rho > 0.0f ? pr / (rho * rho) : 0.0f;
     const float mr = p.mass / fmaxf(rho, 1e-6f);
@@ -770,6 +883,148 @@ __global__ void __launch_bounds__(kNbrBlock, kMinBlocks)
     rec[2 * (size_t)i] = make_float4(xi.x, xi.y, xi.z, pd);
     rec[2 * (size_t)i + 1] = make_float4(vi.x, vi.y, vi.z, mr);
     bnd[i] = make_float4(bgx, bgy, bgz, bd);
+}
+
+// CalculateBoundaryVolume + CalculateDensities + the per-particle part of PressureFromDensityEOS
+// (wcsph_with_boundary_model.slang:102-203), by the bucket walk. Besides the density products it
+// writes particle i's neighbour list: every in-range j except i itself, in visiting order,
+// slot-major (nbr[s * n + i], so a warp's lanes store and later load consecutive words), and its
+// length in nbr_count[i] (a length above nbr_cap means the list overflowed and was truncated).
+// Positions do not change before the force pass, so that list is exactly the force pass's
+// neighbour set. Without a queue every particle is walked; with one (skin lists), the particles
+// k_density_list left in it, by a grid-stride loop. In a stale scene whose build policy allows
+// it, every particle also builds its skin list.
+template <bool kBatch, int kNbrBlock, int kMinBlocks>
+__global__ void __launch_bounds__(kNbrBlock, kMinBlocks)
+    k_density(StepLaunch L, const float4* __restrict__ pos, const float4* __restrict__ vel,
+              float4* __restrict__ rec, const uint32_t* __restrict__ scan,
+              float4* __restrict__ aux, float4* __restrict__ bnd, uint32_t* __restrict__ nbr,
+              uint32_t* __restrict__ nbr_count, SkinLists sk) {
+    __shared__ uint32_t s_j[kListCap * kNbrBlock];
+    const int tid = threadIdx.x;
+    const uint32_t n_work = sk.queue ? *sk.queue_n : L.total;
+    for (uint32_t t = blockIdx.x * kNbrBlock + tid; t < n_work; t += gridDim.x * kNbrBlock) {
+        const uint32_t i = sk.queue ? sk.queue[t] : t;
+        const SceneParams& p = scene_params<kBatch>(L, i);
+        const float4 xi = __ldg(pos + i);
+        bool rebuild = false;
+        if (sk.list) {
+            const uint32_t sc = kBatch ? (uint32_t)__ldg(L.scene_of + i) : 0u;
+            rebuild = sk.stale[sc] != 0u && sk.ctl[sc * kSkinCtl + kCtlAllow] != 0u;
+        }
+        const uint32_t cx = cell_coord(xi.x, p.h), cy = cell_coord(xi.y, p.h),
+                       cz = cell_coord(xi.z, p.h);
+        DensitySum d;
+        d.out = nbr + i;
+        uint32_t s_end = tid;  // shared-memory word one past the last kept candidate (stride kNbrBlock)
+        // Scene constants used per candidate, in registers (a batched launch reads its scene's
+        // parameters from a device table).
+        const float s_inv_h = p.inv_h;
+        const uint32_t s_nbr_cap = p.nbr_cap;
+        auto drain = [&]() {
+#pragma unroll 2
+            for (uint32_t o = tid; o < s_end; o += kNbrBlock) {
+                const uint32_t j = s_j[o];
+                d.add(i, xi, j, __ldg(pos + j), s_inv_h, s_nbr_cap, L.total);
+            }
+            s_end = tid;
+        };
+        const bool distinct = distinct_keys(p, cx, cy, cz);
+        const float h2 = p.h2;
+        // Branch-free append: every candidate is stored at the list's end and kept only when in
+        // range (the next one overwrites it otherwise). Lists are drained above kDrainAt, so the
+        // slot index stays below kListCap.
+        for_each_candidate(p, scan, pos, xi, cx, cy, cz, [&](uint32_t j, const float4& xj) {
+            s_j[s_end] = j;
+            s_end += in_range2(xi, xj) <= h2 ? kNbrBlock : 0u;
+        }, [&]() {
+            if (s_end > tid + kDrainAt * kNbrBlock) drain();
+        });
+        drain();
+        if (rebuild) {
+            // This substep's sorted index becomes the particle's build index.
+            sk.x_build[i] = xi;
+            sk.b_of_id[__float_as_uint(xi.w)] = i;
+            const bool usable = skin_keys_distinct(p, cx, cy, cz);
+            const uint32_t c = usable ? skin_walk(p, scan, pos, xi, cx, cy, cz, sk.list + i,
+                                                  L.total, sk.cap)
+                                      : 0u;
+            sk.count[i] = min(c, sk.cap) | (usable && c <= sk.cap ? kSkinUsable : 0u);
+        }
+        density_finish(p, i, xi, vel, cx, cy, cz, distinct, d, rec, aux, bnd, nbr_count);
+    }
+}
+
+// The density pass over the skin lists: a particle of a scene that is not stale, whose list is
+// usable, sums the in-range members of its list (the same in-range set as the walk: every
+// pair within h was within h (1 + skin) at the build; each once: the particle has moved less than
+// h / 4 since the build, so its 27 cells lie in the build's 5x5x5 block, whose keys were
+// distinct), in the list's order. Every other particle is appended to the queue for k_density.
+// No shared memory: the pass is bound by its chains of dependent loads, so it runs at the
+// occupancy its registers allow.
+constexpr int kListBlock = 128;
+
+template <bool kBatch>
+__global__ void __launch_bounds__(kListBlock, 8)
+    k_density_list(StepLaunch L, const float4* __restrict__ pos, const float4* __restrict__ vel,
+                   float4* __restrict__ rec, float4* __restrict__ aux, float4* __restrict__ bnd,
+                   uint32_t* __restrict__ nbr, uint32_t* __restrict__ nbr_count, SkinLists sk) {
+    const uint32_t i = blockIdx.x * kListBlock + threadIdx.x;
+    bool walk = false;
+    if (i < L.total) {
+        const SceneParams& p = scene_params<kBatch>(L, i);
+        const float4 xi = __ldg(pos + i);
+        uint32_t c = 0u, row = 0u;
+        walk = sk.stale[kBatch ? (uint32_t)__ldg(L.scene_of + i) : 0u] != 0u;
+        if (!walk) {
+            row = __ldg(sk.b_of_id + __float_as_uint(xi.w));
+            c = __ldg(sk.count + row);
+            walk = (c & kSkinUsable) == 0u;
+        }
+        if (!walk) {
+            const uint32_t cx = cell_coord(xi.x, p.h), cy = cell_coord(xi.y, p.h),
+                           cz = cell_coord(xi.z, p.h);
+            const uint32_t n_list = c & ~kSkinUsable;
+            const float h2 = p.h2, s_inv_h = p.inv_h;
+            const uint32_t s_nbr_cap = p.nbr_cap;
+            DensitySum d;
+            d.out = nbr + i;
+            const size_t stride = L.total;
+            const uint32_t* q = sk.list + row;
+            uint32_t k = 0;
+#pragma unroll 1
+            for (; k + 4u <= n_list; k += 4u, q += 4 * stride) {
+                uint32_t j[4];
+                float4 xj[4];
+#pragma unroll
+                for (int u = 0; u < 4; u++) j[u] = __ldg(q + u * stride);
+#pragma unroll
+                for (int u = 0; u < 4; u++) j[u] = __ldg(sk.cur + j[u]);
+#pragma unroll
+                for (int u = 0; u < 4; u++) xj[u] = __ldg(pos + j[u]);
+#pragma unroll
+                for (int u = 0; u < 4; u++)
+                    if (in_range2(xi, xj[u]) <= h2) d.add(i, xi, j[u], xj[u], s_inv_h, s_nbr_cap, L.total);
+            }
+#pragma unroll 1
+            for (; k < n_list; k++, q += stride) {
+                const uint32_t j = __ldg(sk.cur + __ldg(q));
+                const float4 xj = __ldg(pos + j);
+                if (in_range2(xi, xj) <= h2) d.add(i, xi, j, xj, s_inv_h, s_nbr_cap, L.total);
+            }
+            density_finish(p, i, xi, vel, cx, cy, cz, distinct_keys(p, cx, cy, cz), d, rec, aux,
+                           bnd, nbr_count);
+        }
+    }
+    // The walkers join the queue, a warp at a time.
+    const uint32_t m = __ballot_sync(0xffffffffu, walk);
+    if (m) {
+        const int lane = threadIdx.x & 31, lead = __ffs(m) - 1;
+        uint32_t base = 0u;
+        if (lane == lead) base = atomicAdd(sk.queue_n, (uint32_t)__popc(m));
+        base = __shfl_sync(0xffffffffu, base, lead);
+        if (walk) sk.queue[base + __popc(m & ((1u << lane) - 1u))] = i;
+    }
 }
 
 // W(|x_j - x_i|) / sigma with the density drain's explicitly rounded arithmetic.
@@ -991,8 +1246,38 @@ __global__ void __launch_bounds__(kNbrBlock, kMinBlocks)
             const float4* __restrict__ bnd,
             const uint32_t* __restrict__ scan, const uint32_t* __restrict__ nbr,
             const uint32_t* __restrict__ nbr_count, float4* __restrict__ pos_out,
-            float4* __restrict__ vel_out, float4* __restrict__ acc_out) {
+            float4* __restrict__ vel_out, float4* __restrict__ acc_out,
+            uint32_t* __restrict__ skin_stale, uint32_t* __restrict__ skin_ctl,
+            uint32_t* __restrict__ skin_queue_n) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    // The density pass is done with the skin lists' flags: run each scene's build policy and clear
+    // the flags for the next substep.
+    if (skin_stale && blockIdx.x == 0) {
+        for (uint32_t sc = threadIdx.x; sc < L.n_scenes; sc += blockDim.x) {
+            uint32_t* c = skin_ctl + sc * kSkinCtl;
+            uint32_t age = c[kCtlAge], wait = c[kCtlWait];
+            if (skin_stale[sc]) {
+                if (c[kCtlFresh]) {  // how long the last build's lists lasted
+                    wait = age < kSkinMinLife ? min(2u * wait, kSkinMaxWait) : 1u;
+                    c[kCtlFresh] = 0u;
+                }
+                if (c[kCtlAllow]) {  // the density pass rebuilt
+                    c[kCtlBuilds]++;
+                    c[kCtlFresh] = 1u;
+                    age = 0u;
+                } else {
+                    age++;
+                }
+                skin_stale[sc] = 0u;
+            } else {
+                age++;
+            }
+            c[kCtlAge] = age;
+            c[kCtlWait] = wait;
+            c[kCtlAllow] = age >= wait ? 1u : 0u;
+        }
+        if (threadIdx.x == 0) *skin_queue_n = 0u;
+    }
     if (i >= L.total) return;
     const SceneParams& p = scene_params<kBatch>(L, i);
     const float4 xi = __ldg(pos + i);
@@ -1411,68 +1696,86 @@ cudaError_t launch_sort(uint32_t n, const SortConfig& sc, const SortScratch& scr
     return cudaSuccess;
 }
 
-cudaError_t launch_cells_reorder(uint32_t n, const uint32_t* skeys, const uint32_t* perm,
+cudaError_t launch_cells_reorder(const StepLaunch& L, uint32_t n, const uint32_t* skeys, const uint32_t* perm,
                                  uint32_t* cell_scan, const float4* pos_in, const float4* vel_in,
                                  float4* pos_out, float4* vel_out, uint32_t* zero,
                                  uint32_t zero_words, uint32_t* pkeys_out, uint32_t* guess,
-                                 const KernelConfig& kc, cudaStream_t s) {
+                                 const SkinLists& sk, const KernelConfig& kc, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
     switch (kc.cell_block) {
         case 128:
-            k_cells_reorder<128><<<(n + 128u) / 128u, 128, 0, s>>>(n, skeys, perm, cell_scan, pos_in,
-                                                                 vel_in, pos_out, vel_out, zero, zero_words, pkeys_out, guess);
+            k_cells_reorder<128><<<(n + 128u) / 128u, 128, 0, s>>>(L, n, skeys, perm, cell_scan, pos_in,
+                                                                 vel_in, pos_out, vel_out, zero, zero_words, pkeys_out, guess, sk.b_of_id, sk.cur, sk.x_build, sk.stale);
             break;
         case 512:
-            k_cells_reorder<512><<<(n + 512u) / 512u, 512, 0, s>>>(n, skeys, perm, cell_scan, pos_in,
-                                                                 vel_in, pos_out, vel_out, zero, zero_words, pkeys_out, guess);
+            k_cells_reorder<512><<<(n + 512u) / 512u, 512, 0, s>>>(L, n, skeys, perm, cell_scan, pos_in,
+                                                                 vel_in, pos_out, vel_out, zero, zero_words, pkeys_out, guess, sk.b_of_id, sk.cur, sk.x_build, sk.stale);
             break;
         default:
-            k_cells_reorder<256><<<(n + 256u) / 256u, 256, 0, s>>>(n, skeys, perm, cell_scan, pos_in,
-                                                                 vel_in, pos_out, vel_out, zero, zero_words, pkeys_out, guess);
+            k_cells_reorder<256><<<(n + 256u) / 256u, 256, 0, s>>>(L, n, skeys, perm, cell_scan, pos_in,
+                                                                 vel_in, pos_out, vel_out, zero, zero_words, pkeys_out, guess, sk.b_of_id, sk.cur, sk.x_build, sk.stale);
     }
     return cudaGetLastError();
+}
+
+// SMs of the current device (0 if unknown), cached per device.
+static int sm_count() {
+    static std::atomic<int> sms[16];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 16) return 0;
+    int n = sms[dev].load(std::memory_order_relaxed);
+    if (n == 0) {
+        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
+        sms[dev].store(n, std::memory_order_relaxed);
+    }
+    return n;
 }
 
 template <int B, int M>
 void density_shape(const StepLaunch& L, const float4* pos, const float4* vel, float4* rec,
                    const uint32_t* cell_scan, float4* aux, float4* bnd, uint32_t* nbr,
-                   uint32_t* nbr_count, cudaStream_t s) {
-    const uint32_t blocks = (L.total + B - 1) / B;
+                   uint32_t* nbr_count, const SkinLists& sk, cudaStream_t s) {
+    uint32_t blocks = (L.total + B - 1) / B;
+    if (sk.list) {
+        // Skin lists: the list pass first; the walk pass then takes the queue it leaves, one wave
+        // of blocks looping over it.
+        const uint32_t lb = (L.total + kListBlock - 1) / kListBlock;
+        if (L.n_scenes > 1)
+            k_density_list<true><<<lb, kListBlock, 0, s>>>(L, pos, vel, rec, aux, bnd, nbr, nbr_count, sk);
+        else
+            k_density_list<false><<<lb, kListBlock, 0, s>>>(L, pos, vel, rec, aux, bnd, nbr, nbr_count, sk);
+        const int sms = sm_count();
+        if (sms > 0) blocks = std::min<uint32_t>(blocks, (uint32_t)sms * M);
+    }
     if (L.n_scenes > 1)
-        k_density<true, B, M><<<blocks, B, 0, s>>>(L, pos, vel, rec, cell_scan, aux, bnd, nbr, nbr_count);
+        k_density<true, B, M><<<blocks, B, 0, s>>>(L, pos, vel, rec, cell_scan, aux, bnd, nbr, nbr_count, sk);
     else
-        k_density<false, B, M><<<blocks, B, 0, s>>>(L, pos, vel, rec, cell_scan, aux, bnd, nbr, nbr_count);
+        k_density<false, B, M><<<blocks, B, 0, s>>>(L, pos, vel, rec, cell_scan, aux, bnd, nbr, nbr_count, sk);
 }
 
 template <int B, int M>
 void force_shape(const StepLaunch& L, const float4* pos, const float4* vel, const float4* aux,
                  const float4* rec, const float4* bnd, const uint32_t* cell_scan, const uint32_t* nbr,
                  const uint32_t* nbr_count, float4* pos_out, float4* vel_out, float4* acc_out,
-                 cudaStream_t s) {
+                 const SkinLists& sk, cudaStream_t s) {
     const uint32_t blocks = (L.total + B - 1) / B;
     if (L.n_scenes > 1)
         k_force<true, B, M><<<blocks, B, 0, s>>>(L, pos, vel, aux, rec, bnd, cell_scan, nbr, nbr_count,
-                                                 pos_out, vel_out, acc_out);
+                                                 pos_out, vel_out, acc_out, sk.stale, sk.ctl, sk.queue_n);
     else
         k_force<false, B, M><<<blocks, B, 0, s>>>(L, pos, vel, aux, rec, bnd, cell_scan, nbr, nbr_count,
-                                                  pos_out, vel_out, acc_out);
+                                                  pos_out, vel_out, acc_out, sk.stale, sk.ctl, sk.queue_n);
 }
 
 bool planes_mode(uint32_t total) {
-    static std::atomic<int> sms[16];
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 16) return false;
-    int n = sms[dev].load(std::memory_order_relaxed);
-    if (n == 0) {
-        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return false;
-        sms[dev].store(n, std::memory_order_relaxed);
-    }
-    return (uint64_t)total * 3u <= (uint64_t)n * 768u;
+    const int n = sm_count();
+    return n > 0 && (uint64_t)total * 3u <= (uint64_t)n * 768u;
 }
 
 cudaError_t launch_density(const StepLaunch& L, const float4* pos, const float4* vel, float4* rec,
                            const uint32_t* cell_scan, float4* aux, float4* bnd, uint32_t* nbr,
-                           uint32_t* nbr_count, const KernelConfig& kc, cudaStream_t s) {
+                           uint32_t* nbr_count, const SkinLists& sk, const KernelConfig& kc,
+                           cudaStream_t s) {
     if (L.total == 0) return cudaSuccess;
     if (planes_mode(L.total)) {
         const uint32_t blocks = (L.total + 29u) / 30u;
@@ -1485,10 +1788,10 @@ cudaError_t launch_density(const StepLaunch& L, const float4* pos, const float4*
         return cudaGetLastError();
     }
     switch (kc.nbr_shape) {
-        case kNbr128x8: density_shape<128, 8>(L, pos, vel, rec, cell_scan, aux, bnd, nbr, nbr_count, s); break;
-        case kNbr96x8: density_shape<96, 8>(L, pos, vel, rec, cell_scan, aux, bnd, nbr, nbr_count, s); break;
-        case kNbr64x12: density_shape<64, 12>(L, pos, vel, rec, cell_scan, aux, bnd, nbr, nbr_count, s); break;
-        default: density_shape<128, 6>(L, pos, vel, rec, cell_scan, aux, bnd, nbr, nbr_count, s);
+        case kNbr128x8: density_shape<128, 8>(L, pos, vel, rec, cell_scan, aux, bnd, nbr, nbr_count, sk, s); break;
+        case kNbr96x8: density_shape<96, 8>(L, pos, vel, rec, cell_scan, aux, bnd, nbr, nbr_count, sk, s); break;
+        case kNbr64x12: density_shape<64, 12>(L, pos, vel, rec, cell_scan, aux, bnd, nbr, nbr_count, sk, s); break;
+        default: density_shape<128, 6>(L, pos, vel, rec, cell_scan, aux, bnd, nbr, nbr_count, sk, s);
     }
     return cudaGetLastError();
 }
@@ -1496,20 +1799,21 @@ cudaError_t launch_density(const StepLaunch& L, const float4* pos, const float4*
 cudaError_t launch_force(const StepLaunch& L, const float4* pos, const float4* vel,
                          const float4* aux, const float4* rec, const float4* bnd, const uint32_t* cell_scan,
                          const uint32_t* nbr, const uint32_t* nbr_count, float4* pos_out,
-                         float4* vel_out, float4* acc_out, const KernelConfig& kc, cudaStream_t s) {
+                         float4* vel_out, float4* acc_out, const SkinLists& sk,
+                         const KernelConfig& kc, cudaStream_t s) {
     if (L.total == 0) return cudaSuccess;
     switch (kc.force_shape) {
         case kNbr128x8:
-            force_shape<128, 8>(L, pos, vel, aux, rec, bnd, cell_scan, nbr, nbr_count, pos_out, vel_out, acc_out, s);
+            force_shape<128, 8>(L, pos, vel, aux, rec, bnd, cell_scan, nbr, nbr_count, pos_out, vel_out, acc_out, sk, s);
             break;
         case kNbr96x8:
-            force_shape<96, 8>(L, pos, vel, aux, rec, bnd, cell_scan, nbr, nbr_count, pos_out, vel_out, acc_out, s);
+            force_shape<96, 8>(L, pos, vel, aux, rec, bnd, cell_scan, nbr, nbr_count, pos_out, vel_out, acc_out, sk, s);
             break;
         case kNbr64x12:
-            force_shape<64, 12>(L, pos, vel, aux, rec, bnd, cell_scan, nbr, nbr_count, pos_out, vel_out, acc_out, s);
+            force_shape<64, 12>(L, pos, vel, aux, rec, bnd, cell_scan, nbr, nbr_count, pos_out, vel_out, acc_out, sk, s);
             break;
         default:
-            force_shape<128, 6>(L, pos, vel, aux, rec, bnd, cell_scan, nbr, nbr_count, pos_out, vel_out, acc_out, s);
+            force_shape<128, 6>(L, pos, vel, aux, rec, bnd, cell_scan, nbr, nbr_count, pos_out, vel_out, acc_out, sk, s);
     }
     return cudaGetLastError();
 }

@@ -69,6 +69,8 @@ struct Model {
     uint32_t* nbr = nullptr;        // nbr_cap slot-major neighbour lists
     uint32_t nbr_cap = kNbrCap;     // slots per particle (longer lists fall back to a walk)
     uint32_t* nbr_count = nullptr;  // list length per particle
+    SkinLists skin{};               // candidate lists with a skin (absent in three-lane mode)
+    float skin_fraction = 0.1f;     // skin / h; 0 turns the lists off
     float* stage = nullptr;         // 32 bytes per particle of host-transfer staging
     uint32_t* scratch = nullptr;
     size_t scratch_words = 0;
@@ -97,6 +99,9 @@ struct Model {
     int refresh_params();
     void invalidate_graph();
     int alloc_sort_scratch();
+    int alloc_skin();
+    int invalidate_skin();
+    SkinLists active_skin() const;
     int enqueue_substep(cudaEvent_t* ev);
     int run_substeps(int count);
     int check_device();
@@ -124,6 +129,9 @@ void* device_alias(const void* p);
 int profile_phases(Model& m, int32_t count, float* phase_ms);
 int set_sort_config(Model& m, int32_t digit_bits, int32_t tile_items);
 int set_neighbor_capacity(Model& m, int32_t slots);
+int set_skin(Model& m, float skin);
+float get_skin(const Model& m);
+int get_skin_builds(Model& m, uint32_t scene, uint32_t* builds);
 
 }  // namespace vfs
 

@@ -450,6 +450,22 @@ class WCSPHWithBoundaryModel:
     def set_neighbor_capacity(self, slots: int) -> None:
         check(self._lib.vfs_model_set_neighbor_capacity(self._h, slots))
 
+    @property
+    def skin(self) -> float:
+        """Skin of the candidate lists as a fraction of h (0: no lists, every particle walks)."""
+        s = C.c_float()
+        check(self._lib.vfs_model_get_skin(self._h, C.byref(s)))
+        return float(s.value)
+
+    def set_skin(self, skin: float) -> None:
+        check(self._lib.vfs_model_set_skin(self._h, skin))
+
+    def skin_builds(self) -> int:
+        """Candidate-list builds so far."""
+        b = C.c_uint32()
+        check(self._lib.vfs_model_get_skin_builds(self._h, C.byref(b)))
+        return int(b.value)
+
     def get_sort_config(self):
         d, t, p = C.c_int32(), C.c_int32(), C.c_int32()
         check(self._lib.vfs_model_get_sort_config(self._h, C.byref(d), C.byref(t), C.byref(p)))
@@ -666,6 +682,20 @@ class Batch:
 
     def set_neighbor_capacity(self, slots: int) -> None:
         check(self._lib.vfs_batch_set_neighbor_capacity(self._h, slots))
+
+    @property
+    def skin(self) -> float:
+        s = C.c_float()
+        check(self._lib.vfs_batch_get_skin(self._h, C.byref(s)))
+        return float(s.value)
+
+    def set_skin(self, skin: float) -> None:
+        check(self._lib.vfs_batch_set_skin(self._h, skin))
+
+    def skin_builds(self, scene: int) -> int:
+        b = C.c_uint32()
+        check(self._lib.vfs_batch_get_skin_builds(self._h, scene, C.byref(b)))
+        return int(b.value)
 
     def export_state(self, scene: int, prefix) -> None:
         check(self._lib.vfs_batch_export_state(self._h, scene, str(prefix).encode()))
