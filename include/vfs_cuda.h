@@ -210,13 +210,16 @@ int32_t vfs_model_get_neighbor_capacity(const vfs_model* m);
 /* Candidate lists with a skin (Verlet lists). At a build, each particle lists the particles within
  * h (1 + skin); until some particle of the scene has moved more than h skin / 2 since then
  * (checked every substep from the current positions, so state set by any route is seen), a
- * particle whose list was built from 125 distinct cell keys (its 5x5x5 block in one hash block)
- * sums the list instead of walking the 27 buckets of CalculateDensities
- * (wcsph_with_boundary_model.slang:153-197). The in-range sets are the reference's; the sums follow
- * the visiting order of the last build. skin in [0, 0.5], default 0.1; 0 walks the buckets every
- * substep. Models of up to ~39,000 particles (three lanes per particle in the density pass) and
- * models whose lists do not fit in device memory (288 bytes per particle) have no lists; the
- * getter then reports 0. */
+ * particle whose list was built from 125 provably distinct cell keys sums the list instead of
+ * walking the 27 buckets of CalculateDensities (wcsph_with_boundary_model.slang:153-197). The
+ * in-range sets are the reference's; the sums follow the visiting order of the last build. Lists
+ * that go stale within 12 substeps of their build (a build costs about three bucket walks) make
+ * the scene wait up to 256 substeps before building again (it walks meanwhile), so the lists pay
+ * off where the fastest particle moves less than about h skin / 24 per substep and cost a few
+ * percent where particles move faster. skin in [0, 0.5],
+ * default 0.05; 0 walks the buckets every substep. Models of up to ~39,000 particles (three lanes
+ * per particle in the density pass) and models whose lists do not fit in device memory (224 bytes
+ * per particle) have no lists; the getter then reports 0. */
 int vfs_model_set_skin(vfs_model* m, float skin);
 int vfs_model_get_skin(const vfs_model* m, float* skin);
 /* Number of list builds so far (synchronises the handle's stream). */

@@ -67,40 +67,42 @@ class _DeviceRows:
                                          "version": 2}
 
 
-def test_device_pointer_edits_keep_or_rebuild_the_lists():
+def test_device_pointer_edits_keep_or_invalidate_the_lists():
+    """A small edit keeps the lists (no new build, still the oracle's step); a large one makes the
+    scene stale, so it walks (the oracle's step again)."""
     torch = pytest.importorskip("torch")
     w = moving_scene(seed=3, speed=0.05)
     m = W.build_model(w)
-    m.set_skin(0.4)  # rebuild after 0.2 h of displacement
+    m.set_skin(0.1)  # stale after 0.05 h of displacement
     m.substeps(2)
     assert m.skin_builds() == 1
     h = w.sim.smooth_radius
     g = torch.Generator(device="cuda").manual_seed(0)
-    for shift, expect_build in ((0.05 * h, False), (0.5 * h, True)):
+    for shift in (0.02 * h, 0.5 * h):
         m.synchronize()
         p, _ = m.device_state()
         P = torch.as_tensor(_DeviceRows(p, w.n), device="cuda")
         P[:, :3] += (torch.rand((w.n, 3), device="cuda", generator=g) - 0.5) * (2.0 * shift / 3 ** 0.5)
         torch.cuda.synchronize()
-        before = m.skin_builds()
         s = m.copy_data_buffers()
         o = oracle_for(w, m, pos=s["positions"], vel=s["velocities"], ids=m.get_ids())
         compare_step(m, o, f"device_edit_{shift / h:.2f}h")
-        assert (m.skin_builds() == before + 1) == expect_build
+        if shift < 0.05 * h:
+            assert m.skin_builds() == 1
 
 
 def test_batched_scenes_keep_their_own_builds():
     fast, slow = moving_scene(seed=4, speed=1.0), moving_scene(seed=5, speed=0.0)
     b = W.build_batch([fast, slow])
     b.set_skin(0.02)
-    b.substeps(10)
+    b.substeps(16)
     nf, ns = b.skin_builds(0), b.skin_builds(1)
     assert nf > ns >= 1, (nf, ns)
     # Each scene equals a plain model of it, which builds on the same schedule.
     for s, w in enumerate((fast, slow)):
         m = W.build_model(w)
         m.set_skin(0.02)
-        m.substeps(10)
+        m.substeps(16)
         assert m.skin_builds() == b.skin_builds(s)
         for x, y in zip(b.get_neighbor_arrays(s), m.get_neighbor_arrays()):
             assert np.array_equal(x, y)
@@ -117,7 +119,7 @@ def test_fast_flow_backs_off_building():
     m.set_skin(0.02)
     m.substeps(40)
     builds = m.skin_builds()
-    assert 2 <= builds <= 6, builds  # waits of 1, 2, 4, 8, 16 substeps
+    assert 2 <= builds <= 4, builds  # 8, then 16 stale substeps walked before each build
     s = m.copy_data_buffers()
     o = oracle_for(w, m, pos=s["positions"], vel=s["velocities"], ids=m.get_ids())
     for k in range(3):

@@ -459,7 +459,7 @@ Model::~Model() {
     cudaFree(skin.stale);
     cudaFree(skin.ctl);
     cudaFree(skin.queue);
-    cudaFree(skin.queue_n);
+    cudaFree(skin.seg_n);
     cudaFree(scratch);
     cudaFree(err);
     if (err_host) cudaFreeHost(err_host);
@@ -553,7 +553,7 @@ int Model::init() {
     return refresh_params();
 }
 
-// Candidate lists with a skin, 288 bytes per particle. Three-lane (small) models do not use them,
+// Candidate lists with a skin, 224 bytes per particle. Three-lane (small) models do not use them,
 // and a model too large for them on this device runs without (every particle walks its buckets).
 int Model::alloc_skin() {
     if (n == 0 || planes_mode(n)) return VFS_OK;
@@ -568,7 +568,7 @@ int Model::alloc_skin() {
         cudaMalloc(&s.stale, scenes.size() * sizeof(uint32_t)) != cudaSuccess ||
         cudaMalloc(&s.ctl, scenes.size() * kSkinCtl * sizeof(uint32_t)) != cudaSuccess ||
         cudaMalloc(&s.queue, N * sizeof(uint32_t)) != cudaSuccess ||
-        cudaMalloc(&s.queue_n, sizeof(uint32_t)) != cudaSuccess) {
+        cudaMalloc(&s.seg_n, ((N + 127) / 128) * sizeof(uint32_t)) != cudaSuccess) {
         cudaGetLastError();  // out of memory is not sticky: clear it and go on without lists
         cudaFree(s.list);
         cudaFree(s.count);
@@ -578,13 +578,12 @@ int Model::alloc_skin() {
         cudaFree(s.stale);
         cudaFree(s.ctl);
         cudaFree(s.queue);
-        cudaFree(s.queue_n);
+        cudaFree(s.seg_n);
         return VFS_OK;
     }
     VFS_CUDA_TRY(cudaMemset(s.count, 0, N * sizeof(uint32_t)));
     VFS_CUDA_TRY(cudaMemset(s.b_of_id, 0, N * sizeof(uint32_t)));  // any index below n until a build
     VFS_CUDA_TRY(cudaMemset(s.stale, 0, scenes.size() * sizeof(uint32_t)));
-    VFS_CUDA_TRY(cudaMemset(s.queue_n, 0, sizeof(uint32_t)));
     skin = s;
     return invalidate_skin();
 }
@@ -596,10 +595,7 @@ int Model::invalidate_skin() {
     if (!skin.x_build) return VFS_OK;
     VFS_CUDA_TRY(cudaMemsetAsync(skin.x_build, 0x7F, (size_t)n * sizeof(float4), stream));
     std::vector<uint32_t> ctl(scenes.size() * kSkinCtl, 0u);
-    for (size_t s = 0; s < scenes.size(); s++) {
-        ctl[s * kSkinCtl + kCtlAllow] = 1u;
-        ctl[s * kSkinCtl + kCtlWait] = 1u;
-    }
+    for (size_t s = 0; s < scenes.size(); s++) ctl[s * kSkinCtl + kCtlAllow] = 1u;
     VFS_CUDA_TRY(cudaMemcpyAsync(skin.ctl, ctl.data(), ctl.size() * sizeof(uint32_t),
                                  cudaMemcpyHostToDevice, stream));
     VFS_CUDA_TRY(cudaStreamSynchronize(stream));  // ctl is a local

@@ -128,9 +128,10 @@ enum NbrShape : int { kNbr128x6 = 0, kNbr128x8 = 1, kNbr96x8 = 2, kNbr64x12 = 3,
 // in-range set, multiplicity one). The cell pass keeps `cur`, the current sorted index of every
 // build index, checks every displacement against `x_build` and marks the scene stale; in a stale
 // scene every particle walks, and the lists are rebuilt when the scene's build policy allows it.
-// The force pass runs the policy: lists that went stale within kSkinMinLife substeps of their build
-// double the substeps the scene waits before its next build (up to kSkinMaxWait), longer-lived ones
-// reset the wait to one, so a fast flow walks instead of rebuilding every substep.
+// The force pass runs the policy: a stale scene walks at least one substep before it rebuilds;
+// lists that went stale within kSkinMinLife substeps of their build, or a build that left fewer
+// than half of the scene's lists usable, double the substeps it walks before the next build
+// (from kSkinMinWait to kSkinMaxWait); longer-lived lists rebuild as soon as they go stale.
 struct SkinLists {
     uint32_t* list = nullptr;     // slot-major: list[k * total + b] = build index of candidate k of b
     uint32_t* count = nullptr;    // per build index: list length, kSkinUsable when it can be summed
@@ -139,20 +140,25 @@ struct SkinLists {
     uint32_t* cur = nullptr;      // per build index: current sorted index (written by the cell pass)
     uint32_t* stale = nullptr;    // per scene: nonzero when some particle moved past h skin / 2
     uint32_t* ctl = nullptr;      // per scene, kSkinCtl words: the build policy's state (kCtl*)
-    uint32_t* queue = nullptr;    // the particles the density pass walks this substep
-    uint32_t* queue_n = nullptr;  // their number (cleared by the force pass)
+    uint32_t* queue = nullptr;    // the particles the density pass walks this substep: those of
+                                  // list block b at [128 b, 128 b + seg_n[b]), in index order
+    uint32_t* seg_n = nullptr;    // per list block (128 particles): its walkers
     uint32_t cap = 0;             // slots per particle
 };
 constexpr uint32_t kSkinUsable = 1u << 31;
 constexpr uint32_t kSkinCtl = 8;       // words of policy state per scene:
 constexpr uint32_t kCtlAllow = 0;      //   a stale scene may rebuild this substep
 constexpr uint32_t kCtlAge = 1;        //   substeps since the last build
-constexpr uint32_t kCtlWait = 2;       //   substeps to wait after a build before the next
+constexpr uint32_t kCtlWait = 2;       //   stale substeps to walk before the next build
 constexpr uint32_t kCtlBuilds = 3;     //   builds so far
 constexpr uint32_t kCtlFresh = 4;      //   the lists of the last build have not gone stale yet
-constexpr uint32_t kSkinMinLife = 4;
-constexpr uint32_t kSkinMaxWait = 64;
-constexpr uint32_t kSkinCap = 64;
+constexpr uint32_t kCtlSince = 5;      //   stale substeps since the lists went stale
+constexpr uint32_t kCtlUsable = 6;     //   usable lists left by this substep's build
+constexpr uint32_t kCtlPoor = 7;       //   the last build left fewer than half of them usable
+constexpr uint32_t kSkinMinLife = 12;  // a build costs ~2.7 walks; a list pass saves ~0.4 of one
+constexpr uint32_t kSkinMinWait = 8;
+constexpr uint32_t kSkinMaxWait = 256;
+constexpr uint32_t kSkinCap = 48;  // also the density walk's shared list, where a build is staged
 
 // Launch shapes chosen per model (by default or by the autotuner); none changes any result.
 struct KernelConfig {

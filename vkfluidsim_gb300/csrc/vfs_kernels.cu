@@ -547,6 +547,8 @@ __global__ void __launch_bounds__(kCellBlock)
         s_hi = guess ? lower_bound_near(skeys, n, c1, ((volatile uint32_t*)guess)[blockIdx.x + 1])
                      : lower_bound_keys(skeys, n, c1);
     const uint32_t i = c0 + tid;
+    bool exceed = false;  // skin lists: the particle moved past h skin / 2 since its list build
+    uint32_t exceed_sc = 0u;
     if (i < n) {
         uint32_t src = perm[i];
         if (src >= n) src = i;  // only after a reported sort failure
@@ -564,11 +566,20 @@ __global__ void __launch_bounds__(kCellBlock)
                 const float dx = x.x - b.x, dy = x.y - b.y, dz = x.z - b.z;
                 const uint32_t sc = L.n_scenes > 1 ? (uint32_t)__ldg(L.scene_of + i) : 0u;
                 const float lim = L.n_scenes > 1 ? L.scenes[sc].skin_half2 : L.one.skin_half2;
-                if (!(dx * dx + dy * dy + dz * dz <= lim) && ld_volatile(stale + sc) == 0u)
-                    atomicOr(stale + sc, 1u);
+                exceed = !(dx * dx + dy * dy + dz * dz <= lim);
+                exceed_sc = sc;
             }
         }
         if (pkeys_out) pkeys_out[i] = skeys[i];
+    }
+    // Stale scenes, one atomic per warp and scene at most (most particles of a fast scene exceed).
+    if (cur) {
+        const uint32_t m = __ballot_sync(0xffffffffu, exceed);
+        if (exceed) {
+            const uint32_t g = __match_any_sync(m, exceed_sc);
+            if ((tid & 31u) == (uint32_t)(__ffs(g) - 1) && ld_volatile(stale + exceed_sc) == 0u)
+                atomicOr(stale + exceed_sc, 1u);
+        }
     }
     __syncthreads();
     const uint32_t lo = s_lo, hi = max(s_lo, s_hi);
@@ -772,8 +783,8 @@ __device__ __forceinline__ float slab_dist2(int d, float f) {
 }
 
 // The list build of a particle whose 125 keys are distinct: the sorted indices (this substep's,
-// which become the build indices) of every particle within h (1 + skin), stored slot-major from
-// `out`, from the 5x5x5 cells around (cx, cy, cz) whose boxes lie within that radius: planes dz and
+// which become the build indices) of every particle within h (1 + skin), stored at out[k stride],
+// from the 5x5x5 cells around (cx, cy, cz) whose boxes lie within that radius: planes dz and
 // rows dy in increasing order, the cells of a row in increasing x as runs of consecutive keys (a
 // run ends at a hash-block boundary; a run whose keys pass n - 1 continues at key 0) - the
 // reference's visiting order restricted to its 27 cells. Returns the number found (ids past
@@ -830,6 +841,10 @@ __device__ __forceinline__ uint32_t skin_walk(const SceneParams& p, const uint32
     }
     return c;
 }
+
+// Threads per block of the density pass over the skin lists; the walk queue is kept in segments of
+// one such block.
+constexpr int kListBlock = 128;
 
 // Particle i's density sum and neighbour list as the density pass builds them: add() takes one
 // in-range neighbour, adds its W / sigma (explicitly rounded, so every launch shape and both the
@@ -891,27 +906,35 @@ __device__ __forceinline__ void density_finish(const SceneParams& p, uint32_t i,
 // slot-major (nbr[s * n + i], so a warp's lanes store and later load consecutive words), and its
 // length in nbr_count[i] (a length above nbr_cap means the list overflowed and was truncated).
 // Positions do not change before the force pass, so that list is exactly the force pass's
-// neighbour set. Without a queue every particle is walked; with one (skin lists), the particles
-// k_density_list left in it, by a grid-stride loop. In a stale scene whose build policy allows
-// it, every particle also builds its skin list.
+// neighbour set. Without skin lists every particle is walked. With them, the particles
+// k_density_list left in its queue, one per thread: each list block's walkers in index order, so
+// a stale scene is walked in index order and a warp whose slots are empty returns at once. In a
+// stale scene whose build policy allows it, every particle also builds its skin list.
 template <bool kBatch, int kNbrBlock, int kMinBlocks>
 __global__ void __launch_bounds__(kNbrBlock, kMinBlocks)
     k_density(StepLaunch L, const float4* __restrict__ pos, const float4* __restrict__ vel,
               float4* __restrict__ rec, const uint32_t* __restrict__ scan,
               float4* __restrict__ aux, float4* __restrict__ bnd, uint32_t* __restrict__ nbr,
               uint32_t* __restrict__ nbr_count, SkinLists sk) {
+    static_assert(kSkinCap <= (uint32_t)kListCap, "a list build is staged in the shared list");
     __shared__ uint32_t s_j[kListCap * kNbrBlock];
     const int tid = threadIdx.x;
-    const uint32_t n_work = sk.queue ? *sk.queue_n : L.total;
-    for (uint32_t t = blockIdx.x * kNbrBlock + tid; t < n_work; t += gridDim.x * kNbrBlock) {
-        const uint32_t i = sk.queue ? sk.queue[t] : t;
-        const SceneParams& p = scene_params<kBatch>(L, i);
-        const float4 xi = __ldg(pos + i);
+    {
+        const uint32_t t = blockIdx.x * kNbrBlock + tid;
+        if (t >= L.total) return;
+        uint32_t i = t, sc = 0u;
         bool rebuild = false;
         if (sk.list) {
-            const uint32_t sc = kBatch ? (uint32_t)__ldg(L.scene_of + i) : 0u;
+            if (kBatch || sk.stale[0] == 0u) {
+                // Slot t of the queue: valid below its list block's count of walkers.
+                if (t % kListBlock >= __ldg(sk.seg_n + t / kListBlock)) return;
+                i = __ldg(sk.queue + t);
+                sc = kBatch ? (uint32_t)__ldg(L.scene_of + i) : 0u;
+            }  // else a stale single scene: every particle, in index order (no queue)
             rebuild = sk.stale[sc] != 0u && sk.ctl[sc * kSkinCtl + kCtlAllow] != 0u;
         }
+        const SceneParams& p = scene_params<kBatch>(L, i);
+        const float4 xi = __ldg(pos + i);
         const uint32_t cx = cell_coord(xi.x, p.h), cy = cell_coord(xi.y, p.h),
                        cz = cell_coord(xi.z, p.h);
         DensitySum d;
@@ -931,25 +954,46 @@ __global__ void __launch_bounds__(kNbrBlock, kMinBlocks)
         };
         const bool distinct = distinct_keys(p, cx, cy, cz);
         const float h2 = p.h2;
-        // Branch-free append: every candidate is stored at the list's end and kept only when in
-        // range (the next one overwrites it otherwise). Lists are drained above kDrainAt, so the
-        // slot index stays below kListCap.
-        for_each_candidate(p, scan, pos, xi, cx, cy, cz, [&](uint32_t j, const float4& xj) {
-            s_j[s_end] = j;
-            s_end += in_range2(xi, xj) <= h2 ? kNbrBlock : 0u;
-        }, [&]() {
-            if (s_end > tid + kDrainAt * kNbrBlock) drain();
-        });
-        drain();
+        uint32_t c = 0;
+        bool usable = false;
+        if (rebuild && skin_keys_distinct(p, cx, cy, cz)) {
+            // A list build, staged in this thread's column of the shared list.
+            c = skin_walk(p, scan, pos, xi, cx, cy, cz, s_j + tid, (size_t)kNbrBlock, sk.cap);
+            usable = c <= sk.cap;
+        }
+        if (usable) {
+            // The density from the staged list (its in-range members, in the visiting order), then
+            // the list written out a slot at a time (a warp's lanes store consecutive words).
+#pragma unroll 1
+            for (uint32_t k = 0; k < c; k++) {
+                const uint32_t j = s_j[k * kNbrBlock + tid];
+                const float4 xj = __ldg(pos + j);
+                if (in_range2(xi, xj) <= h2) d.add(i, xi, j, xj, s_inv_h, s_nbr_cap, L.total);
+            }
+#pragma unroll 1
+            for (uint32_t k = 0; k < c; k++) sk.list[(size_t)k * L.total + i] = s_j[k * kNbrBlock + tid];
+        } else {
+            // Branch-free append: every candidate is stored at the list's end and kept only when
+            // in range (the next one overwrites it otherwise). Lists are drained above kDrainAt,
+            // so the slot index stays below kListCap.
+            for_each_candidate(p, scan, pos, xi, cx, cy, cz, [&](uint32_t j, const float4& xj) {
+                s_j[s_end] = j;
+                s_end += in_range2(xi, xj) <= h2 ? kNbrBlock : 0u;
+            }, [&]() {
+                if (s_end > tid + kDrainAt * kNbrBlock) drain();
+            });
+            drain();
+        }
         if (rebuild) {
             // This substep's sorted index becomes the particle's build index.
             sk.x_build[i] = xi;
             sk.b_of_id[__float_as_uint(xi.w)] = i;
-            const bool usable = skin_keys_distinct(p, cx, cy, cz);
-            const uint32_t c = usable ? skin_walk(p, scan, pos, xi, cx, cy, cz, sk.list + i,
-                                                  L.total, sk.cap)
-                                      : 0u;
-            sk.count[i] = min(c, sk.cap) | (usable && c <= sk.cap ? kSkinUsable : 0u);
+            sk.count[i] = min(c, sk.cap) | (usable ? kSkinUsable : 0u);
+            // The scene's usable lists, one atomic per warp and scene.
+            const uint32_t g = __match_any_sync(__activemask(), sc);
+            const uint32_t u = __ballot_sync(g, usable);
+            if ((uint32_t)(tid & 31) == (uint32_t)(__ffs(g) - 1) && u)
+                atomicAdd(sk.ctl + sc * kSkinCtl + kCtlUsable, (uint32_t)__popc(u));
         }
         density_finish(p, i, xi, vel, cx, cy, cz, distinct, d, rec, aux, bnd, nbr_count);
     }
@@ -959,17 +1003,16 @@ __global__ void __launch_bounds__(kNbrBlock, kMinBlocks)
 // usable, sums the in-range members of its list (the same in-range set as the walk: every
 // pair within h was within h (1 + skin) at the build; each once: the particle has moved less than
 // h / 4 since the build, so its 27 cells lie in the build's 5x5x5 block, whose keys were
-// distinct), in the list's order. Every other particle is appended to the queue for k_density.
+// distinct), in the list's order. Every other particle goes to the queue for k_density.
 // No shared memory: the pass is bound by its chains of dependent loads, so it runs at the
 // occupancy its registers allow.
-constexpr int kListBlock = 128;
-
 template <bool kBatch>
 __global__ void __launch_bounds__(kListBlock, 8)
     k_density_list(StepLaunch L, const float4* __restrict__ pos, const float4* __restrict__ vel,
                    float4* __restrict__ rec, float4* __restrict__ aux, float4* __restrict__ bnd,
                    uint32_t* __restrict__ nbr, uint32_t* __restrict__ nbr_count, SkinLists sk) {
     const uint32_t i = blockIdx.x * kListBlock + threadIdx.x;
+    if (!kBatch && sk.stale[0] != 0u) return;  // a stale single scene: k_density walks it in order
     bool walk = false;
     if (i < L.total) {
         const SceneParams& p = scene_params<kBatch>(L, i);
@@ -1016,15 +1059,20 @@ __global__ void __launch_bounds__(kListBlock, 8)
                            bnd, nbr_count);
         }
     }
-    // The walkers join the queue, a warp at a time.
+    // The walkers go to this block's segment of the queue, in index order.
+    __shared__ uint32_t s_cnt[kListBlock / 32];
     const uint32_t m = __ballot_sync(0xffffffffu, walk);
-    if (m) {
-        const int lane = threadIdx.x & 31, lead = __ffs(m) - 1;
-        uint32_t base = 0u;
-        if (lane == lead) base = atomicAdd(sk.queue_n, (uint32_t)__popc(m));
-        base = __shfl_sync(0xffffffffu, base, lead);
-        if (walk) sk.queue[base + __popc(m & ((1u << lane) - 1u))] = i;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) s_cnt[warp] = (uint32_t)__popc(m);
+    __syncthreads();
+    uint32_t base = blockIdx.x * kListBlock, total = 0u;
+#pragma unroll
+    for (int w = 0; w < kListBlock / 32; w++) {
+        base += w < warp ? s_cnt[w] : 0u;
+        total += s_cnt[w];
     }
+    if (walk) sk.queue[base + (uint32_t)__popc(m & ((1u << lane) - 1u))] = i;
+    if (threadIdx.x == 0) sk.seg_n[blockIdx.x] = total;
 }
 
 // W(|x_j - x_i|) / sigma with the density drain's explicitly rounded arithmetic.
@@ -1247,36 +1295,37 @@ __global__ void __launch_bounds__(kNbrBlock, kMinBlocks)
             const uint32_t* __restrict__ scan, const uint32_t* __restrict__ nbr,
             const uint32_t* __restrict__ nbr_count, float4* __restrict__ pos_out,
             float4* __restrict__ vel_out, float4* __restrict__ acc_out,
-            uint32_t* __restrict__ skin_stale, uint32_t* __restrict__ skin_ctl,
-            uint32_t* __restrict__ skin_queue_n) {
+            uint32_t* __restrict__ skin_stale, uint32_t* __restrict__ skin_ctl) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     // The density pass is done with the skin lists' flags: run each scene's build policy and clear
     // the flags for the next substep.
     if (skin_stale && blockIdx.x == 0) {
         for (uint32_t sc = threadIdx.x; sc < L.n_scenes; sc += blockDim.x) {
             uint32_t* c = skin_ctl + sc * kSkinCtl;
-            uint32_t age = c[kCtlAge], wait = c[kCtlWait];
-            if (skin_stale[sc]) {
-                if (c[kCtlFresh]) {  // how long the last build's lists lasted
-                    wait = age < kSkinMinLife ? min(2u * wait, kSkinMaxWait) : 1u;
-                    c[kCtlFresh] = 0u;
-                }
-                if (c[kCtlAllow]) {  // the density pass rebuilt
-                    c[kCtlBuilds]++;
-                    c[kCtlFresh] = 1u;
-                    age = 0u;
-                } else {
-                    age++;
-                }
-                skin_stale[sc] = 0u;
+            const bool stale = skin_stale[sc] != 0u;
+            uint32_t age = c[kCtlAge], wait = c[kCtlWait], since = c[kCtlSince];
+            if (stale && c[kCtlFresh]) {  // the last build's lists just went stale: were they worth it?
+                wait = age < kSkinMinLife || c[kCtlPoor] ? min(max(2u * wait, kSkinMinWait), kSkinMaxWait) : 0u;
+                c[kCtlFresh] = 0u;
+                since = 0u;
+            }
+            if (stale && c[kCtlAllow]) {  // the density pass rebuilt
+                const uint32_t n = L.n_scenes > 1 ? L.scenes[sc].n : L.one.n;
+                c[kCtlBuilds]++;
+                c[kCtlFresh] = 1u;
+                c[kCtlPoor] = 2u * c[kCtlUsable] < n ? 1u : 0u;
+                c[kCtlUsable] = 0u;
+                age = 0u;
             } else {
                 age++;
+                if (stale) since++;
             }
+            skin_stale[sc] = 0u;
             c[kCtlAge] = age;
             c[kCtlWait] = wait;
-            c[kCtlAllow] = age >= wait ? 1u : 0u;
+            c[kCtlSince] = since;
+            c[kCtlAllow] = !c[kCtlFresh] && since >= wait ? 1u : 0u;
         }
-        if (threadIdx.x == 0) *skin_queue_n = 0u;
     }
     if (i >= L.total) return;
     const SceneParams& p = scene_params<kBatch>(L, i);
@@ -1735,17 +1784,14 @@ template <int B, int M>
 void density_shape(const StepLaunch& L, const float4* pos, const float4* vel, float4* rec,
                    const uint32_t* cell_scan, float4* aux, float4* bnd, uint32_t* nbr,
                    uint32_t* nbr_count, const SkinLists& sk, cudaStream_t s) {
-    uint32_t blocks = (L.total + B - 1) / B;
+    const uint32_t blocks = (L.total + B - 1) / B;
     if (sk.list) {
-        // Skin lists: the list pass first; the walk pass then takes the queue it leaves, one wave
-        // of blocks looping over it.
+        // Skin lists: the list pass first; the walk pass then takes the queue it leaves.
         const uint32_t lb = (L.total + kListBlock - 1) / kListBlock;
         if (L.n_scenes > 1)
             k_density_list<true><<<lb, kListBlock, 0, s>>>(L, pos, vel, rec, aux, bnd, nbr, nbr_count, sk);
         else
             k_density_list<false><<<lb, kListBlock, 0, s>>>(L, pos, vel, rec, aux, bnd, nbr, nbr_count, sk);
-        const int sms = sm_count();
-        if (sms > 0) blocks = std::min<uint32_t>(blocks, (uint32_t)sms * M);
     }
     if (L.n_scenes > 1)
         k_density<true, B, M><<<blocks, B, 0, s>>>(L, pos, vel, rec, cell_scan, aux, bnd, nbr, nbr_count, sk);
@@ -1761,10 +1807,10 @@ void force_shape(const StepLaunch& L, const float4* pos, const float4* vel, cons
     const uint32_t blocks = (L.total + B - 1) / B;
     if (L.n_scenes > 1)
         k_force<true, B, M><<<blocks, B, 0, s>>>(L, pos, vel, aux, rec, bnd, cell_scan, nbr, nbr_count,
-                                                 pos_out, vel_out, acc_out, sk.stale, sk.ctl, sk.queue_n);
+                                                 pos_out, vel_out, acc_out, sk.stale, sk.ctl);
     else
         k_force<false, B, M><<<blocks, B, 0, s>>>(L, pos, vel, aux, rec, bnd, cell_scan, nbr, nbr_count,
-                                                  pos_out, vel_out, acc_out, sk.stale, sk.ctl, sk.queue_n);
+                                                  pos_out, vel_out, acc_out, sk.stale, sk.ctl);
 }
 
 bool planes_mode(uint32_t total) {

@@ -70,7 +70,7 @@ struct Model {
     uint32_t nbr_cap = kNbrCap;     // slots per particle (longer lists fall back to a walk)
     uint32_t* nbr_count = nullptr;  // list length per particle
     SkinLists skin{};               // candidate lists with a skin (absent in three-lane mode)
-    float skin_fraction = 0.1f;     // skin / h; 0 turns the lists off
+    float skin_fraction = 0.05f;    // skin / h; 0 turns the lists off
     float* stage = nullptr;         // 32 bytes per particle of host-transfer staging
     uint32_t* scratch = nullptr;
     size_t scratch_words = 0;
