@@ -625,6 +625,7 @@ def run_gpu(args):
     barrier()
 
     # ---- value: device-timed substeps, L2 flushed between steps.
+    builds0 = m.skin_builds()  # candidate-list builds so far (read outside the timed region)
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     with ClockSampler(local) as clk:
@@ -637,11 +638,16 @@ def run_gpu(args):
         barrier()
         t_wall = time.perf_counter() - t_wall0
     step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    builds_timed = m.skin_builds() - builds0
     value, total_ms = replica_throughput(n, args.steps, sum(step_ms), world, device="cuda")
     ms_per_step = total_ms / args.steps
 
     # ---- per-kernel timing (same stream, CUDA events between the passes).
     prof = m.profile_substeps(max(3, min(args.steps, 10)))
+    skin_build_ms = None
+    if m.skin > 0:
+        m.set_skin(m.skin)  # every list is rebuilt by the next substep: time a build substep
+        skin_build_ms = m.profile_substeps(1)["density"]
     digits, items, passes = m.get_sort_config()
     kernel_phases = {k: v for k, v in prof.items() if k in B_PHASE}
     dom = max(kernel_phases, key=kernel_phases.get)
@@ -730,8 +736,11 @@ def run_gpu(args):
                               "achieved_gbs": B_STEP * n / (ms_per_step * 1e-3) / 1e9,
                               "frac": B_STEP * n / (ms_per_step * 1e-3) / 1e9 / hbm},
             "phase_ms": prof,
-            # keys+delta, `passes` onesweep passes, merge, cells+reorder, density, force.
-            "gpu_launches": (5 + passes) * args.steps,
+            # keys+delta, `passes` onesweep passes, merge, cells+reorder, density (with skin lists:
+            # the list pass and the walk of the rest), force.
+            "gpu_launches": (5 + passes + (1 if m.skin > 0 else 0)) * args.steps,
+            "skin": {"fraction": m.skin, "builds_in_timed_region": builds_timed,
+                     "build_substep_density_ms": skin_build_ms},
             "clocks": clk.summary(),
             "wall_s_timed_region": t_wall,
         }
