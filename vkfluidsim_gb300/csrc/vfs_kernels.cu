@@ -1035,12 +1035,22 @@ __global__ void __launch_bounds__(kListBlock, 8)
             const size_t stride = L.total;
             const uint32_t* q = sk.list + row;
             uint32_t k = 0;
+            // The next batch's build indices load while the current batch is resolved and summed.
+            uint32_t jn[4];
+            if (n_list >= 4u) {
+#pragma unroll
+                for (int u = 0; u < 4; u++) jn[u] = __ldg(q + u * stride);
+            }
 #pragma unroll 1
             for (; k + 4u <= n_list; k += 4u, q += 4 * stride) {
                 uint32_t j[4];
                 float4 xj[4];
 #pragma unroll
-                for (int u = 0; u < 4; u++) j[u] = __ldg(q + u * stride);
+                for (int u = 0; u < 4; u++) j[u] = jn[u];
+                if (k + 8u <= n_list) {
+#pragma unroll
+                    for (int u = 0; u < 4; u++) jn[u] = __ldg(q + (4 + u) * stride);
+                }
 #pragma unroll
                 for (int u = 0; u < 4; u++) j[u] = __ldg(sk.cur + j[u]);
 #pragma unroll
