@@ -213,7 +213,7 @@ int32_t vfs_model_get_neighbor_capacity(const vfs_model* m);
  * particle whose list was built from 125 provably distinct cell keys sums the list instead of
  * walking the 27 buckets of CalculateDensities (wcsph_with_boundary_model.slang:153-197). The
  * in-range sets are the reference's; the sums follow the visiting order of the last build. Lists
- * that go stale within 12 substeps of their build (a build costs about three bucket walks) make
+ * that go stale within 12 substeps of their build (a build substep costs about two walks) make
  * the scene wait up to 256 substeps before building again (it walks meanwhile), so the lists pay
  * off where the fastest particle moves less than about h skin / 24 per substep and cost a few
  * percent where particles move faster. skin in [0, 0.5],

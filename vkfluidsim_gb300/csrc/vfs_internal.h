@@ -155,7 +155,7 @@ constexpr uint32_t kCtlFresh = 4;      //   the lists of the last build have not
 constexpr uint32_t kCtlSince = 5;      //   stale substeps since the lists went stale
 constexpr uint32_t kCtlUsable = 6;     //   usable lists left by this substep's build
 constexpr uint32_t kCtlPoor = 7;       //   the last build left fewer than half of them usable
-constexpr uint32_t kSkinMinLife = 12;  // a build costs ~2.7 walks; a list pass saves ~0.4 of one
+constexpr uint32_t kSkinMinLife = 12;  // a build substep costs about two walks; a list pass saves ~0.45 of one
 constexpr uint32_t kSkinMinWait = 8;
 constexpr uint32_t kSkinMaxWait = 256;
 constexpr uint32_t kSkinCap = 48;  // also the density walk's shared list, where a build is staged
