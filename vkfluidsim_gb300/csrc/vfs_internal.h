@@ -131,7 +131,9 @@ enum NbrShape : int { kNbr128x6 = 0, kNbr128x8 = 1, kNbr96x8 = 2, kNbr64x12 = 3,
 // The force pass runs the policy: a stale scene walks at least one substep before it rebuilds;
 // lists that went stale within kSkinMinLife substeps of their build, or a build that left fewer
 // than half of the scene's lists usable, double the substeps it walks before the next build
-// (from kSkinMinWait to kSkinMaxWait); longer-lived lists rebuild as soon as they go stale.
+// (from kSkinMinWait to kSkinMaxWait); longer-lived lists rebuild as soon as they go stale. A
+// single scene whose last build left most lists unusable is walked in index order, as a stale
+// one is, until its next build.
 struct SkinLists {
     uint32_t* list = nullptr;     // slot-major: list[k * total + b] = build index of candidate k of b
     uint32_t* count = nullptr;    // per build index: list length, kSkinUsable when it can be summed

@@ -925,12 +925,13 @@ __global__ void __launch_bounds__(kNbrBlock, kMinBlocks)
         uint32_t i = t, sc = 0u;
         bool rebuild = false;
         if (sk.list) {
-            if (kBatch || sk.stale[0] == 0u) {
+            if (kBatch || (sk.stale[0] == 0u && sk.ctl[kCtlPoor] == 0u)) {
                 // Slot t of the queue: valid below its list block's count of walkers.
                 if (t % kListBlock >= __ldg(sk.seg_n + t / kListBlock)) return;
                 i = __ldg(sk.queue + t);
                 sc = kBatch ? (uint32_t)__ldg(L.scene_of + i) : 0u;
-            }  // else a stale single scene: every particle, in index order (no queue)
+            }  // else a single scene that is stale or whose lists are mostly unusable: every
+               // particle, in index order (no queue)
             rebuild = sk.stale[sc] != 0u && sk.ctl[sc * kSkinCtl + kCtlAllow] != 0u;
         }
         const SceneParams& p = scene_params<kBatch>(L, i);
@@ -1012,7 +1013,9 @@ __global__ void __launch_bounds__(kListBlock, 8)
                    float4* __restrict__ rec, float4* __restrict__ aux, float4* __restrict__ bnd,
                    uint32_t* __restrict__ nbr, uint32_t* __restrict__ nbr_count, SkinLists sk) {
     const uint32_t i = blockIdx.x * kListBlock + threadIdx.x;
-    if (!kBatch && sk.stale[0] != 0u) return;  // a stale single scene: k_density walks it in order
+    // A single scene that is stale, or whose last build left most lists unusable: k_density walks
+    // it in index order.
+    if (!kBatch && (sk.stale[0] != 0u || sk.ctl[kCtlPoor] != 0u)) return;
     bool walk = false;
     if (i < L.total) {
         const SceneParams& p = scene_params<kBatch>(L, i);
