@@ -268,22 +268,63 @@ def time_cpu(w, model=None, budget_s=12.0, max_steps=200, threads=None):
                       f"({dt:.1f} s wall)"}
 
 
+def workload_config(name: str, n: int, h: float, dt: float, boundary: str) -> dict:
+    """The `config` both arms print for the timed workload (identical dicts: the arms run the
+    same scene from the same seeded initial state and time the same substeps)."""
+    return {"workload": name, "particles": int(n), "h": float(h), "dt": float(dt),
+            "boundary": boundary, "substeps_timed": "the --steps substeps after --warmup, from "
+                                                    "the seeded initial state",
+            "l2": "GPU arm: flushed between timed steps (256 MiB write)"}
+
+
+def _mapped_libraries() -> list:
+    """Shared objects of this repository mapped into this process (from /proc/self/maps)."""
+    out = set()
+    try:
+        with open("/proc/self/maps") as f:
+            for line in f:
+                p = line.split()[-1] if line.strip() else ""
+                if p.endswith(".so") and str(ROOT) in p:
+                    out.add(os.path.relpath(p, ROOT))
+    except OSError:
+        pass
+    return sorted(out)
+
+
 def run_reference(args):
+    """The reference arm: the CPU restatement of the reference's shader math (the oracle) on every
+    host thread, on the same workload as the GPU arm: --warmup untimed substeps, then exactly
+    --steps timed substeps (wall clock). It never imports the product package."""
     world, rank, _ = dist_env()
     if rank != 0:
         return
-    from vkfluidsim_gb300 import workloads as W
+    from oracle import binding as ob
+    from oracle.workloads import Obstacle1M
 
-    w = W.obstacle_1m()
-    cpu = time_cpu(w, None, budget_s=args.cpu_budget, threads=os.cpu_count())
-    line = {"metric": METRIC, "value": cpu["value"], "unit": UNIT, "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * w.n / cpu["value"],
+    w = Obstacle1M()
+    o = w.oracle()  # boundary grids built with every host thread
+    ob.set_threads(os.cpu_count() or 1)
+    o.substeps(args.warmup)
+    t0 = time.perf_counter()
+    o.substeps(args.steps)
+    dt = time.perf_counter() - t0
+    value = w.n * args.steps / dt
+    libs = _mapped_libraries()
+    if any("vkfluidsim_gb300" in p for p in libs):
+        raise RuntimeError(f"the reference arm mapped the product library: {libs}")
+    cpu = {"value": value, "unit": UNIT, "cores": ob.get_threads(), "kind": "port",
+           "sample": f"{w.name}: {args.steps} substeps of {w.n} particles after {args.warmup} "
+                     f"warm-up substeps ({dt:.1f} s wall)"}
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic: seeded jittered lattice", "impl": "reference",
-            "config": {"workload": w.name, "particles": w.n},
+            "data": "synthetic: seeded jittered lattice (no dataset exists for this path)",
+            "impl": "reference",
+            "config": workload_config(w.name, w.n, w.h, w.dt, "sphere r=0.2, 128^3 volume map"),
             "cpu_baseline": cpu,
-            "e2e": {"value": cpu["value"], "unit": UNIT, "h2d_bytes_per_step": 0,
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0},
+            "libraries_mapped": libs,
             "note": "the reference's own compute path is Vulkan/Slang and cannot run on this box "
                     "(no Vulkan stack or software renderer); this is the project's CPU restatement "
                     "of its shader math (oracle), OpenMP on all host threads"}
@@ -565,7 +606,7 @@ def time_full_run(args, stream, torch):
     return {"workload": w.name, "particles": w.n, "substeps": done, "ms_total": total,
             "ms_per_substep": total / done, "value": w.n * done / (total * 1e-3),
             "ms_per_substep_by_segment": seg, "final_max_speed_m_s": float(v.max()),
-            "launch_shapes": tuned}
+            "skin_builds": m.skin_builds(), "launch_shapes": tuned}
 
 
 def time_small(args, stream, torch):
@@ -721,12 +762,11 @@ def run_gpu(args):
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic: seeded jittered lattice (no dataset exists for this path)",
-            "config": {"workload": w.name, "particles": n, "h": w.sim.smooth_radius,
-                       "dt": w.sph.fixed_dt, "boundary": "sphere r=0.2, 128^3 volume map",
-                       "l2": "flushed between timed steps (256 MiB write)",
-                       "sort": {"digit_bits": digits, "tile_items": items, "passes": passes},
-                       "launch_shapes": tuned, "autotuned": bool(args.autotune),
-                       "cuda_graph": True, "parallelism": f"replicas x{world}"},
+            "config": workload_config(w.name, n, w.sim.smooth_radius, w.sph.fixed_dt,
+                                      "sphere r=0.2, 128^3 volume map"),
+            "impl_config": {"sort": {"digit_bits": digits, "tile_items": items, "passes": passes},
+                            "launch_shapes": tuned, "autotuned": bool(args.autotune),
+                            "cuda_graph": True, "parallelism": f"replicas x{world}"},
             "e2e": e2e,
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm,
                          "unit": "GB/s", "frac": achieved / hbm, "peak_kind": peak_kind,
@@ -758,11 +798,64 @@ def run_gpu(args):
             line["full_run"] = full_run
         if cpu:
             line["cpu_baseline"] = cpu
+        # The figures the other legs exist for, last on the line (short keys).
+        summ = {"plain_ms": ms_per_step, "plain_value": value, "e2e_value": e2e_value,
+                "dominant_frac": achieved / hbm, "step_frac": B_STEP * n / (ms_per_step * 1e-3) / 1e9 / hbm,
+                "skin_builds_timed": builds_timed}
+        if full_run:
+            summ["amortised_ms_1000"] = full_run["ms_per_substep"]
+            summ["amortised_ms_first_250"] = full_run["ms_per_substep_by_segment"].get("to_250")
+            summ["full_run_builds"] = full_run.get("skin_builds")
+        if batched:
+            summ["batched_value"] = batched["value"]
+            summ["batched_ms"] = batched["ms_per_step"]
+            summ["batched_loop_ms"] = batched["loop_ms_per_step"]
+            summ["batched_speedup"] = batched["speedup_vs_loop"]
+        if adjoint:
+            summ["fwd_adjoint_cost"] = adjoint["cost_vs_forward"]
+            summ["fwd_ms"] = adjoint["forward_ms_per_step"]
+        if stress:
+            summ["stress_ms"] = stress["ms_per_step"]
+        if cpu:
+            summ["cpu_value"] = cpu["value"]
+        line["summary"] = summ
         print(json.dumps(line), flush=True)
     if world > 1:
         import torch.distributed as dist
 
         dist.destroy_process_group()
+
+
+def run_profile(args):
+    """A short run for profilers (no timing line): `--profile step` runs --steps substeps of
+    --workload with one launch per pass (no CUDA graph) after one warm-up substep and prints the
+    per-pass event times; `--profile adjoint` runs a checkpointed forward + adjoint rollout of the
+    65,536-particle dam break over --steps substeps."""
+    from vkfluidsim_gb300 import workloads as W
+
+    if args.profile == "step":
+        w = W.WORKLOADS[args.workload]()
+        m = W.build_model(w)
+        m.use_graph(False)
+        m.substeps(1)
+        prof = m.profile_substeps(max(1, args.steps - 1))
+        m.synchronize()
+        print(json.dumps({"workload": w.name, "particles": w.n, "phase_ms": prof,
+                          "sort": m.get_sort_config()}))
+        return
+    import vkfluidsim_gb300 as vfs
+    from vkfluidsim_gb300.adjoint import Rollout
+
+    w = W.dam_break_64k()
+    w.vel = vfs.generate_fourier_velocity(w.pos, 8, 0.5, 4)
+    m = W.build_model(w)
+    ro = Rollout(m, args.steps, 25)
+    t0 = time.perf_counter()
+    ro.forward()
+    xf = ro.final_positions_by_id()
+    g = ro.backward(2.0 * (xf - w.pos) / xf.size)
+    print(json.dumps({"particles": w.n, "steps": args.steps, "seconds": time.perf_counter() - t0,
+                      "dnu": g["dnu"], "dk": g["dk"], "dv0_max": float(np.abs(g["dv0"]).max())}))
 
 
 def main():
@@ -780,7 +873,13 @@ def main():
     ap.add_argument("--next-rows", type=int, default=1)
     ap.add_argument("--small", type=int, default=1)
     ap.add_argument("--full-run", type=int, default=1)
+    ap.add_argument("--profile", choices=["step", "adjoint"], default=None,
+                    help="a short untimed run for profilers instead of the benchmark")
+    ap.add_argument("--workload", default="obstacle_1m", help="workload of --profile step")
     args = ap.parse_args()
+    if args.profile:
+        run_profile(args)
+        return
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":

@@ -394,15 +394,13 @@ int vfs_scene_reset(vfs_model* m);
  * items[] is the sorting permutation and keys[] the sorted keys. Keys must be <= max_value.
  * Temporary buffers come from the stream-ordered allocator. */
 int vfs_sort_pairs(uint32_t* items, uint32_t* keys, uint32_t n, uint32_t max_value, void* stream);
-/* The same sort without any allocation, for callers that cannot allocate device memory: code in
- * a frame loop or inside a host framework that owns the GPU memory budget, where a cudaMalloc
- * could synchronise the device, fragment the host's pool or break a stream capture. This entry
- * point has no counterpart in the reference. Its temporaries live in one fixed device array of
- * 2.3 MB that every GPU loading the library holds until the process exits; n above
- * VFS_SORT_NOALLOC_MAX_PAIRS is rejected with VFS_ERR_CAPACITY. The first call on each device
- * looks up that array's device address (cudaGetSymbolAddress) and should come before any stream
- * capture. All calls share the array, so calls whose work overlaps on the GPU (other streams,
- * other threads) race; serialise them on one stream. */
+/* Status of the pair sorts (vfs_sort_pairs, vfs_sort_pairs_noalloc) enqueued on the current device
+ * since the previous status call: synchronises `stream`, returns the OR of their device error
+ * words in *err_word (may be NULL) and clears it. VFS_ERR_DEVICE_CHECK when a sort's bounded
+ * look-back wait timed out (that sort's output is invalid), else VFS_OK. The sorts themselves
+ * return without synchronising, so their device errors surface here. The reference's counting
+ * sort (src/compute/sort.cpp:107-143) has no wait that can fail, hence no counterpart. */
+int vfs_sort_pairs_status(void* stream, uint32_t* err_word);
 /* Signed distances (double) of n_points points (x, y, z floats) to a triangle mesh, computed on
  * the GPU exactly as the mesh objects' SDF grids are (the primitive behind them). */
 int vfs_mesh_signed_distance(const float* vertices, uint32_t n_vertices, const uint32_t* triangles,
@@ -420,6 +418,16 @@ int vfs_mesh_signed_distance(const float* vertices, uint32_t n_vertices, const u
 int vfs_selftest_lookback(int32_t predecessor_published, int32_t spin_limit, uint32_t* err_word,
                           uint32_t* exclusive);
 
+/* The same sort without any allocation, for callers that cannot allocate device memory: code in
+ * a frame loop or inside a host framework that owns the GPU memory budget, where a cudaMalloc
+ * could synchronise the device, fragment the host's pool or break a stream capture. This entry
+ * point has no counterpart in the reference. Its temporaries live in one fixed device array of
+ * 2.3 MB that every GPU loading the library holds until the process exits; n above
+ * VFS_SORT_NOALLOC_MAX_PAIRS is rejected with VFS_ERR_CAPACITY. The first call on each device
+ * looks up that array's device address (cudaGetSymbolAddress) and should come before any stream
+ * capture. All calls share the array, so calls whose work overlaps on the GPU (other streams,
+ * other threads) race; serialise them on one stream. Errors of the sort itself are reported by
+ * vfs_sort_pairs_status, as for vfs_sort_pairs. */
 #define VFS_SORT_NOALLOC_MAX_PAIRS 262144u
 int vfs_sort_pairs_noalloc(uint32_t* items, uint32_t* keys, uint32_t n, uint32_t max_value,
                            void* stream);

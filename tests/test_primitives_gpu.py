@@ -25,6 +25,7 @@ def test_sort_pairs_is_the_stable_counting_sort(n, max_value):
     items = torch.full((n,), 12345, dtype=torch.int32, device="cuda")
     P.sort_pairs(items.data_ptr(), k.data_ptr(), n, max_value)
     torch.cuda.synchronize()
+    assert P.sort_status() == 0  # no look-back timed out
     perm = np.argsort(keys, kind="stable").astype(np.uint32)
     assert np.array_equal(items.cpu().numpy().view(np.uint32), perm)
     assert np.array_equal(k.cpu().numpy().view(np.uint32), keys[perm])

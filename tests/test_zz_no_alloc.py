@@ -42,6 +42,8 @@ def test_no_alloc_sort_matches_the_allocating_sort_twice_in_a_row():
         rc_ref, items_ref, keys_ref = _run(lib.vfs_sort_pairs, keys, max_value)
         rc_new, items_new, keys_new = _run(lib.vfs_sort_pairs_noalloc, keys, max_value)
         assert rc_ref == 0 and rc_new == 0, lib.vfs_last_error()
+        err = C.c_uint32(7)
+        assert lib.vfs_sort_pairs_status(None, C.byref(err)) == 0 and err.value == 0
         assert np.array_equal(items_new, items_ref)
         assert np.array_equal(keys_new, keys_ref)
         assert np.array_equal(items_new, np.argsort(keys, kind="stable").astype(np.uint32))
@@ -54,3 +56,22 @@ def test_no_alloc_sort_rejects_sizes_beyond_its_array():
                                     MAX_PAIRS + 1, 7, None)
     assert rc == CAPACITY_ERROR
     assert b"at most" in lib.vfs_last_error()
+
+
+def test_no_alloc_sort_leaves_device_memory_unchanged():
+    # Free device memory is the same before and after many calls (after one warm-up call that
+    # loads the module and looks up the array's address).
+    lib = load_library()
+    n = 50_000
+    keys = np.random.default_rng(5).integers(0, n, size=n).astype(np.uint32)
+    d_keys = torch.from_numpy(keys.view(np.int32).copy()).cuda()
+    d_items = torch.empty(n, dtype=torch.int32, device="cuda")
+    args = (C.c_void_p(d_items.data_ptr()), C.c_void_p(d_keys.data_ptr()), n, n - 1, None)
+    assert lib.vfs_sort_pairs_noalloc(*args) == 0
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    for _ in range(100):
+        assert lib.vfs_sort_pairs_noalloc(*args) == 0
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0

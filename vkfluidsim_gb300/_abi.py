@@ -205,6 +205,7 @@ SIGNATURES = {
     "vfs_scene_reset": (_I, [_P]),
     "vfs_sort_pairs": (_I, [_P, _P, _U32, _U32, _P]),
     "vfs_sort_pairs_noalloc": (_I, [_P, _P, _U32, _U32, _P]),
+    "vfs_sort_pairs_status": (_I, [_P, _U]),
     "vfs_spatial_offsets": (_I, [_P, _P, _U32, _P]),
     "vfs_reorder_float3": (_I, [_P, _P, _P, _U32, _P]),
     "vfs_generate_lattice": (_I, [_U, _F, C.c_float, C.c_float, C.c_uint64, _F]),

@@ -48,6 +48,16 @@ __global__ void k_reorder_float3(const uint32_t* __restrict__ idx, const float* 
     dst[3 * (size_t)i + 2] = src[3 * (size_t)s + 2];
 }
 
+// Error bits of every pair sort on this device since the last vfs_sort_pairs_status: each sort's
+// own error word (its look-back timeouts) is OR-ed in after its passes. A fixed device word, so
+// the no-allocation sort can report through it too.
+__device__ uint32_t g_sort_status;
+
+__global__ void k_sort_status_accumulate(const uint32_t* __restrict__ err) {
+    const uint32_t e = *err;
+    if (e) atomicOr(&g_sort_status, e);
+}
+
 }  // namespace
 
 // Enqueues a stable sort of (keys, index) with caller-provided scratch: tmp_keys / tmp_items
@@ -68,6 +78,8 @@ int enqueue_sort_pairs(uint32_t* items, uint32_t* keys, uint32_t n, const SortCo
     if (sk != keys) VFS_PRIM_TRY(cudaMemcpyAsync(keys, sk, (size_t)n * 4, cudaMemcpyDeviceToDevice, s));
     if (sp != items)
         VFS_PRIM_TRY(cudaMemcpyAsync(items, sp, (size_t)n * 4, cudaMemcpyDeviceToDevice, s));
+    k_sort_status_accumulate<<<1, 1, 0, s>>>(scr.err);
+    VFS_PRIM_TRY(cudaGetLastError());
     return VFS_OK;
 }
 
@@ -93,6 +105,19 @@ int vfs_sort_pairs(uint32_t* items, uint32_t* keys, uint32_t n, uint32_t max_val
     cudaFreeAsync(ti, s);
     cudaFreeAsync(scratch, s);
     return rc;
+}
+
+int vfs_sort_pairs_status(void* stream, uint32_t* err_word) {
+    cudaStream_t s = (cudaStream_t)stream;
+    VFS_PRIM_TRY(cudaStreamSynchronize(s));
+    uint32_t e = 0u;
+    const uint32_t zero = 0u;
+    VFS_PRIM_TRY(cudaMemcpyFromSymbol(&e, vfs::g_sort_status, sizeof(e)));
+    VFS_PRIM_TRY(cudaMemcpyToSymbol(vfs::g_sort_status, &zero, sizeof(zero)));
+    if (err_word) *err_word = e;
+    if (e) return fail(VFS_ERR_DEVICE_CHECK, "pair sort error word set: " + std::to_string(e) +
+                                                 " (look-back timeout; the sorted output is invalid)");
+    return VFS_OK;
 }
 
 int vfs_spatial_offsets(const uint32_t* sorted_keys, uint32_t* offsets, uint32_t n, void* stream) {

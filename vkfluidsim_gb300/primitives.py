@@ -17,6 +17,15 @@ def sort_pairs(items_ptr: int, keys_ptr: int, n: int, max_value: int, stream: in
                                         C.c_void_p(stream)))
 
 
+def sort_status(stream: int = 0) -> int:
+    """Synchronises the stream and returns (then clears) the error bits of the pair sorts run
+    since the last call; raises VfsError (VFS_ERR_DEVICE_CHECK) when a sort's look-back timed
+    out."""
+    err = C.c_uint32(0)
+    check(load_library().vfs_sort_pairs_status(C.c_void_p(stream), C.byref(err)))
+    return int(err.value)
+
+
 def spatial_offsets(sorted_keys_ptr: int, offsets_ptr: int, n: int, stream: int = 0) -> None:
     """offsets[k] = first index of key k in the sorted keys, n for absent keys."""
     check(load_library().vfs_spatial_offsets(C.c_void_p(sorted_keys_ptr), C.c_void_p(offsets_ptr),
