@@ -1,0 +1,80 @@
+"""GPU parity against the reference itself: the CUDA path (through the C ABI) stepped from the
+inputs of the reference-step fixtures (tests/golden/ref_step, outputs of the reference's own step
+shaders compiled as C++), one WCSPHWithBoundaryModel::Step per comparison from the reference's own
+state before that step.
+
+Bars: sorted keys, sorted indices and spatial offsets bit-exact; every float field within 1e-5
+normwise; densities within 1e-5 element-wise and position components within 1e-5 of
+max(|x|, h) element-wise (tests/helpers.py). The element-wise maxima and 99.9th percentiles of
+every field are printed.
+"""
+from __future__ import annotations
+
+import json
+
+import numpy as np
+import pytest
+
+import vkfluidsim_gb300 as vfs
+from tests.helpers import RTOL, elementwise_quantile, elementwise_rel, normwise_rel
+from tests.ref_fixtures import FLOAT_FIELDS, INT_FIELDS, Fixture, names
+
+pytestmark = pytest.mark.gpu
+
+
+def gpu_model(fx: Fixture, pos, vel):
+    m = vfs.WCSPHWithBoundaryModel(*fx.product_params())
+    for o in fx.objects:
+        m.add_boundary_object(o["transform"], o["rotation"], o["box_size"], o["box_pos"],
+                              o["resolution"], o["sdf"], o["volume_map"])
+    m.set_particle_state(pos, vel)
+    m.record_fields(True)
+    return m
+
+
+def gpu_snapshot(m):
+    k, p, off = m.get_neighbor_arrays()
+    g = m.copy_data_buffers(with_acc=True)
+    bd, bg = m.get_boundary_fields()
+    return {"keys": k, "sorted_indices": p, "offsets": off, "positions": g["positions"],
+            "velocities": g["velocities"], "densities": g["densities"],
+            "accelerations": g["accelerations"], "boundary_density": bd, "boundary_gradient": bg}
+
+
+def compare(got, ref, h, label):
+    for k in INT_FIELDS:
+        assert np.array_equal(got[k], ref[k]), f"{label}: {k} differ from the reference"
+    errs = {}
+    for k in FLOAT_FIELDS:
+        floor = h if k == "positions" else 0.0
+        errs[k] = {"normwise": normwise_rel(got[k], ref[k]),
+                   "elementwise_max": elementwise_rel(got[k], ref[k], floor),
+                   "elementwise_p999": elementwise_quantile(got[k], ref[k], 0.999, floor)}
+    print(label, json.dumps({k: {a: float(f"{b:.3g}") for a, b in v.items()} for k, v in errs.items()}))
+    for k, e in errs.items():
+        assert e["normwise"] <= RTOL, f"{label}: {k} normwise {e['normwise']:.3g}"
+    assert errs["densities"]["elementwise_max"] <= RTOL, label
+    assert errs["positions"]["elementwise_max"] <= RTOL, label
+    return errs
+
+
+@pytest.mark.parametrize("name", names())
+def test_each_step_matches_the_reference_from_its_own_state(name):
+    fx = Fixture(name)
+    pos, vel = fx.pos0, fx.vel0
+    for s, ref in enumerate(fx.snaps):
+        m = gpu_model(fx, pos, vel)
+        m.step()
+        m.synchronize()
+        compare(gpu_snapshot(m), ref, fx.h, f"{name} step {s + 1}")
+        pos, vel = ref["positions"], ref["velocities"]
+
+
+@pytest.mark.parametrize("name", ["box_dam_break", "three_iterations_wall"])
+def test_continuous_run_stays_on_the_reference(name):
+    fx = Fixture(name)
+    m = gpu_model(fx, fx.pos0, fx.vel0)
+    for s, ref in enumerate(fx.snaps):
+        m.step()
+        m.synchronize()
+        compare(gpu_snapshot(m), ref, fx.h, f"{name} continuous step {s + 1}")
