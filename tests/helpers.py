@@ -12,6 +12,8 @@ FP32-vs-FP64 error of the oracle itself is reported beside it.
 """
 from __future__ import annotations
 
+import json
+
 import numpy as np
 
 from oracle import binding as ob
@@ -70,3 +72,58 @@ def by_id(arr, ids):
     out = np.empty_like(arr)
     out[ids] = arr
     return out
+
+
+def compare_step(model, oracle, label="", fp64_oracle=None, check_fields=True):
+    """Runs one substep on both and checks the bars; returns the error table."""
+    model.record_fields(True)
+    model.substeps(1)
+    oracle.substeps(1)
+    gk, gp, go = model.get_neighbor_arrays()
+    ok, op, oo = oracle.neighbors()
+    assert np.array_equal(gk, ok), f"{label}: sorted keys differ"
+    assert np.array_equal(gp, op), f"{label}: permutation differs"
+    assert np.array_equal(go, oo), f"{label}: spatial offsets differ"
+    g = model.copy_data_buffers(with_acc=True)
+    o = oracle.state()
+    assert np.array_equal(model.get_ids(), o["ids"])
+    errs = {}
+    if check_fields:
+        bd, bg = model.get_boundary_fields()
+        f = oracle.fields()
+        errs["boundary_density"] = normwise_rel(bd, f["boundary_density"])
+        errs["boundary_gradient"] = normwise_rel(bg, f["boundary_gradient"])
+        errs["accelerations"] = normwise_rel(g["accelerations"], f["accelerations"])
+    errs["densities"] = normwise_rel(g["densities"], o["densities"])
+    errs["velocities"] = normwise_rel(g["velocities"], o["velocities"])
+    errs["positions"] = normwise_rel(g["positions"], o["positions"])
+    # Element-wise: densities relative to themselves (asserted); position components relative to
+    # max(|x|, h) and velocity components relative to max(|v|, 1e-3 max|v|) (reported: a
+    # particle's position and velocity errors follow its acceleration error, which is bounded
+    # only normwise where forces nearly cancel or particles nearly coincide).
+    h = float(model.get_parameters()[0].smooth_radius)
+    vfloor = 1e-3 * max(float(np.abs(o["velocities"]).max()), 1e-30)
+    ew = {"ew_densities": elementwise_rel(g["densities"], o["densities"]),
+          "ew_p999_densities": elementwise_quantile(g["densities"], o["densities"], 0.999),
+          "ew_positions": elementwise_rel(g["positions"], o["positions"], h),
+          "ew_p999_positions": elementwise_quantile(g["positions"], o["positions"], 0.999, h),
+          "ew_velocities": elementwise_rel(g["velocities"], o["velocities"], vfloor),
+          "ew_p999_velocities": elementwise_quantile(g["velocities"], o["velocities"], 0.999,
+                                                     vfloor)}
+    if fp64_oracle is not None:
+        fp64_oracle.substeps(1)
+        d = fp64_oracle.state()
+        for k in ("densities", "velocities", "positions"):
+            ref = by_id(d[k], d["ids"])
+            errs[f"gpu_vs_fp64_{k}"] = normwise_rel(by_id(g[k], o["ids"]), ref)
+            errs[f"oracle32_vs_fp64_{k}"] = normwise_rel(by_id(o[k], o["ids"]), ref)
+        ref = by_id(d["densities"], d["ids"])
+        errs["gpu_vs_fp64_ew_densities"] = elementwise_rel(by_id(g["densities"], o["ids"]), ref)
+        errs["oracle32_vs_fp64_ew_densities"] = elementwise_rel(by_id(o["densities"], o["ids"]), ref)
+    print(label, json.dumps({k: float(f"{v:.3g}") for k, v in {**errs, **ew}.items()}))
+    for k, v in errs.items():
+        if not k.startswith(("gpu_vs_fp64", "oracle32_vs_fp64")):
+            assert v <= RTOL, f"{label}: {k} normwise error {v:.3g} > {RTOL}"
+    assert ew["ew_densities"] <= RTOL, f"{label}: densities element-wise {ew['ew_densities']:.3g}"
+    errs.update(ew)
+    return errs

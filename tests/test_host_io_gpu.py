@@ -110,7 +110,7 @@ def test_state_edited_through_device_pointers_is_stepped():
     substep steps: keys, permutation and offsets bit-exact and the fields within the parity bar
     against the oracle started from the edited state."""
     from tests.helpers import oracle_for
-    from tests.test_parity_gpu import compare_step
+    from tests.helpers import compare_step
 
     w = small_scene(seed=3)
     m = W.build_model(w)

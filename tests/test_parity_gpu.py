@@ -14,7 +14,7 @@ import numpy as np
 import pytest
 
 import vkfluidsim_gb300 as vfs
-from tests.helpers import RTOL, by_id, elementwise_quantile, elementwise_rel, normwise_rel, oracle_for
+from tests.helpers import RTOL, by_id, compare_step, normwise_rel, oracle_for
 from vkfluidsim_gb300 import workloads as W
 
 pytestmark = pytest.mark.gpu
@@ -30,53 +30,6 @@ def np_keys(pos, h, n):
     bh = (blk[:, 0] * 15823 + blk[:, 1] * 9737333 + blk[:, 2] * 440817757) & 0xFFFFFFFF
     hsh = (loc[:, 0] + 50 * (loc[:, 1] + 50 * loc[:, 2]) + bh) & 0xFFFFFFFF
     return (hsh % n).astype(np.uint32)
-
-
-def compare_step(model, oracle, label="", fp64_oracle=None, check_fields=True):
-    """Runs one substep on both and checks the bars; returns the error table."""
-    model.record_fields(True)
-    model.substeps(1)
-    oracle.substeps(1)
-    gk, gp, go = model.get_neighbor_arrays()
-    ok, op, oo = oracle.neighbors()
-    assert np.array_equal(gk, ok), f"{label}: sorted keys differ"
-    assert np.array_equal(gp, op), f"{label}: permutation differs"
-    assert np.array_equal(go, oo), f"{label}: spatial offsets differ"
-    g = model.copy_data_buffers(with_acc=True)
-    o = oracle.state()
-    assert np.array_equal(model.get_ids(), o["ids"])
-    errs = {}
-    if check_fields:
-        bd, bg = model.get_boundary_fields()
-        f = oracle.fields()
-        errs["boundary_density"] = normwise_rel(bd, f["boundary_density"])
-        errs["boundary_gradient"] = normwise_rel(bg, f["boundary_gradient"])
-        errs["accelerations"] = normwise_rel(g["accelerations"], f["accelerations"])
-    errs["densities"] = normwise_rel(g["densities"], o["densities"])
-    errs["velocities"] = normwise_rel(g["velocities"], o["velocities"])
-    errs["positions"] = normwise_rel(g["positions"], o["positions"])
-    # Element-wise: densities relative to themselves, position components relative to max(|x|, h).
-    h = float(model.get_parameters()[0].smooth_radius)
-    ew = {"ew_densities": elementwise_rel(g["densities"], o["densities"]),
-          "ew_positions": elementwise_rel(g["positions"], o["positions"], h),
-          "ew_p999_densities": elementwise_quantile(g["densities"], o["densities"], 0.999),
-          "ew_p999_velocities": elementwise_quantile(g["velocities"], o["velocities"], 0.999,
-                                                     1e-3 * max(float(np.abs(o["velocities"]).max()), 1e-30))}
-    if fp64_oracle is not None:
-        fp64_oracle.substeps(1)
-        d = fp64_oracle.state()
-        for k in ("densities", "velocities", "positions"):
-            ref = by_id(d[k], d["ids"])
-            errs[f"gpu_vs_fp64_{k}"] = normwise_rel(by_id(g[k], o["ids"]), ref)
-            errs[f"oracle32_vs_fp64_{k}"] = normwise_rel(by_id(o[k], o["ids"]), ref)
-    print(label, json.dumps({k: float(f"{v:.3g}") for k, v in {**errs, **ew}.items()}))
-    for k, v in errs.items():
-        if not k.startswith(("gpu_vs_fp64", "oracle32_vs_fp64")):
-            assert v <= RTOL, f"{label}: {k} normwise error {v:.3g} > {RTOL}"
-    assert ew["ew_densities"] <= RTOL, f"{label}: densities element-wise {ew['ew_densities']:.3g}"
-    assert ew["ew_positions"] <= RTOL, f"{label}: positions element-wise {ew['ew_positions']:.3g}"
-    errs.update(ew)
-    return errs
 
 
 @pytest.fixture(scope="module")

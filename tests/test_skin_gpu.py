@@ -11,7 +11,7 @@ import numpy as np
 import pytest
 
 from tests.helpers import RTOL, normwise_rel, oracle_for
-from tests.test_parity_gpu import compare_step
+from tests.helpers import compare_step
 from vkfluidsim_gb300 import workloads as W
 
 pytestmark = pytest.mark.gpu
