@@ -292,27 +292,45 @@ def _mapped_libraries() -> list:
 
 
 def run_reference(args):
-    """The reference arm: the CPU restatement of the reference's shader math (the oracle) on every
-    host thread, on the same workload as the GPU arm: --warmup untimed substeps, then exactly
-    --steps timed substeps (wall clock). It never imports the product package."""
+    """The reference arm, on every host thread, on the same workload as the GPU arm: --warmup
+    untimed substeps, then exactly --steps timed substeps (wall clock). It runs the reference's
+    own step code (its Slang compute shaders compiled as C++ for the host, oracle/_ref, driven in
+    the order of its host code) when that build exists, else the project's CPU restatement of it
+    (the oracle, pinned bit for bit to that build). It never imports the product package."""
     world, rank, _ = dist_env()
     if rank != 0:
         return
     from oracle import binding as ob
+    from oracle import ref_binding as rb
     from oracle.workloads import Obstacle1M
 
     w = Obstacle1M()
-    o = w.oracle()  # boundary grids built with every host thread
-    ob.set_threads(os.cpu_count() or 1)
-    o.substeps(args.warmup)
+    w.objects()  # the sphere's grids, built by the oracle's generator on every host thread
+    threads = os.cpu_count() or 1
+    if rb.available():
+        r = rb.RefShaderModel(w.params(), w.n)
+        for info in w.objects():
+            r.add_object(info)
+        r.set_state(w.pos, w.vel)
+        rb.set_threads(threads)
+        step, kind, cores = r.step, "reference", rb.get_threads()
+        what = ("the reference's step shaders compiled as C++ for the host (oracle/_ref), OpenMP "
+                "over each dispatch's ids; the counting sort's atomic passes in index order")
+    else:
+        o = w.oracle()
+        ob.set_threads(threads)
+        step, kind, cores = o.substeps, "port", ob.get_threads()
+        what = ("the project's CPU restatement of the reference's shader math (oracle), OpenMP "
+                "on all host threads")
+    step(args.warmup)
     t0 = time.perf_counter()
-    o.substeps(args.steps)
+    step(args.steps)
     dt = time.perf_counter() - t0
     value = w.n * args.steps / dt
     libs = _mapped_libraries()
     if any("vkfluidsim_gb300" in p for p in libs):
         raise RuntimeError(f"the reference arm mapped the product library: {libs}")
-    cpu = {"value": value, "unit": UNIT, "cores": ob.get_threads(), "kind": "port",
+    cpu = {"value": value, "unit": UNIT, "cores": cores, "kind": kind,
            "sample": f"{w.name}: {args.steps} substeps of {w.n} particles after {args.warmup} "
                      f"warm-up substeps ({dt:.1f} s wall)"}
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
@@ -325,9 +343,8 @@ def run_reference(args):
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0},
             "libraries_mapped": libs,
-            "note": "the reference's own compute path is Vulkan/Slang and cannot run on this box "
-                    "(no Vulkan stack or software renderer); this is the project's CPU restatement "
-                    "of its shader math (oracle), OpenMP on all host threads"}
+            "note": "the reference's own pipeline is Vulkan/Slang, which cannot run on this box "
+                    "(no Vulkan stack or software renderer); timed here: " + what}
     print(json.dumps(line), flush=True)
 
 

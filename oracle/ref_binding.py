@@ -40,6 +40,8 @@ def load() -> C.CDLL:
         "vfs_ref_set_state": (None, [C.c_void_p, _F, _F]),
         "vfs_ref_step": (None, [C.c_void_p, C.c_int]),
         "vfs_ref_get": (None, [C.c_void_p, _F, _F, _F, _F, _F, _F, _U, _U, _U]),
+        "vfs_ref_set_threads": (None, [C.c_int]),
+        "vfs_ref_get_threads": (C.c_int, []),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -49,13 +51,22 @@ def load() -> C.CDLL:
     return lib
 
 
+def set_threads(t: int) -> None:
+    load().vfs_ref_set_threads(int(t))
+
+
+def get_threads() -> int:
+    return int(load().vfs_ref_get_threads())
+
+
 def _fp(a):
     return a.ctypes.data_as(_F)
 
 
 class RefShaderModel:
-    """The reference's WCSPHWithBoundaryModel step run from its own shader code on the CPU, one
-    thread at a time (the counting sort's atomics in index order: a stable sort)."""
+    """The reference's WCSPHWithBoundaryModel step run from its own shader code on the CPU (the
+    counting sort's atomic passes in index order on one thread: a stable sort; the other
+    dispatches across the host's threads)."""
 
     def __init__(self, params: OracleParams, n: int):
         self._lib = load()

@@ -12,7 +12,8 @@ copied into the repository.
      * ``module`` lines are dropped and each ``import`` is replaced by the imported module's text
        (once per program);
      * ``[shader(..)]``, ``[numthreads(..)]``, ``[[vk::binding(..)]]``, ``public``, ``uniform``
-       and ``: SV_*`` system-value semantics are dropped; ``groupshared`` becomes ``static``;
+       and ``: SV_*`` system-value semantics are dropped; ``groupshared`` becomes
+       ``static thread_local`` (one copy per host thread, which runs one workgroup at a time);
      * ``let`` becomes ``const auto`` and ``var`` becomes ``auto``;
      * namespace access written with a dot (``simulation.parameters``) becomes ``::``;
      * the ``.xyz`` swizzle becomes a call, ``.xyz()``;
@@ -25,8 +26,11 @@ copied into the repository.
    shader entry points in the order of the reference's host code (WCSPHWithBoundaryModel::Step,
    SPHModel::RunSpatialHash, SpatialHash::Run, GPUCountSort::Run, GPUScan::Run,
    SpatialOffset::Run, BufferReorder), one thread at a time; it is compiled with
-   ``-fsingle-precision-constant`` (Slang's unsuffixed float literals are 32-bit) and
-   ``-ffp-contract=off`` into ``oracle/_ref/libvfs_ref_shaders.so``.
+   ``-fsingle-precision-constant`` (Slang's unsuffixed float literals are 32-bit),
+   ``-ffp-contract=off`` and OpenMP into ``oracle/_ref/libvfs_ref_shaders.so``.
+
+``build_generated()`` compiles an already generated ``oracle/_ref/ref_shaders_gen.cpp`` where the
+reference tree is absent (the generated unit travels with the working tree).
 """
 from __future__ import annotations
 
@@ -35,7 +39,11 @@ import subprocess
 import sys
 from pathlib import Path
 
+import os
+
 HERE = Path(__file__).resolve().parent
+# Where build_default() looks for the reference source tree (override: VFS_REFERENCE_TREE).
+REFERENCE_TREE = Path(os.environ.get("VFS_REFERENCE_TREE", "/root/reference"))
 OUT = HERE / "_ref"
 SHIM = HERE / "ref_shim"
 SHADERS = Path("assets/shaders/simulation")
@@ -93,13 +101,13 @@ def translate(text: str) -> str:
     t = re.sub(r"\bpublic\s+", "", t)
     t = re.sub(r"\buniform\s+", "", t)
     t = re.sub(r"\s*:\s*SV_\w+", "", t)
-    t = re.sub(r"\bgroupshared\b", "static", t)
+    t = re.sub(r"\bthread_local\b", "thread_local_", t)
+    t = re.sub(r"\bgroupshared\b", "static thread_local", t)
     t = re.sub(r"\blet\b", "const auto", t)
     t = re.sub(r"\bvar\b", "auto", t)
     t = re.sub(r"\b(simulation|sph_model|wcsph_model)\.", r"\1::", t)
     t = re.sub(r"\.xyz\b(?!\s*\()", ".xyz()", t)
     t = re.sub(r"\b(\w+)\*\s+(\w+)", r"ref_ptr<\1> \2", t)
-    t = re.sub(r"\bthread_local\b", "thread_local_", t)
     return _close_structs(t)
 
 
@@ -132,21 +140,43 @@ def generate(ref: Path) -> Path:
         src.append(flatten(root, root / rel))
         src.append(f"}}  // namespace prog_{name}")
     gen = OUT / "ref_shaders_gen.cpp"
-    gen.write_text("\n".join(src) + "\n")
+    text = "\n".join(src) + "\n"
+    if not gen.exists() or gen.read_text() != text:
+        gen.write_text(text)
     return gen
 
 
 def build(ref: Path) -> Path:
     generate(ref)
+    return build_generated()
+
+
+def build_generated() -> Path:
+    gen = OUT / "ref_shaders_gen.cpp"
+    if not gen.exists():
+        raise FileNotFoundError(f"{gen} has not been generated")
     lib = OUT / "libvfs_ref_shaders.so"
-    cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-fsingle-precision-constant",
-           "-ffp-contract=off", "-Wno-attributes", f"-I{SHIM}", f"-I{OUT}",
+    deps = [gen, SHIM / "ref_harness.cpp", SHIM / "slang_shim.h"]
+    if lib.exists() and all(d.stat().st_mtime <= lib.stat().st_mtime for d in deps):
+        return lib
+    cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-fopenmp", "-fsingle-precision-constant",
+           "-ffp-contract=off", "-U_FORTIFY_SOURCE", "-Wno-attributes", f"-I{SHIM}", f"-I{OUT}",
            str(SHIM / "ref_harness.cpp"), "-o", str(lib)]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("building the reference shaders failed:\n" + " ".join(cmd) + "\n" +
                            r.stdout + r.stderr)
     return lib
+
+
+def build_default():
+    """The build step's entry: regenerates and builds from the reference tree when it is present,
+    else builds an already generated unit, else does nothing. Returns the library or None."""
+    if (REFERENCE_TREE / SHADERS).is_dir():
+        return build(REFERENCE_TREE)
+    if (OUT / "ref_shaders_gen.cpp").exists():
+        return build_generated()
+    return None
 
 
 if __name__ == "__main__":

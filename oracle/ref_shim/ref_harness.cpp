@@ -2,9 +2,12 @@
 //
 // It includes oracle/_ref/ref_shaders_gen.cpp, which oracle/ref_build.py generates from the
 // reference's Slang sources, and runs their entry points in the order of the reference's host
-// code, one thread at a time (a dispatch of G groups of 256 threads runs ids 0..n-1; every entry
-// returns early for larger ids except CalculateBoundaryVolume, whose writes past n the reference
-// leaves unguarded and which runs ids below n only):
+// code. A dispatch of G groups of 256 threads runs ids 0..n-1 (every entry returns early for larger
+// ids except CalculateBoundaryVolume, whose writes past n the reference leaves unguarded and which
+// runs ids below n only). The counting sort's two atomic passes (CalculateCounts, ScatterOutputs)
+// run their ids in index order on one host thread, so the sort is stable; every other entry writes
+// only its own id's outputs and runs its ids across the host's threads (OpenMP), and the scan's
+// workgroups run on separate host threads, each as cooperative fibers:
 //   WCSPHWithBoundaryModel::Step        src/models/wcsph_with_boundary_model.cpp:81-117
 //   SPHModel::RunSpatialHash            src/models/model.cpp:210-223
 //   SpatialHash::Run                    src/compute/spatial_hash.cpp:52-63
@@ -16,6 +19,8 @@
 // (src/scenes/generic_scene.cpp:125-145): the inverse of the object transform and its rotation
 // as glm (column-major) 4x4 matrices, the SDF grid box, resolution, SDF and volume-map grids.
 #include "ref_shaders_gen.cpp"
+
+#include <omp.h>
 
 #include <cstring>
 #include <vector>
@@ -71,13 +76,21 @@ float4x4 from_glm(const float* m) {  // column-major 16 floats -> rows
 }
 
 // ---------------------------------------------------------------- dispatch helpers
+// Ids in index order on the calling thread (the sort's atomic passes).
 template <class F>
-void each(uint32_t n, F f) {
+void each_in_order(uint32_t n, F f) {
     for (uint32_t id = 0; id < n; id++) f(id);
 }
 
-prog_scan::Constants g_scan_k;
-uint g_scan_group;
+// Ids whose writes are disjoint, across the host's threads.
+template <class F>
+void each(uint32_t n, F f) {
+#pragma omp parallel for schedule(static)
+    for (int64_t id = 0; id < (int64_t)n; id++) f((uint32_t)id);
+}
+
+thread_local prog_scan::Constants g_scan_k;
+thread_local uint g_scan_group;
 void scan_block_thread(int t) {
     prog_scan::ScanBlock(g_scan_group * 256u + (uint)t, (uint)t, g_scan_group, g_scan_k);
 }
@@ -94,16 +107,16 @@ void gpu_scan(Model& m, std::vector<uint>& elements, size_t level) {
     k.elements = view(elements);
     k.group_sums = view(sums);
     k.item_count = count;
-    for (uint g = 0; g < num_groups; g++) {
+#pragma omp parallel for schedule(dynamic, 4)
+    for (int64_t g = 0; g < (int64_t)num_groups; g++) {
         g_scan_k = k;
-        g_scan_group = g;
+        g_scan_group = (uint)g;
         slang_shim::run_group(256, scan_block_thread);
     }
     if (num_groups > 1) {
         gpu_scan(m, sums, level + 1);
         k.group_sums = view(m.group_sums[level]);
-        for (uint g = 0; g < num_groups; g++)
-            for (uint t = 0; t < 256u; t++) prog_scan::ScanCombine(g * 256u + t, g, k);
+        each(num_groups * 256u, [&](uint id) { prog_scan::ScanCombine(id, id / 256u, k); });
     }
 }
 
@@ -125,9 +138,9 @@ void run_spatial_hash(Model& m) {
     sk.counts = view(m.counts);
     sk.item_count = n;
     each(n, [&](uint id) { prog_sort::ClearCounts(id, sk); });
-    each(n, [&](uint id) { prog_sort::CalculateCounts(id, sk); });
+    each_in_order(n, [&](uint id) { prog_sort::CalculateCounts(id, sk); });
     gpu_scan(m, m.counts, 0);
-    each(n, [&](uint id) { prog_sort::ScatterOutputs(id, sk); });
+    each_in_order(n, [&](uint id) { prog_sort::ScatterOutputs(id, sk); });
     each(n, [&](uint id) { prog_sort::CopyBack(id, sk); });
     // SpatialOffset::Run with init.
     prog_offsets::Constants ok;
@@ -250,6 +263,12 @@ void* vfs_ref_create(const RefParams* p, uint32_t n) {
 }
 
 void vfs_ref_destroy(void* h) { delete static_cast<Model*>(h); }
+
+void vfs_ref_set_threads(int threads) {
+    if (threads > 0) omp_set_num_threads(threads);
+}
+
+int vfs_ref_get_threads() { return omp_get_max_threads(); }
 
 int vfs_ref_add_object(void* h, const float* transform, const float* rotation, const float* box_size,
                        const float* box_pos, const uint32_t* res, const float* sdf, const float* vm) {

@@ -4,9 +4,9 @@
 // It supplies the HLSL/Slang vocabulary those shaders use: scalar-layout vectors (float3 is 12
 // bytes, as the reference's glm::vec3 buffers), a row-major float4x4 with mul(M, v) = M v, the
 // intrinsics (floor, sqrt, pow, length, dot, min, max, abs, any), ConstantBuffer<T>, the
-// Interlocked adds, and group barriers. Dispatches run thread by thread in id order, so the
-// counting sort's atomics are taken in index order (a stable sort); a kernel with group barriers
-// runs its group's threads as cooperative fibers that switch at every barrier.
+// Interlocked adds (plain adds: the host driver runs the passes that use them in index order on one
+// thread, so the counting sort is stable), and group barriers (a kernel with barriers runs its
+// group's threads as cooperative fibers that switch at every barrier).
 //
 // Buffer pointers are bounds-checked views (ref_ptr): an out-of-range access aborts with a
 // message instead of reading past the buffer, and so do float -> integer conversions that C++
@@ -17,6 +17,8 @@
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
+#include <csetjmp>
+#include <setjmp.h>
 #include <ucontext.h>
 
 typedef uint32_t uint;
@@ -161,21 +163,26 @@ inline void InterlockedAdd(uint& dst, uint v, uint& original) {
 
 // ------------------------------------------------------------------ group barriers
 // A group's threads run as fibers; GroupMemoryBarrierWithGroupSync returns control to the
-// scheduler, which resumes every thread up to its next barrier before any passes it.
+// scheduler, which resumes every thread up to its next barrier before any passes it. A fiber is
+// entered once through its ucontext and afterwards switched with _setjmp/_longjmp (no signal-mask
+// system call per switch). Each host thread has its own scheduler, so different workgroups can
+// run on different host threads.
 namespace slang_shim {
 struct FiberGroup {
     static constexpr int kMaxThreads = 1024;
     static constexpr size_t kStack = 64 * 1024;
-    ucontext_t main_ctx;
+    jmp_buf main_jb;
+    jmp_buf jb[kMaxThreads];
     ucontext_t ctx[kMaxThreads];
     bool done[kMaxThreads];
+    bool started[kMaxThreads];
     char* stacks = nullptr;
     int current = -1;
-    int threads = 0;
     void (*body)(int thread) = nullptr;
+    ~FiberGroup() { std::free(stacks); }
 };
 inline FiberGroup& fibers() {
-    static FiberGroup g;
+    static thread_local FiberGroup g;
     return g;
 }
 inline void fiber_entry() {
@@ -183,21 +190,17 @@ inline void fiber_entry() {
     const int t = g.current;
     g.body(t);
     g.done[t] = true;
+    _longjmp(g.main_jb, 1);
 }
 // Runs body(t) for t in [0, threads) as one workgroup with barrier semantics.
 inline void run_group(int threads, void (*body)(int)) {
     FiberGroup& g = fibers();
     if (threads > FiberGroup::kMaxThreads) fault("workgroup too large", threads);
     if (!g.stacks) g.stacks = static_cast<char*>(std::malloc(FiberGroup::kStack * FiberGroup::kMaxThreads));
-    g.threads = threads;
     g.body = body;
     for (int t = 0; t < threads; t++) {
         g.done[t] = false;
-        getcontext(&g.ctx[t]);
-        g.ctx[t].uc_stack.ss_sp = g.stacks + FiberGroup::kStack * (size_t)t;
-        g.ctx[t].uc_stack.ss_size = FiberGroup::kStack;
-        g.ctx[t].uc_link = &g.main_ctx;
-        makecontext(&g.ctx[t], fiber_entry, 0);
+        g.started[t] = false;
     }
     for (;;) {
         int live = 0;
@@ -205,7 +208,19 @@ inline void run_group(int threads, void (*body)(int)) {
             if (g.done[t]) continue;
             live++;
             g.current = t;
-            swapcontext(&g.main_ctx, &g.ctx[t]);
+            if (!_setjmp(g.main_jb)) {
+                if (!g.started[t]) {
+                    g.started[t] = true;
+                    getcontext(&g.ctx[t]);
+                    g.ctx[t].uc_stack.ss_sp = g.stacks + FiberGroup::kStack * (size_t)t;
+                    g.ctx[t].uc_stack.ss_size = FiberGroup::kStack;
+                    g.ctx[t].uc_link = nullptr;
+                    makecontext(&g.ctx[t], fiber_entry, 0);
+                    setcontext(&g.ctx[t]);
+                } else {
+                    _longjmp(g.jb[t], 1);
+                }
+            }
         }
         if (!live) break;
     }
@@ -216,5 +231,5 @@ inline void run_group(int threads, void (*body)(int)) {
 inline void GroupMemoryBarrierWithGroupSync() {
     slang_shim::FiberGroup& g = slang_shim::fibers();
     if (g.current < 0) slang_shim::fault("group barrier outside a workgroup");
-    swapcontext(&g.ctx[g.current], &g.main_ctx);
+    if (!_setjmp(g.jb[g.current])) _longjmp(g.main_jb, 1);
 }

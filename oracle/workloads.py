@@ -79,17 +79,24 @@ class Obstacle1M:
                                (C.c_float * 3)(2.0, 1.0, 1.0), (C.c_float * 3)(0.0, 0.0, 0.0),
                                1e4, 50.0, 7.0, 0.01)
 
+    def objects(self):
+        """The sphere as a boundary object: grids from the oracle's volume-map generator (margin
+        8 h, 16-point quadrature), built once."""
+        if getattr(self, "_objects", None) is None:
+            res = (self.map_res,) * 3
+            bs, bp, sdf, vm = ob.volume_map(SHAPE_SPHERE, (self.sphere_radius,), self.h, res,
+                                            np.float32(8.0 * self.h))
+            t = np.eye(4, dtype=np.float32)
+            t[:3, 3] = -np.asarray(self.sphere_center, np.float32)
+            self._objects = [type("Obj", (), dict(
+                transform=t.T.ravel(), rotation=np.eye(4, dtype=np.float32).ravel(), box_size=bs,
+                box_pos=bp, resolution=res, sdf=sdf, volume_map=vm))]
+        return self._objects
+
     def oracle(self) -> ob.OracleModel:
-        """The oracle model of the scene at its initial state; the sphere's grids come from the
-        oracle's own volume-map generator (margin 8 h, 16-point quadrature)."""
+        """The oracle model of the scene at its initial state."""
         o = ob.OracleModel(self.params(), self.n)
-        res = (self.map_res,) * 3
-        bs, bp, sdf, vm = ob.volume_map(SHAPE_SPHERE, (self.sphere_radius,), self.h, res,
-                                        np.float32(8.0 * self.h))
-        t = np.eye(4, dtype=np.float32)
-        t[:3, 3] = -np.asarray(self.sphere_center, np.float32)
-        o.add_object(type("Obj", (), dict(
-            transform=t.T.ravel(), rotation=np.eye(4, dtype=np.float32).ravel(), box_size=bs,
-            box_pos=bp, resolution=res, sdf=sdf, volume_map=vm)))
+        for info in self.objects():
+            o.add_object(info)
         o.set_state(self.pos, self.vel)
         return o
