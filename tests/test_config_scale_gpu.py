@@ -88,15 +88,16 @@ def test_batch_256_scenes_equal_each_scene_alone(batch256):
     scenes, b = batch256["scenes"], batch256["batch"]
     assert len(scenes) == 256 and sum(w.n for w in scenes) > 4_000_000
     assert batch256["substeps"] == 5
-    states = [b.copy_data_buffers(s) for s in range(len(scenes))]
+    states = [dict(b.copy_data_buffers(s), ids=b.get_ids(s)) for s in range(len(scenes))]
     b.substeps(1)
     batch256["substeps"] += 1
     worst, worst_ew, worst_drift = 0.0, 0.0, 0.0
     for s, w in enumerate(scenes):
         m = W.build_model(w)
         m.substeps(5)  # the continuous run, as a loop of plain models would do it
-        c = m.copy_data_buffers()
-        drift = max(normwise_rel(c[k], states[s][k]) for k in ("positions", "densities"))
+        c, cid, st = m.copy_data_buffers(), m.get_ids(), states[s]
+        drift = max(normwise_rel(by_id(c[k], cid), by_id(st[k], st["ids"]))
+                    for k in ("positions", "densities"))
         worst_drift = max(worst_drift, drift)
         assert drift <= 1e-4, (s, drift)
         m.set_particle_state(states[s]["positions"], states[s]["velocities"])

@@ -455,11 +455,12 @@ Model::~Model() {
     cudaFree(skin.count);
     cudaFree(skin.x_build);
     cudaFree(skin.b_of_id);
-    cudaFree(skin.cur);
+    cudaFree(skin.xcur);
     cudaFree(skin.stale);
     cudaFree(skin.ctl);
     cudaFree(skin.queue);
     cudaFree(skin.seg_n);
+    cudaFree(skin.wcount);
     cudaFree(scratch);
     cudaFree(err);
     if (err_host) cudaFreeHost(err_host);
@@ -564,26 +565,29 @@ int Model::alloc_skin() {
         cudaMalloc(&s.count, N * sizeof(uint32_t)) != cudaSuccess ||
         cudaMalloc(&s.x_build, N * sizeof(float4)) != cudaSuccess ||
         cudaMalloc(&s.b_of_id, N * sizeof(uint32_t)) != cudaSuccess ||
-        cudaMalloc(&s.cur, N * sizeof(uint32_t)) != cudaSuccess ||
+        cudaMalloc(&s.xcur, N * sizeof(float4)) != cudaSuccess ||
         cudaMalloc(&s.stale, scenes.size() * sizeof(uint32_t)) != cudaSuccess ||
         cudaMalloc(&s.ctl, scenes.size() * kSkinCtl * sizeof(uint32_t)) != cudaSuccess ||
         cudaMalloc(&s.queue, N * sizeof(uint32_t)) != cudaSuccess ||
-        cudaMalloc(&s.seg_n, ((N + 127) / 128) * sizeof(uint32_t)) != cudaSuccess) {
+        cudaMalloc(&s.seg_n, ((N + 127) / 128) * sizeof(uint32_t)) != cudaSuccess ||
+        cudaMalloc(&s.wcount, sizeof(uint32_t)) != cudaSuccess) {
         cudaGetLastError();  // out of memory is not sticky: clear it and go on without lists
         cudaFree(s.list);
         cudaFree(s.count);
         cudaFree(s.x_build);
         cudaFree(s.b_of_id);
-        cudaFree(s.cur);
+        cudaFree(s.xcur);
         cudaFree(s.stale);
         cudaFree(s.ctl);
         cudaFree(s.queue);
         cudaFree(s.seg_n);
+        cudaFree(s.wcount);
         return VFS_OK;
     }
     VFS_CUDA_TRY(cudaMemset(s.count, 0, N * sizeof(uint32_t)));
     VFS_CUDA_TRY(cudaMemset(s.b_of_id, 0, N * sizeof(uint32_t)));  // any index below n until a build
     VFS_CUDA_TRY(cudaMemset(s.stale, 0, scenes.size() * sizeof(uint32_t)));
+    VFS_CUDA_TRY(cudaMemset(s.wcount, 0, sizeof(uint32_t)));
     skin = s;
     return invalidate_skin();
 }

@@ -139,12 +139,14 @@ struct SkinLists {
     uint32_t* count = nullptr;    // per build index: list length, kSkinUsable when it can be summed
     float4* x_build = nullptr;    // per build index: position at the last build
     uint32_t* b_of_id = nullptr;  // per id: build index
-    uint32_t* cur = nullptr;      // per build index: current sorted index (written by the cell pass)
+    float4* xcur = nullptr;       // per build index: current position (x, y, z) and current sorted
+                                  // index (w, as bits), written by the cell pass
     uint32_t* stale = nullptr;    // per scene: nonzero when some particle moved past h skin / 2
     uint32_t* ctl = nullptr;      // per scene, kSkinCtl words: the build policy's state (kCtl*)
     uint32_t* queue = nullptr;    // the particles the density pass walks this substep: those of
                                   // list block b at [128 b, 128 b + seg_n[b]), in index order
     uint32_t* seg_n = nullptr;    // per list block (128 particles): its walkers
+    uint32_t* wcount = nullptr;   // single scene: walkers in `queue`, packed from 0 (one word)
     uint32_t cap = 0;             // slots per particle
 };
 constexpr uint32_t kSkinUsable = 1u << 31;

@@ -525,7 +525,7 @@ __global__ void __launch_bounds__(kCellBlock)
                     float4* __restrict__ pos_out, float4* __restrict__ vel_out,
                     uint32_t* __restrict__ zero, uint32_t zero_words,
                     uint32_t* __restrict__ pkeys_out, uint32_t* guess,
-                    const uint32_t* __restrict__ b_of_id, uint32_t* __restrict__ cur,
+                    const uint32_t* __restrict__ b_of_id, float4* __restrict__ xcur,
                     const float4* __restrict__ x_build, uint32_t* __restrict__ stale) {
     __shared__ uint32_t s_lo, s_hi;
     // The sort is done with its scratch (histograms, tile counters, look-back status): clear it
@@ -555,13 +555,14 @@ __global__ void __launch_bounds__(kCellBlock)
         const float4 x = __ldg(pos_in + src);
         pos_out[i] = x;
         vel_out[i] = __ldg(vel_in + src);
-        if (cur) {
-            // Skin lists: where the particle's build index sits now, and its displacement since
-            // the build.
+        if (xcur) {
+            // Skin lists: the particle's current position and sorted index under its build
+            // index (the list pass gathers both with one load), and its displacement since the
+            // build.
             const uint32_t id = __float_as_uint(x.w);
             const uint32_t bi = id < n ? __ldg(b_of_id + id) : n;
             if (bi < n) {
-                cur[bi] = i;
+                xcur[bi] = make_float4(x.x, x.y, x.z, __uint_as_float(i));
                 const float4 b = __ldg(x_build + bi);
                 const float dx = x.x - b.x, dy = x.y - b.y, dz = x.z - b.z;
                 const uint32_t sc = L.n_scenes > 1 ? (uint32_t)__ldg(L.scene_of + i) : 0u;
@@ -573,7 +574,7 @@ __global__ void __launch_bounds__(kCellBlock)
         if (pkeys_out) pkeys_out[i] = skeys[i];
     }
     // Stale scenes, one atomic per warp and scene at most (most particles of a fast scene exceed).
-    if (cur) {
+    if (xcur) {
         const uint32_t m = __ballot_sync(0xffffffffu, exceed);
         if (exceed) {
             const uint32_t g = __match_any_sync(m, exceed_sc);
@@ -925,11 +926,13 @@ __global__ void __launch_bounds__(kNbrBlock, kMinBlocks)
         uint32_t i = t, sc = 0u;
         bool rebuild = false;
         if (sk.list) {
-            if (kBatch || (sk.stale[0] == 0u && sk.ctl[kCtlPoor] == 0u)) {
+            if (kBatch) {
                 // Slot t of the queue: valid below its list block's count of walkers.
                 if (t % kListBlock >= __ldg(sk.seg_n + t / kListBlock)) return;
                 i = __ldg(sk.queue + t);
-                sc = kBatch ? (uint32_t)__ldg(L.scene_of + i) : 0u;
+                sc = (uint32_t)__ldg(L.scene_of + i);
+            } else if (sk.stale[0] == 0u && sk.ctl[kCtlPoor] == 0u) {
+                return;  // k_density_walkers walks the single scene's queued particles
             }  // else a single scene that is stale or whose lists are mostly unusable: every
                // particle, in index order (no queue)
             rebuild = sk.stale[sc] != 0u && sk.ctl[sc * kSkinCtl + kCtlAllow] != 0u;
@@ -1055,37 +1058,46 @@ __global__ void __launch_bounds__(kListBlock, 8)
                     for (int u = 0; u < 4; u++) jn[u] = __ldg(q + (4 + u) * stride);
                 }
 #pragma unroll
-                for (int u = 0; u < 4; u++) j[u] = __ldg(sk.cur + j[u]);
-#pragma unroll
-                for (int u = 0; u < 4; u++) xj[u] = __ldg(pos + j[u]);
+                for (int u = 0; u < 4; u++) xj[u] = __ldg(sk.xcur + j[u]);  // position, sorted index
 #pragma unroll
                 for (int u = 0; u < 4; u++)
-                    if (in_range2(xi, xj[u]) <= h2) d.add(i, xi, j[u], xj[u], s_inv_h, s_nbr_cap, L.total);
+                    if (in_range2(xi, xj[u]) <= h2)
+                        d.add(i, xi, __float_as_uint(xj[u].w), xj[u], s_inv_h, s_nbr_cap, L.total);
             }
 #pragma unroll 1
             for (; k < n_list; k++, q += stride) {
-                const uint32_t j = __ldg(sk.cur + __ldg(q));
-                const float4 xj = __ldg(pos + j);
-                if (in_range2(xi, xj) <= h2) d.add(i, xi, j, xj, s_inv_h, s_nbr_cap, L.total);
+                const float4 xj = __ldg(sk.xcur + __ldg(q));
+                if (in_range2(xi, xj) <= h2)
+                    d.add(i, xi, __float_as_uint(xj.w), xj, s_inv_h, s_nbr_cap, L.total);
             }
             density_finish(p, i, xi, vel, cx, cy, cz, distinct_keys(p, cx, cy, cz), d, rec, aux,
                            bnd, nbr_count);
         }
     }
-    // The walkers go to this block's segment of the queue, in index order.
+    // The walkers go to the queue in index order within the block: batched, to this block's
+    // segment (k_density takes slot t below its segment's count); a single scene, packed from 0
+    // in blocks claimed by one atomic each (k_density_walkers takes one walker per warp).
     __shared__ uint32_t s_cnt[kListBlock / 32];
+    __shared__ uint32_t s_base;
     const uint32_t m = __ballot_sync(0xffffffffu, walk);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     if (lane == 0) s_cnt[warp] = (uint32_t)__popc(m);
     __syncthreads();
-    uint32_t base = blockIdx.x * kListBlock, total = 0u;
+    uint32_t base = 0u, total = 0u;
 #pragma unroll
     for (int w = 0; w < kListBlock / 32; w++) {
         base += w < warp ? s_cnt[w] : 0u;
         total += s_cnt[w];
     }
+    if (kBatch) {
+        base += blockIdx.x * kListBlock;
+        if (threadIdx.x == 0) sk.seg_n[blockIdx.x] = total;
+    } else {
+        if (threadIdx.x == 0) s_base = total ? atomicAdd(sk.wcount, total) : 0u;
+        __syncthreads();
+        base += s_base;  // at most L.total walkers in all: the slots stay inside the queue
+    }
     if (walk) sk.queue[base + (uint32_t)__popc(m & ((1u << lane) - 1u))] = i;
-    if (threadIdx.x == 0) sk.seg_n[blockIdx.x] = total;
 }
 
 // W(|x_j - x_i|) / sigma with the density drain's explicitly rounded arithmetic.
@@ -1100,6 +1112,124 @@ __device__ __forceinline__ float w_over_sigma(const float4& xi, const float4& xj
     const float w_in = __fmaf_rn(6.0f, __fmul_rn(q2, q), __fmaf_rn(-6.0f, q2, 1.0f));
     return q <= 1.0f ? (q > 0.5f ? w_out : w_in) : 0.0f;
 }
+
+// Warps per block of k_density_walkers.
+constexpr int kWalkerWarps = 4;
+
+// The density pass of a single scene's walkers (the particles k_density_list queued: no usable
+// list this substep), one warp per walker, so a walker's ~280 candidates are tested 32 at a time
+// instead of in one thread's chain of dependent loads. Lane r < 27 holds candidate segment r of
+// the walk (row r / 3, part r % 3 of the rows of for_each_candidate: the same buckets, the same
+// pruning), the segments' candidates are numbered in visiting order and taken in chunks of 32,
+// and the in-range ones are summed in visiting order (every lane adds them one by one through
+// shuffles) and listed in visiting order: exactly the sum and the list of the one-thread walk.
+__global__ void __launch_bounds__(kWalkerWarps * 32)
+    k_density_walkers(StepLaunch L, const float4* __restrict__ pos, const float4* __restrict__ vel,
+                      float4* __restrict__ rec, const uint32_t* __restrict__ scan,
+                      float4* __restrict__ aux, float4* __restrict__ bnd, uint32_t* __restrict__ nbr,
+                      uint32_t* __restrict__ nbr_count, SkinLists sk) {
+    if (sk.stale[0] != 0u || sk.ctl[kCtlPoor] != 0u) return;  // k_density walks every particle
+    const uint32_t walkers = min(*sk.wcount, L.total);
+    const int lane = threadIdx.x & 31;
+    const uint32_t lt = (1u << lane) - 1u;
+    const SceneParams& p = L.one;
+    const uint32_t* sc = scan + p.off;
+    for (uint32_t w = blockIdx.x * kWalkerWarps + (threadIdx.x >> 5); w < walkers;
+         w += gridDim.x * kWalkerWarps) {
+        const uint32_t i = __ldg(sk.queue + w);
+        const float4 xi = __ldg(pos + i);
+        const uint32_t cx = cell_coord(xi.x, p.h), cy = cell_coord(xi.y, p.h),
+                       cz = cell_coord(xi.z, p.h);
+        const bool distinct = distinct_keys(p, cx, cy, cz);
+        // Segment r of the walk: [b, b + len).
+        uint32_t b = 0u, len = 0u;
+        if (lane < 27) {
+            const float lim = distinct ? kPruneLimit : 1e30f;
+            const float fx = fmaf(-(float)(int)cx, p.h, xi.x) * p.inv_h;
+            const float fy = fmaf(-(float)(int)cy, p.h, xi.y) * p.inv_h;
+            const float fz = fmaf(-(float)(int)cz, p.h, xi.z) * p.inv_h;
+            const int t = lane / 3, part = lane % 3;
+            const uint32_t dy = (uint32_t)(t % 3) - 1u, dz = (uint32_t)(t / 3) - 1u;
+            const float dyz = face_dist2(dy, fy) + face_dist2(dz, fz);
+            if (dyz <= lim) {
+                const bool skip_l = dyz + face_dist2(0xFFFFFFFFu, fx) > lim;
+                const bool skip_r = dyz + face_dist2(1u, fx) > lim;
+                const uint32_t ry = cy + dy, rz = cz + dz;
+                const uint32_t hA = hash_cell(cx - 1u, ry, rz);
+                const uint32_t kA = key_mod(hA, p.mod_magic, p.n);
+                const bool same_block = (cx + 24u) / 50u == (cx + 26u) / 50u && hA <= 0xFFFFFFFDu;
+                uint32_t e = 0u;
+                if (same_block && kA + 2u < p.n) {
+                    if (part == 0) {
+                        b = __ldg(sc + kA + (skip_l ? 1u : 0u));
+                        e = __ldg(sc + kA + (skip_r ? 2u : 3u));
+                    }
+                } else if (part == 0) {
+                    b = __ldg(sc + kA);
+                    e = skip_l ? b : __ldg(sc + kA + 1u);
+                } else if (part == 1) {
+                    const uint32_t kB = key_mod(hash_cell(cx, ry, rz), p.mod_magic, p.n);
+                    b = __ldg(sc + kB);
+                    e = __ldg(sc + kB + 1u);
+                } else if (!skip_r) {
+                    const uint32_t kC = key_mod(hash_cell(cx + 1u, ry, rz), p.mod_magic, p.n);
+                    b = __ldg(sc + kC);
+                    e = __ldg(sc + kC + 1u);
+                }
+                len = e > b ? e - b : 0u;
+            }
+        }
+        // Exclusive prefix of the segment lengths: the visiting-order number of each segment's
+        // first candidate.
+        uint32_t incl = len;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += v;
+        }
+        const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+        const uint32_t start = incl - len;
+        float rho = 0.0f;
+        uint32_t listed = 0u;
+        for (uint32_t base = 0; base < total; base += 32u) {
+            const uint32_t f = base + (uint32_t)lane;
+            // The segment holding candidate f: the last one starting at or before f.
+            int r = 0;
+#pragma unroll
+            for (int step = 16; step >= 1; step >>= 1) {
+                const uint32_t s_probe = __shfl_sync(0xffffffffu, start, (r + step) & 31);
+                if (r + step < 27 && s_probe <= f) r += step;
+            }
+            const uint32_t rb = __shfl_sync(0xffffffffu, b, r);
+            const uint32_t rs = __shfl_sync(0xffffffffu, start, r);
+            const bool valid = f < total;
+            const uint32_t j = rb + (f - rs);
+            float4 xj = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (valid) xj = __ldg(pos + j);
+            const bool inr = valid && in_range2(xi, xj) <= p.h2;
+            const float wv = inr ? w_over_sigma(xi, xj, p.inv_h) : 0.0f;
+            uint32_t mask = __ballot_sync(0xffffffffu, inr);
+            const uint32_t listm = __ballot_sync(0xffffffffu, inr && j != i);
+            if (inr && j != i) {
+                const uint32_t slot = listed + (uint32_t)__popc(listm & lt);
+                if (slot < p.nbr_cap) nbr[(size_t)slot * L.total + i] = j;
+            }
+            listed += (uint32_t)__popc(listm);
+            while (mask) {
+                const int l = __ffs(mask) - 1;
+                rho = __fadd_rn(rho, __shfl_sync(0xffffffffu, wv, l));
+                mask &= mask - 1u;
+            }
+        }
+        if (lane == 0) {
+            DensitySum d;
+            d.rho = rho;
+            d.listed = listed;
+            density_finish(p, i, xi, vel, cx, cy, cz, distinct, d, rec, aux, bnd, nbr_count);
+        }
+    }
+}
+
 
 // Small models, where three lanes per particle still fit one wave of the GPU and one lane per
 // particle would leave the SMs waiting on each thread's chain of candidate loads: the density pass
@@ -1767,15 +1897,15 @@ cudaError_t launch_cells_reorder(const StepLaunch& L, uint32_t n, const uint32_t
     switch (kc.cell_block) {
         case 128:
             k_cells_reorder<128><<<(n + 128u) / 128u, 128, 0, s>>>(L, n, skeys, perm, cell_scan, pos_in,
-                                                                 vel_in, pos_out, vel_out, zero, zero_words, pkeys_out, guess, sk.b_of_id, sk.cur, sk.x_build, sk.stale);
+                                                                 vel_in, pos_out, vel_out, zero, zero_words, pkeys_out, guess, sk.b_of_id, sk.xcur, sk.x_build, sk.stale);
             break;
         case 512:
             k_cells_reorder<512><<<(n + 512u) / 512u, 512, 0, s>>>(L, n, skeys, perm, cell_scan, pos_in,
-                                                                 vel_in, pos_out, vel_out, zero, zero_words, pkeys_out, guess, sk.b_of_id, sk.cur, sk.x_build, sk.stale);
+                                                                 vel_in, pos_out, vel_out, zero, zero_words, pkeys_out, guess, sk.b_of_id, sk.xcur, sk.x_build, sk.stale);
             break;
         default:
             k_cells_reorder<256><<<(n + 256u) / 256u, 256, 0, s>>>(L, n, skeys, perm, cell_scan, pos_in,
-                                                                 vel_in, pos_out, vel_out, zero, zero_words, pkeys_out, guess, sk.b_of_id, sk.cur, sk.x_build, sk.stale);
+                                                                 vel_in, pos_out, vel_out, zero, zero_words, pkeys_out, guess, sk.b_of_id, sk.xcur, sk.x_build, sk.stale);
     }
     return cudaGetLastError();
 }
@@ -1799,12 +1929,18 @@ void density_shape(const StepLaunch& L, const float4* pos, const float4* vel, fl
                    uint32_t* nbr_count, const SkinLists& sk, cudaStream_t s) {
     const uint32_t blocks = (L.total + B - 1) / B;
     if (sk.list) {
-        // Skin lists: the list pass first; the walk pass then takes the queue it leaves.
+        // Skin lists: the list pass first; the walk passes then take the queue it leaves.
         const uint32_t lb = (L.total + kListBlock - 1) / kListBlock;
-        if (L.n_scenes > 1)
+        if (L.n_scenes > 1) {
             k_density_list<true><<<lb, kListBlock, 0, s>>>(L, pos, vel, rec, aux, bnd, nbr, nbr_count, sk);
-        else
+        } else {
+            cudaMemsetAsync(sk.wcount, 0, sizeof(uint32_t), s);
             k_density_list<false><<<lb, kListBlock, 0, s>>>(L, pos, vel, rec, aux, bnd, nbr, nbr_count, sk);
+            const int sms = sm_count();
+            const uint32_t wb = (uint32_t)(sms > 0 ? sms : 148) * 8u;  // 32 warps per SM
+            k_density_walkers<<<wb, kWalkerWarps * 32, 0, s>>>(L, pos, vel, rec, cell_scan, aux, bnd,
+                                                               nbr, nbr_count, sk);
+        }
     }
     if (L.n_scenes > 1)
         k_density<true, B, M><<<blocks, B, 0, s>>>(L, pos, vel, rec, cell_scan, aux, bnd, nbr, nbr_count, sk);
