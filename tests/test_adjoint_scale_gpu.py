@@ -71,7 +71,7 @@ def _host_grads(w, target):
     v0 = torch.zeros((w.n, 3), dtype=torch.float64, device="cuda", requires_grad=True)
     loss = ((R.rollout(w, nu, k, v0, STEPS, EVERY, grad=True) - tgt) ** 2).mean()
     loss.backward()
-    return {"loss": float(loss), "dnu": float(nu.grad), "dk": float(k.grad),
+    return {"loss": float(loss.detach()), "dnu": float(nu.grad), "dk": float(k.grad),
             "dv0": v0.grad.cpu().numpy()}
 
 
