@@ -222,6 +222,12 @@ int32_t vfs_model_get_neighbor_capacity(const vfs_model* m);
  * per particle) have no lists; the getter then reports 0. */
 int vfs_model_set_skin(vfs_model* m, float skin);
 int vfs_model_get_skin(const vfs_model* m, float* skin);
+/* Block-per-cell staging in the density pass's bucket walk (CalculateDensities,
+ * wcsph_with_boundary_model.slang:153-197), on by default: a warp whose particles share one row of
+ * cells loads the 3 x 3 rows of cells around it into shared memory once and tests every staged
+ * particle against each of its own, instead of each thread walking its 27 buckets from global
+ * memory. Results are bit-identical either way; 0 turns it off. */
+int vfs_model_set_walk_staging(vfs_model* m, int32_t enable);
 /* Number of list builds so far (synchronises the handle's stream). */
 int vfs_model_get_skin_builds(vfs_model* m, uint32_t* builds);
 /* Device pointers of the current state: float4 (x, y, z, id bits) and (vx, vy, vz, 0). They stay
@@ -343,6 +349,7 @@ int vfs_batch_profile_substeps(vfs_batch* b, int32_t count, float* phase_ms);
 int vfs_batch_set_sort_config(vfs_batch* b, int32_t digit_bits, int32_t tile_items);
 int vfs_batch_set_neighbor_capacity(vfs_batch* b, int32_t slots);
 int vfs_batch_set_skin(vfs_batch* b, float skin);
+int vfs_batch_set_walk_staging(vfs_batch* b, int32_t enable);
 int vfs_batch_get_skin(const vfs_batch* b, float* skin);
 int vfs_batch_get_skin_builds(vfs_batch* b, uint32_t scene, uint32_t* builds);
 int vfs_batch_export_state(vfs_batch* b, int32_t scene, const char* path_prefix);

@@ -160,6 +160,8 @@ SIGNATURES = {
     "vfs_model_set_neighbor_capacity": (_I, [_P, C.c_int32]),
     "vfs_model_set_skin": (_I, [_P, C.c_float]),
     "vfs_model_get_skin": (_I, [_P, C.POINTER(C.c_float)]),
+    "vfs_model_set_walk_staging": (_I, [_P, C.c_int32]),
+    "vfs_batch_set_walk_staging": (_I, [_P, C.c_int32]),
     "vfs_batch_set_skin": (_I, [_P, C.c_float]),
     "vfs_batch_get_skin": (_I, [_P, C.POINTER(C.c_float)]),
     "vfs_model_get_skin_builds": (_I, [_P, C.POINTER(C.c_uint32)]),

@@ -1340,6 +1340,13 @@ int vfs_model_set_skin(vfs_model* h, float skin) {
     return vfs::set_skin(m, skin);
 }
 
+int vfs_model_set_walk_staging(vfs_model* h, int32_t enable) {
+    VFS_HANDLE(h);
+    m.kc.walk_staging = enable != 0;
+    m.invalidate_graph();
+    return VFS_OK;
+}
+
 int vfs_model_get_skin_builds(vfs_model* h, uint32_t* builds) {
     VFS_HANDLE(h);
     if (!builds) return vfs::fail(VFS_ERR_INVALID_ARGUMENT, "NULL output");
@@ -1513,6 +1520,13 @@ int vfs_batch_profile_substeps(vfs_batch* h, int32_t count, float* phase_ms) {
 int vfs_batch_set_neighbor_capacity(vfs_batch* h, int32_t slots) {
     VFS_HANDLE(h);
     return vfs::set_neighbor_capacity(m, slots);
+}
+
+int vfs_batch_set_walk_staging(vfs_batch* h, int32_t enable) {
+    VFS_HANDLE(h);
+    m.kc.walk_staging = enable != 0;
+    m.invalidate_graph();
+    return VFS_OK;
 }
 
 int vfs_batch_set_skin(vfs_batch* h, float skin) {

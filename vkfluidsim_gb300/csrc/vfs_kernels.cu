@@ -21,6 +21,7 @@
 #include <stdint.h>
 
 #include <algorithm>
+#include <climits>
 #include <atomic>
 
 #include "vfs_internal.h"
@@ -911,63 +912,152 @@ __device__ __forceinline__ void density_finish(const SceneParams& p, uint32_t i,
 // k_density_list left in its queue, one per thread: each list block's walkers in index order, so
 // a stale scene is walked in index order and a warp whose slots are empty returns at once. In a
 // stale scene whose build policy allows it, every particle also builds its skin list.
+// Block-per-cell staging of the neighbourhood, one warp at a time: when a warp's particles share
+// one row of cells (same scene, same y and z cells, at most four consecutive x cells) and the
+// 3 x 3 rows of cells around them (x from the first cell - 1 to the last + 1) lie in one 50^3 hash
+// block whose keys do not wrap, every row of that union is one run of consecutive keys, hence one
+// contiguous range of the sorted particles, and all of the union's keys are distinct (n > 5110:
+// the union's hashes span at most 5105). The warp then stages each row's particles in shared
+// memory 32 at a time and every lane tests all of them against its particle. Every in-range
+// candidate of a particle lies in its own 27 cells, each of its 27 buckets is met once (distinct
+// keys), and rows and candidates are met in the reference's visiting order, so the in-range
+// sequence and hence the sum are exactly the bucket walk's. Returns false when the warp does not
+// qualify; otherwise the union's first x cell's row keys start at key_lo and each row spans
+// `width` keys. Warp-uniform.
+__device__ __forceinline__ bool warp_row_union(const SceneParams& p, bool act, bool ok, uint32_t cx,
+                                               uint32_t cy, uint32_t cz, uint32_t sc,
+                                               uint32_t& key_lo, uint32_t& width) {
+    const uint32_t am = __ballot_sync(0xffffffffu, act);
+    const int leader = __ffs(am) - 1;
+    const uint32_t cy0 = __shfl_sync(0xffffffffu, cy, leader);
+    const uint32_t cz0 = __shfl_sync(0xffffffffu, cz, leader);
+    const uint32_t sc0 = __shfl_sync(0xffffffffu, sc, leader);
+    int lo = act ? (int)cx : INT_MAX, hi = act ? (int)cx : INT_MIN;
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) {
+        lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+        hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+    }
+    const bool same = !act || (ok && cy == cy0 && cz == cz0 && sc == sc0);
+    if (!__all_sync(0xffffffffu, same)) return false;
+    if ((int64_t)hi - (int64_t)lo > 3 || p.n <= 5110u) return false;
+    const uint32_t c0 = (uint32_t)lo - 1u, c1 = (uint32_t)hi + 1u;
+    if ((c0 + 25u) / 50u != (c1 + 25u) / 50u || (cy0 + 24u) / 50u != (cy0 + 26u) / 50u ||
+        (cz0 + 24u) / 50u != (cz0 + 26u) / 50u)
+        return false;
+    const uint32_t h_lo = hash_cell(c0, cy0 - 1u, cz0 - 1u);
+    const uint32_t h_hi = hash_cell(c1, cy0 + 1u, cz0 + 1u);
+    if (h_hi < h_lo) return false;  // the block's hashes wrap past 2^32
+    const uint32_t k_lo = key_mod(h_lo, p.mod_magic, p.n);
+    if ((uint64_t)k_lo + (h_hi - h_lo) >= p.n) return false;  // keys wrap past n - 1
+    key_lo = k_lo;
+    width = c1 - c0 + 1u;
+    return true;
+}
+
+// CalculateBoundaryVolume + CalculateDensities + the per-particle part of PressureFromDensityEOS
+// (wcsph_with_boundary_model.slang:102-203), by the bucket walk. Besides the density products it
+// writes particle i's neighbour list: every in-range j except i itself, in visiting order,
+// slot-major (nbr[s * n + i], so a warp's lanes store and later load consecutive words), and its
+// length in nbr_count[i] (a length above nbr_cap means the list overflowed and was truncated).
+// Positions do not change before the force pass, so that list is exactly the force pass's
+// neighbour set. Without skin lists every particle is walked. With them, the particles
+// k_density_list left in its queue, one per thread: each list block's walkers in index order, so
+// a stale scene is walked in index order and a warp whose slots are empty returns at once. In a
+// stale scene whose build policy allows it, every particle also builds its skin list. A warp
+// whose particles share a row of cells walks the staged rows of warp_row_union; any other warp
+// walks per thread (for_each_candidate).
 template <bool kBatch, int kNbrBlock, int kMinBlocks>
 __global__ void __launch_bounds__(kNbrBlock, kMinBlocks)
     k_density(StepLaunch L, const float4* __restrict__ pos, const float4* __restrict__ vel,
               float4* __restrict__ rec, const uint32_t* __restrict__ scan,
               float4* __restrict__ aux, float4* __restrict__ bnd, uint32_t* __restrict__ nbr,
-              uint32_t* __restrict__ nbr_count, SkinLists sk) {
+              uint32_t* __restrict__ nbr_count, SkinLists sk, bool staging) {
     static_assert(kSkinCap <= (uint32_t)kListCap, "a list build is staged in the shared list");
+    static_assert(kNbrBlock % 32 == 0, "whole warps");
     __shared__ uint32_t s_j[kListCap * kNbrBlock];
+    __shared__ float4 s_stage[kNbrBlock];  // each warp's 32 staged candidates
     const int tid = threadIdx.x;
-    {
-        const uint32_t t = blockIdx.x * kNbrBlock + tid;
-        if (t >= L.total) return;
-        uint32_t i = t, sc = 0u;
-        bool rebuild = false;
-        if (sk.list) {
-            if (kBatch) {
-                // Slot t of the queue: valid below its list block's count of walkers.
-                if (t % kListBlock >= __ldg(sk.seg_n + t / kListBlock)) return;
+    const uint32_t lane = (uint32_t)(tid & 31);
+    // No lane returns before the warp's collective steps: inactive lanes carry act = false.
+    const uint32_t t = blockIdx.x * kNbrBlock + tid;
+    bool act = t < L.total;
+    uint32_t i = act ? t : 0u, sc = 0u;
+    bool rebuild = false;
+    if (act && sk.list) {
+        if (kBatch) {
+            // Slot t of the queue: valid below its list block's count of walkers.
+            if (t % kListBlock >= __ldg(sk.seg_n + t / kListBlock)) {
+                act = false;
+            } else {
                 i = __ldg(sk.queue + t);
                 sc = (uint32_t)__ldg(L.scene_of + i);
-            } else if (sk.stale[0] == 0u && sk.ctl[kCtlPoor] == 0u) {
-                return;  // k_density_walkers walks the single scene's queued particles
-            }  // else a single scene that is stale or whose lists are mostly unusable: every
-               // particle, in index order (no queue)
-            rebuild = sk.stale[sc] != 0u && sk.ctl[sc * kSkinCtl + kCtlAllow] != 0u;
-        }
-        const SceneParams& p = scene_params<kBatch>(L, i);
-        const float4 xi = __ldg(pos + i);
-        const uint32_t cx = cell_coord(xi.x, p.h), cy = cell_coord(xi.y, p.h),
-                       cz = cell_coord(xi.z, p.h);
-        DensitySum d;
-        d.out = nbr + i;
-        uint32_t s_end = tid;  // shared-memory word one past the last kept candidate (stride kNbrBlock)
-        // Scene constants used per candidate, in registers (a batched launch reads its scene's
-        // parameters from a device table).
-        const float s_inv_h = p.inv_h;
-        const uint32_t s_nbr_cap = p.nbr_cap;
-        auto drain = [&]() {
-#pragma unroll 2
-            for (uint32_t o = tid; o < s_end; o += kNbrBlock) {
-                const uint32_t j = s_j[o];
-                d.add(i, xi, j, __ldg(pos + j), s_inv_h, s_nbr_cap, L.total);
             }
-            s_end = tid;
-        };
-        const bool distinct = distinct_keys(p, cx, cy, cz);
-        const float h2 = p.h2;
-        uint32_t c = 0;
-        bool usable = false;
+        } else if (sk.stale[0] == 0u && sk.ctl[kCtlPoor] == 0u) {
+            act = false;  // k_density_walkers walks the single scene's queued particles
+        }  // else a single scene that is stale or whose lists are mostly unusable: every
+           // particle, in index order (no queue)
+        rebuild = act && sk.stale[sc] != 0u && sk.ctl[sc * kSkinCtl + kCtlAllow] != 0u;
+    }
+    if (__ballot_sync(0xffffffffu, act) == 0u) return;  // the whole warp is idle
+    const SceneParams& p = scene_params<kBatch>(L, i);
+    const float4 xi = act ? __ldg(pos + i) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    const uint32_t cx = cell_coord(xi.x, p.h), cy = cell_coord(xi.y, p.h), cz = cell_coord(xi.z, p.h);
+    DensitySum d;
+    d.out = nbr + i;
+    uint32_t s_end = tid;  // shared-memory word one past the last kept candidate (stride kNbrBlock)
+    // Scene constants used per candidate, in registers (a batched launch reads its scene's
+    // parameters from a device table).
+    const float s_inv_h = p.inv_h;
+    const uint32_t s_nbr_cap = p.nbr_cap;
+    auto drain = [&]() {
+#pragma unroll 2
+        for (uint32_t o = tid; o < s_end; o += kNbrBlock) {
+            const uint32_t j = s_j[o];
+            d.add(i, xi, j, __ldg(pos + j), s_inv_h, s_nbr_cap, L.total);
+        }
+        s_end = tid;
+    };
+    const bool distinct = distinct_keys(p, cx, cy, cz);
+    const float h2 = p.h2;
+    uint32_t c = 0;
+    bool usable = false;
+    uint32_t key_lo = 0u, width = 0u;
+    if (staging && warp_row_union(p, act, !rebuild, cx, cy, cz, sc, key_lo, width)) {
+        // The staged walk: branch-free append as below, candidates read from shared memory.
+        const uint32_t* scs = scan + p.off;
+        float4* stage = s_stage + (tid & ~31);
+#pragma unroll 1
+        for (uint32_t r = 0; r < 9u; r++) {
+            const uint32_t kA = key_lo + 50u * (r % 3u) + 2500u * (r / 3u);
+            const uint32_t b = __ldg(scs + kA), e = __ldg(scs + kA + width);
+#pragma unroll 1
+            for (uint32_t base = b; base < e; base += 32u) {
+                const uint32_t jl = base + lane;
+                if (jl < e) stage[lane] = __ldg(pos + jl);
+                __syncwarp();
+                const uint32_t cnt = min(32u, e - base);
+#pragma unroll 4
+                for (uint32_t k = 0; k < cnt; k++) {
+                    const float4 xj = stage[k];
+                    s_j[s_end] = base + k;
+                    s_end += act && in_range2(xi, xj) <= h2 ? kNbrBlock : 0u;
+                    if ((k & 3u) == 3u && s_end > tid + kDrainAt * kNbrBlock) drain();
+                }
+                if (s_end > tid + kDrainAt * kNbrBlock) drain();
+                __syncwarp();  // the next chunk overwrites the stage
+            }
+        }
+        drain();
+    } else if (act) {
         if (rebuild && skin_keys_distinct(p, cx, cy, cz)) {
             // A list build, staged in this thread's column of the shared list.
             c = skin_walk(p, scan, pos, xi, cx, cy, cz, s_j + tid, (size_t)kNbrBlock, sk.cap);
             usable = c <= sk.cap;
         }
         if (usable) {
-            // The density from the staged list (its in-range members, in the visiting order), then
-            // the list written out a slot at a time (a warp's lanes store consecutive words).
+            // The density from the staged list (its in-range members, in the visiting order),
+            // then the list written out a slot at a time (a warp's lanes store consecutive words).
 #pragma unroll 1
             for (uint32_t k = 0; k < c; k++) {
                 const uint32_t j = s_j[k * kNbrBlock + tid];
@@ -988,19 +1078,20 @@ __global__ void __launch_bounds__(kNbrBlock, kMinBlocks)
             });
             drain();
         }
-        if (rebuild) {
-            // This substep's sorted index becomes the particle's build index.
-            sk.x_build[i] = xi;
-            sk.b_of_id[__float_as_uint(xi.w)] = i;
-            sk.count[i] = min(c, sk.cap) | (usable ? kSkinUsable : 0u);
-            // The scene's usable lists, one atomic per warp and scene.
-            const uint32_t g = __match_any_sync(__activemask(), sc);
-            const uint32_t u = __ballot_sync(g, usable);
-            if ((uint32_t)(tid & 31) == (uint32_t)(__ffs(g) - 1) && u)
-                atomicAdd(sk.ctl + sc * kSkinCtl + kCtlUsable, (uint32_t)__popc(u));
-        }
-        density_finish(p, i, xi, vel, cx, cy, cz, distinct, d, rec, aux, bnd, nbr_count);
     }
+    if (!act) return;
+    if (rebuild) {
+        // This substep's sorted index becomes the particle's build index.
+        sk.x_build[i] = xi;
+        sk.b_of_id[__float_as_uint(xi.w)] = i;
+        sk.count[i] = min(c, sk.cap) | (usable ? kSkinUsable : 0u);
+        // The scene's usable lists, one atomic per warp and scene.
+        const uint32_t g = __match_any_sync(__activemask(), sc);
+        const uint32_t u = __ballot_sync(g, usable);
+        if ((uint32_t)(tid & 31) == (uint32_t)(__ffs(g) - 1) && u)
+            atomicAdd(sk.ctl + sc * kSkinCtl + kCtlUsable, (uint32_t)__popc(u));
+    }
+    density_finish(p, i, xi, vel, cx, cy, cz, distinct, d, rec, aux, bnd, nbr_count);
 }
 
 // The density pass over the skin lists: a particle of a scene that is not stale, whose list is
@@ -1926,7 +2017,7 @@ static int sm_count() {
 template <int B, int M>
 void density_shape(const StepLaunch& L, const float4* pos, const float4* vel, float4* rec,
                    const uint32_t* cell_scan, float4* aux, float4* bnd, uint32_t* nbr,
-                   uint32_t* nbr_count, const SkinLists& sk, cudaStream_t s) {
+                   uint32_t* nbr_count, const SkinLists& sk, bool staging, cudaStream_t s) {
     const uint32_t blocks = (L.total + B - 1) / B;
     if (sk.list) {
         // Skin lists: the list pass first; the walk passes then take the queue it leaves.
@@ -1943,9 +2034,11 @@ void density_shape(const StepLaunch& L, const float4* pos, const float4* vel, fl
         }
     }
     if (L.n_scenes > 1)
-        k_density<true, B, M><<<blocks, B, 0, s>>>(L, pos, vel, rec, cell_scan, aux, bnd, nbr, nbr_count, sk);
+        k_density<true, B, M><<<blocks, B, 0, s>>>(L, pos, vel, rec, cell_scan, aux, bnd, nbr, nbr_count, sk,
+                                                   staging);
     else
-        k_density<false, B, M><<<blocks, B, 0, s>>>(L, pos, vel, rec, cell_scan, aux, bnd, nbr, nbr_count, sk);
+        k_density<false, B, M><<<blocks, B, 0, s>>>(L, pos, vel, rec, cell_scan, aux, bnd, nbr, nbr_count, sk,
+                                                    staging);
 }
 
 template <int B, int M>
@@ -1982,11 +2075,12 @@ cudaError_t launch_density(const StepLaunch& L, const float4* pos, const float4*
                                                                    nbr, nbr_count);
         return cudaGetLastError();
     }
+    const bool st = kc.walk_staging != 0;
     switch (kc.nbr_shape) {
-        case kNbr128x8: density_shape<128, 8>(L, pos, vel, rec, cell_scan, aux, bnd, nbr, nbr_count, sk, s); break;
-        case kNbr96x8: density_shape<96, 8>(L, pos, vel, rec, cell_scan, aux, bnd, nbr, nbr_count, sk, s); break;
-        case kNbr64x12: density_shape<64, 12>(L, pos, vel, rec, cell_scan, aux, bnd, nbr, nbr_count, sk, s); break;
-        default: density_shape<128, 6>(L, pos, vel, rec, cell_scan, aux, bnd, nbr, nbr_count, sk, s);
+        case kNbr128x8: density_shape<128, 8>(L, pos, vel, rec, cell_scan, aux, bnd, nbr, nbr_count, sk, st, s); break;
+        case kNbr96x8: density_shape<96, 8>(L, pos, vel, rec, cell_scan, aux, bnd, nbr, nbr_count, sk, st, s); break;
+        case kNbr64x12: density_shape<64, 12>(L, pos, vel, rec, cell_scan, aux, bnd, nbr, nbr_count, sk, st, s); break;
+        default: density_shape<128, 6>(L, pos, vel, rec, cell_scan, aux, bnd, nbr, nbr_count, sk, st, s);
     }
     return cudaGetLastError();
 }

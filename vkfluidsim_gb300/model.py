@@ -460,6 +460,10 @@ class WCSPHWithBoundaryModel:
     def set_skin(self, skin: float) -> None:
         check(self._lib.vfs_model_set_skin(self._h, skin))
 
+    def set_walk_staging(self, enable: bool) -> None:
+        """Block-per-cell staging of the density walk (on by default; bit-identical results)."""
+        check(self._lib.vfs_model_set_walk_staging(self._h, int(bool(enable))))
+
     def skin_builds(self) -> int:
         """Candidate-list builds so far."""
         b = C.c_uint32()
@@ -691,6 +695,9 @@ class Batch:
 
     def set_skin(self, skin: float) -> None:
         check(self._lib.vfs_batch_set_skin(self._h, skin))
+
+    def set_walk_staging(self, enable: bool) -> None:
+        check(self._lib.vfs_batch_set_walk_staging(self._h, int(bool(enable))))
 
     def skin_builds(self, scene: int) -> int:
         b = C.c_uint32()
