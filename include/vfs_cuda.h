@@ -298,6 +298,7 @@ typedef struct vfs_tune_config {
     int32_t cell_block;      /* keys per block of the cell-range / reorder kernel: 128, 256, 512 */
     int32_t force_block;     /* force pass: threads per block and minimum resident blocks per */
     int32_t force_min_blocks;/* SM, the same four shapes; 0, 0 = the neighbour passes' shape */
+    int32_t walk_staging;    /* block-per-cell staging of the density walk: 1 on, 0 off */
 } vfs_tune_config;
 /* Times every candidate of each stage (sort, neighbour passes, cell ranges) for `repeats`
  * substeps from the model's current state, keeps the fastest, and restores the state (the

@@ -19,13 +19,19 @@ def test_tune_cache_file_round_trip(tmp_path):
     out = tmp_path / "out.txt"
     vfs.tune_cache_save(str(out))
     lines = [ln for ln in out.read_text().splitlines() if not ln.startswith("#")]
-    assert lines == ["sm103_152sms_n32768_s1_00000000000000aa 7 12 96 8 512 128 8",
-                     "sm103_152sms_n65536_s1_00000000000000bb 8 16 64 12 256 64 12"]
+    assert lines == ["sm103_152sms_n32768_s1_00000000000000aa 7 12 96 8 512 128 8 1",
+                     "sm103_152sms_n65536_s1_00000000000000bb 8 16 64 12 256 64 12 1"]
+    # A line with the walk-staging value keeps it.
+    f.write_text("sm103_152sms_n9_s1_00000000000000cc 8 16 128 8 256 128 8 0\n")
+    vfs.tune_cache_load(str(f))
+    vfs.tune_cache_save(str(out))
+    assert "sm103_152sms_n9_s1_00000000000000cc 8 16 128 8 256 128 8 0" in out.read_text()
     vfs.tune_cache_clear()
 
 
 @pytest.mark.parametrize("bad", ["key 7 12 100 3 512\n", "key 9 12 128 6 256\n", "key 7\n",
-                                 "key 7 12 128 6 256 100 3\n", "key 7 12 128 6 256 128\n"])
+                                 "key 7 12 128 6 256 100 3\n", "key 7 12 128 6 256 128\n",
+                                 "key 7 12 128 6 256 128 6 2\n"])
 def test_tune_cache_rejects_bad_lines(tmp_path, bad):
     f = tmp_path / "bad.txt"
     f.write_text(bad)

@@ -104,7 +104,8 @@ class MeshObject(C.Structure):
 class TuneConfig(C.Structure):
     _fields_ = [("sort_digit_bits", C.c_int32), ("sort_tile_items", C.c_int32),
                 ("nbr_block", C.c_int32), ("nbr_min_blocks", C.c_int32), ("cell_block", C.c_int32),
-                ("force_block", C.c_int32), ("force_min_blocks", C.c_int32)]
+                ("force_block", C.c_int32), ("force_min_blocks", C.c_int32),
+                ("walk_staging", C.c_int32)]
 
 
 SIGNATURES = {

@@ -2,7 +2,9 @@
 // dispatch sizes are fixed in the shaders' numthreads). It chooses, per model or batch:
 //   * the radix sort's digit width (6, 7 or 8 bits) and items per thread (8, 12 or 16),
 //   * the neighbour passes' block shape (threads per block x minimum resident blocks per SM),
-//   * the cells-per-block of the cell-range / reorder kernel (128, 256 or 512 keys).
+//   * the cells-per-block of the cell-range / reorder kernel (128, 256 or 512 keys),
+//   * whether the density walk stages a warp's row of cells in shared memory (block-per-cell
+//     staging; it helps where walking warps share rows and the per-thread walk prunes little).
 // None of these changes any result: the sort is stable whatever its digits, and every particle's
 // sums are accumulated by one thread in the same order whatever the block shape. Candidates are
 // timed with CUDA events on the model's stream from the same saved state (restored before every
@@ -50,6 +52,7 @@ vfs_tune_config current(const Model& m) {
     c.cell_block = m.kc.cell_block;
     c.force_block = kShapes[m.kc.force_shape].threads;
     c.force_min_blocks = kShapes[m.kc.force_shape].min_blocks;
+    c.walk_staging = m.kc.walk_staging;
     return c;
 }
 
@@ -97,6 +100,8 @@ int apply_tune_config(Model& m, const vfs_tune_config& c) {
                     "force block shape must be 128x6, 128x8, 96x8 or 64x12, or 0x0 for the neighbour shape");
     if (c.cell_block != 128 && c.cell_block != 256 && c.cell_block != 512)
         return fail(VFS_ERR_INVALID_ARGUMENT, "cell_block must be 128, 256 or 512");
+    if (c.walk_staging != 0 && c.walk_staging != 1)
+        return fail(VFS_ERR_INVALID_ARGUMENT, "walk_staging must be 0 or 1");
     if (c.sort_digit_bits != m.digit_bits || c.sort_tile_items != m.tile_items) {
         const int rc = set_sort_config(m, c.sort_digit_bits, c.sort_tile_items);
         if (rc) return rc;
@@ -105,6 +110,7 @@ int apply_tune_config(Model& m, const vfs_tune_config& c) {
     m.kc.nbr_shape = shape;
     m.kc.force_shape = fshape;
     m.kc.cell_block = c.cell_block;
+    m.kc.walk_staging = c.walk_staging;
     m.invalidate_graph();
     return VFS_OK;
 }
@@ -194,7 +200,21 @@ int autotune(Model& m, int repeats, bool use_cache, vfs_tune_config* chosen) {
             }
         }
     }
-    // Stage 3: cells per block of the cell-range / reorder kernel.
+    // Stage 3: staging of the density walk, with the chosen density shape.
+    if (rc == VFS_OK) {
+        float best_t = 1e30f;
+        vfs_tune_config c = best;
+        for (int st : {1, 0}) {
+            c.walk_staging = st;
+            measure(c, ph);
+            if (rc) break;
+            if (ph[3] < best_t) {
+                best_t = ph[3];
+                best.walk_staging = st;
+            }
+        }
+    }
+    // Stage 4: cells per block of the cell-range / reorder kernel.
     if (rc == VFS_OK) {
         float best_t = 1e30f;
         vfs_tune_config c = best;
@@ -231,11 +251,12 @@ int tune_cache_save(const char* path) {
     FILE* f = std::fopen(path, "w");
     if (!f) return fail(VFS_ERR_IO, std::string("cannot write ") + path);
     std::fprintf(f, "# vkfluidsim_gb300 tune cache: key digit_bits tile_items nbr_block nbr_min_blocks "
-                    "cell_block force_block force_min_blocks\n");
+                    "cell_block force_block force_min_blocks walk_staging\n");
     for (const auto& kv : g_cache)
-        std::fprintf(f, "%s %d %d %d %d %d %d %d\n", kv.first.c_str(), kv.second.sort_digit_bits,
+        std::fprintf(f, "%s %d %d %d %d %d %d %d %d\n", kv.first.c_str(), kv.second.sort_digit_bits,
                      kv.second.sort_tile_items, kv.second.nbr_block, kv.second.nbr_min_blocks,
-                     kv.second.cell_block, kv.second.force_block, kv.second.force_min_blocks);
+                     kv.second.cell_block, kv.second.force_block, kv.second.force_min_blocks,
+                     kv.second.walk_staging);
     const bool ok = std::fclose(f) == 0;
     return ok ? VFS_OK : fail(VFS_ERR_IO, std::string("cannot write ") + path);
 }
@@ -251,17 +272,20 @@ int tune_cache_load(const char* path) {
         if (line[0] == '#' || line[0] == '\n') continue;
         char key[256];
         vfs_tune_config c{};
-        // Lines of 6 values (no force shape) take the neighbour shape for the force pass.
-        const int got = std::sscanf(line, "%255s %d %d %d %d %d %d %d", key, &c.sort_digit_bits,
+        // Lines of 6 values (no force shape) take the neighbour shape for the force pass; lines
+        // without the walk-staging value (6 or 8 values) stage the walk.
+        c.walk_staging = 1;
+        const int got = std::sscanf(line, "%255s %d %d %d %d %d %d %d %d", key, &c.sort_digit_bits,
                                     &c.sort_tile_items, &c.nbr_block, &c.nbr_min_blocks,
-                                    &c.cell_block, &c.force_block, &c.force_min_blocks);
+                                    &c.cell_block, &c.force_block, &c.force_min_blocks,
+                                    &c.walk_staging);
         if (got == 6) {
             c.force_block = c.nbr_block;
             c.force_min_blocks = c.nbr_min_blocks;
         }
-        if ((got != 6 && got != 8) || shape_of(c.nbr_block, c.nbr_min_blocks) < 0 ||
+        if ((got != 6 && got != 8 && got != 9) || shape_of(c.nbr_block, c.nbr_min_blocks) < 0 ||
             shape_of(c.force_block, c.force_min_blocks) < 0 || c.sort_digit_bits < 4 ||
-            c.sort_digit_bits > 8) {
+            c.sort_digit_bits > 8 || (c.walk_staging != 0 && c.walk_staging != 1)) {
             rc = fail(VFS_ERR_PARSE, std::string("bad tune cache line in ") + path);
             break;
         }
