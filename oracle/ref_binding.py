@@ -1,6 +1,7 @@
-"""ctypes binding of ``oracle/_ref/libvfs_ref_shaders.so``: the reference's own step shaders
-compiled as C++ by ``oracle/ref_build.py`` (present only where the reference source tree was
-available when the recipe ran).
+"""ctypes bindings of the reference's own code built by ``oracle/ref_build.py`` into
+``oracle/_ref/``: ``libvfs_ref_shaders.so`` (its step shaders compiled as C++) and
+``libvfs_ref_volume_map.so`` (its CPU mesh SDF and volume-map code), present only where the recipe
+could run (the volume-map library needs the reference source tree itself).
 
 TEST INFRASTRUCTURE ONLY: used by tests/ and the fixture script under tests/golden/ to pin the
 oracle against the reference's code. The product package never imports it.
@@ -15,6 +16,7 @@ import numpy as np
 from .binding import OracleParams
 
 LIB_PATH = Path(__file__).resolve().parent / "_ref" / "libvfs_ref_shaders.so"
+VOLUME_MAP_LIB_PATH = Path(__file__).resolve().parent / "_ref" / "libvfs_ref_volume_map.so"
 
 _F = C.POINTER(C.c_float)
 _U = C.POINTER(C.c_uint32)
@@ -49,6 +51,31 @@ def load() -> C.CDLL:
         fn.argtypes = args
     _lib = lib
     return lib
+
+
+def volume_map_available() -> bool:
+    return VOLUME_MAP_LIB_PATH.exists()
+
+
+def mesh_volume_map(vertices, triangles, h: float, res):
+    """The reference's own MeshSDF + GenerateVolumeMap (src/util/mesh_sdf.cpp,
+    src/util/volume_map.cpp) for a triangle mesh, margin 8 h, grids rounded to float as
+    GenericScene uploads them: (box_size, box_pos, sdf, volume_map)."""
+    lib = C.CDLL(str(VOLUME_MAP_LIB_PATH))
+    fn = lib.vfs_ref_mesh_volume_map
+    fn.restype = C.c_int
+    fn.argtypes = [_F, C.c_uint32, _U, C.c_uint32, C.c_float, _U, _F, _F, _F, _F]
+    v = np.ascontiguousarray(vertices, np.float32).reshape(-1, 3)
+    t = np.ascontiguousarray(triangles, np.uint32).reshape(-1, 3)
+    r = np.asarray(res, np.uint32)
+    cnt = int(r[0]) * int(r[1]) * int(r[2])
+    bs, bp = np.empty(3, np.float32), np.empty(3, np.float32)
+    sdf, vm = np.empty(cnt, np.float32), np.empty(cnt, np.float32)
+    rc = fn(_fp(v), len(v), t.ctypes.data_as(_U), len(t), h, r.ctypes.data_as(_U), _fp(bs), _fp(bp),
+            _fp(sdf), _fp(vm))
+    if rc != 0:
+        raise ValueError("the reference volume-map code rejected the mesh")
+    return bs, bp, sdf, vm
 
 
 def set_threads(t: int) -> None:

@@ -29,6 +29,13 @@ copied into the repository.
    ``-fsingle-precision-constant`` (Slang's unsuffixed float literals are 32-bit),
    ``-ffp-contract=off`` and OpenMP into ``oracle/_ref/libvfs_ref_shaders.so``.
 
+3. The reference's CPU volume-map code (``src/util/``: geometry, mesh_bvh, mesh_pseudonormals,
+   mesh_sdf, discretization, gaussian_quadrature, kernel, volume_map ``.cpp``) is compiled where it
+   lies, unchanged, against ``oracle/ref_shim/cpu/`` (a project-written stand-in for the part of
+   glm it uses, and for ``gfx/common.h`` / ``gfx/mesh.h`` without Vulkan), with the host driver
+   ``oracle/ref_shim/ref_volume_map.cpp`` (MeshSDF + GenerateVolumeMap as GenericScene calls them)
+   into ``oracle/_ref/libvfs_ref_volume_map.so``. This part needs the reference tree itself.
+
 ``build_generated()`` compiles an already generated ``oracle/_ref/ref_shaders_gen.cpp`` where the
 reference tree is absent (the generated unit travels with the working tree).
 """
@@ -169,10 +176,33 @@ def build_generated() -> Path:
     return lib
 
 
+VOLUME_MAP_SOURCES = ("geometry", "mesh_bvh", "mesh_pseudonormals", "mesh_sdf", "discretization",
+                      "gaussian_quadrature", "kernel", "volume_map")
+
+
+def build_volume_map(ref: Path) -> Path:
+    """The reference's CPU volume-map code and its driver, as one shared library."""
+    src = (ref / "src").resolve()
+    OUT.mkdir(parents=True, exist_ok=True)
+    lib = OUT / "libvfs_ref_volume_map.so"
+    files = [src / "util" / f"{f}.cpp" for f in VOLUME_MAP_SOURCES] + [SHIM / "ref_volume_map.cpp"]
+    deps = files + sorted((SHIM / "cpu").rglob("*.h*"))
+    if lib.exists() and all(d.stat().st_mtime <= lib.stat().st_mtime for d in deps):
+        return lib
+    cmd = ["g++", "-std=c++20", "-O2", "-fPIC", "-shared", "-ffp-contract=off", "-w",
+           f"-I{SHIM / 'cpu'}", f"-I{src}", *map(str, files), "-o", str(lib)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("building the reference volume-map code failed:\n" + " ".join(cmd) +
+                           "\n" + r.stdout + r.stderr)
+    return lib
+
+
 def build_default():
     """The build step's entry: regenerates and builds from the reference tree when it is present,
     else builds an already generated unit, else does nothing. Returns the library or None."""
     if (REFERENCE_TREE / SHADERS).is_dir():
+        build_volume_map(REFERENCE_TREE)
         return build(REFERENCE_TREE)
     if (OUT / "ref_shaders_gen.cpp").exists():
         return build_generated()
@@ -182,4 +212,4 @@ def build_default():
 if __name__ == "__main__":
     if len(sys.argv) != 2:
         sys.exit("usage: python oracle/ref_build.py <path of the VkFluidSim source tree>")
-    print(build(Path(sys.argv[1])))
+    print(build(Path(sys.argv[1])), build_volume_map(Path(sys.argv[1])))

@@ -1,0 +1,2 @@
+#pragma once
+#include "../glm_shim.hpp"

@@ -16,6 +16,8 @@ import pytest
 
 from oracle import binding as ob
 from tests.helpers import normwise_rel
+from pathlib import Path
+
 from tests.ref_fixtures import FLOAT_FIELDS, INT_FIELDS, Fixture, names
 
 
@@ -103,3 +105,53 @@ def test_oracle_matches_the_reference_build_on_seeded_scenes(seed):
         o.step()
         r.step(1)
         check_equal(oracle_snapshot(o), r.state(), True, f"seed {seed} step {s + 1}")
+
+
+# ---- the volume-map generator (the step's boundary input), pinned to the reference's CPU code
+
+VM_DIR = Path(__file__).resolve().parent / "golden" / "ref_volume_map"
+
+
+def vm_fixtures():
+    return sorted(p.stem for p in VM_DIR.glob("*.npz"))
+
+
+def test_volume_map_fixture_set_is_complete():
+    assert set(vm_fixtures()) >= {"icosphere", "box", "l_prism", "bumpy_sphere"}
+
+
+@pytest.mark.parametrize("name", vm_fixtures())
+def test_oracle_mesh_volume_map_reproduces_the_reference(name):
+    """The oracle's mesh SDF and volume map (BVH-free brute force, Eberly point-triangle
+    distance, angle-weighted pseudonormals, 16-point Gauss-Legendre) against the reference's own
+    MeshSDF + GenerateVolumeMap: grid box and both grids bit for bit on this host."""
+    z = np.load(VM_DIR / f"{name}.npz")
+    h = float(z["h"])
+    res = tuple(int(r) for r in z["resolution"])
+    bs, bp, sdf, vm = ob.mesh_volume_map(z["vertices"], z["triangles"], h, res, np.float32(8.0 * h))
+    assert np.array_equal(bs, z["box_size"]) and np.array_equal(bp, z["box_pos"])
+    if platform.machine() == "x86_64":
+        assert np.array_equal(sdf, z["sdf"]), normwise_rel(sdf, z["sdf"])
+        assert np.array_equal(vm, z["volume_map"]), normwise_rel(vm, z["volume_map"])
+    else:
+        assert normwise_rel(sdf, z["sdf"]) <= 1e-6 and normwise_rel(vm, z["volume_map"]) <= 1e-6
+    assert (z["volume_map"] > 0).sum() > 100
+
+
+@pytest.mark.parametrize("seed", [11, 12])
+def test_oracle_mesh_volume_map_matches_the_reference_build(seed):
+    from oracle import ref_binding as rb
+
+    if not rb.volume_map_available():
+        pytest.skip("the reference volume-map build (oracle/_ref) is not present on this machine")
+    from tests.golden.make_ref_volume_map_golden import icosphere
+
+    rng = np.random.default_rng(seed)
+    v, t = icosphere(float(rng.uniform(0.1, 0.3)), 1)
+    v = (v * (1.0 + 0.2 * rng.random((len(v), 1))) + rng.uniform(-1, 1, 3)).astype(np.float32)
+    h = float(rng.uniform(0.02, 0.06))
+    res = tuple(int(x) for x in rng.integers(8, 20, 3))
+    a = rb.mesh_volume_map(v, t, h, res)
+    b = ob.mesh_volume_map(v, t, h, res, np.float32(8.0 * h))
+    for x, y in zip(a, b):
+        assert np.array_equal(x, y)

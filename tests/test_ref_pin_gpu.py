@@ -85,3 +85,30 @@ def test_continuous_run_stays_on_the_reference(name):
         print(f"{name} continuous step {s + 1} drift:",
               json.dumps({k: float(f"{v:.3g}") for k, v in drift.items()}))
         assert drift["positions"] <= RTOL and drift["densities"] <= RTOL
+
+
+@pytest.mark.parametrize("name", ["icosphere", "box", "l_prism", "bumpy_sphere"])
+def test_gpu_mesh_volume_map_matches_the_reference(name):
+    """The GPU's mesh SDF grid and volume map (vfs_model_add_mesh_object) against the reference's
+    own MeshSDF + GenerateVolumeMap (tests/golden/ref_volume_map): same grid box, SDF within 1e-6
+    (FP64 distances rounded to float), volume map within 1e-5 of its largest value (the GPU
+    evaluates the quadrature's integrand in FP32 and sums it in FP64)."""
+    from pathlib import Path
+
+    from vkfluidsim_gb300 import workloads as W
+
+    z = np.load(Path(__file__).resolve().parent / "golden" / "ref_volume_map" / f"{name}.npz")
+    h = float(z["h"])
+    w = W.dam_break(dims=(4, 4, 4), map_res=0)
+    from dataclasses import replace
+
+    w.sim = replace(w.sim, smooth_radius=h)
+    m = W.build_model(w)
+    m.add_mesh_object(vfs.MeshObject(vertices=z["vertices"], triangles=z["triangles"],
+                                     resolution=tuple(int(r) for r in z["resolution"])))
+    g = m.get_boundary_object(0)
+    assert np.array_equal(g.box_size, z["box_size"]) and np.array_equal(g.box_pos, z["box_pos"])
+    e_sdf = float(np.abs(g.sdf - z["sdf"]).max())
+    e_vm = float(np.abs(g.volume_map - z["volume_map"]).max() / np.abs(z["volume_map"]).max())
+    print(f"{name}: sdf max |diff| {e_sdf:.3g} m, volume map {e_vm:.3g} of its maximum")
+    assert e_sdf < 1e-6 and e_vm <= 1e-5
