@@ -223,10 +223,11 @@ int32_t vfs_model_get_neighbor_capacity(const vfs_model* m);
 int vfs_model_set_skin(vfs_model* m, float skin);
 int vfs_model_get_skin(const vfs_model* m, float* skin);
 /* Block-per-cell staging in the density pass's bucket walk (CalculateDensities,
- * wcsph_with_boundary_model.slang:153-197), on by default: a warp whose particles share one row of
+ * wcsph_with_boundary_model.slang:153-197): a warp whose particles share one row of
  * cells loads the 3 x 3 rows of cells around it into shared memory once and tests every staged
  * particle against each of its own, instead of each thread walking its 27 buckets from global
- * memory. Results are bit-identical either way; 0 turns it off. */
+ * memory. Results are bit-identical either way. Off by default; the autotuner's choice
+ * (vfs_tune_config.walk_staging) turns it on for workloads where it is faster. */
 int vfs_model_set_walk_staging(vfs_model* m, int32_t enable);
 /* Number of list builds so far (synchronises the handle's stream). */
 int vfs_model_get_skin_builds(vfs_model* m, uint32_t* builds);

@@ -19,13 +19,13 @@ def test_tune_cache_file_round_trip(tmp_path):
     out = tmp_path / "out.txt"
     vfs.tune_cache_save(str(out))
     lines = [ln for ln in out.read_text().splitlines() if not ln.startswith("#")]
-    assert lines == ["sm103_152sms_n32768_s1_00000000000000aa 7 12 96 8 512 128 8 1",
-                     "sm103_152sms_n65536_s1_00000000000000bb 8 16 64 12 256 64 12 1"]
+    assert lines == ["sm103_152sms_n32768_s1_00000000000000aa 7 12 96 8 512 128 8 0",
+                     "sm103_152sms_n65536_s1_00000000000000bb 8 16 64 12 256 64 12 0"]
     # A line with the walk-staging value keeps it.
-    f.write_text("sm103_152sms_n9_s1_00000000000000cc 8 16 128 8 256 128 8 0\n")
+    f.write_text("sm103_152sms_n9_s1_00000000000000cc 8 16 128 8 256 128 8 1\n")
     vfs.tune_cache_load(str(f))
     vfs.tune_cache_save(str(out))
-    assert "sm103_152sms_n9_s1_00000000000000cc 8 16 128 8 256 128 8 0" in out.read_text()
+    assert "sm103_152sms_n9_s1_00000000000000cc 8 16 128 8 256 128 8 1" in out.read_text()
     vfs.tune_cache_clear()
 
 

@@ -204,7 +204,7 @@ int autotune(Model& m, int repeats, bool use_cache, vfs_tune_config* chosen) {
     if (rc == VFS_OK) {
         float best_t = 1e30f;
         vfs_tune_config c = best;
-        for (int st : {1, 0}) {
+        for (int st : {0, 1}) {
             c.walk_staging = st;
             measure(c, ph);
             if (rc) break;
@@ -273,8 +273,8 @@ int tune_cache_load(const char* path) {
         char key[256];
         vfs_tune_config c{};
         // Lines of 6 values (no force shape) take the neighbour shape for the force pass; lines
-        // without the walk-staging value (6 or 8 values) stage the walk.
-        c.walk_staging = 1;
+        // without the walk-staging value (6 or 8 values) walk per thread.
+        c.walk_staging = 0;
         const int got = std::sscanf(line, "%255s %d %d %d %d %d %d %d %d", key, &c.sort_digit_bits,
                                     &c.sort_tile_items, &c.nbr_block, &c.nbr_min_blocks,
                                     &c.cell_block, &c.force_block, &c.force_min_blocks,

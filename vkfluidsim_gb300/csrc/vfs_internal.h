@@ -169,7 +169,8 @@ struct KernelConfig {
     int nbr_shape = kNbr96x8;     // density pass (and the adjoint's recomputed forward)
     int force_shape = kNbr128x8;  // force pass (no shared memory: it takes the larger blocks)
     int cell_block = 256;  // keys per block of the cell-range / reorder kernel: 128, 256 or 512
-    int walk_staging = 1;  // density walk: warps whose particles share a row of cells stage it
+    int walk_staging = 0;  // density walk: warps whose particles share a row of cells stage it
+                           // (off by default: the autotuner turns it on where it is faster)
 };
 size_t sort_scratch_words(const SortConfig& c);
 
