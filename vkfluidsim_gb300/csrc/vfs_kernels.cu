@@ -857,8 +857,11 @@ struct DensitySum {
     uint32_t* out;  // slot `listed` of i's list (slot-major, stride = particles)
     __device__ __forceinline__ void add(uint32_t i, const float4& xi, uint32_t j, const float4& xj,
                                         float inv_h, uint32_t cap, uint32_t stride) {
-        const float dx = __fsub_rn(xj.x, xi.x), dy = __fsub_rn(xj.y, xi.y), dz = __fsub_rn(xj.z, xi.z);
-        const float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+        add_r2(i, j, in_range2(xi, xj), inv_h, cap, stride);
+    }
+    // The same with r2 = in_range2(x_i, x_j) already computed (by the in-range test).
+    __device__ __forceinline__ void add_r2(uint32_t i, uint32_t j, float r2, float inv_h,
+                                           uint32_t cap, uint32_t stride) {
         const float r = r2 > 0.0f ? __fmul_rn(r2, rsqrtf(r2)) : 0.0f;
         // W(q) / sigma, branch-free: 2 (1-q)^3 above q = 1/2, 6q^3 - 6q^2 + 1 below, 0 past 1.
         const float q = __fmul_rn(r, inv_h);
@@ -967,16 +970,18 @@ __device__ __forceinline__ bool warp_row_union(const SceneParams& p, bool act, b
 // stale scene whose build policy allows it, every particle also builds its skin list. A warp
 // whose particles share a row of cells walks the staged rows of warp_row_union; any other warp
 // walks per thread (for_each_candidate).
-template <bool kBatch, int kNbrBlock, int kMinBlocks>
+template <bool kBatch, int kNbrBlock, int kMinBlocks, bool kStaging>
 __global__ void __launch_bounds__(kNbrBlock, kMinBlocks)
     k_density(StepLaunch L, const float4* __restrict__ pos, const float4* __restrict__ vel,
               float4* __restrict__ rec, const uint32_t* __restrict__ scan,
               float4* __restrict__ aux, float4* __restrict__ bnd, uint32_t* __restrict__ nbr,
-              uint32_t* __restrict__ nbr_count, SkinLists sk, bool staging) {
+              uint32_t* __restrict__ nbr_count, SkinLists sk) {
     static_assert(kSkinCap <= (uint32_t)kListCap, "a list build is staged in the shared list");
     static_assert(kNbrBlock % 32 == 0, "whole warps");
     __shared__ uint32_t s_j[kListCap * kNbrBlock];
-    __shared__ float4 s_stage[kNbrBlock];  // each warp's 32 staged candidates
+    // Each warp's 32 staged candidates (one placeholder element without staging, so that the
+    // shared memory the per-thread walk does not use stays L1 for its candidate loads).
+    __shared__ float4 s_stage[kStaging ? kNbrBlock : 1];
     const int tid = threadIdx.x;
     const uint32_t lane = (uint32_t)(tid & 31);
     // No lane returns before the warp's collective steps: inactive lanes carry act = false.
@@ -1023,7 +1028,7 @@ __global__ void __launch_bounds__(kNbrBlock, kMinBlocks)
     uint32_t c = 0;
     bool usable = false;
     uint32_t key_lo = 0u, width = 0u;
-    if (staging && warp_row_union(p, act, !rebuild, cx, cy, cz, sc, key_lo, width)) {
+    if (kStaging && warp_row_union(p, act, !rebuild, cx, cy, cz, sc, key_lo, width)) {
         // The staged walk: branch-free append as below, candidates read from shared memory.
         const uint32_t* scs = scan + p.off;
         float4* stage = s_stage + (tid & ~31);
@@ -1061,8 +1066,8 @@ __global__ void __launch_bounds__(kNbrBlock, kMinBlocks)
 #pragma unroll 1
             for (uint32_t k = 0; k < c; k++) {
                 const uint32_t j = s_j[k * kNbrBlock + tid];
-                const float4 xj = __ldg(pos + j);
-                if (in_range2(xi, xj) <= h2) d.add(i, xi, j, xj, s_inv_h, s_nbr_cap, L.total);
+                const float r2 = in_range2(xi, __ldg(pos + j));
+                if (r2 <= h2) d.add_r2(i, j, r2, s_inv_h, s_nbr_cap, L.total);
             }
 #pragma unroll 1
             for (uint32_t k = 0; k < c; k++) sk.list[(size_t)k * L.total + i] = s_j[k * kNbrBlock + tid];
@@ -1102,7 +1107,7 @@ __global__ void __launch_bounds__(kNbrBlock, kMinBlocks)
 // No shared memory: the pass is bound by its chains of dependent loads, so it runs at the
 // occupancy its registers allow.
 template <bool kBatch>
-__global__ void __launch_bounds__(kListBlock, 8)
+__global__ void __launch_bounds__(kListBlock, 10)
     k_density_list(StepLaunch L, const float4* __restrict__ pos, const float4* __restrict__ vel,
                    float4* __restrict__ rec, float4* __restrict__ aux, float4* __restrict__ bnd,
                    uint32_t* __restrict__ nbr, uint32_t* __restrict__ nbr_count, SkinLists sk) {
@@ -1151,15 +1156,16 @@ __global__ void __launch_bounds__(kListBlock, 8)
 #pragma unroll
                 for (int u = 0; u < 4; u++) xj[u] = __ldg(sk.xcur + j[u]);  // position, sorted index
 #pragma unroll
-                for (int u = 0; u < 4; u++)
-                    if (in_range2(xi, xj[u]) <= h2)
-                        d.add(i, xi, __float_as_uint(xj[u].w), xj[u], s_inv_h, s_nbr_cap, L.total);
+                for (int u = 0; u < 4; u++) {
+                    const float r2 = in_range2(xi, xj[u]);
+                    if (r2 <= h2) d.add_r2(i, __float_as_uint(xj[u].w), r2, s_inv_h, s_nbr_cap, L.total);
+                }
             }
 #pragma unroll 1
             for (; k < n_list; k++, q += stride) {
                 const float4 xj = __ldg(sk.xcur + __ldg(q));
-                if (in_range2(xi, xj) <= h2)
-                    d.add(i, xi, __float_as_uint(xj.w), xj, s_inv_h, s_nbr_cap, L.total);
+                const float r2 = in_range2(xi, xj);
+                if (r2 <= h2) d.add_r2(i, __float_as_uint(xj.w), r2, s_inv_h, s_nbr_cap, L.total);
             }
             density_finish(p, i, xi, vel, cx, cy, cz, distinct_keys(p, cx, cy, cz), d, rec, aux,
                            bnd, nbr_count);
@@ -1191,10 +1197,9 @@ __global__ void __launch_bounds__(kListBlock, 8)
     if (walk) sk.queue[base + (uint32_t)__popc(m & ((1u << lane) - 1u))] = i;
 }
 
-// W(|x_j - x_i|) / sigma with the density drain's explicitly rounded arithmetic.
-__device__ __forceinline__ float w_over_sigma(const float4& xi, const float4& xj, float inv_h) {
-    const float dx = __fsub_rn(xj.x, xi.x), dy = __fsub_rn(xj.y, xi.y), dz = __fsub_rn(xj.z, xi.z);
-    const float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+// W(|x_j - x_i|) / sigma with the density drain's explicitly rounded arithmetic, from
+// r2 = in_range2(x_i, x_j).
+__device__ __forceinline__ float w_over_sigma_r2(float r2, float inv_h) {
     const float r = r2 > 0.0f ? __fmul_rn(r2, rsqrtf(r2)) : 0.0f;
     const float q = __fmul_rn(r, inv_h);
     const float t = __fsub_rn(1.0f, q);
@@ -1297,8 +1302,9 @@ __global__ void __launch_bounds__(kWalkerWarps * 32)
             const uint32_t j = rb + (f - rs);
             float4 xj = make_float4(0.f, 0.f, 0.f, 0.f);
             if (valid) xj = __ldg(pos + j);
-            const bool inr = valid && in_range2(xi, xj) <= p.h2;
-            const float wv = inr ? w_over_sigma(xi, xj, p.inv_h) : 0.0f;
+            const float r2 = in_range2(xi, xj);
+            const bool inr = valid && r2 <= p.h2;
+            const float wv = inr ? w_over_sigma_r2(r2, p.inv_h) : 0.0f;
             uint32_t mask = __ballot_sync(0xffffffffu, inr);
             const uint32_t listm = __ballot_sync(0xffffffffu, inr && j != i);
             if (inr && j != i) {
@@ -1360,7 +1366,7 @@ __global__ void __launch_bounds__(kPlaneBlock)
 #pragma unroll 2
             for (uint32_t o = tid; o < s_end; o += kPlaneBlock) {
                 const uint32_t j = s_j[o];
-                rho = __fadd_rn(rho, w_over_sigma(xi, __ldg(pos + j), s_inv_h));
+                rho = __fadd_rn(rho, w_over_sigma_r2(in_range2(xi, __ldg(pos + j)), s_inv_h));
                 n_pl += j != i ? 1u : 0u;
             }
         };
@@ -2033,12 +2039,17 @@ void density_shape(const StepLaunch& L, const float4* pos, const float4* vel, fl
                                                                nbr, nbr_count, sk);
         }
     }
-    if (L.n_scenes > 1)
-        k_density<true, B, M><<<blocks, B, 0, s>>>(L, pos, vel, rec, cell_scan, aux, bnd, nbr, nbr_count, sk,
-                                                   staging);
-    else
-        k_density<false, B, M><<<blocks, B, 0, s>>>(L, pos, vel, rec, cell_scan, aux, bnd, nbr, nbr_count, sk,
-                                                    staging);
+    if (L.n_scenes > 1) {
+        if (staging)
+            k_density<true, B, M, true><<<blocks, B, 0, s>>>(L, pos, vel, rec, cell_scan, aux, bnd, nbr, nbr_count, sk);
+        else
+            k_density<true, B, M, false><<<blocks, B, 0, s>>>(L, pos, vel, rec, cell_scan, aux, bnd, nbr, nbr_count, sk);
+    } else {
+        if (staging)
+            k_density<false, B, M, true><<<blocks, B, 0, s>>>(L, pos, vel, rec, cell_scan, aux, bnd, nbr, nbr_count, sk);
+        else
+            k_density<false, B, M, false><<<blocks, B, 0, s>>>(L, pos, vel, rec, cell_scan, aux, bnd, nbr, nbr_count, sk);
+    }
 }
 
 template <int B, int M>
