@@ -231,9 +231,8 @@ int vfs_model_get_skin(const vfs_model* m, float* skin);
 int vfs_model_set_walk_staging(vfs_model* m, int32_t enable);
 /* Number of list builds so far (synchronises the handle's stream). */
 int vfs_model_get_skin_builds(vfs_model* m, uint32_t* builds);
-/* Device pointers of the current state: float4 (x, y, z, id bits) and (vx, vy, vz, w), w reserved
- * for the library (any value written there is checked: an unexpected one only makes the next
- * substep rebuild the skin lists). They stay valid for the model's lifetime. Positions and velocities written through them (ordered with
+/* Device pointers of the current state: float4 (x, y, z, id bits) and (vx, vy, vz, 0). They stay
+ * valid for the model's lifetime. Positions and velocities written through them (ordered with
  * the model's stream) are what the next substep steps: every substep recomputes each particle's
  * key from its position, as UpdateSpatialHash does. */
 int vfs_model_device_state(vfs_model* m, void** pos4, void** vel4);

@@ -157,24 +157,3 @@ def test_single_scene_walkers_match_the_batched_walk():
     sb, sm = b.copy_data_buffers(0), m.copy_data_buffers()
     for k in ("positions", "velocities", "densities"):
         assert np.array_equal(sb[k], sm[k]), k
-
-
-def test_overwritten_build_indices_force_a_rebuild():
-    """The skin lists' build index travels in the velocity's w. Velocities written from outside
-    with w = 0 (as vfs_model_set_particle_state writes them) must not be taken for build indices:
-    the scene goes stale, rebuilds, and the step is still the oracle's."""
-    torch = pytest.importorskip("torch")
-    w = moving_scene(seed=6, speed=0.05)
-    m = W.build_model(w)
-    m.substeps(3)
-    assert m.skin_builds() == 1
-    m.synchronize()
-    _, v = m.device_state()
-    V = torch.as_tensor(_DeviceRows(v, w.n), device="cuda")
-    V[:, 3] = 0.0
-    torch.cuda.synchronize()
-    s = m.copy_data_buffers()
-    o = oracle_for(w, m, pos=s["positions"], vel=s["velocities"], ids=m.get_ids())
-    compare_step(m, o, "build_indices_zeroed")
-    m.substeps(16)  # lists that went stale 3 substeps after their build wait 8 before the next
-    assert m.skin_builds() >= 2

@@ -454,6 +454,7 @@ Model::~Model() {
     cudaFree(skin.list);
     cudaFree(skin.count);
     cudaFree(skin.x_build);
+    cudaFree(skin.b_of_id);
     cudaFree(skin.xcur);
     cudaFree(skin.stale);
     cudaFree(skin.ctl);
@@ -563,6 +564,7 @@ int Model::alloc_skin() {
     if (cudaMalloc(&s.list, N * s.cap * sizeof(uint32_t)) != cudaSuccess ||
         cudaMalloc(&s.count, N * sizeof(uint32_t)) != cudaSuccess ||
         cudaMalloc(&s.x_build, N * sizeof(float4)) != cudaSuccess ||
+        cudaMalloc(&s.b_of_id, N * sizeof(uint32_t)) != cudaSuccess ||
         cudaMalloc(&s.xcur, N * sizeof(float4)) != cudaSuccess ||
         cudaMalloc(&s.stale, scenes.size() * sizeof(uint32_t)) != cudaSuccess ||
         cudaMalloc(&s.ctl, scenes.size() * kSkinCtl * sizeof(uint32_t)) != cudaSuccess ||
@@ -573,6 +575,7 @@ int Model::alloc_skin() {
         cudaFree(s.list);
         cudaFree(s.count);
         cudaFree(s.x_build);
+        cudaFree(s.b_of_id);
         cudaFree(s.xcur);
         cudaFree(s.stale);
         cudaFree(s.ctl);
@@ -582,6 +585,7 @@ int Model::alloc_skin() {
         return VFS_OK;
     }
     VFS_CUDA_TRY(cudaMemset(s.count, 0, N * sizeof(uint32_t)));
+    VFS_CUDA_TRY(cudaMemset(s.b_of_id, 0, N * sizeof(uint32_t)));  // any index below n until a build
     VFS_CUDA_TRY(cudaMemset(s.stale, 0, scenes.size() * sizeof(uint32_t)));
     VFS_CUDA_TRY(cudaMemset(s.wcount, 0, sizeof(uint32_t)));
     skin = s;

@@ -138,6 +138,7 @@ struct SkinLists {
     uint32_t* list = nullptr;     // slot-major: list[k * total + b] = build index of candidate k of b
     uint32_t* count = nullptr;    // per build index: list length, kSkinUsable when it can be summed
     float4* x_build = nullptr;    // per build index: position at the last build
+    uint32_t* b_of_id = nullptr;  // per id: build index
     float4* xcur = nullptr;       // per build index: current position (x, y, z) and current sorted
                                   // index (w, as bits), written by the cell pass
     uint32_t* stale = nullptr;    // per scene: nonzero when some particle moved past h skin / 2
@@ -198,10 +199,9 @@ cudaError_t launch_sort(uint32_t n, const SortConfig& sc, const SortScratch& scr
 // zero[0, zero_words) (the sort scratch, for the next substep); copies skeys to pkeys_out (the next
 // substep's previous sorted keys) when pkeys_out is not NULL. guess (n / 128 + 2 words, any
 // contents) keeps each block's bound of the sorted keys as the next call's starting point; NULL
-// searches from scratch. With skin lists (sk.xcur set), also xcur[b] = (position, sorted index)
-// for each particle whose velocity's w holds its build index b (trusted when the build recorded
-// the particle's id in x_build[b].w), and flags every scene of L with a particle that moved more
-// than h skin / 2 since its list build or whose build index does not check.
+// searches from scratch. With skin lists (sk.cur set), also sk.cur[sk.b_of_id[id]] = sorted index
+// for the ids in x.w, and flags every scene of L with a particle that moved more than h skin / 2
+// since its list build.
 cudaError_t launch_cells_reorder(const StepLaunch& L, uint32_t n, const uint32_t* skeys, const uint32_t* perm,
                                  uint32_t* cell_scan, const float4* pos_in, const float4* vel_in,
                                  float4* pos_out, float4* vel_out, uint32_t* zero,

@@ -526,7 +526,7 @@ __global__ void __launch_bounds__(kCellBlock)
                     float4* __restrict__ pos_out, float4* __restrict__ vel_out,
                     uint32_t* __restrict__ zero, uint32_t zero_words,
                     uint32_t* __restrict__ pkeys_out, uint32_t* guess,
-                    float4* __restrict__ xcur,
+                    const uint32_t* __restrict__ b_of_id, float4* __restrict__ xcur,
                     const float4* __restrict__ x_build, uint32_t* __restrict__ stale) {
     __shared__ uint32_t s_lo, s_hi;
     // The sort is done with its scratch (histograms, tile counters, look-back status): clear it
@@ -554,28 +554,22 @@ __global__ void __launch_bounds__(kCellBlock)
         uint32_t src = perm[i];
         if (src >= n) src = i;  // only after a reported sort failure
         const float4 x = __ldg(pos_in + src);
-        const float4 v = __ldg(vel_in + src);
         pos_out[i] = x;
-        vel_out[i] = v;
+        vel_out[i] = __ldg(vel_in + src);
         if (xcur) {
             // Skin lists: the particle's current position and sorted index under its build
             // index (the list pass gathers both with one load), and its displacement since the
-            // build. The build index travels in the velocity's w; it is trusted only when the
-            // build recorded this particle's id there (x_build.w), so a state written from
-            // outside (w = 0) makes the scene stale and rebuild.
+            // build.
             const uint32_t id = __float_as_uint(x.w);
-            const uint32_t bi = __float_as_uint(v.w);
-            const uint32_t sc = L.n_scenes > 1 ? (uint32_t)__ldg(L.scene_of + i) : 0u;
-            exceed = true;
-            exceed_sc = sc;
+            const uint32_t bi = id < n ? __ldg(b_of_id + id) : n;
             if (bi < n) {
+                xcur[bi] = make_float4(x.x, x.y, x.z, __uint_as_float(i));
                 const float4 b = __ldg(x_build + bi);
-                if (__float_as_uint(b.w) == id) {
-                    xcur[bi] = make_float4(x.x, x.y, x.z, __uint_as_float(i));
-                    const float dx = x.x - b.x, dy = x.y - b.y, dz = x.z - b.z;
-                    const float lim = L.n_scenes > 1 ? L.scenes[sc].skin_half2 : L.one.skin_half2;
-                    exceed = !(dx * dx + dy * dy + dz * dz <= lim);
-                }
+                const float dx = x.x - b.x, dy = x.y - b.y, dz = x.z - b.z;
+                const uint32_t sc = L.n_scenes > 1 ? (uint32_t)__ldg(L.scene_of + i) : 0u;
+                const float lim = L.n_scenes > 1 ? L.scenes[sc].skin_half2 : L.one.skin_half2;
+                exceed = !(dx * dx + dy * dy + dz * dz <= lim);
+                exceed_sc = sc;
             }
         }
         if (pkeys_out) pkeys_out[i] = skeys[i];
@@ -1093,9 +1087,8 @@ __global__ void __launch_bounds__(kNbrBlock, kMinBlocks)
     if (!act) return;
     if (rebuild) {
         // This substep's sorted index becomes the particle's build index.
-        sk.x_build[i] = xi;  // w: the particle's id, which the cell pass checks
-        // The build index travels with the particle in its velocity's w (the force pass keeps it).
-        reinterpret_cast<uint32_t*>(const_cast<float4*>(vel) + i)[3] = i;
+        sk.x_build[i] = xi;
+        sk.b_of_id[__float_as_uint(xi.w)] = i;
         sk.count[i] = min(c, sk.cap) | (usable ? kSkinUsable : 0u);
         // The scene's usable lists, one atomic per warp and scene.
         const uint32_t g = __match_any_sync(__activemask(), sc);
@@ -1129,7 +1122,7 @@ __global__ void __launch_bounds__(kListBlock, 10)
         uint32_t c = 0u, row = 0u;
         walk = sk.stale[kBatch ? (uint32_t)__ldg(L.scene_of + i) : 0u] != 0u;
         if (!walk) {
-            row = __float_as_uint(__ldg(vel + i).w);  // the build index (checked by the cell pass)
+            row = __ldg(sk.b_of_id + __float_as_uint(xi.w));
             c = __ldg(sk.count + row);
             walk = (c & kSkinUsable) == 0u;
         }
@@ -1527,7 +1520,7 @@ __device__ __forceinline__ void force_finish(const SceneParams& p, uint32_t i, c
     }
     if (acc_out) acc_out[i] = make_float4(ax, ay, az, 0.0f);
     const float nvx = vi.x + ax * p.dt, nvy = vi.y + ay * p.dt, nvz = vi.z + az * p.dt;
-    vel_out[i] = make_float4(nvx, nvy, nvz, vi.w);  // w: the skin lists' build index
+    vel_out[i] = make_float4(nvx, nvy, nvz, 0.0f);
     pos_out[i] = make_float4(xi.x + nvx * p.dt, xi.y + nvy * p.dt, xi.z + nvz * p.dt, xi.w);
 }
 
@@ -2001,15 +1994,15 @@ cudaError_t launch_cells_reorder(const StepLaunch& L, uint32_t n, const uint32_t
     switch (kc.cell_block) {
         case 128:
             k_cells_reorder<128><<<(n + 128u) / 128u, 128, 0, s>>>(L, n, skeys, perm, cell_scan, pos_in,
-                                                                 vel_in, pos_out, vel_out, zero, zero_words, pkeys_out, guess, sk.xcur, sk.x_build, sk.stale);
+                                                                 vel_in, pos_out, vel_out, zero, zero_words, pkeys_out, guess, sk.b_of_id, sk.xcur, sk.x_build, sk.stale);
             break;
         case 512:
             k_cells_reorder<512><<<(n + 512u) / 512u, 512, 0, s>>>(L, n, skeys, perm, cell_scan, pos_in,
-                                                                 vel_in, pos_out, vel_out, zero, zero_words, pkeys_out, guess, sk.xcur, sk.x_build, sk.stale);
+                                                                 vel_in, pos_out, vel_out, zero, zero_words, pkeys_out, guess, sk.b_of_id, sk.xcur, sk.x_build, sk.stale);
             break;
         default:
             k_cells_reorder<256><<<(n + 256u) / 256u, 256, 0, s>>>(L, n, skeys, perm, cell_scan, pos_in,
-                                                                 vel_in, pos_out, vel_out, zero, zero_words, pkeys_out, guess, sk.xcur, sk.x_build, sk.stale);
+                                                                 vel_in, pos_out, vel_out, zero, zero_words, pkeys_out, guess, sk.b_of_id, sk.xcur, sk.x_build, sk.stale);
     }
     return cudaGetLastError();
 }
