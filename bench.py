@@ -457,7 +457,7 @@ def time_stress(args, stream, torch):
     m.set_stream(stream.cuda_stream)
     m.set_neighbor_capacity(STRESS_NBR_SLOTS)  # the blob's ~900 neighbours fit the lists
     # Launch shapes for this state (the autotuner restores the state before every candidate).
-    tuned = m.autotune(repeats=1, use_cache=False) if args.autotune else m.get_tune_config()
+    tuned = m.autotune(repeats=3, use_cache=False) if args.autotune else m.get_tune_config()
     reps = max(3, min(args.steps, 10))
     for _ in range(args.warmup):
         m.set_particle_state(w.pos, w.vel)
