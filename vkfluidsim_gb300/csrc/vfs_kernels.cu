@@ -737,17 +737,39 @@ __device__ __forceinline__ int first_block_cells(uint32_t c) {
     return n;
 }
 
-// True when the 125 cells around (cx, cy, cz) provably have distinct keys, so that a walk of their
-// buckets meets every particle once. The block splits into at most eight boxes, one per hash
-// block it touches; inside a box the hashes are hmin + lx + 50 ly + 2500 lz, so its keys lie in the
+// Whether box a (keys (ka + x + 50 y + 2500 z) mod n for x, y, z below its widths wa) and box b
+// (keys from kb, widths wb) share a key: each key of a, minus kb modulo n, is one of b's offsets
+// exactly when its digits in base 50 / 2500 lie below b's widths (every offset is < 5 + 50 * 5 +
+// 2500 * 5 < n, so the decomposition is unique).
+__device__ __forceinline__ bool boxes_share_a_key(uint32_t ka, const uint32_t wa[3], uint32_t kb,
+                                                  const uint32_t wb[3], uint32_t n) {
+#pragma unroll 1
+    for (uint32_t z = 0; z < wa[2]; z++)
+#pragma unroll 1
+        for (uint32_t y = 0; y < wa[1]; y++)
+#pragma unroll 1
+            for (uint32_t x = 0; x < wa[0]; x++) {
+                uint32_t key = ka + x + 50u * y + 2500u * z;
+                if (key >= n) key -= n;  // ka < n and the offset is below n
+                const uint32_t d = key >= kb ? key - kb : key + (n - kb);
+                const uint32_t oz = d / 2500u, r = d - 2500u * oz, oy = r / 50u, ox = r - 50u * oy;
+                if (ox < wb[0] && oy < wb[1] && oz < wb[2]) return true;
+            }
+    return false;
+}
+
+// True when the 125 cells around (cx, cy, cz) have distinct keys, so that a walk of their buckets
+// meets every particle once. The block splits into at most eight boxes, one per hash block it
+// touches; inside a box the hashes are hmin + lx + 50 ly + 2500 lz, so its keys lie in the
 // circular interval [hmin mod n, hmin mod n + span] (span <= 10204) and are distinct when
 // n > 10204 and the box's hashes do not wrap 2^32. Boxes whose intervals are disjoint modulo n
-// share no key.
+// share no key; boxes whose intervals overlap are compared key by key (boxes_share_a_key), so
+// the answer is exact under those two conditions.
 __device__ __forceinline__ bool skin_keys_distinct(const SceneParams& p, uint32_t cx, uint32_t cy,
                                                    uint32_t cz) {
     if (p.n <= 10204u) return false;
     const int fx = first_block_cells(cx), fy = first_block_cells(cy), fz = first_block_cells(cz);
-    uint32_t k[8], span[8];
+    uint32_t k[8], span[8], w[8][3];
     int boxes = 0;
 #pragma unroll 1
     for (int bz = 0; bz < (fz < 5 ? 2 : 1); bz++)
@@ -763,6 +785,9 @@ __device__ __forceinline__ bool skin_keys_distinct(const SceneParams& p, uint32_
                 if (hi < lo) return false;
                 k[boxes] = key_mod(lo, p.mod_magic, p.n);
                 span[boxes] = hi - lo;
+                w[boxes][0] = x1 - x0 + 1u;
+                w[boxes][1] = y1 - y0 + 1u;
+                w[boxes][2] = z1 - z0 + 1u;
                 boxes++;
             }
 #pragma unroll 1
@@ -771,7 +796,8 @@ __device__ __forceinline__ bool skin_keys_distinct(const SceneParams& p, uint32_
         for (int b = 0; b < a; b++) {
             const uint32_t ab = k[b] >= k[a] ? k[b] - k[a] : k[b] + (p.n - k[a]);  // (k_b - k_a) mod n
             const uint32_t ba = k[a] >= k[b] ? k[a] - k[b] : k[a] + (p.n - k[b]);
-            if (ab <= span[a] || ba <= span[b]) return false;
+            if ((ab <= span[a] || ba <= span[b]) && boxes_share_a_key(k[a], w[a], k[b], w[b], p.n))
+                return false;
         }
     return true;
 }
