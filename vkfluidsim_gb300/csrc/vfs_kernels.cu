@@ -1010,119 +1010,123 @@ __global__ void __launch_bounds__(kNbrBlock, kMinBlocks)
     __shared__ float4 s_stage[kStaging ? kNbrBlock : 1];
     const int tid = threadIdx.x;
     const uint32_t lane = (uint32_t)(tid & 31);
-    // No lane returns before the warp's collective steps: inactive lanes carry act = false.
-    const uint32_t t = blockIdx.x * kNbrBlock + tid;
-    bool act = t < L.total;
-    uint32_t i = act ? t : 0u, sc = 0u;
-    bool rebuild = false;
-    if (act && sk.list) {
-        if (kBatch) {
-            // Slot t of the queue: valid below its list block's count of walkers.
-            if (t % kListBlock >= __ldg(sk.seg_n + t / kListBlock)) {
-                act = false;
-            } else {
-                i = __ldg(sk.queue + t);
-                sc = (uint32_t)__ldg(L.scene_of + i);
-            }
-        } else if (sk.stale[0] == 0u && sk.ctl[kCtlPoor] == 0u) {
-            act = false;  // k_density_walkers walks the single scene's queued particles
-        }  // else a single scene that is stale or whose lists are mostly unusable: every
-           // particle, in index order (no queue)
-        rebuild = act && sk.stale[sc] != 0u && sk.ctl[sc * kSkinCtl + kCtlAllow] != 0u;
-    }
-    if (__ballot_sync(0xffffffffu, act) == 0u) return;  // the whole warp is idle
-    const SceneParams& p = scene_params<kBatch>(L, i);
-    const float4 xi = act ? __ldg(pos + i) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    const uint32_t cx = cell_coord(xi.x, p.h), cy = cell_coord(xi.y, p.h), cz = cell_coord(xi.z, p.h);
-    DensitySum d;
-    d.out = nbr + i;
-    uint32_t s_end = tid;  // shared-memory word one past the last kept candidate (stride kNbrBlock)
-    // Scene constants used per candidate, in registers (a batched launch reads its scene's
-    // parameters from a device table).
-    const float s_inv_h = p.inv_h;
-    const uint32_t s_nbr_cap = p.nbr_cap;
-    auto drain = [&]() {
-#pragma unroll 2
-        for (uint32_t o = tid; o < s_end; o += kNbrBlock) {
-            const uint32_t j = s_j[o];
-            d.add(i, xi, j, __ldg(pos + j), s_inv_h, s_nbr_cap, L.total);
-        }
-        s_end = tid;
-    };
-    const bool distinct = distinct_keys(p, cx, cy, cz);
-    const float h2 = p.h2;
-    uint32_t c = 0;
-    bool usable = false;
-    uint32_t key_lo = 0u, width = 0u;
-    if (kStaging && warp_row_union(p, act, !rebuild, cx, cy, cz, sc, key_lo, width)) {
-        // The staged walk: branch-free append as below, candidates read from shared memory.
-        const uint32_t* scs = scan + p.off;
-        float4* stage = s_stage + (tid & ~31);
-#pragma unroll 1
-        for (uint32_t r = 0; r < 9u; r++) {
-            const uint32_t kA = key_lo + 50u * (r % 3u) + 2500u * (r / 3u);
-            const uint32_t b = __ldg(scs + kA), e = __ldg(scs + kA + width);
-#pragma unroll 1
-            for (uint32_t base = b; base < e; base += 32u) {
-                const uint32_t jl = base + lane;
-                if (jl < e) stage[lane] = __ldg(pos + jl);
-                __syncwarp();
-                const uint32_t cnt = min(32u, e - base);
-#pragma unroll 4
-                for (uint32_t k = 0; k < cnt; k++) {
-                    const float4 xj = stage[k];
-                    s_j[s_end] = base + k;
-                    s_end += act && in_range2(xi, xj) <= h2 ? kNbrBlock : 0u;
-                    if ((k & 3u) == 3u && s_end > tid + kDrainAt * kNbrBlock) drain();
+    // No lane leaves an iteration before the warp's collective steps: inactive lanes carry
+    // act = false. The grid strides over the slots (a launch of one or two waves whose blocks
+    // return at once when a single scene's particles are all summed from their lists).
+    for (uint32_t base = blockIdx.x * kNbrBlock; base < L.total; base += gridDim.x * kNbrBlock) {
+        const uint32_t t = base + tid;
+        bool act = t < L.total;
+        uint32_t i = act ? t : 0u, sc = 0u;
+        bool rebuild = false;
+        if (act && sk.list) {
+            if (kBatch) {
+                // Slot t of the queue: valid below its list block's count of walkers.
+                if (t % kListBlock >= __ldg(sk.seg_n + t / kListBlock)) {
+                    act = false;
+                } else {
+                    i = __ldg(sk.queue + t);
+                    sc = (uint32_t)__ldg(L.scene_of + i);
                 }
-                if (s_end > tid + kDrainAt * kNbrBlock) drain();
-                __syncwarp();  // the next chunk overwrites the stage
-            }
+            } else if (sk.stale[0] == 0u && sk.ctl[kCtlPoor] == 0u) {
+                act = false;  // k_density_walkers walks the single scene's queued particles
+            }  // else a single scene that is stale or whose lists are mostly unusable: every
+               // particle, in index order (no queue)
+            rebuild = act && sk.stale[sc] != 0u && sk.ctl[sc * kSkinCtl + kCtlAllow] != 0u;
         }
-        drain();
-    } else if (act) {
-        if (rebuild && skin_keys_distinct(p, cx, cy, cz)) {
-            // A list build, staged in this thread's column of the shared list.
-            c = skin_walk(p, scan, pos, xi, cx, cy, cz, s_j + tid, (size_t)kNbrBlock, sk.cap);
-            usable = c <= sk.cap;
-        }
-        if (usable) {
-            // The density from the staged list (its in-range members, in the visiting order),
-            // then the list written out a slot at a time (a warp's lanes store consecutive words).
-#pragma unroll 1
-            for (uint32_t k = 0; k < c; k++) {
-                const uint32_t j = s_j[k * kNbrBlock + tid];
-                const float r2 = in_range2(xi, __ldg(pos + j));
-                if (r2 <= h2) d.add_r2(i, j, r2, s_inv_h, s_nbr_cap, L.total);
+        if (__ballot_sync(0xffffffffu, act) == 0u) continue;  // the whole warp is idle
+        const SceneParams& p = scene_params<kBatch>(L, i);
+        const float4 xi = act ? __ldg(pos + i) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        const uint32_t cx = cell_coord(xi.x, p.h), cy = cell_coord(xi.y, p.h), cz = cell_coord(xi.z, p.h);
+        DensitySum d;
+        d.out = nbr + i;
+        uint32_t s_end = tid;  // shared-memory word one past the last kept candidate (stride kNbrBlock)
+        // Scene constants used per candidate, in registers (a batched launch reads its scene's
+        // parameters from a device table).
+        const float s_inv_h = p.inv_h;
+        const uint32_t s_nbr_cap = p.nbr_cap;
+        auto drain = [&]() {
+    #pragma unroll 2
+            for (uint32_t o = tid; o < s_end; o += kNbrBlock) {
+                const uint32_t j = s_j[o];
+                d.add(i, xi, j, __ldg(pos + j), s_inv_h, s_nbr_cap, L.total);
             }
-#pragma unroll 1
-            for (uint32_t k = 0; k < c; k++) sk.list[(size_t)k * L.total + i] = s_j[k * kNbrBlock + tid];
-        } else {
-            // Branch-free append: every candidate is stored at the list's end and kept only when
-            // in range (the next one overwrites it otherwise). Lists are drained above kDrainAt,
-            // so the slot index stays below kListCap.
-            for_each_candidate(p, scan, pos, xi, cx, cy, cz, [&](uint32_t j, const float4& xj) {
-                s_j[s_end] = j;
-                s_end += in_range2(xi, xj) <= h2 ? kNbrBlock : 0u;
-            }, [&]() {
-                if (s_end > tid + kDrainAt * kNbrBlock) drain();
-            });
+            s_end = tid;
+        };
+        const bool distinct = distinct_keys(p, cx, cy, cz);
+        const float h2 = p.h2;
+        uint32_t c = 0;
+        bool usable = false;
+        uint32_t key_lo = 0u, width = 0u;
+        if (kStaging && warp_row_union(p, act, !rebuild, cx, cy, cz, sc, key_lo, width)) {
+            // The staged walk: branch-free append as below, candidates read from shared memory.
+            const uint32_t* scs = scan + p.off;
+            float4* stage = s_stage + (tid & ~31);
+    #pragma unroll 1
+            for (uint32_t r = 0; r < 9u; r++) {
+                const uint32_t kA = key_lo + 50u * (r % 3u) + 2500u * (r / 3u);
+                const uint32_t b = __ldg(scs + kA), e = __ldg(scs + kA + width);
+    #pragma unroll 1
+                for (uint32_t base = b; base < e; base += 32u) {
+                    const uint32_t jl = base + lane;
+                    if (jl < e) stage[lane] = __ldg(pos + jl);
+                    __syncwarp();
+                    const uint32_t cnt = min(32u, e - base);
+    #pragma unroll 4
+                    for (uint32_t k = 0; k < cnt; k++) {
+                        const float4 xj = stage[k];
+                        s_j[s_end] = base + k;
+                        s_end += act && in_range2(xi, xj) <= h2 ? kNbrBlock : 0u;
+                        if ((k & 3u) == 3u && s_end > tid + kDrainAt * kNbrBlock) drain();
+                    }
+                    if (s_end > tid + kDrainAt * kNbrBlock) drain();
+                    __syncwarp();  // the next chunk overwrites the stage
+                }
+            }
             drain();
+        } else if (act) {
+            if (rebuild && skin_keys_distinct(p, cx, cy, cz)) {
+                // A list build, staged in this thread's column of the shared list.
+                c = skin_walk(p, scan, pos, xi, cx, cy, cz, s_j + tid, (size_t)kNbrBlock, sk.cap);
+                usable = c <= sk.cap;
+            }
+            if (usable) {
+                // The density from the staged list (its in-range members, in the visiting order),
+                // then the list written out a slot at a time (a warp's lanes store consecutive words).
+    #pragma unroll 1
+                for (uint32_t k = 0; k < c; k++) {
+                    const uint32_t j = s_j[k * kNbrBlock + tid];
+                    const float r2 = in_range2(xi, __ldg(pos + j));
+                    if (r2 <= h2) d.add_r2(i, j, r2, s_inv_h, s_nbr_cap, L.total);
+                }
+    #pragma unroll 1
+                for (uint32_t k = 0; k < c; k++) sk.list[(size_t)k * L.total + i] = s_j[k * kNbrBlock + tid];
+            } else {
+                // Branch-free append: every candidate is stored at the list's end and kept only when
+                // in range (the next one overwrites it otherwise). Lists are drained above kDrainAt,
+                // so the slot index stays below kListCap.
+                for_each_candidate(p, scan, pos, xi, cx, cy, cz, [&](uint32_t j, const float4& xj) {
+                    s_j[s_end] = j;
+                    s_end += in_range2(xi, xj) <= h2 ? kNbrBlock : 0u;
+                }, [&]() {
+                    if (s_end > tid + kDrainAt * kNbrBlock) drain();
+                });
+                drain();
+            }
         }
+        if (!act) continue;
+        if (rebuild) {
+            // This substep's sorted index becomes the particle's build index.
+            sk.x_build[i] = xi;
+            sk.b_of_id[__float_as_uint(xi.w)] = i;
+            sk.count[i] = min(c, sk.cap) | (usable ? kSkinUsable : 0u);
+            // The scene's usable lists, one atomic per warp and scene.
+            const uint32_t g = __match_any_sync(__activemask(), sc);
+            const uint32_t u = __ballot_sync(g, usable);
+            if ((uint32_t)(tid & 31) == (uint32_t)(__ffs(g) - 1) && u)
+                atomicAdd(sk.ctl + sc * kSkinCtl + kCtlUsable, (uint32_t)__popc(u));
+        }
+        density_finish(p, i, xi, vel, cx, cy, cz, distinct, d, rec, aux, bnd, nbr_count);
     }
-    if (!act) return;
-    if (rebuild) {
-        // This substep's sorted index becomes the particle's build index.
-        sk.x_build[i] = xi;
-        sk.b_of_id[__float_as_uint(xi.w)] = i;
-        sk.count[i] = min(c, sk.cap) | (usable ? kSkinUsable : 0u);
-        // The scene's usable lists, one atomic per warp and scene.
-        const uint32_t g = __match_any_sync(__activemask(), sc);
-        const uint32_t u = __ballot_sync(g, usable);
-        if ((uint32_t)(tid & 31) == (uint32_t)(__ffs(g) - 1) && u)
-            atomicAdd(sk.ctl + sc * kSkinCtl + kCtlUsable, (uint32_t)__popc(u));
-    }
-    density_finish(p, i, xi, vel, cx, cy, cz, distinct, d, rec, aux, bnd, nbr_count);
 }
 
 // The density pass over the skin lists: a particle of a scene that is not stale, whose list is
@@ -2050,7 +2054,10 @@ template <int B, int M>
 void density_shape(const StepLaunch& L, const float4* pos, const float4* vel, float4* rec,
                    const uint32_t* cell_scan, float4* aux, float4* bnd, uint32_t* nbr,
                    uint32_t* nbr_count, const SkinLists& sk, bool staging, cudaStream_t s) {
-    const uint32_t blocks = (L.total + B - 1) / B;
+    const uint32_t all_blocks = (L.total + B - 1) / B;
+    const int sms_ = sm_count();
+    // The walk kernel strides over its slots with two waves of blocks at most.
+    const uint32_t blocks = sms_ > 0 ? min(all_blocks, (uint32_t)sms_ * (uint32_t)M * 2u) : all_blocks;
     if (sk.list) {
         // Skin lists: the list pass first; the walk passes then take the queue it leaves.
         const uint32_t lb = (L.total + kListBlock - 1) / kListBlock;
