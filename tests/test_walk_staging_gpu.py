@@ -54,6 +54,24 @@ def test_staging_is_bit_identical_on_a_dam_break_and_a_batch():
         _same(a, b, f"batch scene {s}")
 
 
+@pytest.mark.parametrize("skin", [0.0, 0.05])
+def test_staging_is_bit_identical_on_a_batch_with_small_scenes(skin):
+    """Scenes of 2048 to 65,536 particles, so that list blocks and the last warp straddle scenes
+    whose tables are too small to stage (n <= 5110) and scenes that stage: an idle lane holding a
+    slot of another scene must not change the warp's choice or the rows it stages."""
+    scenes = W.batched_scenes(n_scenes=48, n_min=2048, n_max=65536, map_res=24, seed=3)
+    assert min(w.n for w in scenes) <= 5110 < max(w.n for w in scenes)
+    bon, boff = W.build_batch(scenes), W.build_batch(scenes)
+    boff.set_walk_staging(False)
+    for b in (bon, boff):
+        b.set_skin(skin)
+        b.substeps(5)
+    for s in range(len(scenes)):
+        a = list(bon.get_neighbor_arrays(s)) + list(bon.copy_data_buffers(s).values())
+        b = list(boff.get_neighbor_arrays(s)) + list(boff.copy_data_buffers(s).values())
+        _same(a, b, f"batch scene {s} (skin {skin})")
+
+
 def test_staging_is_bit_identical_on_the_stress_workload():
     w = W.stress_4m()
     on, off = W.build_model(w), W.build_model(w)

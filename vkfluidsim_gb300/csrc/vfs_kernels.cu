@@ -951,8 +951,10 @@ __device__ __forceinline__ void density_finish(const SceneParams& p, uint32_t i,
 // candidate of a particle lies in its own 27 cells, each of its 27 buckets is met once (distinct
 // keys), and rows and candidates are met in the reference's visiting order, so the in-range
 // sequence and hence the sum are exactly the bucket walk's. Returns false when the warp does not
-// qualify; otherwise the union's first x cell's row keys start at key_lo and each row spans
-// `width` keys. Warp-uniform.
+// qualify; otherwise the union's first x cell's row keys start at index key_lo of the cell scan
+// (the leader's scene offset included) and each row spans `width` keys. Warp-uniform: every test
+// reads the leader's scene (an idle lane of a batched launch holds a slot of another scene), so
+// all 32 lanes take the same branch and stage the same rows.
 __device__ __forceinline__ bool warp_row_union(const SceneParams& p, bool act, bool ok, uint32_t cx,
                                                uint32_t cy, uint32_t cz, uint32_t sc,
                                                uint32_t& key_lo, uint32_t& width) {
@@ -961,6 +963,10 @@ __device__ __forceinline__ bool warp_row_union(const SceneParams& p, bool act, b
     const uint32_t cy0 = __shfl_sync(0xffffffffu, cy, leader);
     const uint32_t cz0 = __shfl_sync(0xffffffffu, cz, leader);
     const uint32_t sc0 = __shfl_sync(0xffffffffu, sc, leader);
+    const uint32_t n0 = __shfl_sync(0xffffffffu, p.n, leader);
+    const uint32_t off0 = __shfl_sync(0xffffffffu, p.off, leader);
+    const unsigned long long magic0 =
+        __shfl_sync(0xffffffffu, (unsigned long long)p.mod_magic, leader);
     int lo = act ? (int)cx : INT_MAX, hi = act ? (int)cx : INT_MIN;
 #pragma unroll
     for (int o = 16; o >= 1; o >>= 1) {
@@ -969,7 +975,7 @@ __device__ __forceinline__ bool warp_row_union(const SceneParams& p, bool act, b
     }
     const bool same = !act || (ok && cy == cy0 && cz == cz0 && sc == sc0);
     if (!__all_sync(0xffffffffu, same)) return false;
-    if ((int64_t)hi - (int64_t)lo > 3 || p.n <= 5110u) return false;
+    if ((int64_t)hi - (int64_t)lo > 3 || n0 <= 5110u) return false;
     const uint32_t c0 = (uint32_t)lo - 1u, c1 = (uint32_t)hi + 1u;
     if ((c0 + 25u) / 50u != (c1 + 25u) / 50u || (cy0 + 24u) / 50u != (cy0 + 26u) / 50u ||
         (cz0 + 24u) / 50u != (cz0 + 26u) / 50u)
@@ -977,9 +983,9 @@ __device__ __forceinline__ bool warp_row_union(const SceneParams& p, bool act, b
     const uint32_t h_lo = hash_cell(c0, cy0 - 1u, cz0 - 1u);
     const uint32_t h_hi = hash_cell(c1, cy0 + 1u, cz0 + 1u);
     if (h_hi < h_lo) return false;  // the block's hashes wrap past 2^32
-    const uint32_t k_lo = key_mod(h_lo, p.mod_magic, p.n);
-    if ((uint64_t)k_lo + (h_hi - h_lo) >= p.n) return false;  // keys wrap past n - 1
-    key_lo = k_lo;
+    const uint32_t k_lo = key_mod(h_lo, (uint64_t)magic0, n0);
+    if ((uint64_t)k_lo + (h_hi - h_lo) >= n0) return false;  // keys wrap past n - 1
+    key_lo = off0 + k_lo;
     width = c1 - c0 + 1u;
     return true;
 }
@@ -1045,7 +1051,7 @@ __global__ void __launch_bounds__(kNbrBlock, kMinBlocks)
         const float s_inv_h = p.inv_h;
         const uint32_t s_nbr_cap = p.nbr_cap;
         auto drain = [&]() {
-    #pragma unroll 2
+#pragma unroll 2
             for (uint32_t o = tid; o < s_end; o += kNbrBlock) {
                 const uint32_t j = s_j[o];
                 d.add(i, xi, j, __ldg(pos + j), s_inv_h, s_nbr_cap, L.total);
@@ -1059,22 +1065,22 @@ __global__ void __launch_bounds__(kNbrBlock, kMinBlocks)
         uint32_t key_lo = 0u, width = 0u;
         if (kStaging && warp_row_union(p, act, !rebuild, cx, cy, cz, sc, key_lo, width)) {
             // The staged walk: branch-free append as below, candidates read from shared memory.
-            const uint32_t* scs = scan + p.off;
+            // key_lo indexes the cell scan directly (the warp's scene offset included).
             float4* stage = s_stage + (tid & ~31);
-    #pragma unroll 1
+#pragma unroll 1
             for (uint32_t r = 0; r < 9u; r++) {
                 const uint32_t kA = key_lo + 50u * (r % 3u) + 2500u * (r / 3u);
-                const uint32_t b = __ldg(scs + kA), e = __ldg(scs + kA + width);
-    #pragma unroll 1
-                for (uint32_t base = b; base < e; base += 32u) {
-                    const uint32_t jl = base + lane;
+                const uint32_t b = __ldg(scan + kA), e = __ldg(scan + kA + width);
+#pragma unroll 1
+                for (uint32_t jb = b; jb < e; jb += 32u) {
+                    const uint32_t jl = jb + lane;
                     if (jl < e) stage[lane] = __ldg(pos + jl);
                     __syncwarp();
-                    const uint32_t cnt = min(32u, e - base);
-    #pragma unroll 4
+                    const uint32_t cnt = min(32u, e - jb);
+#pragma unroll 4
                     for (uint32_t k = 0; k < cnt; k++) {
                         const float4 xj = stage[k];
-                        s_j[s_end] = base + k;
+                        s_j[s_end] = jb + k;
                         s_end += act && in_range2(xi, xj) <= h2 ? kNbrBlock : 0u;
                         if ((k & 3u) == 3u && s_end > tid + kDrainAt * kNbrBlock) drain();
                     }
@@ -1092,13 +1098,13 @@ __global__ void __launch_bounds__(kNbrBlock, kMinBlocks)
             if (usable) {
                 // The density from the staged list (its in-range members, in the visiting order),
                 // then the list written out a slot at a time (a warp's lanes store consecutive words).
-    #pragma unroll 1
+#pragma unroll 1
                 for (uint32_t k = 0; k < c; k++) {
                     const uint32_t j = s_j[k * kNbrBlock + tid];
                     const float r2 = in_range2(xi, __ldg(pos + j));
                     if (r2 <= h2) d.add_r2(i, j, r2, s_inv_h, s_nbr_cap, L.total);
                 }
-    #pragma unroll 1
+#pragma unroll 1
                 for (uint32_t k = 0; k < c; k++) sk.list[(size_t)k * L.total + i] = s_j[k * kNbrBlock + tid];
             } else {
                 // Branch-free append: every candidate is stored at the list's end and kept only when
