@@ -375,7 +375,8 @@ int Model::enqueue_substep(cudaEvent_t* ev) {
                                       scratch, (uint32_t)sort_scratch_words(sc), pkeys, cell_guess,
                                       sk, kc, s));
     if (ev) VFS_CUDA_TRY(cudaEventRecord(ev[4], s));
-    VFS_CUDA_TRY(launch_density(launch, pos[o], vel[o], rec, cell_scan, aux, bnd, nbr, nbr_count, sk, kc, s));
+    VFS_CUDA_TRY(launch_density(launch, pos[o], vel[o], rec, cell_scan, aux, bnd, nbr, nbr_count, sk,
+                                walk_sched, kc, s));
     if (ev) VFS_CUDA_TRY(cudaEventRecord(ev[5], s));
     VFS_CUDA_TRY(launch_force(launch, pos[o], vel[o], aux, rec, bnd, cell_scan, nbr, nbr_count, pos[c],
                               vel[c], record ? acc : nullptr, sk, kc, s));
@@ -463,6 +464,7 @@ Model::~Model() {
     cudaFree(skin.wcount);
     cudaFree(scratch);
     cudaFree(err);
+    cudaFree(walk_sched);
     if (err_host) cudaFreeHost(err_host);
     cudaFree(d_scenes);
     cudaFree(d_scene_of);
@@ -512,6 +514,8 @@ int Model::init() {
     VFS_CUDA_TRY(cudaMalloc(&nbr_count, N * sizeof(uint32_t)));
     VFS_CUDA_TRY(cudaMalloc(&err, 4));
     VFS_CUDA_TRY(cudaMemset(err, 0, 4));
+    VFS_CUDA_TRY(cudaMalloc(&walk_sched, 2 * sizeof(uint32_t)));
+    VFS_CUDA_TRY(cudaMemset(walk_sched, 0, 2 * sizeof(uint32_t)));
     VFS_CUDA_TRY(cudaMallocHost(&err_host, 4));
     for (int b = 0; b < 2; b++) {
         VFS_CUDA_TRY(cudaMemset(pos[b], 0, N * sizeof(float4)));

@@ -217,10 +217,12 @@ bool planes_mode(uint32_t total);
 // Boundary volume + density + EOS epilogue; writes each particle's neighbour list.
 // Also writes rec[2i], rec[2i+1] = (x, y, z, p/rho^2), (v, m/max(rho, 1e-6)) for the force pass.
 // With skin lists (sk.list set): sums the lists where they are usable and rebuilds flagged scenes.
+// walk_sched: two device words, zero between launches (the walk kernel's run counter, put back to
+// zero by its last warp).
 cudaError_t launch_density(const StepLaunch& L, const float4* pos, const float4* vel, float4* rec,
                            const uint32_t* cell_scan, float4* aux, float4* bnd, uint32_t* nbr,
-                           uint32_t* nbr_count, const SkinLists& sk, const KernelConfig& kc,
-                           cudaStream_t s);
+                           uint32_t* nbr_count, const SkinLists& sk, uint32_t* walk_sched,
+                           const KernelConfig& kc, cudaStream_t s);
 // Pressure + viscosity + wall + symplectic Euler over the density pass's neighbour lists; runs the
 // skin lists' build policy and clears their flags (when sk.stale is set).
 cudaError_t launch_force(const StepLaunch& L, const float4* pos, const float4* vel,

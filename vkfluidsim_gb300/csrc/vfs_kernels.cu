@@ -1007,20 +1007,29 @@ __global__ void __launch_bounds__(kNbrBlock, kMinBlocks)
     k_density(StepLaunch L, const float4* __restrict__ pos, const float4* __restrict__ vel,
               float4* __restrict__ rec, const uint32_t* __restrict__ scan,
               float4* __restrict__ aux, float4* __restrict__ bnd, uint32_t* __restrict__ nbr,
-              uint32_t* __restrict__ nbr_count, SkinLists sk) {
+              uint32_t* __restrict__ nbr_count, SkinLists sk, uint32_t* __restrict__ sched) {
     static_assert(kSkinCap <= (uint32_t)kListCap, "a list build is staged in the shared list");
     static_assert(kNbrBlock % 32 == 0, "whole warps");
+    static_assert(kListBlock % 32 == 0, "a warp's 32 slots lie in one list block");
     __shared__ uint32_t s_j[kListCap * kNbrBlock];
     // Each warp's 32 staged candidates (one placeholder element without staging, so that the
     // shared memory the per-thread walk does not use stays L1 for its candidate loads).
     __shared__ float4 s_stage[kStaging ? kNbrBlock : 1];
     const int tid = threadIdx.x;
     const uint32_t lane = (uint32_t)(tid & 31);
-    // No lane leaves an iteration before the warp's collective steps: inactive lanes carry
-    // act = false. The grid strides over the slots (a launch of one or two waves whose blocks
-    // return at once when a single scene's particles are all summed from their lists).
-    for (uint32_t base = blockIdx.x * kNbrBlock; base < L.total; base += gridDim.x * kNbrBlock) {
-        const uint32_t t = base + tid;
+    // A single scene whose lists are current and mostly usable: k_density_list and
+    // k_density_walkers cover every particle, and the whole launch returns here.
+    if (!kBatch && sk.list && sk.stale[0] == 0u && sk.ctl[kCtlPoor] == 0u) return;
+    // Every warp takes runs of 32 slots: first the run of its own index, then runs claimed from
+    // the launch's counter (sched[0]), until none is left. Walks differ widely in length (the
+    // queued walkers of a batch, the list builds of a stale scene), and a warp that finishes early
+    // takes the next run. No lane leaves a run before the warp's collective steps: inactive lanes
+    // carry act = false.
+    const uint32_t runs = (L.total + 31u) / 32u;
+    const uint32_t warps = gridDim.x * (uint32_t)(kNbrBlock / 32);
+    uint32_t run = blockIdx.x * (uint32_t)(kNbrBlock / 32) + (uint32_t)(tid >> 5);
+    for (; run < runs;) {
+        const uint32_t t = run * 32u + lane;
         bool act = t < L.total;
         uint32_t i = act ? t : 0u, sc = 0u;
         bool rebuild = false;
@@ -1039,7 +1048,14 @@ __global__ void __launch_bounds__(kNbrBlock, kMinBlocks)
                // particle, in index order (no queue)
             rebuild = act && sk.stale[sc] != 0u && sk.ctl[sc * kSkinCtl + kCtlAllow] != 0u;
         }
-        if (__ballot_sync(0xffffffffu, act) == 0u) continue;  // the whole warp is idle
+        // The next run, claimed now so that the counter's latency hides behind this one.
+        uint32_t next = 0u;
+        if (lane == 0u) next = warps + atomicAdd(sched, 1u);
+        next = __shfl_sync(0xffffffffu, next, 0);
+        if (__ballot_sync(0xffffffffu, act) == 0u) {  // the whole warp is idle
+            run = next;
+            continue;
+        }
         const SceneParams& p = scene_params<kBatch>(L, i);
         const float4 xi = act ? __ldg(pos + i) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         const uint32_t cx = cell_coord(xi.x, p.h), cy = cell_coord(xi.y, p.h), cz = cell_coord(xi.z, p.h);
@@ -1119,6 +1135,7 @@ __global__ void __launch_bounds__(kNbrBlock, kMinBlocks)
                 drain();
             }
         }
+        run = next;
         if (!act) continue;
         if (rebuild) {
             // This substep's sorted index becomes the particle's build index.
@@ -1132,6 +1149,15 @@ __global__ void __launch_bounds__(kNbrBlock, kMinBlocks)
                 atomicAdd(sk.ctl + sc * kSkinCtl + kCtlUsable, (uint32_t)__popc(u));
         }
         density_finish(p, i, xi, vel, cx, cy, cz, distinct, d, rec, aux, bnd, nbr_count);
+    }
+    // The last warp out puts the counter back to zero for the next launch (every other warp has
+    // made its last claim before it counts itself out).
+    if (lane == 0u) {
+        __threadfence();
+        if (atomicAdd(sched + 1, 1u) == warps - 1u) {
+            atomicExch(sched, 0u);
+            atomicExch(sched + 1, 0u);
+        }
     }
 }
 
@@ -2056,14 +2082,34 @@ static int sm_count() {
     return n;
 }
 
+// One resident wave of the walk kernel: its blocks take runs of slots until none is left, so
+// more blocks would only start after the work is gone. Residency per SM is asked of the
+// occupancy calculator once per instantiation.
+template <bool kBatch, int B, int M, bool kStaging>
+void launch_walk(const StepLaunch& L, const float4* pos, const float4* vel, float4* rec,
+                 const uint32_t* cell_scan, float4* aux, float4* bnd, uint32_t* nbr,
+                 uint32_t* nbr_count, const SkinLists& sk, uint32_t* sched, cudaStream_t s) {
+    static std::atomic<int> per_sm{0};
+    int r = per_sm.load(std::memory_order_relaxed);
+    if (r == 0) {
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, k_density<kBatch, B, M, kStaging>, B, 0) ==
+                cudaSuccess && r > 0)
+            per_sm.store(r, std::memory_order_relaxed);
+        else
+            r = M;
+    }
+    const int sms = sm_count();
+    const uint32_t all_blocks = (L.total + B - 1) / B;
+    const uint32_t blocks = sms > 0 ? min(all_blocks, (uint32_t)sms * (uint32_t)r) : all_blocks;
+    k_density<kBatch, B, M, kStaging><<<blocks, B, 0, s>>>(L, pos, vel, rec, cell_scan, aux, bnd, nbr,
+                                                           nbr_count, sk, sched);
+}
+
 template <int B, int M>
 void density_shape(const StepLaunch& L, const float4* pos, const float4* vel, float4* rec,
                    const uint32_t* cell_scan, float4* aux, float4* bnd, uint32_t* nbr,
-                   uint32_t* nbr_count, const SkinLists& sk, bool staging, cudaStream_t s) {
-    const uint32_t all_blocks = (L.total + B - 1) / B;
-    const int sms_ = sm_count();
-    // The walk kernel strides over its slots with two waves of blocks at most.
-    const uint32_t blocks = sms_ > 0 ? min(all_blocks, (uint32_t)sms_ * (uint32_t)M * 2u) : all_blocks;
+                   uint32_t* nbr_count, const SkinLists& sk, uint32_t* sched, bool staging,
+                   cudaStream_t s) {
     if (sk.list) {
         // Skin lists: the list pass first; the walk passes then take the queue it leaves.
         const uint32_t lb = (L.total + kListBlock - 1) / kListBlock;
@@ -2080,14 +2126,14 @@ void density_shape(const StepLaunch& L, const float4* pos, const float4* vel, fl
     }
     if (L.n_scenes > 1) {
         if (staging)
-            k_density<true, B, M, true><<<blocks, B, 0, s>>>(L, pos, vel, rec, cell_scan, aux, bnd, nbr, nbr_count, sk);
+            launch_walk<true, B, M, true>(L, pos, vel, rec, cell_scan, aux, bnd, nbr, nbr_count, sk, sched, s);
         else
-            k_density<true, B, M, false><<<blocks, B, 0, s>>>(L, pos, vel, rec, cell_scan, aux, bnd, nbr, nbr_count, sk);
+            launch_walk<true, B, M, false>(L, pos, vel, rec, cell_scan, aux, bnd, nbr, nbr_count, sk, sched, s);
     } else {
         if (staging)
-            k_density<false, B, M, true><<<blocks, B, 0, s>>>(L, pos, vel, rec, cell_scan, aux, bnd, nbr, nbr_count, sk);
+            launch_walk<false, B, M, true>(L, pos, vel, rec, cell_scan, aux, bnd, nbr, nbr_count, sk, sched, s);
         else
-            k_density<false, B, M, false><<<blocks, B, 0, s>>>(L, pos, vel, rec, cell_scan, aux, bnd, nbr, nbr_count, sk);
+            launch_walk<false, B, M, false>(L, pos, vel, rec, cell_scan, aux, bnd, nbr, nbr_count, sk, sched, s);
     }
 }
 
@@ -2112,8 +2158,8 @@ bool planes_mode(uint32_t total) {
 
 cudaError_t launch_density(const StepLaunch& L, const float4* pos, const float4* vel, float4* rec,
                            const uint32_t* cell_scan, float4* aux, float4* bnd, uint32_t* nbr,
-                           uint32_t* nbr_count, const SkinLists& sk, const KernelConfig& kc,
-                           cudaStream_t s) {
+                           uint32_t* nbr_count, const SkinLists& sk, uint32_t* walk_sched,
+                           const KernelConfig& kc, cudaStream_t s) {
     if (L.total == 0) return cudaSuccess;
     if (planes_mode(L.total)) {
         const uint32_t blocks = (L.total + 29u) / 30u;
@@ -2127,10 +2173,10 @@ cudaError_t launch_density(const StepLaunch& L, const float4* pos, const float4*
     }
     const bool st = kc.walk_staging != 0;
     switch (kc.nbr_shape) {
-        case kNbr128x8: density_shape<128, 8>(L, pos, vel, rec, cell_scan, aux, bnd, nbr, nbr_count, sk, st, s); break;
-        case kNbr96x8: density_shape<96, 8>(L, pos, vel, rec, cell_scan, aux, bnd, nbr, nbr_count, sk, st, s); break;
-        case kNbr64x12: density_shape<64, 12>(L, pos, vel, rec, cell_scan, aux, bnd, nbr, nbr_count, sk, st, s); break;
-        default: density_shape<128, 6>(L, pos, vel, rec, cell_scan, aux, bnd, nbr, nbr_count, sk, st, s);
+        case kNbr128x8: density_shape<128, 8>(L, pos, vel, rec, cell_scan, aux, bnd, nbr, nbr_count, sk, walk_sched, st, s); break;
+        case kNbr96x8: density_shape<96, 8>(L, pos, vel, rec, cell_scan, aux, bnd, nbr, nbr_count, sk, walk_sched, st, s); break;
+        case kNbr64x12: density_shape<64, 12>(L, pos, vel, rec, cell_scan, aux, bnd, nbr, nbr_count, sk, walk_sched, st, s); break;
+        default: density_shape<128, 6>(L, pos, vel, rec, cell_scan, aux, bnd, nbr, nbr_count, sk, walk_sched, st, s);
     }
     return cudaGetLastError();
 }

@@ -76,6 +76,7 @@ struct Model {
     size_t scratch_words = 0;
     uint32_t* err = nullptr;
     uint32_t* err_host = nullptr;  // pinned copy of the error word read by check_device
+    uint32_t* walk_sched = nullptr;  // two words: the density walk's run counter (zero between launches)
     SceneParams* d_scenes = nullptr;   // batched launches: the scene table
     uint16_t* d_scene_of = nullptr;    // batched launches: scene id per particle
     DevObject* d_objects = nullptr;    // boundary objects of all scenes
