@@ -18,8 +18,10 @@ density, pressure + viscosity + integration).
   blows up near substep 250 with the configured parameters, in the oracle as on the GPU; its
   per-segment times show what that does to the cost).
 
-``--impl reference`` times that CPU restatement alone, on every host thread (the reference's own
-Vulkan pipeline has no runnable form here: no Vulkan stack or software renderer exists).
+``--impl reference`` times the reference's own step code on every host thread: its Slang compute
+shaders compiled as C++ for the host and driven in the order of its host code (oracle/_ref), or,
+where that build is absent, the oracle. The reference's Vulkan pipeline itself has no runnable
+form here (no Vulkan stack or software renderer exists).
 """
 from __future__ import annotations
 
@@ -704,8 +706,13 @@ def run_gpu(args):
     prof = m.profile_substeps(max(3, min(args.steps, 10)))
     skin_build_ms = None
     if m.skin > 0:
-        m.set_skin(m.skin)  # every list is rebuilt by the next substep: time a build substep
-        skin_build_ms = m.profile_substeps(1)["density"]
+        # set_skin drops every list, so the next substep rebuilds them: the median of three such
+        # build substeps' density phases.
+        builds = []
+        for _ in range(3):
+            m.set_skin(m.skin)
+            builds.append(m.profile_substeps(1)["density"])
+        skin_build_ms = float(statistics.median(builds))
     digits, items, passes = m.get_sort_config()
     kernel_phases = {k: v for k, v in prof.items() if k in B_PHASE}
     dom = max(kernel_phases, key=kernel_phases.get)

@@ -758,47 +758,58 @@ __device__ __forceinline__ bool boxes_share_a_key(uint32_t ka, const uint32_t wa
     return false;
 }
 
+// Box `slot` of the 5 x 5 x 5 block around (cx, cy, cz): bit 0 (1, 2) of the slot picks the
+// cells of the block's first or second 50-cell hash block along x (y, z). Returns false when the
+// slot is not a box of this block (the block lies in one hash block along that axis); otherwise
+// its first key k, the span of its hashes (its last minus its first) and its widths, or wraps =
+// true when its hashes wrap 2^32. Computed from the slot alone, so no per-box array is kept.
+__device__ __forceinline__ bool key_box(const SceneParams& p, uint32_t cx, uint32_t cy, uint32_t cz,
+                                        uint32_t fx, uint32_t fy, uint32_t fz, uint32_t slot,
+                                        uint32_t& k, uint32_t& span, uint32_t w[3], bool& wraps) {
+    const bool bx = slot & 1u, by = slot & 2u, bz = slot & 4u;
+    if ((bx && fx == 5u) || (by && fy == 5u) || (bz && fz == 5u)) return false;
+    const uint32_t x0 = bx ? fx : 0u, x1 = bx ? 4u : fx - 1u;
+    const uint32_t y0 = by ? fy : 0u, y1 = by ? 4u : fy - 1u;
+    const uint32_t z0 = bz ? fz : 0u, z1 = bz ? 4u : fz - 1u;
+    const uint32_t lo = hash_cell(cx - 2u + x0, cy - 2u + y0, cz - 2u + z0);
+    const uint32_t hi = hash_cell(cx - 2u + x1, cy - 2u + y1, cz - 2u + z1);
+    wraps = hi < lo;
+    k = key_mod(lo, p.mod_magic, p.n);
+    span = hi - lo;
+    w[0] = x1 - x0 + 1u;
+    w[1] = y1 - y0 + 1u;
+    w[2] = z1 - z0 + 1u;
+    return true;
+}
+
 // True when the 125 cells around (cx, cy, cz) have distinct keys, so that a walk of their buckets
 // meets every particle once. The block splits into at most eight boxes, one per hash block it
 // touches; inside a box the hashes are hmin + lx + 50 ly + 2500 lz, so its keys lie in the
 // circular interval [hmin mod n, hmin mod n + span] (span <= 10204) and are distinct when
 // n > 10204 and the box's hashes do not wrap 2^32. Boxes whose intervals are disjoint modulo n
 // share no key; boxes whose intervals overlap are compared key by key (boxes_share_a_key), so
-// the answer is exact under those two conditions.
+// the answer is exact under those two conditions. Most blocks lie in one hash block (one box, no
+// pair to compare); the boxes of a pair are recomputed from their slots rather than kept in a
+// per-thread array, which would live in local memory.
 __device__ __forceinline__ bool skin_keys_distinct(const SceneParams& p, uint32_t cx, uint32_t cy,
                                                    uint32_t cz) {
     if (p.n <= 10204u) return false;
-    const int fx = first_block_cells(cx), fy = first_block_cells(cy), fz = first_block_cells(cz);
-    uint32_t k[8], span[8], w[8][3];
-    int boxes = 0;
+    const uint32_t fx = (uint32_t)first_block_cells(cx), fy = (uint32_t)first_block_cells(cy),
+                   fz = (uint32_t)first_block_cells(cz);
+    uint32_t ka, sa, wa[3], kb, sb, wb[3];
+    bool wraps;
 #pragma unroll 1
-    for (int bz = 0; bz < (fz < 5 ? 2 : 1); bz++)
+    for (uint32_t a = 0; a < 8u; a++) {
+        if (!key_box(p, cx, cy, cz, fx, fy, fz, a, ka, sa, wa, wraps)) continue;
+        if (wraps) return false;
 #pragma unroll 1
-        for (int by = 0; by < (fy < 5 ? 2 : 1); by++)
-#pragma unroll 1
-            for (int bx = 0; bx < (fx < 5 ? 2 : 1); bx++) {
-                const uint32_t x0 = bx ? fx : 0, x1 = bx ? 4 : fx - 1;
-                const uint32_t y0 = by ? fy : 0, y1 = by ? 4 : fy - 1;
-                const uint32_t z0 = bz ? fz : 0, z1 = bz ? 4 : fz - 1;
-                const uint32_t lo = hash_cell(cx - 2u + x0, cy - 2u + y0, cz - 2u + z0);
-                const uint32_t hi = hash_cell(cx - 2u + x1, cy - 2u + y1, cz - 2u + z1);
-                if (hi < lo) return false;
-                k[boxes] = key_mod(lo, p.mod_magic, p.n);
-                span[boxes] = hi - lo;
-                w[boxes][0] = x1 - x0 + 1u;
-                w[boxes][1] = y1 - y0 + 1u;
-                w[boxes][2] = z1 - z0 + 1u;
-                boxes++;
-            }
-#pragma unroll 1
-    for (int a = 1; a < boxes; a++)
-#pragma unroll 1
-        for (int b = 0; b < a; b++) {
-            const uint32_t ab = k[b] >= k[a] ? k[b] - k[a] : k[b] + (p.n - k[a]);  // (k_b - k_a) mod n
-            const uint32_t ba = k[a] >= k[b] ? k[a] - k[b] : k[a] + (p.n - k[b]);
-            if ((ab <= span[a] || ba <= span[b]) && boxes_share_a_key(k[a], w[a], k[b], w[b], p.n))
-                return false;
+        for (uint32_t b = 0; b < a; b++) {
+            if (!key_box(p, cx, cy, cz, fx, fy, fz, b, kb, sb, wb, wraps)) continue;
+            const uint32_t ab = kb >= ka ? kb - ka : kb + (p.n - ka);  // (k_b - k_a) mod n
+            const uint32_t ba = ka >= kb ? ka - kb : ka + (p.n - kb);
+            if ((ab <= sa || ba <= sb) && boxes_share_a_key(ka, wa, kb, wb, p.n)) return false;
         }
+    }
     return true;
 }
 
