@@ -1708,24 +1708,17 @@ __global__ void __launch_bounds__(kNbrBlock, kMinBlocks)
 // ones in index order; and the digit histograms of the moved keys. A tile is 256 threads x kDeltaItems particles
 // (particle tile * kDeltaTile + item * 256 + thread, so every load is coalesced); tiles are
 // claimed in order and chained by a bounded decoupled look-back over their moved counts.
-// Decoupled look-back of tile `tile` over single-counter status words, a whole block of kThreads
-// threads wide: thread r reads tile - 1 - r, so each step covers kThreads predecessors. Sums the
-// aggregates up to and including the nearest inclusive prefix. When every tile of a launch runs
-// at once, the inclusive prefixes spread only as fast as the look-back steps: one warp wide, the
-// last tiles of a 1,024-tile launch waited some sixteen dependent rounds; a block-wide step needs
-// at most four. Each thread polls a word that has published nothing at most kLookbackSpinLimit
-// times, then sets kErrLookbackTimeout and counts it as zero. Called by the whole block (it
-// synchronises it); every thread returns the same sum.
-template <int kThreads>
-__device__ __forceinline__ uint32_t block_lookback(const uint32_t* status, uint32_t tile,
-                                                   uint32_t* err) {
-    constexpr int kWarps = kThreads / 32;
-    __shared__ uint32_t s_first[kWarps], s_sum[kWarps];
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+// Decoupled look-back of tile `tile` over single-counter status words, one warp wide: lane l reads
+// tile - 1 - l, so each step covers 32 predecessors. Sums aggregates up to and including the
+// nearest inclusive prefix. Each lane polls a word that has published nothing at most
+// kLookbackSpinLimit times, then sets kErrLookbackTimeout and counts it as zero. Called by a
+// whole warp; every lane returns the same sum.
+__device__ __forceinline__ uint32_t warp_lookback(const uint32_t* status, uint32_t tile, uint32_t* err) {
+    const int lane = threadIdx.x & 31;
     uint32_t excl = 0u;
     int64_t top = (int64_t)tile - 1;  // nearest predecessor not yet summed
     while (top >= 0) {
-        const int64_t t = top - tid;
+        const int64_t t = top - lane;
         uint32_t v = kFlagPrefix;  // below tile 0: an empty prefix
         if (t >= 0) {
             uint32_t spins = 0u;
@@ -1741,21 +1734,13 @@ __device__ __forceinline__ uint32_t block_lookback(const uint32_t* status, uint3
             }
         }
         const uint32_t pre = __ballot_sync(0xffffffffu, (v & ~kCountMask) == kFlagPrefix);
-        if (lane == 0) s_first[warp] = pre ? (uint32_t)(warp * 32 + __ffs(pre) - 1) : 0xffffffffu;
-        __syncthreads();
-        uint32_t stop = 0xffffffffu;  // the nearest predecessor holding an inclusive prefix
-#pragma unroll
-        for (int w = 0; w < kWarps; w++) stop = min(stop, s_first[w]);
-        uint32_t c = (uint32_t)tid <= stop ? (v & kCountMask) : 0u;  // summed up to and with it
+        const int stop = pre ? __ffs(pre) - 1 : 31;  // lanes 0..stop are summed
+        uint32_t c = lane <= stop ? (v & kCountMask) : 0u;
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
-        if (lane == 0) s_sum[warp] = c;
-        __syncthreads();
-#pragma unroll
-        for (int w = 0; w < kWarps; w++) excl += s_sum[w];
-        __syncthreads();  // s_first and s_sum are rewritten by the next step
-        if (stop != 0xffffffffu) break;
-        top -= kThreads;
+        excl += c;
+        if (pre) break;
+        top -= 32;
     }
     return excl;
 }
@@ -1773,7 +1758,7 @@ __global__ void __launch_bounds__(256)
                  uint32_t* __restrict__ err) {
     __shared__ uint32_t s_h[kMaxSortPasses * kMaxSortBins];
     __shared__ uint32_t s_cnt[kDeltaItems * 8];  // moved count per (item, warp), then its offset
-    __shared__ uint32_t s_blk, s_excl, s_total;
+    __shared__ uint32_t s_blk, s_excl;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int bins = 1 << digit_bits;
     const uint32_t mask = (uint32_t)bins - 1u;
@@ -1838,21 +1823,20 @@ __global__ void __launch_bounds__(256)
             run += c[q];
         }
         const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
-        if (lane == 0) {
-            s_total = total;
-            st_volatile(status + tile, (tile == 0u ? kFlagPrefix : kFlagAggregate) | total);
+        uint32_t excl = 0u;
+        if (tile == 0u) {
+            if (lane == 0) st_volatile(status, kFlagPrefix | total);
+        } else {
+            if (lane == 0) st_volatile(status + tile, kFlagAggregate | total);
+            excl = warp_lookback(status, tile, err);
+            if (lane == 0) st_volatile(status + tile, kFlagPrefix | ((excl + total) & kCountMask));
         }
-    }
-    __syncthreads();
-    // The moved particles of all earlier tiles, block-wide (tile 0 has none before it).
-    const uint32_t excl = tile == 0u ? 0u : block_lookback<256>(status, tile, err);
-    if (tid == 0) {
-        const uint32_t total = s_total;
-        if (tile != 0u) st_volatile(status + tile, kFlagPrefix | ((excl + total) & kCountMask));
-        s_excl = excl;
-        if (tile == gridDim.x - 1u) {
-            *mcount = excl + total;
-            bits[2u * ((L.total + 31u) >> 5)] = excl + total;  // pre[W]
+        if (lane == 0) {
+            s_excl = excl;
+            if (tile == gridDim.x - 1u) {
+                *mcount = excl + total;
+                bits[2u * ((L.total + 31u) >> 5)] = excl + total;  // pre[W]
+            }
         }
     }
     __syncthreads();
