@@ -527,7 +527,8 @@ __global__ void __launch_bounds__(kCellBlock)
                     uint32_t* __restrict__ zero, uint32_t zero_words,
                     uint32_t* __restrict__ pkeys_out, uint32_t* guess,
                     const uint32_t* __restrict__ b_of_id, float4* __restrict__ xcur,
-                    const float4* __restrict__ x_build, uint32_t* __restrict__ stale) {
+                    const float4* __restrict__ x_build, uint32_t* __restrict__ stale,
+                    const uint32_t* __restrict__ ctl) {
     __shared__ uint32_t s_lo, s_hi;
     // The sort is done with its scratch (histograms, tile counters, look-back status): clear it
     // for the next substep here instead of in a separate memset.
@@ -557,19 +558,26 @@ __global__ void __launch_bounds__(kCellBlock)
         pos_out[i] = x;
         vel_out[i] = __ldg(vel_in + src);
         if (xcur) {
-            // Skin lists: the particle's current position and sorted index under its build
-            // index (the list pass gathers both with one load), and its displacement since the
-            // build.
-            const uint32_t id = __float_as_uint(x.w);
-            const uint32_t bi = id < n ? __ldg(b_of_id + id) : n;
-            if (bi < n) {
-                xcur[bi] = make_float4(x.x, x.y, x.z, __uint_as_float(i));
-                const float4 b = __ldg(x_build + bi);
-                const float dx = x.x - b.x, dy = x.y - b.y, dz = x.z - b.z;
-                const uint32_t sc = L.n_scenes > 1 ? (uint32_t)__ldg(L.scene_of + i) : 0u;
-                const float lim = L.n_scenes > 1 ? L.scenes[sc].skin_half2 : L.one.skin_half2;
-                exceed = !(dx * dx + dy * dy + dz * dz <= lim);
-                exceed_sc = sc;
+            const uint32_t sc = L.n_scenes > 1 ? (uint32_t)__ldg(L.scene_of + i) : 0u;
+            exceed_sc = sc;
+            if (ctl[sc * kSkinCtl + kCtlFresh] == 0u) {
+                // No build yet, or the last build's lists have gone stale: they stay unusable
+                // until the next build, so the scene is stale without a displacement check, and
+                // nothing reads its positions by build index.
+                exceed = true;
+            } else {
+                // Skin lists: the particle's current position and sorted index under its build
+                // index (the list pass gathers both with one load), and its displacement since
+                // the build.
+                const uint32_t id = __float_as_uint(x.w);
+                const uint32_t bi = id < n ? __ldg(b_of_id + id) : n;
+                if (bi < n) {
+                    xcur[bi] = make_float4(x.x, x.y, x.z, __uint_as_float(i));
+                    const float4 b = __ldg(x_build + bi);
+                    const float dx = x.x - b.x, dy = x.y - b.y, dz = x.z - b.z;
+                    const float lim = L.n_scenes > 1 ? L.scenes[sc].skin_half2 : L.one.skin_half2;
+                    exceed = !(dx * dx + dy * dy + dz * dz <= lim);
+                }
             }
         }
         if (pkeys_out) pkeys_out[i] = skeys[i];
@@ -2072,15 +2080,15 @@ cudaError_t launch_cells_reorder(const StepLaunch& L, uint32_t n, const uint32_t
     switch (kc.cell_block) {
         case 128:
             k_cells_reorder<128><<<(n + 128u) / 128u, 128, 0, s>>>(L, n, skeys, perm, cell_scan, pos_in,
-                                                                 vel_in, pos_out, vel_out, zero, zero_words, pkeys_out, guess, sk.b_of_id, sk.xcur, sk.x_build, sk.stale);
+                                                                 vel_in, pos_out, vel_out, zero, zero_words, pkeys_out, guess, sk.b_of_id, sk.xcur, sk.x_build, sk.stale, sk.ctl);
             break;
         case 512:
             k_cells_reorder<512><<<(n + 512u) / 512u, 512, 0, s>>>(L, n, skeys, perm, cell_scan, pos_in,
-                                                                 vel_in, pos_out, vel_out, zero, zero_words, pkeys_out, guess, sk.b_of_id, sk.xcur, sk.x_build, sk.stale);
+                                                                 vel_in, pos_out, vel_out, zero, zero_words, pkeys_out, guess, sk.b_of_id, sk.xcur, sk.x_build, sk.stale, sk.ctl);
             break;
         default:
             k_cells_reorder<256><<<(n + 256u) / 256u, 256, 0, s>>>(L, n, skeys, perm, cell_scan, pos_in,
-                                                                 vel_in, pos_out, vel_out, zero, zero_words, pkeys_out, guess, sk.b_of_id, sk.xcur, sk.x_build, sk.stale);
+                                                                 vel_in, pos_out, vel_out, zero, zero_words, pkeys_out, guess, sk.b_of_id, sk.xcur, sk.x_build, sk.stale, sk.ctl);
     }
     return cudaGetLastError();
 }
