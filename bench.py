@@ -741,10 +741,11 @@ def run_gpu(args):
     fp = lambda t_: C.cast(C.c_void_p(t_.data_ptr()), C.POINTER(C.c_float))  # noqa: E731
     from vkfluidsim_gb300._abi import check
 
-    for _ in range(2):
+    for _ in range(max(3, args.warmup)):  # the same untimed warm-up as the device-timed leg
         check(lib.vfs_model_set_particle_state(m._h, fp(hp), fp(hv), 0, n))
         check(lib.vfs_model_substeps(m._h, 1))
         check(lib.vfs_model_copy_data_buffers(m._h, fp(hp), fp(hv), fp(hd), None))
+    e2e_builds0 = m.skin_builds()
     barrier()
     t0 = time.perf_counter()
     for _ in range(args.steps):
@@ -755,7 +756,8 @@ def run_gpu(args):
     e2e_value, _ = replica_throughput(n, args.steps, 1e3 * (time.perf_counter() - t0), world,
                                       device="cuda")
     e2e = {"value": e2e_value, "unit": UNIT,
-           "h2d_bytes_per_step": 24 * n, "d2h_bytes_per_step": 28 * n}
+           "h2d_bytes_per_step": 24 * n, "d2h_bytes_per_step": 28 * n,
+           "skin_builds": m.skin_builds() - e2e_builds0}
 
     batched = None
     if args.batch_scenes > 0:
