@@ -8,8 +8,8 @@ density, pressure + viscosity + integration).
 * ``value``  particle-steps/s with the state resident in HBM, device-timed with CUDA events per
   step on the launching stream; L2 is flushed (256 MiB write) between timed steps.
 * ``e2e``    the same metric through the public C ABI with host buffers: per step the state is
-  uploaded from pinned memory (set_particle_state), one substep runs, and positions, velocities
-  and densities are read back (copy_data_buffers); wall-clock over the K steps.
+  uploaded from pinned memory, one substep runs, and positions, velocities and densities are
+  read back, in one vfs_model_step_host call (one wait); wall-clock over the K steps.
 * ``roofline`` the dominant kernel's algorithmic bytes per launch / its mean event-timed duration
   against the measured HBM copy bandwidth.
 * ``cpu_baseline`` the oracle (the project's restatement of the reference's shader math) on the
@@ -741,17 +741,19 @@ def run_gpu(args):
     fp = lambda t_: C.cast(C.c_void_p(t_.data_ptr()), C.POINTER(C.c_float))  # noqa: E731
     from vkfluidsim_gb300._abi import check
 
+    # Each step: the state uploaded from the pinned buffers, one substep, positions, velocities
+    # and densities read back into them, one wait (vfs_model_step_host: the upload kernel reads
+    # the buffers before the substep's passes run; the force pass writes the outputs).
+    def e2e_step():
+        check(lib.vfs_model_step_host(m._h, fp(hp), fp(hv), 1, fp(hp), fp(hv), fp(hd)))
+
     for _ in range(max(3, args.warmup)):  # the same untimed warm-up as the device-timed leg
-        check(lib.vfs_model_set_particle_state(m._h, fp(hp), fp(hv), 0, n))
-        check(lib.vfs_model_substeps(m._h, 1))
-        check(lib.vfs_model_copy_data_buffers(m._h, fp(hp), fp(hv), fp(hd), None))
+        e2e_step()
     e2e_builds0 = m.skin_builds()
     barrier()
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        check(lib.vfs_model_set_particle_state(m._h, fp(hp), fp(hv), 0, n))
-        check(lib.vfs_model_substeps(m._h, 1))
-        check(lib.vfs_model_copy_data_buffers(m._h, fp(hp), fp(hv), fp(hd), None))
+        e2e_step()
     barrier()
     e2e_value, _ = replica_throughput(n, args.steps, 1e3 * (time.perf_counter() - t0), world,
                                       device="cuda")

@@ -169,6 +169,16 @@ int vfs_model_set_particles_in_box(vfs_model* m, const float box_size[3], const 
 /* SPHModel::CopyDataBuffers (src/models/model.cpp:158-170), into host arrays; any may be NULL.
  * acc is the acceleration of the last substep (recorded only while field recording is on). */
 int vfs_model_copy_data_buffers(vfs_model* m, float* pos, float* vel, float* dens, float* acc);
+/* One host round trip: SetParticleState of every particle from pos / vel (both NULL: keep the
+ * state), `substeps` substeps, then CopyDataBuffers into pos_out / vel_out / dens_out (any may be
+ * NULL), with a single wait at the end, as the reference's frame records Step and
+ * CopyDataBuffers into one command buffer (src/models/model.cpp:158-170) behind its staged
+ * SetParticleState (model.cpp:139-147). When every given output is page-locked, the last
+ * substep's force pass writes them itself, so the read-back overlaps that pass; otherwise the
+ * outputs are packed after the substeps. Results equal those of the three separate calls.
+ * Single-scene models only. */
+int vfs_model_step_host(vfs_model* m, const float* pos, const float* vel, int32_t substeps,
+                        float* pos_out, float* vel_out, float* dens_out);
 int vfs_model_get_ids(vfs_model* m, uint32_t* ids);
 /* Neighbour arrays of the last substep: SpatialHash keys / sorted_indices / spatial_offsets
  * (src/compute/spatial_hash.h:15-17; offsets hold N for empty keys). Any may be NULL. */

@@ -1,0 +1,78 @@
+"""vfs_model_step_host (upload, substeps and read-back with one wait; with page-locked outputs the
+last force pass writes them) must give exactly what set_particle_state + substeps +
+copy_data_buffers give (SetParticleState, Step, CopyDataBuffers: src/models/model.cpp:139-170).
+Each case runs the same scene both ways over several host round trips, each round's output fed
+back as the next round's input, and compares every output bit for bit."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from vkfluidsim_gb300 import VfsError
+from vkfluidsim_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+
+def _pinned(shape):
+    import torch
+
+    return torch.empty(shape, dtype=torch.float32, pin_memory=True).numpy()
+
+
+def _round_trips(w, rounds, substeps, pinned, keep_state_round=None):
+    ref, fused = W.build_model(w), W.build_model(w)
+    n = w.n
+    pos, vel = np.array(w.pos, np.float32), np.array(w.vel, np.float32)
+    pos_f, vel_f = pos.copy(), vel.copy()
+    out = None
+    if pinned:
+        out = {"positions": _pinned((n, 3)), "velocities": _pinned((n, 3)),
+               "densities": _pinned((n,))}
+    for r in range(rounds):
+        keep = r == keep_state_round
+        if not keep:
+            ref.set_particle_state(pos, vel)
+        ref.substeps(substeps)
+        a = ref.copy_data_buffers()
+        if keep:
+            b = fused.step_host(None, None, substeps, out=out)
+        else:
+            b = fused.step_host(pos_f, vel_f, substeps, out=out)
+        for k in ("positions", "velocities", "densities"):
+            assert np.array_equal(a[k], b[k]), f"round {r}: {k}"
+        assert np.array_equal(ref.get_ids(), fused.get_ids()), f"round {r}: ids"
+        pos, vel = a["positions"].copy(), a["velocities"].copy()
+        pos_f, vel_f = b["positions"].copy(), b["velocities"].copy()
+    return ref, fused
+
+
+@pytest.mark.parametrize("pinned", [True, False])
+def test_step_host_equals_the_three_calls(pinned):
+    w = W.dam_break(dims=(40, 40, 40), map_res=32, stiffness=200.0)
+    ref, fused = _round_trips(w, rounds=6, substeps=2, pinned=pinned, keep_state_round=3)
+    assert ref.skin_builds() == fused.skin_builds()
+
+
+def test_step_host_on_the_1m_scene_with_its_lists():
+    w = W.obstacle_1m()
+    ref, fused = _round_trips(w, rounds=4, substeps=3, pinned=True)
+    assert fused.skin_builds() > 0
+
+
+def test_step_host_on_a_small_model():
+    # 32,768 particles: the three-lane density pass; the force pass is the same kernel.
+    w = W.dam_break_32k()
+    _round_trips(w, rounds=3, substeps=1, pinned=True)
+
+
+def test_step_host_rejects_bad_arguments():
+    m = W.build_model(W.dam_break(dims=(8, 8, 8), map_res=0))
+    with pytest.raises(VfsError):
+        m.step_host(None, None, 0)
+    with pytest.raises(ValueError):
+        m.step_host(np.zeros((m.n_particles, 3), np.float32), None, 1)
+    with pytest.raises(ValueError):
+        m.step_host(np.zeros((3, 3), np.float32), np.zeros((3, 3), np.float32), 1)
+    with pytest.raises(ValueError):
+        m.step_host(None, None, 1, out={"densities": np.zeros(3, np.float64)})

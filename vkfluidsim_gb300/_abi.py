@@ -125,6 +125,7 @@ SIGNATURES = {
     "vfs_model_set_particle_state": (_I, [_P, _F, _F, _U32, C.c_int64]),
     "vfs_model_set_particles_in_box": (_I, [_P, _F, _F, _U32, C.c_int64, C.c_int32, C.c_uint64]),
     "vfs_model_copy_data_buffers": (_I, [_P, _F, _F, _F, _F]),
+    "vfs_model_step_host": (_I, [_P, _F, _F, _I, _F, _F, _F]),
     "vfs_model_get_ids": (_I, [_P, _U]),
     "vfs_model_get_neighbor_arrays": (_I, [_P, _U, _U, _U]),
     "vfs_model_get_boundary_fields": (_I, [_P, _F, _F]),

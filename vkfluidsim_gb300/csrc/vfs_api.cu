@@ -379,7 +379,7 @@ int Model::enqueue_substep(cudaEvent_t* ev) {
                                 walk_sched, kc, s));
     if (ev) VFS_CUDA_TRY(cudaEventRecord(ev[5], s));
     VFS_CUDA_TRY(launch_force(launch, pos[o], vel[o], aux, rec, bnd, cell_scan, nbr, nbr_count, pos[c],
-                              vel[c], record ? acc : nullptr, sk, kc, s));
+                              vel[c], record ? acc : nullptr, sk, kc, s, host_out));
     if (ev) VFS_CUDA_TRY(cudaEventRecord(ev[6], s));
     return VFS_OK;
 }
@@ -648,6 +648,43 @@ void* device_alias(const void* p) {
 
 int Model::set_state(uint32_t scene, const float* pos3, const float* vel3, uint32_t offset,
                      int64_t count) {
+    const int rc = enqueue_set_state(scene, pos3, vel3, offset, count);
+    if (rc) return rc;
+    VFS_CUDA_TRY(cudaStreamSynchronize(stream));
+    return VFS_OK;
+}
+
+int Model::step_host(const float* pos3, const float* vel3, int32_t count, float* pos_out,
+                     float* vel_out, float* dens_out) {
+    if (count < 1) return fail(VFS_ERR_INVALID_ARGUMENT, "step_host needs at least one substep");
+    if (!pos3 != !vel3) return fail(VFS_ERR_INVALID_ARGUMENT, "pos and vel must both be given or both be NULL");
+    if (scenes.size() != 1) return fail(VFS_ERR_INVALID_ARGUMENT, "step_host steps a single-scene model");
+    if (pos3) {
+        const int rc = enqueue_set_state(0, pos3, vel3, 0, -1);
+        if (rc) return rc;
+    }
+    HostOut ho;
+    ho.pos3 = static_cast<float*>(device_alias(pos_out));
+    ho.vel3 = static_cast<float*>(device_alias(vel_out));
+    ho.dens = static_cast<float*>(device_alias(dens_out));
+    const bool fused = n > 0 && ho.any() && (!pos_out || ho.pos3) && (!vel_out || ho.vel3) &&
+                       (!dens_out || ho.dens);
+    int rc = run_substeps(fused ? count - 1 : count);
+    if (rc) return rc;
+    if (!fused) return get_state(0, pos_out, vel_out, dens_out, nullptr);
+    // The last substep launched directly (not from the graph), its force pass also writing the
+    // page-locked outputs: the read-back overlaps the pass instead of following it.
+    host_out = ho;
+    rc = enqueue_substep(nullptr);
+    host_out = HostOut{};
+    if (rc) return rc;
+    stepped = true;
+    substeps_done += 1;
+    return check_device();
+}
+
+int Model::enqueue_set_state(uint32_t scene, const float* pos3, const float* vel3,
+                             uint32_t offset, int64_t count) {
     if (scene >= scenes.size()) return fail(VFS_ERR_INVALID_ARGUMENT, "scene index out of range");
     const SceneHost& sh = scenes[scene];
     if (offset > sh.n) return fail(VFS_ERR_INVALID_ARGUMENT, "offset beyond the scene's particle count");
@@ -672,7 +709,6 @@ int Model::set_state(uint32_t scene, const float* pos3, const float* vel3, uint3
     k_expand_state<<<(unsigned)((cnt + kIoBlock - 1) / kIoBlock), kIoBlock, 0, stream>>>(
         sh.off + offset, (uint32_t)cnt, sp, sv, pos[cur], vel[cur], aux);
     VFS_CUDA_TRY(cudaGetLastError());
-    VFS_CUDA_TRY(cudaStreamSynchronize(stream));
     return VFS_OK;
 }
 
@@ -1269,6 +1305,12 @@ int vfs_model_set_particle_state(vfs_model* h, const float* pos, const float* ve
                                  uint32_t offset, int64_t count) {
     VFS_HANDLE(h);
     return m.set_state(0, pos, vel, offset, count);
+}
+
+int vfs_model_step_host(vfs_model* h, const float* pos, const float* vel, int32_t substeps,
+                        float* pos_out, float* vel_out, float* dens_out) {
+    VFS_HANDLE(h);
+    return m.step_host(pos, vel, substeps, pos_out, vel_out, dens_out);
 }
 
 int vfs_model_copy_data_buffers(vfs_model* h, float* pos, float* vel, float* dens, float* acc) {

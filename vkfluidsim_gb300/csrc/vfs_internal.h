@@ -225,11 +225,20 @@ cudaError_t launch_density(const StepLaunch& L, const float4* pos, const float4*
                            const KernelConfig& kc, cudaStream_t s);
 // Pressure + viscosity + wall + symplectic Euler over the density pass's neighbour lists; runs the
 // skin lists' build policy and clears their flags (when sk.stale is set).
+// Page-locked host arrays (device addresses of them) the force pass of a single scene writes its
+// results into besides the state buffers: positions and velocities as float3, densities as float,
+// in slot order (any may be null). Written through shared memory in whole 128-byte lines.
+struct HostOut {
+    float* pos3 = nullptr;
+    float* vel3 = nullptr;
+    float* dens = nullptr;
+    bool any() const { return pos3 || vel3 || dens; }
+};
 cudaError_t launch_force(const StepLaunch& L, const float4* pos, const float4* vel,
                          const float4* aux, const float4* rec, const float4* bnd, const uint32_t* cell_scan,
                          const uint32_t* nbr, const uint32_t* nbr_count, float4* pos_out,
                          float4* vel_out, float4* acc_out, const SkinLists& sk,
-                         const KernelConfig& kc, cudaStream_t s);
+                         const KernelConfig& kc, cudaStream_t s, const HostOut& ho = HostOut{});
 // Stable in-place sort of (keys, items) with caller-provided temporaries (n words each) and
 // sort scratch (sort_scratch_words(sc) + 1 words, zeroed here); items become the permutation.
 int enqueue_sort_pairs(uint32_t* items, uint32_t* keys, uint32_t n, const SortConfig& sc,

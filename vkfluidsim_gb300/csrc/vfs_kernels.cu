@@ -1578,7 +1578,8 @@ __device__ __forceinline__ void force_finish(const SceneParams& p, uint32_t i, c
                                              const float4* __restrict__ bnd,
                                              float4* __restrict__ pos_out,
                                              float4* __restrict__ vel_out,
-                                             float4* __restrict__ acc_out) {
+                                             float4* __restrict__ acc_out, float3& x_new,
+                                             float3& v_new) {
     const float pdi = ai.x;
     // The factors force_term leaves out of the sums.
     const float cp = p.mass * p.grad_over_h, cv = p.visc_scale * p.grad_over_h;
@@ -1606,8 +1607,10 @@ __device__ __forceinline__ void force_finish(const SceneParams& p, uint32_t i, c
     }
     if (acc_out) acc_out[i] = make_float4(ax, ay, az, 0.0f);
     const float nvx = vi.x + ax * p.dt, nvy = vi.y + ay * p.dt, nvz = vi.z + az * p.dt;
+    v_new = make_float3(nvx, nvy, nvz);
+    x_new = make_float3(xi.x + nvx * p.dt, xi.y + nvy * p.dt, xi.z + nvz * p.dt);
     vel_out[i] = make_float4(nvx, nvy, nvz, 0.0f);
-    pos_out[i] = make_float4(xi.x + nvx * p.dt, xi.y + nvy * p.dt, xi.z + nvz * p.dt, xi.w);
+    pos_out[i] = make_float4(x_new.x, x_new.y, x_new.z, xi.w);
 }
 
 // CalculatePressureAccel + CalculateViscousAccel + UpdatePositions
@@ -1621,7 +1624,7 @@ __global__ void __launch_bounds__(kNbrBlock, kMinBlocks)
             const uint32_t* __restrict__ scan, const uint32_t* __restrict__ nbr,
             const uint32_t* __restrict__ nbr_count, float4* __restrict__ pos_out,
             float4* __restrict__ vel_out, float4* __restrict__ acc_out,
-            uint32_t* __restrict__ skin_stale, uint32_t* __restrict__ skin_ctl) {
+            uint32_t* __restrict__ skin_stale, uint32_t* __restrict__ skin_ctl, HostOut ho) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     // The density pass is done with the skin lists' flags: run each scene's build policy and clear
     // the flags for the next substep.
@@ -1653,57 +1656,84 @@ __global__ void __launch_bounds__(kNbrBlock, kMinBlocks)
             c[kCtlAllow] = !c[kCtlFresh] && since >= wait ? 1u : 0u;
         }
     }
-    if (i >= L.total) return;
-    const SceneParams& p = scene_params<kBatch>(L, i);
-    const float4 xi = __ldg(pos + i);
-    const float4 vi = __ldg(vel + i);
-    const float4 ai = __ldg(aux + i);
-    const float pdi = ai.x;
+    // The particle's new position and velocity and its density, for the host outputs.
+    float3 x_new = make_float3(0.0f, 0.0f, 0.0f), v_new = x_new;
+    float dens_i = 0.0f;
+    if (i < L.total) {
+        const SceneParams& p = scene_params<kBatch>(L, i);
+        const float4 xi = __ldg(pos + i);
+        const float4 vi = __ldg(vel + i);
+        const float4 ai = __ldg(aux + i);
+        const float pdi = ai.x;
 
-    ForceAcc f{0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
-    const uint32_t listed = nbr_count[i] & kNbrCountMask;
-    if (listed <= p.nbr_cap) {
-        // The density pass's list: the in-range neighbours in the reference's visiting order.
-        uint32_t k = 0;
-        const uint32_t* nl = nbr + i;  // slot k of particle i's list
-        const size_t stride = L.total;
-        // The next batch's indices load while the current batch is gathered and summed, so
-        // each batch waits on one dependent load (the records) instead of two.
-        uint32_t jn[4];
-        if (listed >= 4u) {
-#pragma unroll
-            for (int u = 0; u < 4; u++) jn[u] = __ldg(nl + u * stride);
-        }
-#pragma unroll 1
-        for (; k + 4u <= listed; k += 4u, nl += 4 * stride) {
-            uint32_t j[4];
-            float4 a[4], b[4];
-#pragma unroll
-            for (int u = 0; u < 4; u++) j[u] = jn[u];
-            if (k + 8u <= listed) {
-#pragma unroll
-                for (int u = 0; u < 4; u++) jn[u] = __ldg(nl + (4 + u) * stride);
+        ForceAcc f{0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+        const uint32_t listed = nbr_count[i] & kNbrCountMask;
+        if (listed <= p.nbr_cap) {
+            // The density pass's list: the in-range neighbours in the reference's visiting order.
+            uint32_t k = 0;
+            const uint32_t* nl = nbr + i;  // slot k of particle i's list
+            const size_t stride = L.total;
+            // The next batch's indices load while the current batch is gathered and summed, so
+            // each batch waits on one dependent load (the records) instead of two.
+            uint32_t jn[4];
+            if (listed >= 4u) {
+    #pragma unroll
+                for (int u = 0; u < 4; u++) jn[u] = __ldg(nl + u * stride);
             }
-#pragma unroll
-            for (int u = 0; u < 4; u++) load_record(rec, j[u], a[u], b[u]);
-#pragma unroll
-            for (int u = 0; u < 4; u++) force_term(p, xi, vi, pdi, a[u], make_float2(a[u].w, b[u].w), b[u], f);
+    #pragma unroll 1
+            for (; k + 4u <= listed; k += 4u, nl += 4 * stride) {
+                uint32_t j[4];
+                float4 a[4], b[4];
+    #pragma unroll
+                for (int u = 0; u < 4; u++) j[u] = jn[u];
+                if (k + 8u <= listed) {
+    #pragma unroll
+                    for (int u = 0; u < 4; u++) jn[u] = __ldg(nl + (4 + u) * stride);
+                }
+    #pragma unroll
+                for (int u = 0; u < 4; u++) load_record(rec, j[u], a[u], b[u]);
+    #pragma unroll
+                for (int u = 0; u < 4; u++) force_term(p, xi, vi, pdi, a[u], make_float2(a[u].w, b[u].w), b[u], f);
+            }
+    #pragma unroll 1
+            for (; k < listed; k++, nl += stride) force_term_rec(p, xi, vi, pdi, rec, __ldg(nl), f);
+        } else {
+            // Overflowed list (very dense neighbourhood): walk the candidates again and add every
+            // in-range one as it comes, in the same order. This path needs no shared memory, so
+            // the pass keeps the whole on-chip memory as L1 for its record gathers.
+            const uint32_t cx = cell_coord(xi.x, p.h), cy = cell_coord(xi.y, p.h),
+                           cz = cell_coord(xi.z, p.h);
+            for_each_candidate(p, scan, pos, xi, cx, cy, cz, [&](uint32_t j, const float4& xj) {
+                const float xx = xi.x - xj.x, xy = xi.y - xj.y, xz = xi.z - xj.z;
+                const float r2 = xx * xx + xy * xy + xz * xz;
+                if (r2 <= p.h2 && j != i) force_term_rec(p, xi, vi, pdi, rec, j, f);
+            }, [&]() {});
         }
-#pragma unroll 1
-        for (; k < listed; k++, nl += stride) force_term_rec(p, xi, vi, pdi, rec, __ldg(nl), f);
-    } else {
-        // Overflowed list (very dense neighbourhood): walk the candidates again and add every
-        // in-range one as it comes, in the same order. This path needs no shared memory, so
-        // the pass keeps the whole on-chip memory as L1 for its record gathers.
-        const uint32_t cx = cell_coord(xi.x, p.h), cy = cell_coord(xi.y, p.h),
-                       cz = cell_coord(xi.z, p.h);
-        for_each_candidate(p, scan, pos, xi, cx, cy, cz, [&](uint32_t j, const float4& xj) {
-            const float xx = xi.x - xj.x, xy = xi.y - xj.y, xz = xi.z - xj.z;
-            const float r2 = xx * xx + xy * xy + xz * xz;
-            if (r2 <= p.h2 && j != i) force_term_rec(p, xi, vi, pdi, rec, j, f);
-        }, [&]() {});
+        force_finish(p, i, xi, vi, ai, f, bnd, pos_out, vel_out, acc_out, x_new, v_new);
+        dens_i = ai.z;
     }
-    force_finish(p, i, xi, vi, ai, f, bnd, pos_out, vel_out, acc_out);
+    if (ho.pos3 || ho.vel3 || ho.dens) {
+        // Host outputs (a single scene; the launch gives 7 floats of dynamic shared memory per
+        // thread): the block's particles are consecutive slots, so each array's part is staged
+        // and written out as contiguous words, whole lines over the host link.
+        extern __shared__ float s_io[];
+        const uint32_t t = threadIdx.x, base = blockIdx.x * (uint32_t)kNbrBlock;
+        const uint32_t m = min((uint32_t)kNbrBlock, L.total - base);
+        s_io[3 * t] = x_new.x;
+        s_io[3 * t + 1] = x_new.y;
+        s_io[3 * t + 2] = x_new.z;
+        s_io[3 * kNbrBlock + 3 * t] = v_new.x;
+        s_io[3 * kNbrBlock + 3 * t + 1] = v_new.y;
+        s_io[3 * kNbrBlock + 3 * t + 2] = v_new.z;
+        s_io[6 * kNbrBlock + t] = dens_i;
+        __syncthreads();
+        const size_t b3 = 3 * (size_t)base;
+        for (uint32_t k = t; k < 3 * m; k += kNbrBlock) {
+            if (ho.pos3) ho.pos3[b3 + k] = s_io[k];
+            if (ho.vel3) ho.vel3[b3 + k] = s_io[3 * kNbrBlock + k];
+        }
+        if (ho.dens && t < m) ho.dens[base + t] = s_io[6 * kNbrBlock + t];
+    }
 }
 
 // ---------------------------------------------------------------- incremental sort
@@ -2165,14 +2195,15 @@ template <int B, int M>
 void force_shape(const StepLaunch& L, const float4* pos, const float4* vel, const float4* aux,
                  const float4* rec, const float4* bnd, const uint32_t* cell_scan, const uint32_t* nbr,
                  const uint32_t* nbr_count, float4* pos_out, float4* vel_out, float4* acc_out,
-                 const SkinLists& sk, cudaStream_t s) {
+                 const SkinLists& sk, cudaStream_t s, const HostOut& ho) {
     const uint32_t blocks = (L.total + B - 1) / B;
     if (L.n_scenes > 1)
         k_force<true, B, M><<<blocks, B, 0, s>>>(L, pos, vel, aux, rec, bnd, cell_scan, nbr, nbr_count,
-                                                 pos_out, vel_out, acc_out, sk.stale, sk.ctl);
-    else
-        k_force<false, B, M><<<blocks, B, 0, s>>>(L, pos, vel, aux, rec, bnd, cell_scan, nbr, nbr_count,
-                                                  pos_out, vel_out, acc_out, sk.stale, sk.ctl);
+                                                 pos_out, vel_out, acc_out, sk.stale, sk.ctl, HostOut{});
+    else  // shared memory only for host outputs: without them the whole on-chip memory stays L1
+        k_force<false, B, M><<<blocks, B, ho.any() ? 7 * B * sizeof(float) : 0, s>>>(
+            L, pos, vel, aux, rec, bnd, cell_scan, nbr, nbr_count, pos_out, vel_out, acc_out,
+            sk.stale, sk.ctl, ho);
 }
 
 bool planes_mode(uint32_t total) {
@@ -2209,20 +2240,20 @@ cudaError_t launch_force(const StepLaunch& L, const float4* pos, const float4* v
                          const float4* aux, const float4* rec, const float4* bnd, const uint32_t* cell_scan,
                          const uint32_t* nbr, const uint32_t* nbr_count, float4* pos_out,
                          float4* vel_out, float4* acc_out, const SkinLists& sk,
-                         const KernelConfig& kc, cudaStream_t s) {
+                         const KernelConfig& kc, cudaStream_t s, const HostOut& ho) {
     if (L.total == 0) return cudaSuccess;
     switch (kc.force_shape) {
         case kNbr128x8:
-            force_shape<128, 8>(L, pos, vel, aux, rec, bnd, cell_scan, nbr, nbr_count, pos_out, vel_out, acc_out, sk, s);
+            force_shape<128, 8>(L, pos, vel, aux, rec, bnd, cell_scan, nbr, nbr_count, pos_out, vel_out, acc_out, sk, s, ho);
             break;
         case kNbr96x8:
-            force_shape<96, 8>(L, pos, vel, aux, rec, bnd, cell_scan, nbr, nbr_count, pos_out, vel_out, acc_out, sk, s);
+            force_shape<96, 8>(L, pos, vel, aux, rec, bnd, cell_scan, nbr, nbr_count, pos_out, vel_out, acc_out, sk, s, ho);
             break;
         case kNbr64x12:
-            force_shape<64, 12>(L, pos, vel, aux, rec, bnd, cell_scan, nbr, nbr_count, pos_out, vel_out, acc_out, sk, s);
+            force_shape<64, 12>(L, pos, vel, aux, rec, bnd, cell_scan, nbr, nbr_count, pos_out, vel_out, acc_out, sk, s, ho);
             break;
         default:
-            force_shape<128, 6>(L, pos, vel, aux, rec, bnd, cell_scan, nbr, nbr_count, pos_out, vel_out, acc_out, sk, s);
+            force_shape<128, 6>(L, pos, vel, aux, rec, bnd, cell_scan, nbr, nbr_count, pos_out, vel_out, acc_out, sk, s, ho);
     }
     return cudaGetLastError();
 }

@@ -77,6 +77,7 @@ struct Model {
     uint32_t* err = nullptr;
     uint32_t* err_host = nullptr;  // pinned copy of the error word read by check_device
     uint32_t* walk_sched = nullptr;  // two words: the density walk's run counter (zero between launches)
+    HostOut host_out{};              // set only while step_host enqueues its last substep
     SceneParams* d_scenes = nullptr;   // batched launches: the scene table
     uint16_t* d_scene_of = nullptr;    // batched launches: scene id per particle
     DevObject* d_objects = nullptr;    // boundary objects of all scenes
@@ -109,6 +110,13 @@ struct Model {
     // Scene-relative state I/O (offset and ids are scene-local).
     int set_state(uint32_t scene, const float* pos3, const float* vel3, uint32_t offset,
                   int64_t count);
+    // set_state without the final wait (the conversion kernel may still be reading host memory).
+    int enqueue_set_state(uint32_t scene, const float* pos3, const float* vel3, uint32_t offset,
+                          int64_t count);
+    // set_state of every particle (when pos3 / vel3 are given), `count` substeps and get_state,
+    // with one wait at the end; outputs in page-locked memory come from the last force pass.
+    int step_host(const float* pos3, const float* vel3, int32_t count, float* pos_out,
+                  float* vel_out, float* dens_out);
     int get_state(uint32_t scene, float* pos3, float* vel3, float* dens, uint32_t* ids);
     int get_acc(uint32_t scene, float* acc3);
     int get_neighbors(uint32_t scene, uint32_t* keys, uint32_t* perm, uint32_t* offsets);

@@ -397,6 +397,33 @@ class WCSPHWithBoundaryModel:
             out["accelerations"] = acc
         return out
 
+    def step_host(self, pos=None, vel=None, substeps: int = 1, out: Optional[dict] = None) -> dict:
+        """set_particle_state of every particle (when pos and vel are given), `substeps`
+        substeps and copy_data_buffers, with one wait at the end (vfs_model_step_host). `out`
+        may hold preallocated float32 arrays "positions" (N x 3), "velocities" (N x 3) and
+        "densities" (N); when all of them are page-locked (e.g. numpy views of pinned torch
+        tensors), the last force pass writes them directly."""
+        n = self.n_particles
+        if (pos is None) != (vel is None):
+            raise ValueError("pos and vel must both be given or both be None")
+        p = v = None
+        if pos is not None:
+            p, v = _f32(pos, (-1, 3)), _f32(vel, (-1, 3))
+            if p.shape[0] != n or v.shape[0] != n:
+                raise ValueError("pos and vel must hold every particle")
+        out = dict(out or {})
+        shapes = {"positions": (n, 3), "velocities": (n, 3), "densities": (n,)}
+        for k, shape in shapes.items():
+            a = out.get(k)
+            if a is None:
+                out[k] = np.empty(shape, np.float32)
+            elif a.dtype != np.float32 or a.shape != shape or not a.flags.c_contiguous:
+                raise ValueError(f"out[{k!r}] must be a C-contiguous float32 array of shape {shape}")
+        check(self._lib.vfs_model_step_host(self._h, _fp(p), _fp(v), substeps,
+                                            _fp(out["positions"]), _fp(out["velocities"]),
+                                            _fp(out["densities"])))
+        return {k: out[k] for k in shapes}
+
     def get_ids(self) -> np.ndarray:
         ids = np.empty(self.n_particles, np.uint32)
         check(self._lib.vfs_model_get_ids(self._h, _up(ids)))
