@@ -51,7 +51,9 @@ constexpr uint32_t kIoBlock = 256;
 
 // SetParticleState's layout conversion: packed float3 records (host memory mapped into the
 // device's address space, or a device staging copy) to the float4 state. A block moves its
-// 256 records through shared memory, so every warp reads 128 contiguous bytes.
+// 256 records through shared memory, so every warp reads 128 contiguous bytes. Positions (with
+// the ids and the zeroed densities) and velocities are converted when their source is given, so
+// the two halves can run on different streams.
 __global__ void __launch_bounds__(kIoBlock)
     k_expand_state(uint32_t offset, uint32_t count, const float* __restrict__ pos3,
                    const float* __restrict__ vel3, float4* __restrict__ pos,
@@ -61,15 +63,17 @@ __global__ void __launch_bounds__(kIoBlock)
     const uint32_t m = min(kIoBlock, count - base);
     const size_t b3 = 3 * (size_t)base;
     for (uint32_t k = t; k < 3 * m; k += kIoBlock) {
-        s_p[k] = pos3[b3 + k];
-        s_v[k] = vel3[b3 + k];
+        if (pos3) s_p[k] = pos3[b3 + k];
+        if (vel3) s_v[k] = vel3[b3 + k];
     }
     __syncthreads();
     if (t >= m) return;
     const uint32_t d = offset + base + t;
-    pos[d] = make_float4(s_p[3 * t], s_p[3 * t + 1], s_p[3 * t + 2], __uint_as_float(d));
-    vel[d] = make_float4(s_v[3 * t], s_v[3 * t + 1], s_v[3 * t + 2], 0.0f);
-    aux[d].z = 0.0f;  // SetParticleState zeroes the densities it covers (model.cpp:146)
+    if (pos3) {
+        pos[d] = make_float4(s_p[3 * t], s_p[3 * t + 1], s_p[3 * t + 2], __uint_as_float(d));
+        aux[d].z = 0.0f;  // SetParticleState zeroes the densities it covers (model.cpp:146)
+    }
+    if (vel3) vel[d] = make_float4(s_v[3 * t], s_v[3 * t + 1], s_v[3 * t + 2], 0.0f);
 }
 
 // Packs particles [start, start + n) into float3 / float arrays (any of them may be null);
@@ -371,6 +375,7 @@ int Model::enqueue_substep(cudaEvent_t* ev) {
     skeys = sk_buf;
     sperm = sp_buf;
     if (ev) VFS_CUDA_TRY(cudaEventRecord(ev[3], s));
+    if (cells_wait) VFS_CUDA_TRY(cudaStreamWaitEvent(s, cells_wait, 0));
     VFS_CUDA_TRY(launch_cells_reorder(launch, n, skeys, sperm, cell_scan, pos[c], vel[c], pos[o], vel[o],
                                       scratch, (uint32_t)sort_scratch_words(sc), pkeys, cell_guess,
                                       sk, kc, s));
@@ -465,6 +470,9 @@ Model::~Model() {
     cudaFree(scratch);
     cudaFree(err);
     cudaFree(walk_sched);
+    if (io_ev[0]) cudaEventDestroy(io_ev[0]);
+    if (io_ev[1]) cudaEventDestroy(io_ev[1]);
+    if (io_stream) cudaStreamDestroy(io_stream);
     if (err_host) cudaFreeHost(err_host);
     cudaFree(d_scenes);
     cudaFree(d_scene_of);
@@ -659,17 +667,39 @@ int Model::step_host(const float* pos3, const float* vel3, int32_t count, float*
     if (count < 1) return fail(VFS_ERR_INVALID_ARGUMENT, "step_host needs at least one substep");
     if (!pos3 != !vel3) return fail(VFS_ERR_INVALID_ARGUMENT, "pos and vel must both be given or both be NULL");
     if (scenes.size() != 1) return fail(VFS_ERR_INVALID_ARGUMENT, "step_host steps a single-scene model");
-    if (pos3) {
-        const int rc = enqueue_set_state(0, pos3, vel3, 0, -1);
-        if (rc) return rc;
-    }
     HostOut ho;
     ho.pos3 = static_cast<float*>(device_alias(pos_out));
     ho.vel3 = static_cast<float*>(device_alias(vel_out));
     ho.dens = static_cast<float*>(device_alias(dens_out));
     const bool fused = n > 0 && ho.any() && (!pos_out || ho.pos3) && (!vel_out || ho.vel3) &&
                        (!dens_out || ho.dens);
-    int rc = run_substeps(fused ? count - 1 : count);
+    int remaining = count;
+    if (pos3 && n > 0) {
+        // Positions on the model's stream; velocities, first read by the cell pass, on a side
+        // stream that starts after the work already queued, so their upload overlaps the key and
+        // sort passes. The first substep is launched directly and waits for them before its cell
+        // pass.
+        if (!io_stream) {
+            VFS_CUDA_TRY(cudaStreamCreateWithFlags(&io_stream, cudaStreamNonBlocking));
+            VFS_CUDA_TRY(cudaEventCreateWithFlags(&io_ev[0], cudaEventDisableTiming));
+            VFS_CUDA_TRY(cudaEventCreateWithFlags(&io_ev[1], cudaEventDisableTiming));
+        }
+        VFS_CUDA_TRY(cudaEventRecord(io_ev[0], stream));
+        VFS_CUDA_TRY(cudaStreamWaitEvent(io_stream, io_ev[0], 0));
+        int rc = enqueue_set_state(0, pos3, vel3, 0, -1, io_stream);
+        if (rc) return rc;
+        VFS_CUDA_TRY(cudaEventRecord(io_ev[1], io_stream));
+        cells_wait = io_ev[1];
+        if (fused && count == 1) host_out = ho;
+        rc = enqueue_substep(nullptr);
+        cells_wait = nullptr;
+        host_out = HostOut{};
+        if (rc) return rc;
+        stepped = true;
+        substeps_done += 1;
+        if (--remaining == 0) return fused ? check_device() : get_state(0, pos_out, vel_out, dens_out, nullptr);
+    }
+    int rc = run_substeps(fused ? remaining - 1 : remaining);
     if (rc) return rc;
     if (!fused) return get_state(0, pos_out, vel_out, dens_out, nullptr);
     // The last substep launched directly (not from the graph), its force pass also writing the
@@ -684,7 +714,8 @@ int Model::step_host(const float* pos3, const float* vel3, int32_t count, float*
 }
 
 int Model::enqueue_set_state(uint32_t scene, const float* pos3, const float* vel3,
-                             uint32_t offset, int64_t count) {
+                             uint32_t offset, int64_t count, cudaStream_t vel_stream) {
+    if (!vel_stream) vel_stream = stream;
     if (scene >= scenes.size()) return fail(VFS_ERR_INVALID_ARGUMENT, "scene index out of range");
     const SceneHost& sh = scenes[scene];
     if (offset > sh.n) return fail(VFS_ERR_INVALID_ARGUMENT, "offset beyond the scene's particle count");
@@ -703,11 +734,19 @@ int Model::enqueue_set_state(uint32_t scene, const float* pos3, const float* vel
     }
     if (!sv) {
         float* st = stage + 3 * (size_t)n;
-        VFS_CUDA_TRY(cudaMemcpyAsync(st, vel3, cnt * 12, cudaMemcpyHostToDevice, stream));
+        VFS_CUDA_TRY(cudaMemcpyAsync(st, vel3, cnt * 12, cudaMemcpyHostToDevice, vel_stream));
         sv = st;
     }
-    k_expand_state<<<(unsigned)((cnt + kIoBlock - 1) / kIoBlock), kIoBlock, 0, stream>>>(
-        sh.off + offset, (uint32_t)cnt, sp, sv, pos[cur], vel[cur], aux);
+    const unsigned blocks = (unsigned)((cnt + kIoBlock - 1) / kIoBlock);
+    if (vel_stream == stream) {
+        k_expand_state<<<blocks, kIoBlock, 0, stream>>>(sh.off + offset, (uint32_t)cnt, sp, sv,
+                                                         pos[cur], vel[cur], aux);
+    } else {
+        k_expand_state<<<blocks, kIoBlock, 0, vel_stream>>>(sh.off + offset, (uint32_t)cnt, nullptr,
+                                                             sv, pos[cur], vel[cur], aux);
+        k_expand_state<<<blocks, kIoBlock, 0, stream>>>(sh.off + offset, (uint32_t)cnt, sp, nullptr,
+                                                         pos[cur], vel[cur], aux);
+    }
     VFS_CUDA_TRY(cudaGetLastError());
     return VFS_OK;
 }

@@ -78,6 +78,9 @@ struct Model {
     uint32_t* err_host = nullptr;  // pinned copy of the error word read by check_device
     uint32_t* walk_sched = nullptr;  // two words: the density walk's run counter (zero between launches)
     HostOut host_out{};              // set only while step_host enqueues its last substep
+    cudaEvent_t cells_wait = nullptr;  // set only while step_host enqueues its first substep
+    cudaStream_t io_stream = nullptr;  // step_host's velocity upload (created on first use)
+    cudaEvent_t io_ev[2] = {nullptr, nullptr};
     SceneParams* d_scenes = nullptr;   // batched launches: the scene table
     uint16_t* d_scene_of = nullptr;    // batched launches: scene id per particle
     DevObject* d_objects = nullptr;    // boundary objects of all scenes
@@ -112,7 +115,7 @@ struct Model {
                   int64_t count);
     // set_state without the final wait (the conversion kernel may still be reading host memory).
     int enqueue_set_state(uint32_t scene, const float* pos3, const float* vel3, uint32_t offset,
-                          int64_t count);
+                          int64_t count, cudaStream_t vel_stream = nullptr);
     // set_state of every particle (when pos3 / vel3 are given), `count` substeps and get_state,
     // with one wait at the end; outputs in page-locked memory come from the last force pass.
     int step_host(const float* pos3, const float* vel3, int32_t count, float* pos_out,
