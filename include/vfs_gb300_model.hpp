@@ -71,6 +71,22 @@ public:
                                           nullptr));
     }
 
+    // SetParticleState of every particle from pos / vel, `substeps` substeps, then the
+    // CopyDataBuffers hand-off into the same arrays, with one wait (vfs_model_step_host). With
+    // page-locked storage behind the vectors' data the last force pass writes the outputs.
+    template <class Vec3>
+    void StepHost(std::vector<Vec3>& pos, std::vector<Vec3>& vel, std::vector<float>& dens,
+                  int32_t substeps = 1) {
+        static_assert(sizeof(Vec3) == 3 * sizeof(float), "three packed floats");
+        const uint32_t n = NumParticles();
+        if (pos.size() != n || vel.size() != n)
+            throw std::invalid_argument("pos and vel must hold every particle");
+        dens.resize(n);
+        float* p = reinterpret_cast<float*>(pos.data());
+        float* v = reinterpret_cast<float*>(vel.data());
+        check(vfs_model_step_host(m_, p, v, substeps, p, v, dens.data()));
+    }
+
     // SpatialHash's buffers after the last substep: keys, sorted indices, offsets.
     void GetNeighborArrays(std::vector<uint32_t>& keys, std::vector<uint32_t>& sorted_indices,
                            std::vector<uint32_t>& offsets) {

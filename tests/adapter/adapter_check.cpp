@@ -2,7 +2,9 @@
 // blocks with the reference's field names (stand-ins for vfs::SimulationParameters,
 // vfs::SPHModel::Parameters, vfs::WCSPHWithBoundaryModel::Parameters and glm::vec3), a jittered
 // lattice set with SetParticleState, one Step, then CopyDataBuffers and the spatial hash's
-// buffers written to a binary file for the test to compare with the oracle.
+// buffers written to a binary file for the test to compare with the oracle; then a second model
+// takes the same lattice through StepHost (the same round trip in one call) and its positions,
+// velocities and densities are appended.
 // Usage: adapter_check <output file>. Exit codes: 0 done, 3 the library reported an error (no
 // CUDA device, for instance), 2 bad usage.
 #include <cstdio>
@@ -46,6 +48,7 @@ int main(int argc, char** argv) {
     const uint32_t n = dims[0] * dims[1] * dims[2];
     std::vector<ref::vec3> pos(n), vel(n, ref::vec3{0.0f, 0.0f, 0.0f});
     if (vfs_generate_lattice(dims, origin, 0.02f, 0.1f, 0, &pos[0].x) != VFS_OK) return 3;
+    std::vector<ref::vec3> pos2 = pos, vel2 = vel;
     const ref::SimulationParameters g{{0.0f, 0.0f, -9.81f}, 0.04f};
     const ref::SPHParameters p{1.0f, 1, (int)n, 2e-4f, 1000.0f, {{0.4f, 0.4f, 0.4f}, {0.0f, 0.0f, 0.0f}}};
     const ref::WCSPHParameters w{1e4f, 50.0f, 7.0f, 0.01f};
@@ -68,6 +71,13 @@ int main(int argc, char** argv) {
         std::fwrite(keys.data(), 4, n, f);
         std::fwrite(perm.data(), 4, n, f);
         std::fwrite(offs.data(), 4, n, f);
+        vfs_gb300::GB300WCSPHModel<ref::SimulationParameters, ref::SPHParameters, ref::WCSPHParameters>
+            model2(g, p, w);
+        std::vector<float> dens2;
+        model2.StepHost(pos2, vel2, dens2);
+        std::fwrite(pos2.data(), 12, n, f);
+        std::fwrite(vel2.data(), 12, n, f);
+        std::fwrite(dens2.data(), 4, n, f);
         std::fclose(f);
     } catch (const std::exception& e) {
         std::printf("%s\n", e.what());

@@ -2,7 +2,7 @@
 with the library as a maintainer would add it to the reference: a CPU test builds and runs it
 (without a device the library's error surfaces as the adapter's exception), and a GPU test drives
 one Step through it and compares the result with the oracle (neighbour arrays bit-exact, fields
-within the parity bars)."""
+within the parity bars) and with the same step taken by StepHost (bit for bit)."""
 from __future__ import annotations
 
 import ctypes as C
@@ -62,6 +62,10 @@ def test_adapter_step_matches_the_oracle(tmp_path):
     pos, vel = take(np.float32, 3 * n).reshape(n, 3), take(np.float32, 3 * n).reshape(n, 3)
     dens = take(np.float32, n)
     keys, perm, offs = take(np.uint32, n), take(np.uint32, n), take(np.uint32, n)
+    # StepHost on a second model from the same lattice: the same results, bit for bit.
+    pos2, vel2 = take(np.float32, 3 * n).reshape(n, 3), take(np.float32, 3 * n).reshape(n, 3)
+    dens2 = take(np.float32, n)
+    assert np.array_equal(pos2, pos) and np.array_equal(vel2, vel) and np.array_equal(dens2, dens)
     from oracle.workloads import lattice
 
     prm = ob.OracleParams((C.c_float * 3)(0.0, 0.0, -9.81), 0.04, 1.0, 1, 2e-4, 1000.0,
