@@ -676,19 +676,16 @@ int Model::step_host(const float* pos3, const float* vel3, int32_t count, float*
     int remaining = count;
     if (pos3 && n > 0) {
         // Positions on the model's stream; velocities, first read by the cell pass, on a side
-        // stream that starts after the work already queued, so their upload overlaps the key and
-        // sort passes. The first substep is launched directly and waits for them before its cell
-        // pass.
+        // stream after them (so after all work queued before), their upload overlapping the key
+        // and sort passes. The first substep is launched directly and waits for them before its
+        // cell pass.
         if (!io_stream) {
             VFS_CUDA_TRY(cudaStreamCreateWithFlags(&io_stream, cudaStreamNonBlocking));
             VFS_CUDA_TRY(cudaEventCreateWithFlags(&io_ev[0], cudaEventDisableTiming));
             VFS_CUDA_TRY(cudaEventCreateWithFlags(&io_ev[1], cudaEventDisableTiming));
         }
-        VFS_CUDA_TRY(cudaEventRecord(io_ev[0], stream));
-        VFS_CUDA_TRY(cudaStreamWaitEvent(io_stream, io_ev[0], 0));
         int rc = enqueue_set_state(0, pos3, vel3, 0, -1, io_stream);
         if (rc) return rc;
-        VFS_CUDA_TRY(cudaEventRecord(io_ev[1], io_stream));
         cells_wait = io_ev[1];
         if (fused && count == 1) host_out = ho;
         rc = enqueue_substep(nullptr);
@@ -727,25 +724,34 @@ int Model::enqueue_set_state(uint32_t scene, const float* pos3, const float* vel
     // Page-locked inputs are read by the conversion kernel itself (over NVLink-C2C on GB300);
     // pageable ones are copied into the staging buffer first.
     const float* sp = static_cast<const float*>(device_alias(pos3));
-    const float* sv = static_cast<const float*>(device_alias(vel3));
     if (!sp) {
         VFS_CUDA_TRY(cudaMemcpyAsync(stage, pos3, cnt * 12, cudaMemcpyHostToDevice, stream));
         sp = stage;
     }
-    if (!sv) {
-        float* st = stage + 3 * (size_t)n;
-        VFS_CUDA_TRY(cudaMemcpyAsync(st, vel3, cnt * 12, cudaMemcpyHostToDevice, vel_stream));
-        sv = st;
-    }
     const unsigned blocks = (unsigned)((cnt + kIoBlock - 1) / kIoBlock);
+    float* const vel_stage = stage + 3 * (size_t)n;
     if (vel_stream == stream) {
+        const float* sv = static_cast<const float*>(device_alias(vel3));
+        if (!sv) {
+            VFS_CUDA_TRY(cudaMemcpyAsync(vel_stage, vel3, cnt * 12, cudaMemcpyHostToDevice, stream));
+            sv = vel_stage;
+        }
         k_expand_state<<<blocks, kIoBlock, 0, stream>>>(sh.off + offset, (uint32_t)cnt, sp, sv,
                                                          pos[cur], vel[cur], aux);
     } else {
-        k_expand_state<<<blocks, kIoBlock, 0, vel_stream>>>(sh.off + offset, (uint32_t)cnt, nullptr,
-                                                             sv, pos[cur], vel[cur], aux);
+        // Positions first, alone on the host link; the velocities follow on the side stream by
+        // DMA (a copy engine, so they move while the key and sort passes keep every SM busy)
+        // and are converted there. io_ev[1] marks them done.
         k_expand_state<<<blocks, kIoBlock, 0, stream>>>(sh.off + offset, (uint32_t)cnt, sp, nullptr,
                                                          pos[cur], vel[cur], aux);
+        VFS_CUDA_TRY(cudaGetLastError());
+        VFS_CUDA_TRY(cudaEventRecord(io_ev[0], stream));
+        VFS_CUDA_TRY(cudaStreamWaitEvent(vel_stream, io_ev[0], 0));
+        VFS_CUDA_TRY(cudaMemcpyAsync(vel_stage, vel3, cnt * 12, cudaMemcpyHostToDevice, vel_stream));
+        k_expand_state<<<blocks, kIoBlock, 0, vel_stream>>>(sh.off + offset, (uint32_t)cnt, nullptr,
+                                                             vel_stage, pos[cur], vel[cur], aux);
+        VFS_CUDA_TRY(cudaGetLastError());
+        VFS_CUDA_TRY(cudaEventRecord(io_ev[1], vel_stream));
     }
     VFS_CUDA_TRY(cudaGetLastError());
     return VFS_OK;
