@@ -1031,8 +1031,7 @@ __global__ void __launch_bounds__(kNbrBlock, kMinBlocks)
     k_density(StepLaunch L, const float4* __restrict__ pos, const float4* __restrict__ vel,
               float4* __restrict__ rec, const uint32_t* __restrict__ scan,
               float4* __restrict__ aux, float4* __restrict__ bnd, uint32_t* __restrict__ nbr,
-              uint32_t* __restrict__ nbr_count, SkinLists sk, uint32_t* __restrict__ sched,
-              uint32_t dense_walkers) {
+              uint32_t* __restrict__ nbr_count, SkinLists sk, uint32_t* __restrict__ sched) {
     static_assert(kSkinCap <= (uint32_t)kListCap, "a list build is staged in the shared list");
     static_assert(kNbrBlock % 32 == 0, "whole warps");
     static_assert(kListBlock % 32 == 0, "a warp's 32 slots lie in one list block");
@@ -1042,28 +1041,20 @@ __global__ void __launch_bounds__(kNbrBlock, kMinBlocks)
     __shared__ float4 s_stage[kStaging ? kNbrBlock : 1];
     const int tid = threadIdx.x;
     const uint32_t lane = (uint32_t)(tid & 31);
-    // Slots to walk: every particle (no lists, a stale or poor single scene), a batch's queue
-    // segments, or a single scene's packed queue of walkers. A single scene whose lists are
-    // current and mostly usable leaves its walkers to k_density_walkers (a warp each) unless
-    // there are more than dense_walkers of them; then this launch walks them, a thread each.
-    uint32_t slots = L.total;
-    bool packed = false;
-    if (!kBatch && sk.list && sk.stale[0] == 0u && sk.ctl[kCtlPoor] == 0u) {
-        slots = min(*sk.wcount, L.total);
-        if (slots <= dense_walkers) return;  // the whole launch
-        packed = true;
-    }
+    // A single scene whose lists are current and mostly usable: k_density_list and
+    // k_density_walkers cover every particle, and the whole launch returns here.
+    if (!kBatch && sk.list && sk.stale[0] == 0u && sk.ctl[kCtlPoor] == 0u) return;
     // Every warp takes runs of 32 slots: first the run of its own index, then runs claimed from
     // the launch's counter (sched[0]), until none is left. Walks differ widely in length (the
     // queued walkers of a batch, the list builds of a stale scene), and a warp that finishes early
     // takes the next run. No lane leaves a run before the warp's collective steps: inactive lanes
     // carry act = false.
-    const uint32_t runs = (slots + 31u) / 32u;
+    const uint32_t runs = (L.total + 31u) / 32u;
     const uint32_t warps = gridDim.x * (uint32_t)(kNbrBlock / 32);
     uint32_t run = blockIdx.x * (uint32_t)(kNbrBlock / 32) + (uint32_t)(tid >> 5);
     for (; run < runs;) {
         const uint32_t t = run * 32u + lane;
-        bool act = t < slots;
+        bool act = t < L.total;
         uint32_t i = act ? t : 0u, sc = 0u;
         bool rebuild = false;
         if (act && sk.list) {
@@ -1075,8 +1066,8 @@ __global__ void __launch_bounds__(kNbrBlock, kMinBlocks)
                     i = __ldg(sk.queue + t);
                     sc = (uint32_t)__ldg(L.scene_of + i);
                 }
-            } else if (packed) {
-                i = __ldg(sk.queue + t);  // walker t of the single scene's packed queue
+            } else if (sk.stale[0] == 0u && sk.ctl[kCtlPoor] == 0u) {
+                act = false;  // k_density_walkers walks the single scene's queued particles
             }  // else a single scene that is stale or whose lists are mostly unusable: every
                // particle, in index order (no queue)
             rebuild = act && sk.stale[sc] != 0u && sk.ctl[sc * kSkinCtl + kCtlAllow] != 0u;
@@ -1318,13 +1309,9 @@ __global__ void __launch_bounds__(kWalkerWarps * 32)
     k_density_walkers(StepLaunch L, const float4* __restrict__ pos, const float4* __restrict__ vel,
                       float4* __restrict__ rec, const uint32_t* __restrict__ scan,
                       float4* __restrict__ aux, float4* __restrict__ bnd, uint32_t* __restrict__ nbr,
-                      uint32_t* __restrict__ nbr_count, SkinLists sk, uint32_t dense_walkers) {
+                      uint32_t* __restrict__ nbr_count, SkinLists sk) {
     if (sk.stale[0] != 0u || sk.ctl[kCtlPoor] != 0u) return;  // k_density walks every particle
     const uint32_t walkers = min(*sk.wcount, L.total);
-    // A dense queue (a crowd of walkers, e.g. every particle of a dense blob, whose lists
-    // overflow): k_density walks it a thread per walker, where the in-range sums of a warp's
-    // 32 walkers run side by side instead of one by one through shuffles.
-    if (walkers > dense_walkers) return;
     const int lane = threadIdx.x & 31;
     const uint32_t lt = (1u << lane) - 1u;
     const SceneParams& p = L.one;
@@ -2155,8 +2142,7 @@ static int sm_count() {
 template <bool kBatch, int B, int M, bool kStaging>
 void launch_walk(const StepLaunch& L, const float4* pos, const float4* vel, float4* rec,
                  const uint32_t* cell_scan, float4* aux, float4* bnd, uint32_t* nbr,
-                 uint32_t* nbr_count, const SkinLists& sk, uint32_t* sched, uint32_t dense_walkers,
-                 cudaStream_t s) {
+                 uint32_t* nbr_count, const SkinLists& sk, uint32_t* sched, cudaStream_t s) {
     static std::atomic<int> per_sm{0};
     int r = per_sm.load(std::memory_order_relaxed);
     if (r == 0) {
@@ -2170,7 +2156,7 @@ void launch_walk(const StepLaunch& L, const float4* pos, const float4* vel, floa
     const uint32_t all_blocks = (L.total + B - 1) / B;
     const uint32_t blocks = sms > 0 ? min(all_blocks, (uint32_t)sms * (uint32_t)r) : all_blocks;
     k_density<kBatch, B, M, kStaging><<<blocks, B, 0, s>>>(L, pos, vel, rec, cell_scan, aux, bnd, nbr,
-                                                           nbr_count, sk, sched, dense_walkers);
+                                                           nbr_count, sk, sched);
 }
 
 template <int B, int M>
@@ -2178,10 +2164,6 @@ void density_shape(const StepLaunch& L, const float4* pos, const float4* vel, fl
                    const uint32_t* cell_scan, float4* aux, float4* bnd, uint32_t* nbr,
                    uint32_t* nbr_count, const SkinLists& sk, uint32_t* sched, bool staging,
                    cudaStream_t s) {
-    // A single scene's queue of more than 16 warps of walkers per SM is walked a thread per
-    // walker (k_density), a shorter one a warp per walker (k_density_walkers).
-    const int sms_d = sm_count();
-    const uint32_t dense_walkers = (uint32_t)(sms_d > 0 ? sms_d : 148) * 16u * 32u;
     if (sk.list) {
         // Skin lists: the list pass first; the walk passes then take the queue it leaves.
         const uint32_t lb = (L.total + kListBlock - 1) / kListBlock;
@@ -2193,19 +2175,19 @@ void density_shape(const StepLaunch& L, const float4* pos, const float4* vel, fl
             const int sms = sm_count();
             const uint32_t wb = (uint32_t)(sms > 0 ? sms : 148) * 8u;  // 32 warps per SM
             k_density_walkers<<<wb, kWalkerWarps * 32, 0, s>>>(L, pos, vel, rec, cell_scan, aux, bnd,
-                                                               nbr, nbr_count, sk, dense_walkers);
+                                                               nbr, nbr_count, sk);
         }
     }
     if (L.n_scenes > 1) {
         if (staging)
-            launch_walk<true, B, M, true>(L, pos, vel, rec, cell_scan, aux, bnd, nbr, nbr_count, sk, sched, dense_walkers, s);
+            launch_walk<true, B, M, true>(L, pos, vel, rec, cell_scan, aux, bnd, nbr, nbr_count, sk, sched, s);
         else
-            launch_walk<true, B, M, false>(L, pos, vel, rec, cell_scan, aux, bnd, nbr, nbr_count, sk, sched, dense_walkers, s);
+            launch_walk<true, B, M, false>(L, pos, vel, rec, cell_scan, aux, bnd, nbr, nbr_count, sk, sched, s);
     } else {
         if (staging)
-            launch_walk<false, B, M, true>(L, pos, vel, rec, cell_scan, aux, bnd, nbr, nbr_count, sk, sched, dense_walkers, s);
+            launch_walk<false, B, M, true>(L, pos, vel, rec, cell_scan, aux, bnd, nbr, nbr_count, sk, sched, s);
         else
-            launch_walk<false, B, M, false>(L, pos, vel, rec, cell_scan, aux, bnd, nbr, nbr_count, sk, sched, dense_walkers, s);
+            launch_walk<false, B, M, false>(L, pos, vel, rec, cell_scan, aux, bnd, nbr, nbr_count, sk, sched, s);
     }
 }
 
