@@ -179,6 +179,12 @@ int autotune(Model& m, int repeats, bool use_cache, vfs_tune_config* chosen) {
                 }
             }
     }
+    // The walk kernel's shape and staging matter only in substeps that walk (no lists, a stale
+    // scene, a list build); while a scene's lists are current it returns at once, and a
+    // comparison there would pick by noise. So stages 2 and 3 run with the lists off (every
+    // substep walks); they are switched back on afterwards, and rebuilt by the next substep.
+    const float keep_skin = m.skin_fraction;
+    if (rc == VFS_OK && keep_skin > 0.0f) rc = set_skin(m, 0.0f);
     // Stage 2: block shapes of the density and force passes (independent kernels, one sweep).
     if (rc == VFS_OK) {
         float best_d = 1e30f, best_f = 1e30f;
@@ -213,6 +219,10 @@ int autotune(Model& m, int repeats, bool use_cache, vfs_tune_config* chosen) {
                 best.walk_staging = st;
             }
         }
+    }
+    if (keep_skin > 0.0f) {
+        const int rs = set_skin(m, keep_skin);
+        if (rc == VFS_OK) rc = rs;
     }
     // Stage 4: cells per block of the cell-range / reorder kernel.
     if (rc == VFS_OK) {

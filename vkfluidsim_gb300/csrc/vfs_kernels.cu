@@ -1677,25 +1677,25 @@ __global__ void __launch_bounds__(kNbrBlock, kMinBlocks)
             // each batch waits on one dependent load (the records) instead of two.
             uint32_t jn[4];
             if (listed >= 4u) {
-    #pragma unroll
+#pragma unroll
                 for (int u = 0; u < 4; u++) jn[u] = __ldg(nl + u * stride);
             }
-    #pragma unroll 1
+#pragma unroll 1
             for (; k + 4u <= listed; k += 4u, nl += 4 * stride) {
                 uint32_t j[4];
                 float4 a[4], b[4];
-    #pragma unroll
+#pragma unroll
                 for (int u = 0; u < 4; u++) j[u] = jn[u];
                 if (k + 8u <= listed) {
-    #pragma unroll
+#pragma unroll
                     for (int u = 0; u < 4; u++) jn[u] = __ldg(nl + (4 + u) * stride);
                 }
-    #pragma unroll
+#pragma unroll
                 for (int u = 0; u < 4; u++) load_record(rec, j[u], a[u], b[u]);
-    #pragma unroll
+#pragma unroll
                 for (int u = 0; u < 4; u++) force_term(p, xi, vi, pdi, a[u], make_float2(a[u].w, b[u].w), b[u], f);
             }
-    #pragma unroll 1
+#pragma unroll 1
             for (; k < listed; k++, nl += stride) force_term_rec(p, xi, vi, pdi, rec, __ldg(nl), f);
         } else {
             // Overflowed list (very dense neighbourhood): walk the candidates again and add every
