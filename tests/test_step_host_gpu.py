@@ -66,6 +66,33 @@ def test_step_host_on_a_small_model():
     _round_trips(w, rounds=3, substeps=1, pinned=True)
 
 
+def test_step_host_replays_one_substep_through_the_same_pinned_buffers():
+    """The frame loop: page-locked buffers that are both input and output, one substep per call
+    (captured once per set of buffers and replayed); a second set of buffers midway."""
+    w = W.dam_break(dims=(48, 40, 40), map_res=32, stiffness=200.0)
+    ref, fused = W.build_model(w), W.build_model(w)
+    n = w.n
+    bufs = []
+    for _ in range(2):
+        b = {"positions": _pinned((n, 3)), "velocities": _pinned((n, 3)), "densities": _pinned((n,))}
+        bufs.append(b)
+    bufs[0]["positions"][:] = w.pos
+    bufs[0]["velocities"][:] = w.vel
+    pos, vel = np.array(w.pos, np.float32), np.array(w.vel, np.float32)
+    for r in range(8):
+        if r == 4:  # switch to the second set of buffers, holding the same state
+            for k in ("positions", "velocities"):
+                bufs[1][k][:] = bufs[0][k]
+        b = bufs[0 if r < 4 else 1]
+        ref.set_particle_state(pos, vel)
+        ref.substeps(1)
+        a = ref.copy_data_buffers()
+        fused.step_host(b["positions"], b["velocities"], 1, out=b)
+        for k in ("positions", "velocities", "densities"):
+            assert np.array_equal(a[k], b[k]), f"round {r}: {k}"
+        pos, vel = a["positions"].copy(), a["velocities"].copy()
+
+
 def test_step_host_rejects_bad_arguments():
     m = W.build_model(W.dam_break(dims=(8, 8, 8), map_res=0))
     with pytest.raises(VfsError):

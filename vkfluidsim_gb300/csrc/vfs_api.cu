@@ -328,6 +328,16 @@ int Model::refresh_params() {
 void Model::invalidate_graph() {
     if (graph_exec) cudaGraphExecDestroy(graph_exec);
     graph_exec = nullptr;
+    if (host_graph) cudaGraphExecDestroy(host_graph);
+    host_graph = nullptr;
+}
+
+int Model::ensure_io_stream() {
+    if (io_stream) return VFS_OK;
+    VFS_CUDA_TRY(cudaStreamCreateWithFlags(&io_stream, cudaStreamNonBlocking));
+    VFS_CUDA_TRY(cudaEventCreateWithFlags(&io_ev[0], cudaEventDisableTiming));
+    VFS_CUDA_TRY(cudaEventCreateWithFlags(&io_ev[1], cudaEventDisableTiming));
+    return VFS_OK;
 }
 
 int Model::alloc_sort_scratch() {
@@ -674,17 +684,56 @@ int Model::step_host(const float* pos3, const float* vel3, int32_t count, float*
     const bool fused = n > 0 && ho.any() && (!pos_out || ho.pos3) && (!vel_out || ho.vel3) &&
                        (!dens_out || ho.dens);
     int remaining = count;
+    const void* in_p = pos3 ? device_alias(pos3) : nullptr;
+    const void* in_v = vel3 ? device_alias(vel3) : nullptr;
+    if (fused && count == 1 && in_p && in_v && use_graph) {
+        // The frame loop's case: one substep between a page-locked upload and read-back. The
+        // sequence below (the upload, the velocities on the side stream, the substep with its
+        // host outputs) is captured once for this set of buffers and replayed as one graph.
+        const void* key[10] = {pos3, vel3, pos_out, vel_out, dens_out, in_p, in_v,
+                               ho.pos3, ho.vel3, ho.dens};
+        if (!host_graph || std::memcmp(key, host_graph_key, sizeof key) != 0) {
+            if (host_graph) cudaGraphExecDestroy(host_graph);
+            host_graph = nullptr;
+            int rc = ensure_io_stream();
+            if (rc) return rc;
+            cudaGraph_t g = nullptr;
+            VFS_CUDA_TRY(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+            rc = enqueue_set_state(0, pos3, vel3, 0, -1, io_stream);
+            if (rc == VFS_OK) {
+                cells_wait = io_ev[1];
+                host_out = ho;
+                rc = enqueue_substep(nullptr);
+                cells_wait = nullptr;
+                host_out = HostOut{};
+            }
+            cudaError_t e = cudaStreamEndCapture(stream, &g);
+            if (rc) {
+                if (g) cudaGraphDestroy(g);
+                return rc;
+            }
+            if (e != cudaSuccess) return fail(VFS_ERR_CUDA, std::string("host-step capture: ") + cudaGetErrorString(e));
+            e = cudaGraphInstantiate(&host_graph, g, 0);
+            cudaGraphDestroy(g);
+            if (e != cudaSuccess) {
+                host_graph = nullptr;
+                return fail(VFS_ERR_CUDA, std::string("host-step instantiate: ") + cudaGetErrorString(e));
+            }
+            std::memcpy(host_graph_key, key, sizeof key);
+        }
+        VFS_CUDA_TRY(cudaGraphLaunch(host_graph, stream));
+        stepped = true;
+        substeps_done += 1;
+        return check_device();
+    }
     if (pos3 && n > 0) {
         // Positions on the model's stream; velocities, first read by the cell pass, on a side
         // stream after them (so after all work queued before), their upload overlapping the key
         // and sort passes. The first substep is launched directly and waits for them before its
         // cell pass.
-        if (!io_stream) {
-            VFS_CUDA_TRY(cudaStreamCreateWithFlags(&io_stream, cudaStreamNonBlocking));
-            VFS_CUDA_TRY(cudaEventCreateWithFlags(&io_ev[0], cudaEventDisableTiming));
-            VFS_CUDA_TRY(cudaEventCreateWithFlags(&io_ev[1], cudaEventDisableTiming));
-        }
-        int rc = enqueue_set_state(0, pos3, vel3, 0, -1, io_stream);
+        int rc = ensure_io_stream();
+        if (rc) return rc;
+        rc = enqueue_set_state(0, pos3, vel3, 0, -1, io_stream);
         if (rc) return rc;
         cells_wait = io_ev[1];
         if (fused && count == 1) host_out = ho;

@@ -81,6 +81,10 @@ struct Model {
     cudaEvent_t cells_wait = nullptr;  // set only while step_host enqueues its first substep
     cudaStream_t io_stream = nullptr;  // step_host's velocity upload (created on first use)
     cudaEvent_t io_ev[2] = {nullptr, nullptr};
+    // step_host's one-substep round trip through page-locked buffers, captured once per set of
+    // buffers (host pointers and their device aliases) and replayed.
+    cudaGraphExec_t host_graph = nullptr;
+    const void* host_graph_key[10] = {};
     SceneParams* d_scenes = nullptr;   // batched launches: the scene table
     uint16_t* d_scene_of = nullptr;    // batched launches: scene id per particle
     DevObject* d_objects = nullptr;    // boundary objects of all scenes
@@ -120,6 +124,7 @@ struct Model {
     // with one wait at the end; outputs in page-locked memory come from the last force pass.
     int step_host(const float* pos3, const float* vel3, int32_t count, float* pos_out,
                   float* vel_out, float* dens_out);
+    int ensure_io_stream();
     int get_state(uint32_t scene, float* pos3, float* vel3, float* dens, uint32_t* ids);
     int get_acc(uint32_t scene, float* acc3);
     int get_neighbors(uint32_t scene, uint32_t* keys, uint32_t* perm, uint32_t* offsets);
