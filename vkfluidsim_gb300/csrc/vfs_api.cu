@@ -332,6 +332,14 @@ void Model::invalidate_graph() {
     host_graph = nullptr;
 }
 
+// The host outputs of the next substep enqueued: densities from the density pass (final there,
+// while the host link is idle), positions and velocities from the force pass.
+void Model::set_host_out(const HostOut& ho) {
+    launch.host_dens = ho.dens;
+    host_out = ho;
+    host_out.dens = nullptr;
+}
+
 int Model::ensure_io_stream() {
     if (io_stream) return VFS_OK;
     VFS_CUDA_TRY(cudaStreamCreateWithFlags(&io_stream, cudaStreamNonBlocking));
@@ -702,10 +710,10 @@ int Model::step_host(const float* pos3, const float* vel3, int32_t count, float*
             rc = enqueue_set_state(0, pos3, vel3, 0, -1, io_stream);
             if (rc == VFS_OK) {
                 cells_wait = io_ev[1];
-                host_out = ho;
+                set_host_out(ho);
                 rc = enqueue_substep(nullptr);
                 cells_wait = nullptr;
-                host_out = HostOut{};
+                set_host_out(HostOut{});
             }
             cudaError_t e = cudaStreamEndCapture(stream, &g);
             if (rc) {
@@ -736,10 +744,10 @@ int Model::step_host(const float* pos3, const float* vel3, int32_t count, float*
         rc = enqueue_set_state(0, pos3, vel3, 0, -1, io_stream);
         if (rc) return rc;
         cells_wait = io_ev[1];
-        if (fused && count == 1) host_out = ho;
+        if (fused && count == 1) set_host_out(ho);
         rc = enqueue_substep(nullptr);
         cells_wait = nullptr;
-        host_out = HostOut{};
+        set_host_out(HostOut{});
         if (rc) return rc;
         stepped = true;
         substeps_done += 1;
@@ -750,9 +758,9 @@ int Model::step_host(const float* pos3, const float* vel3, int32_t count, float*
     if (!fused) return get_state(0, pos_out, vel_out, dens_out, nullptr);
     // The last substep launched directly (not from the graph), its force pass also writing the
     // page-locked outputs: the read-back overlaps the pass instead of following it.
-    host_out = ho;
+    set_host_out(ho);
     rc = enqueue_substep(nullptr);
-    host_out = HostOut{};
+    set_host_out(HostOut{});
     if (rc) return rc;
     stepped = true;
     substeps_done += 1;

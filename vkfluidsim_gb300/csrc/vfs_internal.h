@@ -90,6 +90,8 @@ struct StepLaunch {
     const SceneParams* scenes;   // device, n_scenes entries (batched launches)
     const uint16_t* scene_of;    // device, scene id per particle (batched launches)
     SceneParams one;             // the scene of a single-scene launch
+    float* host_dens = nullptr;  // page-locked host array (its device address): the density pass
+                                 // also writes each particle's density there, in slot order
 };
 
 // Scratch of one onesweep sort: global digit histograms, tile counters, look-back status words.

@@ -938,7 +938,8 @@ __device__ __forceinline__ void density_finish(const SceneParams& p, uint32_t i,
                                                uint32_t cy, uint32_t cz, bool distinct,
                                                const DensitySum& d, float4* __restrict__ rec,
                                                float4* __restrict__ aux, float4* __restrict__ bnd,
-                                               uint32_t* __restrict__ nbr_count) {
+                                               uint32_t* __restrict__ nbr_count,
+                                               float* __restrict__ host_dens) {
     nbr_count[i] = nbr_word(d.listed, cx, cy, cz, distinct);
     float bd, bgx, bgy, bgz;
     boundary_terms(p, xi.x, xi.y, xi.z, bd, bgx, bgy, bgz);
@@ -948,6 +949,7 @@ __device__ __forceinline__ void density_finish(const SceneParams& p, uint32_t i,
     const float mr = p.mass / fmaxf(rho, 1e-6f);
     const float pb = rho > 0.0f ? pr / (p.rho0 * p.rho0) : 0.0f;
     aux[i] = make_float4(pd, mr, rho, pb);
+    if (host_dens) host_dens[i] = rho;
     // The force pass's neighbour record of i: one 32-byte sector per gathered neighbour.
     const float4 vi = __ldg(vel + i);
     rec[2 * (size_t)i] = make_float4(xi.x, xi.y, xi.z, pd);
@@ -1172,7 +1174,7 @@ __global__ void __launch_bounds__(kNbrBlock, kMinBlocks)
             if ((uint32_t)(tid & 31) == (uint32_t)(__ffs(g) - 1) && u)
                 atomicAdd(sk.ctl + sc * kSkinCtl + kCtlUsable, (uint32_t)__popc(u));
         }
-        density_finish(p, i, xi, vel, cx, cy, cz, distinct, d, rec, aux, bnd, nbr_count);
+        density_finish(p, i, xi, vel, cx, cy, cz, distinct, d, rec, aux, bnd, nbr_count, L.host_dens);
     }
     // The last warp out puts the counter back to zero for the next launch (every other warp has
     // made its last claim before it counts itself out).
@@ -1254,7 +1256,7 @@ __global__ void __launch_bounds__(kListBlock, 10)
                 if (r2 <= h2) d.add_r2(i, __float_as_uint(xj.w), r2, s_inv_h, s_nbr_cap, L.total);
             }
             density_finish(p, i, xi, vel, cx, cy, cz, distinct_keys(p, cx, cy, cz), d, rec, aux,
-                           bnd, nbr_count);
+                           bnd, nbr_count, L.host_dens);
         }
     }
     // The walkers go to the queue in index order within the block: batched, to this block's
@@ -1408,7 +1410,7 @@ __global__ void __launch_bounds__(kWalkerWarps * 32)
             DensitySum d;
             d.rho = rho;
             d.listed = listed;
-            density_finish(p, i, xi, vel, cx, cy, cz, distinct, d, rec, aux, bnd, nbr_count);
+            density_finish(p, i, xi, vel, cx, cy, cz, distinct, d, rec, aux, bnd, nbr_count, L.host_dens);
         }
     }
 }
@@ -1504,6 +1506,7 @@ __global__ void __launch_bounds__(kPlaneBlock)
     const float mr = p.mass / fmaxf(rho, 1e-6f);
     const float pb = rho > 0.0f ? pr / (p.rho0 * p.rho0) : 0.0f;
     aux[i] = make_float4(pd, mr, rho, pb);
+    if (L.host_dens) L.host_dens[i] = rho;
     const float4 vi = __ldg(vel + i);
     rec[2 * (size_t)i] = make_float4(xi.x, xi.y, xi.z, pd);
     rec[2 * (size_t)i + 1] = make_float4(vi.x, vi.y, vi.z, mr);

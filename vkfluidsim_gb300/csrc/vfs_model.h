@@ -125,6 +125,7 @@ struct Model {
     int step_host(const float* pos3, const float* vel3, int32_t count, float* pos_out,
                   float* vel_out, float* dens_out);
     int ensure_io_stream();
+    void set_host_out(const HostOut& ho);
     int get_state(uint32_t scene, float* pos3, float* vel3, float* dens, uint32_t* ids);
     int get_acc(uint32_t scene, float* acc3);
     int get_neighbors(uint32_t scene, uint32_t* keys, uint32_t* perm, uint32_t* offsets);
