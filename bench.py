@@ -743,7 +743,8 @@ def run_gpu(args):
 
     # Each step: the state uploaded from the pinned buffers, one substep, positions, velocities
     # and densities read back into them, one wait (vfs_model_step_host: the upload kernel reads
-    # the buffers before the substep's passes run; the force pass writes the outputs).
+    # the buffers before the substep's passes run; the density and force passes write the
+    # outputs).
     def e2e_step():
         check(lib.vfs_model_step_host(m._h, fp(hp), fp(hv), 1, fp(hp), fp(hv), fp(hd)))
 

@@ -174,8 +174,9 @@ int vfs_model_copy_data_buffers(vfs_model* m, float* pos, float* vel, float* den
  * NULL), with a single wait at the end, as the reference's frame records Step and
  * CopyDataBuffers into one command buffer (src/models/model.cpp:158-170) behind its staged
  * SetParticleState (model.cpp:139-147). When every given output is page-locked, the last
- * substep's force pass writes them itself, so the read-back overlaps that pass; otherwise the
- * outputs are packed after the substeps. Results equal those of the three separate calls.
+ * substep writes them itself (its density pass the densities, its force pass positions and
+ * velocities), so the read-back overlaps those passes; otherwise the outputs are packed after the
+ * substeps. Results equal those of the three separate calls.
  * Single-scene models only. */
 int vfs_model_step_host(vfs_model* m, const float* pos, const float* vel, int32_t substeps,
                         float* pos_out, float* vel_out, float* dens_out);

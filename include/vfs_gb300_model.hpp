@@ -73,7 +73,7 @@ public:
 
     // SetParticleState of every particle from pos / vel, `substeps` substeps, then the
     // CopyDataBuffers hand-off into the same arrays, with one wait (vfs_model_step_host). With
-    // page-locked storage behind the vectors' data the last force pass writes the outputs.
+    // page-locked storage behind the vectors' data the last substep's passes write the outputs.
     template <class Vec3>
     void StepHost(std::vector<Vec3>& pos, std::vector<Vec3>& vel, std::vector<float>& dens,
                   int32_t substeps = 1) {

@@ -756,8 +756,8 @@ int Model::step_host(const float* pos3, const float* vel3, int32_t count, float*
     int rc = run_substeps(fused ? remaining - 1 : remaining);
     if (rc) return rc;
     if (!fused) return get_state(0, pos_out, vel_out, dens_out, nullptr);
-    // The last substep launched directly (not from the graph), its force pass also writing the
-    // page-locked outputs: the read-back overlaps the pass instead of following it.
+    // The last substep launched directly (not from the graph), its density and force passes also
+    // writing the page-locked outputs: the read-back overlaps the passes instead of following them.
     set_host_out(ho);
     rc = enqueue_substep(nullptr);
     set_host_out(HostOut{});

@@ -121,7 +121,8 @@ struct Model {
     int enqueue_set_state(uint32_t scene, const float* pos3, const float* vel3, uint32_t offset,
                           int64_t count, cudaStream_t vel_stream = nullptr);
     // set_state of every particle (when pos3 / vel3 are given), `count` substeps and get_state,
-    // with one wait at the end; outputs in page-locked memory come from the last force pass.
+    // with one wait at the end; outputs in page-locked memory come from the last substep's
+    // density pass (densities) and force pass (positions, velocities).
     int step_host(const float* pos3, const float* vel3, int32_t count, float* pos_out,
                   float* vel_out, float* dens_out);
     int ensure_io_stream();

@@ -402,7 +402,8 @@ class WCSPHWithBoundaryModel:
         substeps and copy_data_buffers, with one wait at the end (vfs_model_step_host). `out`
         may hold preallocated float32 arrays "positions" (N x 3), "velocities" (N x 3) and
         "densities" (N); when all of them are page-locked (e.g. numpy views of pinned torch
-        tensors), the last force pass writes them directly."""
+        tensors), the last substep writes them directly (its density pass the densities, its
+        force pass positions and velocities)."""
         n = self.n_particles
         if (pos is None) != (vel is None):
             raise ValueError("pos and vel must both be given or both be None")
