@@ -1,7 +1,7 @@
 """vfs_model_step_host (upload, substeps and read-back with one wait; with page-locked outputs the
-last substep's density and force passes write them) must give exactly what
-set_particle_state + substeps +
-copy_data_buffers give (SetParticleState, Step, CopyDataBuffers: src/models/model.cpp:139-170).
+last substep's density and force passes write them) must give exactly what set_particle_state +
+substeps + copy_data_buffers give (SetParticleState, Step, CopyDataBuffers:
+src/models/model.cpp:139-170).
 Each case runs the same scene both ways over several host round trips, each round's output fed
 back as the next round's input, and compares every output bit for bit."""
 from __future__ import annotations
