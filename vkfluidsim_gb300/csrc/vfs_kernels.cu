@@ -957,16 +957,6 @@ __device__ __forceinline__ void density_finish(const SceneParams& p, uint32_t i,
     bnd[i] = make_float4(bgx, bgy, bgz, bd);
 }
 
-// CalculateBoundaryVolume + CalculateDensities + the per-particle part of PressureFromDensityEOS
-// (wcsph_with_boundary_model.slang:102-203), by the bucket walk. Besides the density products it
-// writes particle i's neighbour list: every in-range j except i itself, in visiting order,
-// slot-major (nbr[s * n + i], so a warp's lanes store and later load consecutive words), and its
-// length in nbr_count[i] (a length above nbr_cap means the list overflowed and was truncated).
-// Positions do not change before the force pass, so that list is exactly the force pass's
-// neighbour set. Without skin lists every particle is walked. With them, the particles
-// k_density_list left in its queue, one per thread: each list block's walkers in index order, so
-// a stale scene is walked in index order and a warp whose slots are empty returns at once. In a
-// stale scene whose build policy allows it, every particle also builds its skin list.
 // Block-per-cell staging of the neighbourhood, one warp at a time: when a warp's particles share
 // one row of cells (same scene, same y and z cells, at most four consecutive x cells) and the
 // 3 x 3 rows of cells around them (x from the first cell - 1 to the last + 1) lie in one 50^3 hash
@@ -1022,12 +1012,14 @@ __device__ __forceinline__ bool warp_row_union(const SceneParams& p, bool act, b
 // slot-major (nbr[s * n + i], so a warp's lanes store and later load consecutive words), and its
 // length in nbr_count[i] (a length above nbr_cap means the list overflowed and was truncated).
 // Positions do not change before the force pass, so that list is exactly the force pass's
-// neighbour set. Without skin lists every particle is walked. With them, the particles
-// k_density_list left in its queue, one per thread: each list block's walkers in index order, so
-// a stale scene is walked in index order and a warp whose slots are empty returns at once. In a
-// stale scene whose build policy allows it, every particle also builds its skin list. A warp
-// whose particles share a row of cells walks the staged rows of warp_row_union; any other warp
-// walks per thread (for_each_candidate).
+// neighbour set. Without skin lists every particle is walked, one per thread. With them, a
+// batch's walkers are the queue k_density_list leaves (each list block's walkers in index order,
+// so a stale scene is walked in index order); a single scene is walked here only when it is stale
+// or its lists are mostly unusable (in index order; otherwise k_density_walkers takes its few
+// walkers and this launch returns at its top). In a stale scene whose build policy allows it,
+// every particle also builds its skin list. The launch is one resident wave whose warps claim
+// runs of 32 slots. A warp whose particles share a row of cells walks the staged rows of
+// warp_row_union; any other warp walks per thread (for_each_candidate).
 template <bool kBatch, int kNbrBlock, int kMinBlocks, bool kStaging>
 __global__ void __launch_bounds__(kNbrBlock, kMinBlocks)
     k_density(StepLaunch L, const float4* __restrict__ pos, const float4* __restrict__ vel,
