@@ -799,7 +799,11 @@ def run_gpu(args):
             "e2e": e2e,
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm,
                          "unit": "GB/s", "frac": achieved / hbm, "peak_kind": peak_kind,
-                         "algorithmic_bytes_per_launch": B_PHASE[dom] * n, "traffic": traffic},
+                         "algorithmic_bytes_per_launch": B_PHASE[dom] * n, "traffic": traffic,
+                         # the DRAM bytes the pass really moves per launch (one ncu capture)
+                         # over its live event time: what the memory system sustains for it
+                         "traffic_gbs": traffic / (kernel_phases[dom] * 1e-3) / 1e9 if traffic else None,
+                         "traffic_frac": traffic / (kernel_phases[dom] * 1e-3) / 1e9 / hbm if traffic else None},
             "issue_roofline": issue_roofline(inst_pp, kernel_phases, n, local, clk.summary()),
             "step_roofline": {"bytes_per_particle_step": B_STEP,
                               "achieved_gbs": B_STEP * n / (ms_per_step * 1e-3) / 1e9,
