@@ -589,7 +589,6 @@ struct Rollout {
         float4* own_pos = m->pos[o];
         float4* own_vel = m->vel[o];
         int rc = VFS_OK;
-        m->keep_nbr = true;  // the reverse pass reads each recorded substep's neighbour lists
         for (int t = 0; t < len && rc == VFS_OK; t++) {
             m->aux = s_aux[t];
             m->bnd = s_bnd[t];
@@ -604,7 +603,6 @@ struct Rollout {
                 if (e != cudaSuccess) rc = fail(VFS_ERR_CUDA, cudaGetErrorString(e));
             }
         }
-        m->keep_nbr = false;
         m->aux = own_aux;
         m->bnd = own_bnd;
         m->nbr = own_nbr;

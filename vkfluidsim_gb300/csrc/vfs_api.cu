@@ -485,9 +485,6 @@ Model::~Model() {
     cudaFree(skin.queue);
     cudaFree(skin.seg_n);
     cudaFree(skin.wcount);
-    cudaFree(skin.lrow);
-    cudaFree(skin.lmask);
-    cudaFree(skin.rec_b);
     cudaFree(scratch);
     cudaFree(err);
     cudaFree(walk_sched);
@@ -603,11 +600,7 @@ int Model::alloc_skin() {
         cudaMalloc(&s.ctl, scenes.size() * kSkinCtl * sizeof(uint32_t)) != cudaSuccess ||
         cudaMalloc(&s.queue, N * sizeof(uint32_t)) != cudaSuccess ||
         cudaMalloc(&s.seg_n, ((N + 127) / 128) * sizeof(uint32_t)) != cudaSuccess ||
-        cudaMalloc(&s.wcount, sizeof(uint32_t)) != cudaSuccess ||
-        (scenes.size() == 1 &&
-         (cudaMalloc(&s.lrow, N * sizeof(uint32_t)) != cudaSuccess ||
-          cudaMalloc(&s.lmask, N * sizeof(unsigned long long)) != cudaSuccess ||
-          cudaMalloc(&s.rec_b, 2 * N * sizeof(float4)) != cudaSuccess))) {
+        cudaMalloc(&s.wcount, sizeof(uint32_t)) != cudaSuccess) {
         cudaGetLastError();  // out of memory is not sticky: clear it and go on without lists
         cudaFree(s.list);
         cudaFree(s.count);
@@ -619,16 +612,12 @@ int Model::alloc_skin() {
         cudaFree(s.queue);
         cudaFree(s.seg_n);
         cudaFree(s.wcount);
-        cudaFree(s.lrow);
-        cudaFree(s.lmask);
-        cudaFree(s.rec_b);
         return VFS_OK;
     }
     VFS_CUDA_TRY(cudaMemset(s.count, 0, N * sizeof(uint32_t)));
     VFS_CUDA_TRY(cudaMemset(s.b_of_id, 0, N * sizeof(uint32_t)));  // any index below n until a build
     VFS_CUDA_TRY(cudaMemset(s.stale, 0, scenes.size() * sizeof(uint32_t)));
     VFS_CUDA_TRY(cudaMemset(s.wcount, 0, sizeof(uint32_t)));
-    if (s.lrow) VFS_CUDA_TRY(cudaMemset(s.lrow, 0xFF, N * sizeof(uint32_t)));  // kLrowSorted
     skin = s;
     return invalidate_skin();
 }
@@ -649,12 +638,7 @@ int Model::invalidate_skin() {
 
 // The lists the passes use: none when switched off.
 SkinLists Model::active_skin() const {
-    if (skin_fraction <= 0.0f) return SkinLists{};
-    SkinLists s = skin;
-    // The force pass sums a single scene's skin lists unless substeps are recorded (the adjoint
-    // reads the neighbour lists of the recorded substeps).
-    s.lmode = s.lrow && !record && !keep_nbr ? 1u : 0u;
-    return s;
+    return skin_fraction > 0.0f ? skin : SkinLists{};
 }
 
 int create_model(const std::vector<SceneHost>& scenes, Model** out) {

@@ -149,21 +149,8 @@ struct SkinLists {
                                   // list block b at [128 b, 128 b + seg_n[b]), in index order
     uint32_t* seg_n = nullptr;    // per list block (128 particles): its walkers
     uint32_t* wcount = nullptr;   // single scene: walkers in `queue`, packed from 0 (one word)
-    // A single scene's force pass over the skin lists (lmode = 1, not while substeps are
-    // recorded): per particle (sorted index) of this substep, lrow says what its density pass
-    // left. A build index: the force pass sums that skin list's members under the particle's
-    // lmask (bit k: member k in range and not the particle; the list length in bits 56-63),
-    // with the records under build indices (rec_b). kLrowWalker: a walker, whose neighbour
-    // list holds build indices (records in rec_b). kLrowSorted: a walked particle of a stale or
-    // poor scene, whose neighbour list holds sorted indices (records in the model's rec).
-    uint32_t* lrow = nullptr;
-    unsigned long long* lmask = nullptr;
-    float4* rec_b = nullptr;      // 2 float4 per build index: the force record of its particle
-    uint32_t lmode = 0;
     uint32_t cap = 0;             // slots per particle
 };
-constexpr uint32_t kLrowSorted = 0xFFFFFFFFu;
-constexpr uint32_t kLrowWalker = 0xFFFFFFFEu;
 constexpr uint32_t kSkinUsable = 1u << 31;
 constexpr uint32_t kSkinCtl = 8;       // words of policy state per scene:
 constexpr uint32_t kCtlAllow = 0;      //   a stale scene may rebuild this substep

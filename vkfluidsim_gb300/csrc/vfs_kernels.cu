@@ -912,17 +912,6 @@ struct DensitySum {
     // The same with r2 = in_range2(x_i, x_j) already computed (by the in-range test).
     __device__ __forceinline__ void add_r2(uint32_t i, uint32_t j, float r2, float inv_h,
                                            uint32_t cap, uint32_t stride) {
-        add_w(r2, inv_h);
-        if (j != i) {
-            if (listed < cap) {
-                *out = j;
-                out += stride;
-            }
-            listed++;
-        }
-    }
-    // The density term alone (a list kept elsewhere).
-    __device__ __forceinline__ void add_w(float r2, float inv_h) {
         const float r = r2 > 0.0f ? __fmul_rn(r2, rsqrtf(r2)) : 0.0f;
         // W(q) / sigma, branch-free: 2 (1-q)^3 above q = 1/2, 6q^3 - 6q^2 + 1 below, 0 past 1.
         const float q = __fmul_rn(r, inv_h);
@@ -932,6 +921,13 @@ struct DensitySum {
         const float w_in = __fmaf_rn(6.0f, __fmul_rn(q2, q), __fmaf_rn(-6.0f, q2, 1.0f));
         const float w = q <= 1.0f ? (q > 0.5f ? w_out : w_in) : 0.0f;
         rho = __fadd_rn(rho, w);
+        if (j != i) {
+            if (listed < cap) {
+                *out = j;
+                out += stride;
+            }
+            listed++;
+        }
     }
 };
 
@@ -941,8 +937,7 @@ __device__ __forceinline__ void density_finish(const SceneParams& p, uint32_t i,
                                                const float4* __restrict__ vel, uint32_t cx,
                                                uint32_t cy, uint32_t cz, bool distinct,
                                                const DensitySum& d, float4* __restrict__ rec,
-                                               uint32_t ri, float4* __restrict__ aux,
-                                               float4* __restrict__ bnd,
+                                               float4* __restrict__ aux, float4* __restrict__ bnd,
                                                uint32_t* __restrict__ nbr_count,
                                                float* __restrict__ host_dens) {
     nbr_count[i] = nbr_word(d.listed, cx, cy, cz, distinct);
@@ -955,11 +950,10 @@ __device__ __forceinline__ void density_finish(const SceneParams& p, uint32_t i,
     const float pb = rho > 0.0f ? pr / (p.rho0 * p.rho0) : 0.0f;
     aux[i] = make_float4(pd, mr, rho, pb);
     if (host_dens) host_dens[i] = rho;
-    // The force pass's neighbour record of i (at ri: its sorted index, or its build index when
-    // the force pass sums the skin lists): one 32-byte sector per gathered neighbour.
+    // The force pass's neighbour record of i: one 32-byte sector per gathered neighbour.
     const float4 vi = __ldg(vel + i);
-    rec[2 * (size_t)ri] = make_float4(xi.x, xi.y, xi.z, pd);
-    rec[2 * (size_t)ri + 1] = make_float4(vi.x, vi.y, vi.z, mr);
+    rec[2 * (size_t)i] = make_float4(xi.x, xi.y, xi.z, pd);
+    rec[2 * (size_t)i + 1] = make_float4(vi.x, vi.y, vi.z, mr);
     bnd[i] = make_float4(bgx, bgy, bgz, bd);
 }
 
@@ -1172,10 +1166,7 @@ __global__ void __launch_bounds__(kNbrBlock, kMinBlocks)
             if ((uint32_t)(tid & 31) == (uint32_t)(__ffs(g) - 1) && u)
                 atomicAdd(sk.ctl + sc * kSkinCtl + kCtlUsable, (uint32_t)__popc(u));
         }
-        density_finish(p, i, xi, vel, cx, cy, cz, distinct, d, rec, i, aux, bnd, nbr_count, L.host_dens);
-        // A single scene walked here is stale or poor: its force pass reads this list of sorted
-        // indices and the records under sorted indices.
-        if (!kBatch && sk.lmode) sk.lrow[i] = kLrowSorted;
+        density_finish(p, i, xi, vel, cx, cy, cz, distinct, d, rec, aux, bnd, nbr_count, L.host_dens);
     }
     // The last warp out puts the counter back to zero for the next launch (every other warp has
     // made its last claim before it counts itself out).
@@ -1224,21 +1215,6 @@ __global__ void __launch_bounds__(kListBlock, 10)
             DensitySum d;
             d.out = nbr + i;
             const size_t stride = L.total;
-            // Member k of the list, at sorted index js and squared distance r2. Either its index
-            // goes to the neighbour list, or (a single scene whose force pass sums the skin
-            // lists) bit k of the particle's mask marks it.
-            const bool lm = !kBatch && sk.lmode;
-            unsigned long long mask = 0ull;
-            auto member = [&](uint32_t kk, uint32_t js, float r2) {
-                if (r2 <= h2) {
-                    if (lm) {
-                        d.add_w(r2, s_inv_h);
-                        if (js != i) mask |= 1ull << kk;
-                    } else {
-                        d.add_r2(i, js, r2, s_inv_h, s_nbr_cap, L.total);
-                    }
-                }
-            };
             const uint32_t* q = sk.list + row;
             uint32_t k = 0;
             // The next batch's build indices load while the current batch is resolved and summed.
@@ -1260,27 +1236,19 @@ __global__ void __launch_bounds__(kListBlock, 10)
 #pragma unroll
                 for (int u = 0; u < 4; u++) xj[u] = __ldg(sk.xcur + j[u]);  // position, sorted index
 #pragma unroll
-                for (int u = 0; u < 4; u++)
-                    member(k + (uint32_t)u, __float_as_uint(xj[u].w), in_range2(xi, xj[u]));
+                for (int u = 0; u < 4; u++) {
+                    const float r2 = in_range2(xi, xj[u]);
+                    if (r2 <= h2) d.add_r2(i, __float_as_uint(xj[u].w), r2, s_inv_h, s_nbr_cap, L.total);
+                }
             }
 #pragma unroll 1
             for (; k < n_list; k++, q += stride) {
                 const float4 xj = __ldg(sk.xcur + __ldg(q));
-                member(k, __float_as_uint(xj.w), in_range2(xi, xj));
+                const float r2 = in_range2(xi, xj);
+                if (r2 <= h2) d.add_r2(i, __float_as_uint(xj.w), r2, s_inv_h, s_nbr_cap, L.total);
             }
-            const bool distinct = distinct_keys(p, cx, cy, cz);
-            if (lm) {
-                d.listed = (uint32_t)__popcll(mask);
-                density_finish(p, i, xi, vel, cx, cy, cz, distinct, d, sk.rec_b, row, aux, bnd,
-                               nbr_count, L.host_dens);
-                sk.lmask[i] = mask | ((unsigned long long)n_list << 56);
-                sk.lrow[i] = row;
-            } else {
-                density_finish(p, i, xi, vel, cx, cy, cz, distinct, d, rec, i, aux, bnd, nbr_count,
-                               L.host_dens);
-            }
-        } else if (!kBatch && sk.lmode) {
-            sk.lrow[i] = kLrowWalker;  // k_density_walkers lists it under build indices
+            density_finish(p, i, xi, vel, cx, cy, cz, distinct_keys(p, cx, cy, cz), d, rec, aux,
+                           bnd, nbr_count, L.host_dens);
         }
     }
     // The walkers go to the queue in index order within the block: batched, to this block's
@@ -1421,11 +1389,7 @@ __global__ void __launch_bounds__(kWalkerWarps * 32)
             const uint32_t listm = __ballot_sync(0xffffffffu, inr && j != i);
             if (inr && j != i) {
                 const uint32_t slot = listed + (uint32_t)__popc(listm & lt);
-                // With the force pass summing skin lists, the neighbour is listed under its
-                // build index (its record is there).
-                if (slot < p.nbr_cap)
-                    nbr[(size_t)slot * L.total + i] =
-                        sk.lmode ? __ldg(sk.b_of_id + __float_as_uint(xj.w)) : j;
+                if (slot < p.nbr_cap) nbr[(size_t)slot * L.total + i] = j;
             }
             listed += (uint32_t)__popc(listm);
             while (mask) {
@@ -1438,13 +1402,7 @@ __global__ void __launch_bounds__(kWalkerWarps * 32)
             DensitySum d;
             d.rho = rho;
             d.listed = listed;
-            if (sk.lmode)
-                density_finish(p, i, xi, vel, cx, cy, cz, distinct, d, sk.rec_b,
-                               __ldg(sk.b_of_id + __float_as_uint(xi.w)), aux, bnd, nbr_count,
-                               L.host_dens);
-            else
-                density_finish(p, i, xi, vel, cx, cy, cz, distinct, d, rec, i, aux, bnd, nbr_count,
-                               L.host_dens);
+            density_finish(p, i, xi, vel, cx, cy, cz, distinct, d, rec, aux, bnd, nbr_count, L.host_dens);
         }
     }
 }
@@ -1660,11 +1618,9 @@ __global__ void __launch_bounds__(kNbrBlock, kMinBlocks)
             const float4* __restrict__ bnd,
             const uint32_t* __restrict__ scan, const uint32_t* __restrict__ nbr,
             const uint32_t* __restrict__ nbr_count, float4* __restrict__ pos_out,
-            float4* __restrict__ vel_out, float4* __restrict__ acc_out, SkinLists sk,
-            HostOut ho) {
+            float4* __restrict__ vel_out, float4* __restrict__ acc_out,
+            uint32_t* __restrict__ skin_stale, uint32_t* __restrict__ skin_ctl, HostOut ho) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    uint32_t* const skin_stale = sk.stale;
-    uint32_t* const skin_ctl = sk.ctl;
     // The density pass is done with the skin lists' flags: run each scene's build policy and clear
     // the flags for the next substep.
     if (skin_stale && blockIdx.x == 0) {
@@ -1706,95 +1662,47 @@ __global__ void __launch_bounds__(kNbrBlock, kMinBlocks)
         const float pdi = ai.x;
 
         ForceAcc f{0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
-        const size_t stride = L.total;
-        // What the density pass left for this particle: a single scene whose force pass sums the
-        // skin lists has a build index here for a particle with a usable list.
-        const uint32_t row = !kBatch && sk.lmode ? __ldg(sk.lrow + i) : kLrowSorted;
-        if (row < kLrowWalker) {
-            // Its skin list's members under its mask (the in-range ones other than i, in list
-            // order: the neighbour list the density pass would have written), their records under
-            // build indices. The next batch's build indices load while the current batch is
-            // gathered and summed.
-            const unsigned long long mw = __ldg(sk.lmask + i);
-            const uint32_t n_list = (uint32_t)(mw >> 56);
-            const uint32_t* q = sk.list + row;
+        const uint32_t listed = nbr_count[i] & kNbrCountMask;
+        if (listed <= p.nbr_cap) {
+            // The density pass's list: the in-range neighbours in the reference's visiting order.
             uint32_t k = 0;
+            const uint32_t* nl = nbr + i;  // slot k of particle i's list
+            const size_t stride = L.total;
+            // The next batch's indices load while the current batch is gathered and summed, so
+            // each batch waits on one dependent load (the records) instead of two.
             uint32_t jn[4];
-            if (n_list >= 4u) {
+            if (listed >= 4u) {
 #pragma unroll
-                for (int u = 0; u < 4; u++) jn[u] = __ldg(q + u * stride);
+                for (int u = 0; u < 4; u++) jn[u] = __ldg(nl + u * stride);
             }
 #pragma unroll 1
-            for (; k + 4u <= n_list; k += 4u, q += 4 * stride) {
+            for (; k + 4u <= listed; k += 4u, nl += 4 * stride) {
                 uint32_t j[4];
                 float4 a[4], b[4];
 #pragma unroll
                 for (int u = 0; u < 4; u++) j[u] = jn[u];
-                if (k + 8u <= n_list) {
+                if (k + 8u <= listed) {
 #pragma unroll
-                    for (int u = 0; u < 4; u++) jn[u] = __ldg(q + (4 + u) * stride);
+                    for (int u = 0; u < 4; u++) jn[u] = __ldg(nl + (4 + u) * stride);
                 }
-                const uint32_t bits = (uint32_t)(mw >> k) & 15u;
 #pragma unroll
-                for (int u = 0; u < 4; u++)
-                    if ((bits >> u) & 1u) load_record(sk.rec_b, j[u], a[u], b[u]);
+                for (int u = 0; u < 4; u++) load_record(rec, j[u], a[u], b[u]);
 #pragma unroll
-                for (int u = 0; u < 4; u++)
-                    if ((bits >> u) & 1u)
-                        force_term(p, xi, vi, pdi, a[u], make_float2(a[u].w, b[u].w), b[u], f);
+                for (int u = 0; u < 4; u++) force_term(p, xi, vi, pdi, a[u], make_float2(a[u].w, b[u].w), b[u], f);
             }
 #pragma unroll 1
-            for (; k < n_list; k++, q += stride)
-                if ((mw >> k) & 1ull) force_term_rec(p, xi, vi, pdi, sk.rec_b, __ldg(q), f);
+            for (; k < listed; k++, nl += stride) force_term_rec(p, xi, vi, pdi, rec, __ldg(nl), f);
         } else {
-            // Its neighbour list: sorted indices with the records under sorted indices, or (a
-            // walker of a scene whose force pass sums the skin lists) build indices with the
-            // records under build indices.
-            const bool by_build = row == kLrowWalker;
-            const float4* __restrict__ rs = by_build ? sk.rec_b : rec;
-            const uint32_t listed = nbr_count[i] & kNbrCountMask;
-            if (listed <= p.nbr_cap) {
-                // The density pass's list: the in-range neighbours in the reference's visiting order.
-                uint32_t k = 0;
-                const uint32_t* nl = nbr + i;  // slot k of particle i's list
-                // The next batch's indices load while the current batch is gathered and summed,
-                // so each batch waits on one dependent load (the records) instead of two.
-                uint32_t jn[4];
-                if (listed >= 4u) {
-#pragma unroll
-                    for (int u = 0; u < 4; u++) jn[u] = __ldg(nl + u * stride);
-                }
-#pragma unroll 1
-                for (; k + 4u <= listed; k += 4u, nl += 4 * stride) {
-                    uint32_t j[4];
-                    float4 a[4], b[4];
-#pragma unroll
-                    for (int u = 0; u < 4; u++) j[u] = jn[u];
-                    if (k + 8u <= listed) {
-#pragma unroll
-                        for (int u = 0; u < 4; u++) jn[u] = __ldg(nl + (4 + u) * stride);
-                    }
-#pragma unroll
-                    for (int u = 0; u < 4; u++) load_record(rs, j[u], a[u], b[u]);
-#pragma unroll
-                    for (int u = 0; u < 4; u++) force_term(p, xi, vi, pdi, a[u], make_float2(a[u].w, b[u].w), b[u], f);
-                }
-#pragma unroll 1
-                for (; k < listed; k++, nl += stride) force_term_rec(p, xi, vi, pdi, rs, __ldg(nl), f);
-            } else {
-                // Overflowed list (very dense neighbourhood): walk the candidates again and add
-                // every in-range one as it comes, in the same order. This path needs no shared
-                // memory, so the pass keeps the whole on-chip memory as L1 for its record gathers.
-                const uint32_t cx = cell_coord(xi.x, p.h), cy = cell_coord(xi.y, p.h),
-                               cz = cell_coord(xi.z, p.h);
-                for_each_candidate(p, scan, pos, xi, cx, cy, cz, [&](uint32_t j, const float4& xj) {
-                    const float xx = xi.x - xj.x, xy = xi.y - xj.y, xz = xi.z - xj.z;
-                    const float r2 = xx * xx + xy * xy + xz * xz;
-                    if (r2 <= p.h2 && j != i)
-                        force_term_rec(p, xi, vi, pdi, rs,
-                                       by_build ? __ldg(sk.b_of_id + __float_as_uint(xj.w)) : j, f);
-                }, [&]() {});
-            }
+            // Overflowed list (very dense neighbourhood): walk the candidates again and add every
+            // in-range one as it comes, in the same order. This path needs no shared memory, so
+            // the pass keeps the whole on-chip memory as L1 for its record gathers.
+            const uint32_t cx = cell_coord(xi.x, p.h), cy = cell_coord(xi.y, p.h),
+                           cz = cell_coord(xi.z, p.h);
+            for_each_candidate(p, scan, pos, xi, cx, cy, cz, [&](uint32_t j, const float4& xj) {
+                const float xx = xi.x - xj.x, xy = xi.y - xj.y, xz = xi.z - xj.z;
+                const float r2 = xx * xx + xy * xy + xz * xz;
+                if (r2 <= p.h2 && j != i) force_term_rec(p, xi, vi, pdi, rec, j, f);
+            }, [&]() {});
         }
         force_finish(p, i, xi, vi, ai, f, bnd, pos_out, vel_out, acc_out, x_new, v_new);
         dens_i = ai.z;
@@ -2286,10 +2194,11 @@ void force_shape(const StepLaunch& L, const float4* pos, const float4* vel, cons
     const uint32_t blocks = (L.total + B - 1) / B;
     if (L.n_scenes > 1)
         k_force<true, B, M><<<blocks, B, 0, s>>>(L, pos, vel, aux, rec, bnd, cell_scan, nbr, nbr_count,
-                                                 pos_out, vel_out, acc_out, sk, HostOut{});
+                                                 pos_out, vel_out, acc_out, sk.stale, sk.ctl, HostOut{});
     else  // shared memory only for host outputs: without them the whole on-chip memory stays L1
         k_force<false, B, M><<<blocks, B, ho.any() ? 7 * B * sizeof(float) : 0, s>>>(
-            L, pos, vel, aux, rec, bnd, cell_scan, nbr, nbr_count, pos_out, vel_out, acc_out, sk, ho);
+            L, pos, vel, aux, rec, bnd, cell_scan, nbr, nbr_count, pos_out, vel_out, acc_out,
+            sk.stale, sk.ctl, ho);
 }
 
 bool planes_mode(uint32_t total) {

@@ -98,7 +98,6 @@ struct Model {
     StepLaunch launch{};
 
     bool record = false;
-    bool keep_nbr = false;  // set while a rollout records substeps: their neighbour lists are read back
     uint64_t substeps_done = 0;  // substeps run by run_substeps (the snapshot sidecar's counter)
     bool use_graph = true;
     bool stepped = false;
