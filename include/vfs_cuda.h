@@ -307,8 +307,7 @@ typedef struct vfs_tune_config {
     int32_t sort_tile_items; /* 8, 12 or 16 keys per thread of a onesweep tile */
     int32_t nbr_block;       /* neighbour passes: threads per block ... */
     int32_t nbr_min_blocks;  /* ... and minimum resident blocks per SM: 128x6, 128x8, 96x8, 64x12 */
-    int32_t cell_block;      /* keys per block of the cell-range / reorder kernel: 128, 256, 512, or
-                                1024 (512 threads, two particles each) */
+    int32_t cell_block;      /* keys per block of the cell-range / reorder kernel: 128, 256, 512 */
     int32_t force_block;     /* force pass: threads per block and minimum resident blocks per */
     int32_t force_min_blocks;/* SM, the same four shapes; 0, 0 = the neighbour passes' shape */
     int32_t walk_staging;    /* block-per-cell staging of the density walk: 1 on, 0 off */

@@ -82,7 +82,7 @@ def test_autotuned_model_is_bit_identical_to_default():
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("shape", [(128, 6), (128, 8), (96, 8), (64, 12)])
-@pytest.mark.parametrize("cell_block", [128, 512, 1024])
+@pytest.mark.parametrize("cell_block", [128, 512])
 def test_every_launch_shape_gives_the_same_step(shape, cell_block):
     w = W.dam_break(dims=(48, 48, 48), map_res=24, seed=5)
     ref = W.build_model(w)

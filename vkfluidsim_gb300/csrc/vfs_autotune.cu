@@ -98,8 +98,8 @@ int apply_tune_config(Model& m, const vfs_tune_config& c) {
     if (fshape < 0)
         return fail(VFS_ERR_INVALID_ARGUMENT,
                     "force block shape must be 128x6, 128x8, 96x8 or 64x12, or 0x0 for the neighbour shape");
-    if (c.cell_block != 128 && c.cell_block != 256 && c.cell_block != 512 && c.cell_block != 1024)
-        return fail(VFS_ERR_INVALID_ARGUMENT, "cell_block must be 128, 256, 512 or 1024");
+    if (c.cell_block != 128 && c.cell_block != 256 && c.cell_block != 512)
+        return fail(VFS_ERR_INVALID_ARGUMENT, "cell_block must be 128, 256 or 512");
     if (c.walk_staging != 0 && c.walk_staging != 1)
         return fail(VFS_ERR_INVALID_ARGUMENT, "walk_staging must be 0 or 1");
     if (c.sort_digit_bits != m.digit_bits || c.sort_tile_items != m.tile_items) {
@@ -228,7 +228,7 @@ int autotune(Model& m, int repeats, bool use_cache, vfs_tune_config* chosen) {
     if (rc == VFS_OK) {
         float best_t = 1e30f;
         vfs_tune_config c = best;
-        for (int cb : {256, 128, 512, 1024}) {
+        for (int cb : {256, 128, 512}) {
             c.cell_block = cb;
             measure(c, ph);
             if (rc) break;

@@ -170,8 +170,7 @@ constexpr uint32_t kSkinCap = 48;  // also the density walk's shared list, where
 struct KernelConfig {
     int nbr_shape = kNbr96x8;     // density pass (and the adjoint's recomputed forward)
     int force_shape = kNbr128x8;  // force pass (no shared memory: it takes the larger blocks)
-    int cell_block = 256;  // keys per block of the cell-range / reorder kernel: 128, 256, 512 or
-                           // 1024 (512 threads, two particles each)
+    int cell_block = 256;  // keys per block of the cell-range / reorder kernel: 128, 256 or 512
     int walk_staging = 0;  // density walk: warps whose particles share a row of cells stage it
                            // (off by default: the autotuner turns it on where it is faster)
 };

@@ -518,7 +518,7 @@ __device__ __forceinline__ uint32_t lower_bound_near(const uint32_t* __restrict_
     return lo;
 }
 
-template <uint32_t kCellBlock, uint32_t kItems>
+template <uint32_t kCellBlock>
 __global__ void __launch_bounds__(kCellBlock)
     k_cells_reorder(StepLaunch L, uint32_t n, const uint32_t* __restrict__ skeys,
                     const uint32_t* __restrict__ perm, uint32_t* __restrict__ scan,
@@ -534,11 +534,8 @@ __global__ void __launch_bounds__(kCellBlock)
     // for the next substep here instead of in a separate memset.
     for (uint32_t w = blockIdx.x * kCellBlock + threadIdx.x; w < zero_words; w += gridDim.x * kCellBlock)
         zero[w] = 0u;
-    // The block owns kCellBlock * kItems cells and as many particles; each thread reorders
-    // kItems of them, so their dependent loads are in flight together.
-    constexpr uint32_t kSpan = kCellBlock * kItems;
-    const uint32_t c0 = blockIdx.x * kSpan;
-    const uint32_t c1 = min(c0 + kSpan, n + 1u);
+    const uint32_t c0 = blockIdx.x * kCellBlock;
+    const uint32_t c1 = min(c0 + kCellBlock, n + 1u);
     const uint32_t tid = threadIdx.x;
     // The block's slice of the sorted keys, searched from the previous substep's bounds (cell
     // boundaries move little per substep). guess[b] is block b's lower bound; block b reads its
@@ -551,56 +548,47 @@ __global__ void __launch_bounds__(kCellBlock)
     if (tid == 32)
         s_hi = guess ? lower_bound_near(skeys, n, c1, ((volatile uint32_t*)guess)[blockIdx.x + 1])
                      : lower_bound_keys(skeys, n, c1);
-    // skin lists: whether each particle moved past h skin / 2 since its list build, and its scene
-    bool exceed[kItems];
-    uint32_t exceed_sc[kItems];
-#pragma unroll
-    for (uint32_t it = 0; it < kItems; it++) {
-        const uint32_t i = c0 + it * kCellBlock + tid;
-        exceed[it] = false;
-        exceed_sc[it] = 0u;
-        if (i < n) {
-            uint32_t src = perm[i];
-            if (src >= n) src = i;  // only after a reported sort failure
-            const float4 x = __ldg(pos_in + src);
-            pos_out[i] = x;
-            vel_out[i] = __ldg(vel_in + src);
-            if (xcur) {
-                const uint32_t sc = L.n_scenes > 1 ? (uint32_t)__ldg(L.scene_of + i) : 0u;
-                exceed_sc[it] = sc;
-                if (ctl[sc * kSkinCtl + kCtlFresh] == 0u) {
-                    // No build yet, or the last build's lists have gone stale: they stay unusable
-                    // until the next build, so the scene is stale without a displacement check,
-                    // and nothing reads its positions by build index.
-                    exceed[it] = true;
-                } else {
-                    // Skin lists: the particle's current position and sorted index under its
-                    // build index (the list pass gathers both with one load), and its
-                    // displacement since the build.
-                    const uint32_t id = __float_as_uint(x.w);
-                    const uint32_t bi = id < n ? __ldg(b_of_id + id) : n;
-                    if (bi < n) {
-                        xcur[bi] = make_float4(x.x, x.y, x.z, __uint_as_float(i));
-                        const float4 b = __ldg(x_build + bi);
-                        const float dx = x.x - b.x, dy = x.y - b.y, dz = x.z - b.z;
-                        const float lim = L.n_scenes > 1 ? L.scenes[sc].skin_half2 : L.one.skin_half2;
-                        exceed[it] = !(dx * dx + dy * dy + dz * dz <= lim);
-                    }
+    const uint32_t i = c0 + tid;
+    bool exceed = false;  // skin lists: the particle moved past h skin / 2 since its list build
+    uint32_t exceed_sc = 0u;
+    if (i < n) {
+        uint32_t src = perm[i];
+        if (src >= n) src = i;  // only after a reported sort failure
+        const float4 x = __ldg(pos_in + src);
+        pos_out[i] = x;
+        vel_out[i] = __ldg(vel_in + src);
+        if (xcur) {
+            const uint32_t sc = L.n_scenes > 1 ? (uint32_t)__ldg(L.scene_of + i) : 0u;
+            exceed_sc = sc;
+            if (ctl[sc * kSkinCtl + kCtlFresh] == 0u) {
+                // No build yet, or the last build's lists have gone stale: they stay unusable
+                // until the next build, so the scene is stale without a displacement check, and
+                // nothing reads its positions by build index.
+                exceed = true;
+            } else {
+                // Skin lists: the particle's current position and sorted index under its build
+                // index (the list pass gathers both with one load), and its displacement since
+                // the build.
+                const uint32_t id = __float_as_uint(x.w);
+                const uint32_t bi = id < n ? __ldg(b_of_id + id) : n;
+                if (bi < n) {
+                    xcur[bi] = make_float4(x.x, x.y, x.z, __uint_as_float(i));
+                    const float4 b = __ldg(x_build + bi);
+                    const float dx = x.x - b.x, dy = x.y - b.y, dz = x.z - b.z;
+                    const float lim = L.n_scenes > 1 ? L.scenes[sc].skin_half2 : L.one.skin_half2;
+                    exceed = !(dx * dx + dy * dy + dz * dz <= lim);
                 }
             }
-            if (pkeys_out) pkeys_out[i] = skeys[i];
         }
+        if (pkeys_out) pkeys_out[i] = skeys[i];
     }
     // Stale scenes, one atomic per warp and scene at most (most particles of a fast scene exceed).
     if (xcur) {
-#pragma unroll
-        for (uint32_t it = 0; it < kItems; it++) {
-            const uint32_t m = __ballot_sync(0xffffffffu, exceed[it]);
-            if (exceed[it]) {
-                const uint32_t g = __match_any_sync(m, exceed_sc[it]);
-                if ((tid & 31u) == (uint32_t)(__ffs(g) - 1) && ld_volatile(stale + exceed_sc[it]) == 0u)
-                    atomicOr(stale + exceed_sc[it], 1u);
-            }
+        const uint32_t m = __ballot_sync(0xffffffffu, exceed);
+        if (exceed) {
+            const uint32_t g = __match_any_sync(m, exceed_sc);
+            if ((tid & 31u) == (uint32_t)(__ffs(g) - 1) && ld_volatile(stale + exceed_sc) == 0u)
+                atomicOr(stale + exceed_sc, 1u);
         }
     }
     __syncthreads();
@@ -2114,22 +2102,17 @@ cudaError_t launch_cells_reorder(const StepLaunch& L, uint32_t n, const uint32_t
                                  uint32_t zero_words, uint32_t* pkeys_out, uint32_t* guess,
                                  const SkinLists& sk, const KernelConfig& kc, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
-    // cell_block 1024: 512 threads, two particles each.
     switch (kc.cell_block) {
         case 128:
-            k_cells_reorder<128, 1><<<(n + 128u) / 128u, 128, 0, s>>>(L, n, skeys, perm, cell_scan, pos_in,
+            k_cells_reorder<128><<<(n + 128u) / 128u, 128, 0, s>>>(L, n, skeys, perm, cell_scan, pos_in,
                                                                  vel_in, pos_out, vel_out, zero, zero_words, pkeys_out, guess, sk.b_of_id, sk.xcur, sk.x_build, sk.stale, sk.ctl);
             break;
         case 512:
-            k_cells_reorder<512, 1><<<(n + 512u) / 512u, 512, 0, s>>>(L, n, skeys, perm, cell_scan, pos_in,
-                                                                 vel_in, pos_out, vel_out, zero, zero_words, pkeys_out, guess, sk.b_of_id, sk.xcur, sk.x_build, sk.stale, sk.ctl);
-            break;
-        case 1024:
-            k_cells_reorder<512, 2><<<(n + 1024u) / 1024u, 512, 0, s>>>(L, n, skeys, perm, cell_scan, pos_in,
+            k_cells_reorder<512><<<(n + 512u) / 512u, 512, 0, s>>>(L, n, skeys, perm, cell_scan, pos_in,
                                                                  vel_in, pos_out, vel_out, zero, zero_words, pkeys_out, guess, sk.b_of_id, sk.xcur, sk.x_build, sk.stale, sk.ctl);
             break;
         default:
-            k_cells_reorder<256, 1><<<(n + 256u) / 256u, 256, 0, s>>>(L, n, skeys, perm, cell_scan, pos_in,
+            k_cells_reorder<256><<<(n + 256u) / 256u, 256, 0, s>>>(L, n, skeys, perm, cell_scan, pos_in,
                                                                  vel_in, pos_out, vel_out, zero, zero_words, pkeys_out, guess, sk.b_of_id, sk.xcur, sk.x_build, sk.stale, sk.ctl);
     }
     return cudaGetLastError();
