@@ -18,6 +18,8 @@ def test_readme_example(tmp_path):
     state = m.copy_data_buffers()
     keys, sorted_indices, offsets = m.get_neighbor_arrays()
     assert state["positions"].shape[0] == len(keys) == len(sorted_indices) == len(offsets)
+    state = m.step_host(state["positions"], state["velocities"], substeps=1)
+    assert np.isfinite(state["positions"]).all() and state["densities"].min() > 0.0
 
     view = vfs.look_at((12.0, -8.0, 9.0), (5.0, 5.0, 2.0))
     proj = vfs.perspective(0.8, 16 / 9, 0.1, 100.0)
