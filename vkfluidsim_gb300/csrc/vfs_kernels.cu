@@ -1198,9 +1198,10 @@ __global__ void __launch_bounds__(kListBlock, 10)
     bool walk = false;
     if (i < L.total) {
         const SceneParams& p = scene_params<kBatch>(L, i);
-        const float4 xi = __ldg(pos + i);
         uint32_t c = 0u, row = 0u;
         walk = sk.stale[kBatch ? (uint32_t)__ldg(L.scene_of + i) : 0u] != 0u;
+        // A particle of a stale scene only joins the queue: its position is not read.
+        const float4 xi = walk ? make_float4(0.0f, 0.0f, 0.0f, 0.0f) : __ldg(pos + i);
         if (!walk) {
             row = __ldg(sk.b_of_id + __float_as_uint(xi.w));
             c = __ldg(sk.count + row);
