@@ -364,8 +364,7 @@ int Model::alloc_sort_scratch() {
     sort_scratch.ghist = scratch;
     sort_scratch.counters = scratch + (size_t)sc.passes * sc.bins;
     sort_scratch.status = sort_scratch.counters + sc.passes;
-    sort_scratch.dcounter = sort_scratch.status + (size_t)sc.passes * sc.tiles * sc.bins;
-    sort_scratch.mcount = sort_scratch.dcounter + 1;
+    sort_scratch.mcount = sort_scratch.status + (size_t)sc.passes * sc.tiles * sc.bins;
     sort_scratch.dstatus = sort_scratch.mcount + 1;
     sort_scratch.err = err;
     invalidate_graph();

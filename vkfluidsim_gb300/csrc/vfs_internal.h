@@ -99,8 +99,7 @@ struct SortScratch {
     uint32_t* ghist;     // [passes][bins]
     uint32_t* counters;  // [passes]
     uint32_t* status;    // [passes][tiles][bins]
-    uint32_t* dcounter;  // key/delta pass: block claim counter [1]
-    uint32_t* dstatus;   // key/delta pass: look-back status per block [delta_blocks]
+    uint32_t* dstatus;   // key pass: each tile's moved count, then its exclusive prefix [delta_blocks]
     uint32_t* mcount;    // number of particles whose key changed [1]
     uint32_t* err;       // device error word
 };
@@ -111,7 +110,7 @@ struct SortConfig {
     int bins;
     int tile;        // elements per onesweep tile
     uint32_t tiles;
-    uint32_t delta_blocks;  // tiles of the key/delta pass (1024 particles each)
+    uint32_t delta_blocks;  // tiles of the key pass (1024 particles each)
 };
 
 // ---- launch wrappers (vfs_kernels.cu) ----
@@ -179,9 +178,10 @@ size_t sort_scratch_words(const SortConfig& c);
 // Per-pass digit histograms of caller-provided keys.
 cudaError_t launch_digit_hist(const uint32_t* keys, uint32_t n, const SortConfig& sc,
                               uint32_t* ghist, cudaStream_t s);
-// Incremental sort, pass 1: keys, moved flags (key != pkeys[i]) as a bitmask bits[0, W) with the
-// moved count before each word in bits[W, 2W] (W = ceil(n / 32)), the moved (key, index) pairs
-// compacted in index order, their digit histograms, and the moved count in scr.mcount.
+// Incremental sort, pass 1 (three launches: flags, tile scan, compaction): keys, moved flags
+// (key != pkeys[i]) as a bitmask bits[0, W) with the moved count before each word in bits[W, 2W]
+// (W = ceil(n / 32)), the moved (key, index) pairs compacted in index order, their digit
+// histograms, and the moved count in scr.mcount.
 cudaError_t launch_keys_delta(const StepLaunch& L, const float4* pos, const uint32_t* pkeys,
                               uint32_t* mkeys, uint32_t* midx, uint32_t* bits,
                               const SortConfig& sc, const SortScratch& scr, cudaStream_t s);

@@ -1741,73 +1741,44 @@ __global__ void __launch_bounds__(kNbrBlock, kMinBlocks)
 // sorted pkeys (all moved when pkeys is the all-ones fill of a fresh model), so no step ever
 // needs to know whether pkeys is current.
 
-// Keys, moved flags and the moved particles' compaction: the moved flags as a bitmask with one
-// word per 32 particles, bits[w], and the number of moved particles before each word, pre[w]
-// (pre[W] = total = *mcount, W = ceil(n / 32), pre = bits + W); (mkeys, midx)[rank] for the moved
-// ones in index order; and the digit histograms of the moved keys. A tile is 256 threads x kDeltaItems particles
-// (particle tile * kDeltaTile + item * 256 + thread, so every load is coalesced); tiles are
-// claimed in order and chained by a bounded decoupled look-back over their moved counts.
-// Decoupled look-back of tile `tile` over single-counter status words, one warp wide: lane l reads
-// tile - 1 - l, so each step covers 32 predecessors. Sums aggregates up to and including the
-// nearest inclusive prefix. Each lane polls a word that has published nothing at most
-// kLookbackSpinLimit times, then sets kErrLookbackTimeout and counts it as zero. Called by a
-// whole warp; every lane returns the same sum.
-__device__ __forceinline__ uint32_t warp_lookback(const uint32_t* status, uint32_t tile, uint32_t* err) {
-    const int lane = threadIdx.x & 31;
-    uint32_t excl = 0u;
-    int64_t top = (int64_t)tile - 1;  // nearest predecessor not yet summed
-    while (top >= 0) {
-        const int64_t t = top - lane;
-        uint32_t v = kFlagPrefix;  // below tile 0: an empty prefix
-        if (t >= 0) {
-            uint32_t spins = 0u;
-            while (true) {
-                v = ld_volatile(status + t);
-                if ((v & ~kCountMask) != 0u) break;
-                if (++spins > kLookbackSpinLimit) {
-                    atomicOr(err, kErrLookbackTimeout);
-                    v = kFlagPrefix;
-                    break;
-                }
-                __nanosleep(32);
-            }
-        }
-        const uint32_t pre = __ballot_sync(0xffffffffu, (v & ~kCountMask) == kFlagPrefix);
-        const int stop = pre ? __ffs(pre) - 1 : 31;  // lanes 0..stop are summed
-        uint32_t c = lane <= stop ? (v & kCountMask) : 0u;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
-        excl += c;
-        if (pre) break;
-        top -= 32;
-    }
-    return excl;
-}
-
+// Keys, moved flags and the moved particles' compaction, in three launches without a chain
+// between tiles: the moved flags as a bitmask with one word per 32 particles, bits[w], and the
+// number of moved particles before each word, pre[w] (pre[W] = total = *mcount, W = ceil(n / 32),
+// pre = bits + W); (mkeys, midx)[rank] for the moved ones in index order; and the digit
+// histograms of the moved keys. A tile is 256 threads x kDeltaItems particles (particle
+// tile * kDeltaTile + item * 256 + thread, so every load is coalesced, and a warp's 32 particles
+// of one item are one bitmask word: the tile's words are bits[32 tile, 32 tile + 32), in (item,
+// warp) order).
+//   k_keys_flags:    keys, moved flags, each tile's moved count (tile_cnt), histograms;
+//   k_tile_scan:     one block: the tiles' exclusive prefixes in place, the total;
+//   k_moved_compact: per tile, each word's prefix and the moved particles' (key, index) pairs
+//                    at their ranks (the key recomputed from the position: the same arithmetic).
+// A decoupled look-back over the 1,024 tiles of a 1M-particle model resolves ~32 tiles per L2
+// round trip, so that chain, not the bytes, set the single-launch form's time.
 constexpr int kDeltaItems = 4;
 constexpr uint32_t kDeltaTile = 256u * kDeltaItems;
 
 template <bool kBatch>
+__device__ __forceinline__ uint32_t particle_key(const StepLaunch& L, uint32_t i, const float4& x) {
+    const SceneParams& p = scene_params<kBatch>(L, i);
+    return p.off + key_mod(hash_cell(cell_coord(x.x, p.h), cell_coord(x.y, p.h), cell_coord(x.z, p.h)),
+                           p.mod_magic, p.n);
+}
+
+template <bool kBatch>
 __global__ void __launch_bounds__(256)
-    k_keys_delta(StepLaunch L, const float4* __restrict__ pos, const uint32_t* __restrict__ pkeys,
-                 uint32_t* __restrict__ mkeys, uint32_t* __restrict__ midx,
+    k_keys_flags(StepLaunch L, const float4* __restrict__ pos, const uint32_t* __restrict__ pkeys,
                  uint32_t* __restrict__ bits, int passes, int digit_bits,
-                 uint32_t* __restrict__ ghist, uint32_t* __restrict__ counter,
-                 uint32_t* __restrict__ status, uint32_t* __restrict__ mcount,
-                 uint32_t* __restrict__ err) {
+                 uint32_t* __restrict__ ghist, uint32_t* __restrict__ tile_cnt) {
     __shared__ uint32_t s_h[kMaxSortPasses * kMaxSortBins];
-    __shared__ uint32_t s_cnt[kDeltaItems * 8];  // moved count per (item, warp), then its offset
-    __shared__ uint32_t s_blk, s_excl;
+    __shared__ uint32_t s_n[8];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int bins = 1 << digit_bits;
     const uint32_t mask = (uint32_t)bins - 1u;
-    if (tid == 0) s_blk = atomicAdd(counter, 1u);
     for (int e = tid; e < passes * bins; e += 256) s_h[e] = 0u;
     __syncthreads();
-    const uint32_t tile = s_blk;
-    const uint32_t base = tile * kDeltaTile + (uint32_t)tid;
-    uint32_t key[kDeltaItems];
-    uint32_t ball[kDeltaItems];
+    const uint32_t base = blockIdx.x * kDeltaTile + (uint32_t)tid;
+    const uint32_t W = (L.total + 31u) >> 5;
     // All of the thread's loads first (positions and previous keys), then the key arithmetic.
     float4 xs[kDeltaItems];
     uint32_t pks[kDeltaItems];
@@ -1819,86 +1790,113 @@ __global__ void __launch_bounds__(256)
             pks[k] = __ldg(pkeys + i);
         }
     }
+    uint32_t cnt = 0u;
 #pragma unroll
     for (int k = 0; k < kDeltaItems; k++) {
         const uint32_t i = base + (uint32_t)k * 256u;
         bool moved = false;
-        key[k] = 0u;
         if (i < L.total) {
-            const SceneParams& p = scene_params<kBatch>(L, i);
-            const float4 x = xs[k];
-            key[k] = p.off + key_mod(hash_cell(cell_coord(x.x, p.h), cell_coord(x.y, p.h),
-                                               cell_coord(x.z, p.h)),
-                                     p.mod_magic, p.n);
-            moved = key[k] != pks[k];
+            const uint32_t key = particle_key<kBatch>(L, i, xs[k]);
+            moved = key != pks[k];
             if (moved)
                 for (int ps = 0; ps < passes; ps++)
-                    atomicAdd(&s_h[ps * bins + ((key[k] >> (ps * digit_bits)) & mask)], 1u);
+                    atomicAdd(&s_h[ps * bins + ((key >> (ps * digit_bits)) & mask)], 1u);
         }
-        ball[k] = __ballot_sync(0xffffffffu, moved);
-        if (lane == 0) s_cnt[k * 8 + warp] = __popc(ball[k]);
+        const uint32_t ball = __ballot_sync(0xffffffffu, moved);
+        const uint32_t word = (i - (uint32_t)lane) >> 5;
+        if (lane == 0 && word < W) bits[word] = ball;
+        cnt += (uint32_t)__popc(ball);
     }
+    if (lane == 0) s_n[warp] = cnt;
     __syncthreads();
-    if (warp == 0) {
-        // Exclusive offsets in particle order (item-major, then warp): each lane scans 4 entries.
-        constexpr int kPerLane = kDeltaItems * 8 / 32;
-        static_assert(kDeltaItems % 4 == 0, "whole counters per lane");
-        uint32_t c[kPerLane], sum = 0u;
+    if (tid == 0) {
+        uint32_t t = 0u;
 #pragma unroll
-        for (int q = 0; q < kPerLane; q++) {
-            c[q] = s_cnt[lane * kPerLane + q];
-            sum += c[q];
-        }
-        uint32_t incl = sum;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
-            if (lane >= o) incl += v;
-        }
-        uint32_t run = incl - sum;
-#pragma unroll
-        for (int q = 0; q < kPerLane; q++) {
-            s_cnt[lane * kPerLane + q] = run;
-            run += c[q];
-        }
-        const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
-        uint32_t excl = 0u;
-        if (tile == 0u) {
-            if (lane == 0) st_volatile(status, kFlagPrefix | total);
-        } else {
-            if (lane == 0) st_volatile(status + tile, kFlagAggregate | total);
-            excl = warp_lookback(status, tile, err);
-            if (lane == 0) st_volatile(status + tile, kFlagPrefix | ((excl + total) & kCountMask));
-        }
-        if (lane == 0) {
-            s_excl = excl;
-            if (tile == gridDim.x - 1u) {
-                *mcount = excl + total;
-                bits[2u * ((L.total + 31u) >> 5)] = excl + total;  // pre[W]
-            }
-        }
-    }
-    __syncthreads();
-    const uint32_t lt = (1u << lane) - 1u;
-    const uint32_t W = (L.total + 31u) >> 5;
-#pragma unroll
-    for (int k = 0; k < kDeltaItems; k++) {
-        const uint32_t i = base + (uint32_t)k * 256u;
-        const uint32_t word = i >> 5;  // this warp's 32 particles of item k
-        if (lane == 0 && word < W) {
-            bits[word] = ball[k];
-            bits[W + word] = s_excl + s_cnt[k * 8 + warp];
-        }
-        if (i < L.total) {
-            const uint32_t rank = s_excl + s_cnt[k * 8 + warp] + __popc(ball[k] & lt);
-            if ((ball[k] >> lane) & 1u) {
-                mkeys[rank] = key[k];
-                midx[rank] = i;
-            }
-        }
+        for (int w = 0; w < 8; w++) t += s_n[w];
+        tile_cnt[blockIdx.x] = t;
     }
     for (int e = tid; e < passes * bins; e += 256)
         if (s_h[e]) atomicAdd(&ghist[e], s_h[e]);
+}
+
+// Exclusive prefix sums of the tiles' moved counts, in place, by one block in chunks of 1,024
+// tiles (one chunk up to 1M particles); the total goes to *mcount and pre[W].
+__global__ void __launch_bounds__(1024)
+    k_tile_scan(uint32_t tiles, uint32_t* __restrict__ tile_cnt, uint32_t* __restrict__ bits,
+                uint32_t W, uint32_t* __restrict__ mcount) {
+    __shared__ uint32_t s_w[32];
+    __shared__ uint32_t s_carry;
+    const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+    if (tid == 0) s_carry = 0u;
+    __syncthreads();
+    for (uint32_t b = 0; b < tiles; b += 1024u) {
+        const uint32_t t = b + tid;
+        const uint32_t v = t < tiles ? tile_cnt[t] : 0u;
+        uint32_t x = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if ((int)lane >= o) x += y;
+        }
+        if (lane == 31u) s_w[warp] = x;
+        __syncthreads();
+        if (warp == 0) {
+            uint32_t y = s_w[lane];
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t z = __shfl_up_sync(0xffffffffu, y, o);
+                if ((int)lane >= o) y += z;
+            }
+            s_w[lane] = y;
+        }
+        __syncthreads();
+        const uint32_t incl = s_carry + (warp ? s_w[warp - 1] : 0u) + x;
+        if (t < tiles) tile_cnt[t] = incl - v;
+        __syncthreads();  // every thread has read s_carry and s_w
+        if (tid == 1023u) s_carry = incl;
+        __syncthreads();
+    }
+    if (tid == 0) {
+        *mcount = s_carry;
+        bits[2u * W] = s_carry;  // pre[W]
+    }
+}
+
+template <bool kBatch>
+__global__ void __launch_bounds__(256)
+    k_moved_compact(StepLaunch L, const float4* __restrict__ pos, uint32_t* __restrict__ bits,
+                    const uint32_t* __restrict__ tile_excl, uint32_t* __restrict__ mkeys,
+                    uint32_t* __restrict__ midx) {
+    __shared__ uint32_t s_bits[32], s_off[32];
+    const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+    const uint32_t W = (L.total + 31u) >> 5;
+    if (warp == 0) {
+        const uint32_t w = blockIdx.x * 32u + lane;
+        const uint32_t b = w < W ? bits[w] : 0u;
+        const uint32_t c = (uint32_t)__popc(b);
+        uint32_t x = c;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if ((int)lane >= o) x += y;
+        }
+        const uint32_t off = tile_excl[blockIdx.x] + x - c;
+        s_bits[lane] = b;
+        s_off[lane] = off;
+        if (w < W) bits[W + w] = off;
+    }
+    __syncthreads();
+    const uint32_t lt = (1u << lane) - 1u;
+#pragma unroll
+    for (int k = 0; k < kDeltaItems; k++) {
+        const uint32_t i = blockIdx.x * kDeltaTile + (uint32_t)k * 256u + tid;
+        const uint32_t b = s_bits[k * 8 + warp];
+        if (i < L.total && ((b >> lane) & 1u)) {
+            const uint32_t rank = s_off[k * 8 + warp] + (uint32_t)__popc(b & lt);
+            mkeys[rank] = particle_key<kBatch>(L, i, __ldg(pos + i));
+            midx[rank] = i;
+        }
+    }
 }
 
 __device__ __forceinline__ uint32_t lower_bound_u32(const uint32_t* a, uint32_t n, uint32_t v) {
@@ -2031,7 +2029,7 @@ SortConfig make_sort_config(uint32_t n, int digit_bits, int tile_items, int key_
 
 size_t sort_scratch_words(const SortConfig& c) {
     return (size_t)c.passes * c.bins + (size_t)c.passes + (size_t)c.passes * c.tiles * c.bins +
-           2u + (size_t)c.delta_blocks;
+           1u + (size_t)c.delta_blocks;
 }
 
 
@@ -2039,14 +2037,18 @@ cudaError_t launch_keys_delta(const StepLaunch& L, const float4* pos, const uint
                               uint32_t* mkeys, uint32_t* midx, uint32_t* bits,
                               const SortConfig& sc, const SortScratch& scr, cudaStream_t s) {
     if (L.total == 0) return cudaSuccess;
+    const uint32_t tiles = sc.delta_blocks, W = (L.total + 31u) >> 5;
     if (L.n_scenes > 1)
-        k_keys_delta<true><<<sc.delta_blocks, 256, 0, s>>>(L, pos, pkeys, mkeys, midx, bits,
-                                                          sc.passes, sc.digit_bits, scr.ghist,
-                                                          scr.dcounter, scr.dstatus, scr.mcount, scr.err);
+        k_keys_flags<true><<<tiles, 256, 0, s>>>(L, pos, pkeys, bits, sc.passes, sc.digit_bits,
+                                                 scr.ghist, scr.dstatus);
     else
-        k_keys_delta<false><<<sc.delta_blocks, 256, 0, s>>>(L, pos, pkeys, mkeys, midx, bits,
-                                                           sc.passes, sc.digit_bits, scr.ghist,
-                                                           scr.dcounter, scr.dstatus, scr.mcount, scr.err);
+        k_keys_flags<false><<<tiles, 256, 0, s>>>(L, pos, pkeys, bits, sc.passes, sc.digit_bits,
+                                                  scr.ghist, scr.dstatus);
+    k_tile_scan<<<1, 1024, 0, s>>>(tiles, scr.dstatus, bits, W, scr.mcount);
+    if (L.n_scenes > 1)
+        k_moved_compact<true><<<tiles, 256, 0, s>>>(L, pos, bits, scr.dstatus, mkeys, midx);
+    else
+        k_moved_compact<false><<<tiles, 256, 0, s>>>(L, pos, bits, scr.dstatus, mkeys, midx);
     return cudaGetLastError();
 }
 

@@ -18,7 +18,7 @@ namespace {
 constexpr uint32_t kNoAllocPairs = VFS_SORT_NOALLOC_MAX_PAIRS;
 constexpr uint32_t kNoAllocTile = 256u * 16u;  // onesweep tile of make_sort_config(.., 8, 16, ..)
 constexpr uint32_t kNoAllocTiles = (kNoAllocPairs + kNoAllocTile - 1u) / kNoAllocTile;
-// Digit histograms + tile counters + look-back status words + the key/delta pass's words
+// Digit histograms + tile counters + look-back status words + the key pass's words
 // (unused by a pair sort, but part of sort_scratch_words) + the error word, for any key width.
 constexpr size_t kNoAllocSortWords = (size_t)kMaxSortPasses * kMaxSortBins + kMaxSortPasses +
                                      (size_t)kMaxSortPasses * kNoAllocTiles * kMaxSortBins + 2 +
