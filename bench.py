@@ -809,11 +809,12 @@ def run_gpu(args):
                               "achieved_gbs": B_STEP * n / (ms_per_step * 1e-3) / 1e9,
                               "frac": B_STEP * n / (ms_per_step * 1e-3) / 1e9 / hbm},
             "phase_ms": prof,
-            # the key pass's three kernels (flags, tile scan, compaction), `passes` onesweep
-            # passes, merge, cells+reorder, density (with skin lists:
+            # the key pass's two kernels (flags, compaction; the 1M scene is below the 4M
+            # particles where a tile scan joins them), `passes` onesweep passes, merge,
+            # cells+reorder, density (with skin lists:
             # the list pass, the one-warp-per-particle walk of the queued particles and the
             # per-thread walk, which returns at once unless the scene is stale), force.
-            "gpu_launches": (7 + passes + (2 if m.skin > 0 else 0)) * args.steps,
+            "gpu_launches": (6 + passes + (2 if m.skin > 0 else 0)) * args.steps,
             "skin": {"fraction": m.skin, "builds_in_timed_region": builds_timed,
                      "build_substep_density_ms": skin_build_ms},
             "clocks": clk.summary(),

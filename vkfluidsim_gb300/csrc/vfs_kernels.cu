@@ -1741,7 +1741,7 @@ __global__ void __launch_bounds__(kNbrBlock, kMinBlocks)
 // sorted pkeys (all moved when pkeys is the all-ones fill of a fresh model), so no step ever
 // needs to know whether pkeys is current.
 
-// Keys, moved flags and the moved particles' compaction, in three launches without a chain
+// Keys, moved flags and the moved particles' compaction, in two or three launches without a chain
 // between tiles: the moved flags as a bitmask with one word per 32 particles, bits[w], and the
 // number of moved particles before each word, pre[w] (pre[W] = total = *mcount, W = ceil(n / 32),
 // pre = bits + W); (mkeys, midx)[rank] for the moved ones in index order; and the digit
@@ -1750,7 +1750,8 @@ __global__ void __launch_bounds__(kNbrBlock, kMinBlocks)
 // of one item are one bitmask word: the tile's words are bits[32 tile, 32 tile + 32), in (item,
 // warp) order).
 //   k_keys_flags:    keys, moved flags, each tile's moved count (tile_cnt), histograms;
-//   k_tile_scan:     one block: the tiles' exclusive prefixes in place, the total;
+//   k_tile_scan:     one block: the tiles' exclusive prefixes in place, the total (only above
+//                    kFoldTiles tiles; below, each compaction block sums its predecessors' counts);
 //   k_moved_compact: per tile, each word's prefix and the moved particles' (key, index) pairs
 //                    at their ranks (the key recomputed from the position: the same arithmetic).
 // A decoupled look-back over the 1,024 tiles of a 1M-particle model resolves ~32 tiles per L2
@@ -1862,14 +1863,40 @@ __global__ void __launch_bounds__(1024)
     }
 }
 
-template <bool kBatch>
+// Up to this many tiles (4M particles) the compaction's blocks sum the earlier tiles' counts
+// themselves (at most 16 loads per thread) and the scan kernel is not launched.
+constexpr uint32_t kFoldTiles = 4096u;
+
+// kFolded: tile_cnt holds the tiles' counts (k_tile_scan did not run): the block sums those of
+// the tiles before its own, and the last tile writes the total. Otherwise tile_cnt holds the
+// exclusive prefixes.
+template <bool kBatch, bool kFolded>
 __global__ void __launch_bounds__(256)
     k_moved_compact(StepLaunch L, const float4* __restrict__ pos, uint32_t* __restrict__ bits,
-                    const uint32_t* __restrict__ tile_excl, uint32_t* __restrict__ mkeys,
-                    uint32_t* __restrict__ midx) {
-    __shared__ uint32_t s_bits[32], s_off[32];
+                    const uint32_t* __restrict__ tile_cnt, uint32_t* __restrict__ mkeys,
+                    uint32_t* __restrict__ midx, uint32_t* __restrict__ mcount) {
+    __shared__ uint32_t s_bits[32], s_off[32], s_sum[8];
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
     const uint32_t W = (L.total + 31u) >> 5;
+    uint32_t excl;
+    if (kFolded) {
+        uint32_t part = 0u;
+        for (uint32_t u = tid; u < blockIdx.x; u += 256u) part += tile_cnt[u];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+        if (lane == 0u) s_sum[warp] = part;
+        __syncthreads();
+        excl = 0u;
+#pragma unroll
+        for (int w = 0; w < 8; w++) excl += s_sum[w];
+        if (tid == 0u && blockIdx.x == gridDim.x - 1u) {
+            const uint32_t total = excl + tile_cnt[blockIdx.x];
+            *mcount = total;
+            bits[2u * W] = total;  // pre[W]
+        }
+    } else {
+        excl = tile_cnt[blockIdx.x];
+    }
     if (warp == 0) {
         const uint32_t w = blockIdx.x * 32u + lane;
         const uint32_t b = w < W ? bits[w] : 0u;
@@ -1880,7 +1907,7 @@ __global__ void __launch_bounds__(256)
             const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
             if ((int)lane >= o) x += y;
         }
-        const uint32_t off = tile_excl[blockIdx.x] + x - c;
+        const uint32_t off = excl + x - c;
         s_bits[lane] = b;
         s_off[lane] = off;
         if (w < W) bits[W + w] = off;
@@ -2044,11 +2071,18 @@ cudaError_t launch_keys_delta(const StepLaunch& L, const float4* pos, const uint
     else
         k_keys_flags<false><<<tiles, 256, 0, s>>>(L, pos, pkeys, bits, sc.passes, sc.digit_bits,
                                                   scr.ghist, scr.dstatus);
+    if (tiles <= kFoldTiles) {
+        if (L.n_scenes > 1)
+            k_moved_compact<true, true><<<tiles, 256, 0, s>>>(L, pos, bits, scr.dstatus, mkeys, midx, scr.mcount);
+        else
+            k_moved_compact<false, true><<<tiles, 256, 0, s>>>(L, pos, bits, scr.dstatus, mkeys, midx, scr.mcount);
+        return cudaGetLastError();
+    }
     k_tile_scan<<<1, 1024, 0, s>>>(tiles, scr.dstatus, bits, W, scr.mcount);
     if (L.n_scenes > 1)
-        k_moved_compact<true><<<tiles, 256, 0, s>>>(L, pos, bits, scr.dstatus, mkeys, midx);
+        k_moved_compact<true, false><<<tiles, 256, 0, s>>>(L, pos, bits, scr.dstatus, mkeys, midx, scr.mcount);
     else
-        k_moved_compact<false><<<tiles, 256, 0, s>>>(L, pos, bits, scr.dstatus, mkeys, midx);
+        k_moved_compact<false, false><<<tiles, 256, 0, s>>>(L, pos, bits, scr.dstatus, mkeys, midx, scr.mcount);
     return cudaGetLastError();
 }
 
