@@ -392,13 +392,25 @@ int Model::enqueue_substep(cudaEvent_t* ev) {
     skeys = sk_buf;
     sperm = sp_buf;
     if (ev) VFS_CUDA_TRY(cudaEventRecord(ev[3], s));
-    if (cells_wait) VFS_CUDA_TRY(cudaStreamWaitEvent(s, cells_wait, 0));
+    // Velocities still on their way from the host (a host round trip's first substep): the cell
+    // and density passes run without them, and their sorted copy and the force records' velocity
+    // half follow once they have arrived, before the force pass.
+    struct DeferOff {  // the flag holds for these two passes only, whatever returns
+        StepLaunch& l;
+        ~DeferOff() { l.defer_vel = false; }
+    } defer_off{launch};
+    launch.defer_vel = cells_wait != nullptr;
     VFS_CUDA_TRY(launch_cells_reorder(launch, n, skeys, sperm, cell_scan, pos[c], vel[c], pos[o], vel[o],
                                       scratch, (uint32_t)sort_scratch_words(sc), pkeys, cell_guess,
                                       sk, kc, s));
     if (ev) VFS_CUDA_TRY(cudaEventRecord(ev[4], s));
     VFS_CUDA_TRY(launch_density(launch, pos[o], vel[o], rec, cell_scan, aux, bnd, nbr, nbr_count, sk,
                                 walk_sched, kc, s));
+    launch.defer_vel = false;
+    if (cells_wait) {
+        VFS_CUDA_TRY(cudaStreamWaitEvent(s, cells_wait, 0));
+        VFS_CUDA_TRY(launch_vel_records(n, sperm, vel[c], vel[o], aux, rec, s));
+    }
     if (ev) VFS_CUDA_TRY(cudaEventRecord(ev[5], s));
     VFS_CUDA_TRY(launch_force(launch, pos[o], vel[o], aux, rec, bnd, cell_scan, nbr, nbr_count, pos[c],
                               vel[c], record ? acc : nullptr, sk, kc, s, host_out));

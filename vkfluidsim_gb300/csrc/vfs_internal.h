@@ -92,6 +92,9 @@ struct StepLaunch {
     SceneParams one;             // the scene of a single-scene launch
     float* host_dens = nullptr;  // page-locked host array (its device address): the density pass
                                  // also writes each particle's density there, in slot order
+    bool defer_vel = false;      // velocities still on their way from the host: the cell pass
+                                 // leaves them unsorted and the density pass leaves the force
+                                 // records' velocity half to launch_vel_records
 };
 
 // Scratch of one onesweep sort: global digit histograms, tile counters, look-back status words.
@@ -204,6 +207,11 @@ cudaError_t launch_sort(uint32_t n, const SortConfig& sc, const SortScratch& scr
 // searches from scratch. With skin lists (sk.cur set), also sk.cur[sk.b_of_id[id]] = sorted index
 // for the ids in x.w, and flags every scene of L with a particle that moved more than h skin / 2
 // since its list build.
+// The sorted velocities and the force records' velocity half of a substep whose cell and density
+// passes ran with StepLaunch::defer_vel: vel_out[i] = vel_in[perm[i]], rec[2i + 1] = (that
+// velocity, aux[i].y), the values those passes write otherwise.
+cudaError_t launch_vel_records(uint32_t n, const uint32_t* perm, const float4* vel_in,
+                               float4* vel_out, const float4* aux, float4* rec, cudaStream_t s);
 cudaError_t launch_cells_reorder(const StepLaunch& L, uint32_t n, const uint32_t* skeys, const uint32_t* perm,
                                  uint32_t* cell_scan, const float4* pos_in, const float4* vel_in,
                                  float4* pos_out, float4* vel_out, uint32_t* zero,

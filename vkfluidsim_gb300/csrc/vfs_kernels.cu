@@ -556,7 +556,7 @@ __global__ void __launch_bounds__(kCellBlock)
         if (src >= n) src = i;  // only after a reported sort failure
         const float4 x = __ldg(pos_in + src);
         pos_out[i] = x;
-        vel_out[i] = __ldg(vel_in + src);
+        if (!L.defer_vel) vel_out[i] = __ldg(vel_in + src);
         if (xcur) {
             const uint32_t sc = L.n_scenes > 1 ? (uint32_t)__ldg(L.scene_of + i) : 0u;
             exceed_sc = sc;
@@ -939,7 +939,7 @@ __device__ __forceinline__ void density_finish(const SceneParams& p, uint32_t i,
                                                const DensitySum& d, float4* __restrict__ rec,
                                                float4* __restrict__ aux, float4* __restrict__ bnd,
                                                uint32_t* __restrict__ nbr_count,
-                                               float* __restrict__ host_dens) {
+                                               float* __restrict__ host_dens, bool defer_vel) {
     nbr_count[i] = nbr_word(d.listed, cx, cy, cz, distinct);
     float bd, bgx, bgy, bgz;
     boundary_terms(p, xi.x, xi.y, xi.z, bd, bgx, bgy, bgz);
@@ -950,10 +950,13 @@ __device__ __forceinline__ void density_finish(const SceneParams& p, uint32_t i,
     const float pb = rho > 0.0f ? pr / (p.rho0 * p.rho0) : 0.0f;
     aux[i] = make_float4(pd, mr, rho, pb);
     if (host_dens) host_dens[i] = rho;
-    // The force pass's neighbour record of i: one 32-byte sector per gathered neighbour.
-    const float4 vi = __ldg(vel + i);
+    // The force pass's neighbour record of i: one 32-byte sector per gathered neighbour (the
+    // velocity half later, from launch_vel_records, when the velocities arrive late).
     rec[2 * (size_t)i] = make_float4(xi.x, xi.y, xi.z, pd);
-    rec[2 * (size_t)i + 1] = make_float4(vi.x, vi.y, vi.z, mr);
+    if (!defer_vel) {
+        const float4 vi = __ldg(vel + i);
+        rec[2 * (size_t)i + 1] = make_float4(vi.x, vi.y, vi.z, mr);
+    }
     bnd[i] = make_float4(bgx, bgy, bgz, bd);
 }
 
@@ -1166,7 +1169,8 @@ __global__ void __launch_bounds__(kNbrBlock, kMinBlocks)
             if ((uint32_t)(tid & 31) == (uint32_t)(__ffs(g) - 1) && u)
                 atomicAdd(sk.ctl + sc * kSkinCtl + kCtlUsable, (uint32_t)__popc(u));
         }
-        density_finish(p, i, xi, vel, cx, cy, cz, distinct, d, rec, aux, bnd, nbr_count, L.host_dens);
+        density_finish(p, i, xi, vel, cx, cy, cz, distinct, d, rec, aux, bnd, nbr_count, L.host_dens,
+                       L.defer_vel);
     }
     // The last warp out puts the counter back to zero for the next launch (every other warp has
     // made its last claim before it counts itself out).
@@ -1249,7 +1253,7 @@ __global__ void __launch_bounds__(kListBlock, 10)
                 if (r2 <= h2) d.add_r2(i, __float_as_uint(xj.w), r2, s_inv_h, s_nbr_cap, L.total);
             }
             density_finish(p, i, xi, vel, cx, cy, cz, distinct_keys(p, cx, cy, cz), d, rec, aux,
-                           bnd, nbr_count, L.host_dens);
+                           bnd, nbr_count, L.host_dens, L.defer_vel);
         }
     }
     // The walkers go to the queue in index order within the block: batched, to this block's
@@ -1403,7 +1407,8 @@ __global__ void __launch_bounds__(kWalkerWarps * 32)
             DensitySum d;
             d.rho = rho;
             d.listed = listed;
-            density_finish(p, i, xi, vel, cx, cy, cz, distinct, d, rec, aux, bnd, nbr_count, L.host_dens);
+            density_finish(p, i, xi, vel, cx, cy, cz, distinct, d, rec, aux, bnd, nbr_count, L.host_dens,
+                       L.defer_vel);
         }
     }
 }
@@ -1500,9 +1505,11 @@ __global__ void __launch_bounds__(kPlaneBlock)
     const float pb = rho > 0.0f ? pr / (p.rho0 * p.rho0) : 0.0f;
     aux[i] = make_float4(pd, mr, rho, pb);
     if (L.host_dens) L.host_dens[i] = rho;
-    const float4 vi = __ldg(vel + i);
     rec[2 * (size_t)i] = make_float4(xi.x, xi.y, xi.z, pd);
-    rec[2 * (size_t)i + 1] = make_float4(vi.x, vi.y, vi.z, mr);
+    if (!L.defer_vel) {
+        const float4 vi = __ldg(vel + i);
+        rec[2 * (size_t)i + 1] = make_float4(vi.x, vi.y, vi.z, mr);
+    }
     bnd[i] = make_float4(bgx, bgy, bgz, bd);
 }
 
@@ -2131,6 +2138,28 @@ cudaError_t launch_sort(uint32_t n, const SortConfig& sc, const SortScratch& scr
     *sorted_keys = const_cast<uint32_t*>(kin);
     *sorted_perm = const_cast<uint32_t*>(vin);
     return cudaSuccess;
+}
+
+namespace {
+__global__ void __launch_bounds__(256)
+    k_vel_records(uint32_t n, const uint32_t* __restrict__ perm, const float4* __restrict__ vel_in,
+                  float4* __restrict__ vel_out, const float4* __restrict__ aux,
+                  float4* __restrict__ rec) {
+    const uint32_t i = blockIdx.x * 256u + threadIdx.x;
+    if (i >= n) return;
+    uint32_t src = perm[i];
+    if (src >= n) src = i;  // only after a reported sort failure, as in the cell pass
+    const float4 v = __ldg(vel_in + src);
+    vel_out[i] = v;
+    rec[2 * (size_t)i + 1] = make_float4(v.x, v.y, v.z, __ldg(aux + i).y);
+}
+}  // namespace
+
+cudaError_t launch_vel_records(uint32_t n, const uint32_t* perm, const float4* vel_in,
+                               float4* vel_out, const float4* aux, float4* rec, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    k_vel_records<<<(n + 255u) / 256u, 256, 0, s>>>(n, perm, vel_in, vel_out, aux, rec);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_cells_reorder(const StepLaunch& L, uint32_t n, const uint32_t* skeys, const uint32_t* perm,
