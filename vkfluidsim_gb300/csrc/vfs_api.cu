@@ -377,13 +377,23 @@ int Model::alloc_sort_scratch() {
 int Model::enqueue_substep(cudaEvent_t* ev) {
     cudaStream_t s = stream;
     const int c = cur, o = 1 - cur;
+    // Page-locked positions of a host round trip (enqueue_set_state left them): read by the key
+    // pass itself, the velocities' upload queued behind it. Taken here, whatever returns below.
+    const float* host_pos = keys_host_pos;
+    const float* host_vel = keys_host_vel;
+    keys_host_pos = keys_host_vel = nullptr;
     if (ev) VFS_CUDA_TRY(cudaEventRecord(ev[0], s));
     // The sort scratch is zero here: zeroed when allocated and by every substep's cell pass.
     if (ev) VFS_CUDA_TRY(cudaEventRecord(ev[1], s));
     // Incremental stable sort: keys + the particles whose key changed (compacted into keys/vals),
     // a sort of those alone (count on the device), a merge with the rest.
     const SkinLists sk = active_skin();
-    VFS_CUDA_TRY(launch_keys_delta(launch, pos[c], pkeys, keys, vals, moved, sc, sort_scratch, s));
+    VFS_CUDA_TRY(launch_keys_delta(launch, pos[c], pkeys, keys, vals, moved, sc, sort_scratch, s,
+                                   host_pos, pos[c], aux));
+    if (host_pos) {
+        const int rc = enqueue_vel_upload(scenes[0], 0, n, host_vel, io_stream);
+        if (rc) return rc;
+    }
     if (ev) VFS_CUDA_TRY(cudaEventRecord(ev[2], s));
     uint32_t *mk = nullptr, *mi = nullptr;
     VFS_CUDA_TRY(launch_sort(n, sc, sort_scratch, keys, keys_alt, vals, vals_alt, &mk, &mi, s,
@@ -806,22 +816,36 @@ int Model::enqueue_set_state(uint32_t scene, const float* pos3, const float* vel
         }
         k_expand_state<<<blocks, kIoBlock, 0, stream>>>(sh.off + offset, (uint32_t)cnt, sp, sv,
                                                          pos[cur], vel[cur], aux);
+    } else if (sp != stage && scenes.size() == 1 && offset == 0 && cnt == sh.n) {
+        // Positions first, alone on the host link, read by the next substep's key pass itself
+        // (the upload and the key arithmetic overlap); the velocities follow after that pass.
+        keys_host_pos = sp;
+        keys_host_vel = vel3;
+        return VFS_OK;
     } else {
-        // Positions first, alone on the host link; the velocities follow on the side stream by
-        // DMA (a copy engine, so they move while the key and sort passes keep every SM busy)
-        // and are converted there. io_ev[1] marks them done.
+        // Positions first, alone on the host link; the velocities follow on the side stream.
         k_expand_state<<<blocks, kIoBlock, 0, stream>>>(sh.off + offset, (uint32_t)cnt, sp, nullptr,
                                                          pos[cur], vel[cur], aux);
         VFS_CUDA_TRY(cudaGetLastError());
-        VFS_CUDA_TRY(cudaEventRecord(io_ev[0], stream));
-        VFS_CUDA_TRY(cudaStreamWaitEvent(vel_stream, io_ev[0], 0));
-        VFS_CUDA_TRY(cudaMemcpyAsync(vel_stage, vel3, cnt * 12, cudaMemcpyHostToDevice, vel_stream));
-        k_expand_state<<<blocks, kIoBlock, 0, vel_stream>>>(sh.off + offset, (uint32_t)cnt, nullptr,
-                                                             vel_stage, pos[cur], vel[cur], aux);
-        VFS_CUDA_TRY(cudaGetLastError());
-        VFS_CUDA_TRY(cudaEventRecord(io_ev[1], vel_stream));
+        return enqueue_vel_upload(sh, offset, cnt, vel3, vel_stream);
     }
     VFS_CUDA_TRY(cudaGetLastError());
+    return VFS_OK;
+}
+
+int Model::enqueue_vel_upload(const SceneHost& sh, uint32_t offset, uint64_t cnt, const float* vel3,
+                              cudaStream_t vel_stream) {
+    // By DMA (a copy engine, so the velocities move while the key, sort and later passes keep
+    // every SM busy), converted on the side stream; io_ev[1] marks them done.
+    float* const vel_stage = stage + 3 * (size_t)n;
+    const unsigned blocks = (unsigned)((cnt + kIoBlock - 1) / kIoBlock);
+    VFS_CUDA_TRY(cudaEventRecord(io_ev[0], stream));
+    VFS_CUDA_TRY(cudaStreamWaitEvent(vel_stream, io_ev[0], 0));
+    VFS_CUDA_TRY(cudaMemcpyAsync(vel_stage, vel3, cnt * 12, cudaMemcpyHostToDevice, vel_stream));
+    k_expand_state<<<blocks, kIoBlock, 0, vel_stream>>>(sh.off + offset, (uint32_t)cnt, nullptr,
+                                                         vel_stage, pos[cur], vel[cur], aux);
+    VFS_CUDA_TRY(cudaGetLastError());
+    VFS_CUDA_TRY(cudaEventRecord(io_ev[1], vel_stream));
     return VFS_OK;
 }
 

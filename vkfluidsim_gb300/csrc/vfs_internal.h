@@ -181,13 +181,17 @@ size_t sort_scratch_words(const SortConfig& c);
 // Per-pass digit histograms of caller-provided keys.
 cudaError_t launch_digit_hist(const uint32_t* keys, uint32_t n, const SortConfig& sc,
                               uint32_t* ghist, cudaStream_t s);
-// Incremental sort, pass 1 (three launches: flags, tile scan, compaction): keys, moved flags
+// Incremental sort, pass 1 (flags, compaction, and a tile scan above 4M particles): keys, moved flags
 // (key != pkeys[i]) as a bitmask bits[0, W) with the moved count before each word in bits[W, 2W]
 // (W = ceil(n / 32)), the moved (key, index) pairs compacted in index order, their digit
-// histograms, and the moved count in scr.mcount.
+// histograms, and the moved count in scr.mcount. host3 (a single scene only): the positions are
+// read from that page-locked packed float3 array instead, and stored into pos_out (= pos) as the
+// state upload stores them (id = slot, the densities in aux zeroed).
 cudaError_t launch_keys_delta(const StepLaunch& L, const float4* pos, const uint32_t* pkeys,
                               uint32_t* mkeys, uint32_t* midx, uint32_t* bits,
-                              const SortConfig& sc, const SortScratch& scr, cudaStream_t s);
+                              const SortConfig& sc, const SortScratch& scr, cudaStream_t s,
+                              const float* host3 = nullptr, float4* pos_out = nullptr,
+                              float4* aux = nullptr);
 // Incremental sort, last pass: merge of the unmoved particles with the sorted moved ones into the
 // stable sort of all (key, index) pairs.
 cudaError_t launch_merge(uint32_t n, const uint32_t* pkeys, const uint32_t* bits,

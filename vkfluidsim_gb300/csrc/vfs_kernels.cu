@@ -1773,19 +1773,32 @@ __device__ __forceinline__ uint32_t particle_key(const StepLaunch& L, uint32_t i
                            p.mod_magic, p.n);
 }
 
-template <bool kBatch>
+// kHostIn (a single scene's host round trip): the positions come from page-locked host memory,
+// packed float3 in slot order (host3, its device address), and the kernel also stores them as the
+// model's positions (pos_out, id = slot) and zeroes the densities, as the state upload does; the
+// tile's 12 KB are read into shared memory with coalesced loads first.
+template <bool kBatch, bool kHostIn>
 __global__ void __launch_bounds__(256)
     k_keys_flags(StepLaunch L, const float4* __restrict__ pos, const uint32_t* __restrict__ pkeys,
                  uint32_t* __restrict__ bits, int passes, int digit_bits,
-                 uint32_t* __restrict__ ghist, uint32_t* __restrict__ tile_cnt) {
+                 uint32_t* __restrict__ ghist, uint32_t* __restrict__ tile_cnt,
+                 const float* __restrict__ host3, float4* __restrict__ pos_out,
+                 float4* __restrict__ aux) {
     __shared__ uint32_t s_h[kMaxSortPasses * kMaxSortBins];
     __shared__ uint32_t s_n[8];
+    __shared__ float s_p[kHostIn ? 3 * kDeltaTile : 1];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int bins = 1 << digit_bits;
     const uint32_t mask = (uint32_t)bins - 1u;
     for (int e = tid; e < passes * bins; e += 256) s_h[e] = 0u;
+    const uint32_t t0 = blockIdx.x * kDeltaTile;
+    if (kHostIn) {
+        const uint32_t m3 = 3u * min(kDeltaTile, L.total - t0);
+        const float* src = host3 + 3 * (size_t)t0;
+        for (uint32_t k = (uint32_t)tid; k < m3; k += 256u) s_p[k] = src[k];
+    }
     __syncthreads();
-    const uint32_t base = blockIdx.x * kDeltaTile + (uint32_t)tid;
+    const uint32_t base = t0 + (uint32_t)tid;
     const uint32_t W = (L.total + 31u) >> 5;
     // All of the thread's loads first (positions and previous keys), then the key arithmetic.
     float4 xs[kDeltaItems];
@@ -1794,7 +1807,14 @@ __global__ void __launch_bounds__(256)
     for (int k = 0; k < kDeltaItems; k++) {
         const uint32_t i = base + (uint32_t)k * 256u;
         if (i < L.total) {
-            xs[k] = __ldg(pos + i);
+            if (kHostIn) {
+                const uint32_t l = 3u * ((uint32_t)k * 256u + (uint32_t)tid);
+                xs[k] = make_float4(s_p[l], s_p[l + 1u], s_p[l + 2u], __uint_as_float(i));
+                pos_out[i] = xs[k];
+                aux[i].z = 0.0f;
+            } else {
+                xs[k] = __ldg(pos + i);
+            }
             pks[k] = __ldg(pkeys + i);
         }
     }
@@ -2069,15 +2089,19 @@ size_t sort_scratch_words(const SortConfig& c) {
 
 cudaError_t launch_keys_delta(const StepLaunch& L, const float4* pos, const uint32_t* pkeys,
                               uint32_t* mkeys, uint32_t* midx, uint32_t* bits,
-                              const SortConfig& sc, const SortScratch& scr, cudaStream_t s) {
+                              const SortConfig& sc, const SortScratch& scr, cudaStream_t s,
+                              const float* host3, float4* pos_out, float4* aux) {
     if (L.total == 0) return cudaSuccess;
     const uint32_t tiles = sc.delta_blocks, W = (L.total + 31u) >> 5;
     if (L.n_scenes > 1)
-        k_keys_flags<true><<<tiles, 256, 0, s>>>(L, pos, pkeys, bits, sc.passes, sc.digit_bits,
-                                                 scr.ghist, scr.dstatus);
+        k_keys_flags<true, false><<<tiles, 256, 0, s>>>(L, pos, pkeys, bits, sc.passes, sc.digit_bits,
+                                                        scr.ghist, scr.dstatus, nullptr, nullptr, nullptr);
+    else if (host3)
+        k_keys_flags<false, true><<<tiles, 256, 0, s>>>(L, pos, pkeys, bits, sc.passes, sc.digit_bits,
+                                                        scr.ghist, scr.dstatus, host3, pos_out, aux);
     else
-        k_keys_flags<false><<<tiles, 256, 0, s>>>(L, pos, pkeys, bits, sc.passes, sc.digit_bits,
-                                                  scr.ghist, scr.dstatus);
+        k_keys_flags<false, false><<<tiles, 256, 0, s>>>(L, pos, pkeys, bits, sc.passes, sc.digit_bits,
+                                                         scr.ghist, scr.dstatus, nullptr, nullptr, nullptr);
     if (tiles <= kFoldTiles) {
         if (L.n_scenes > 1)
             k_moved_compact<true, true><<<tiles, 256, 0, s>>>(L, pos, bits, scr.dstatus, mkeys, midx, scr.mcount);

@@ -81,6 +81,11 @@ struct Model {
     cudaEvent_t cells_wait = nullptr;  // set only while step_host enqueues its first substep
     cudaStream_t io_stream = nullptr;  // step_host's velocity upload (created on first use)
     cudaEvent_t io_ev[2] = {nullptr, nullptr};
+    // step_host with page-locked inputs: the next substep's key pass reads the positions from
+    // this device alias of the host array, and its velocity upload (from keys_host_vel) starts
+    // after that pass. Set by enqueue_set_state, taken by the next enqueue_substep.
+    const float* keys_host_pos = nullptr;
+    const float* keys_host_vel = nullptr;
     // step_host's one-substep round trip through page-locked buffers, captured once per set of
     // buffers (host pointers and their device aliases) and replayed.
     cudaGraphExec_t host_graph = nullptr;
@@ -120,6 +125,10 @@ struct Model {
     // set_state without the final wait (the conversion kernel may still be reading host memory).
     int enqueue_set_state(uint32_t scene, const float* pos3, const float* vel3, uint32_t offset,
                           int64_t count, cudaStream_t vel_stream = nullptr);
+    // The velocities' upload on vel_stream after the work queued on the model's stream so far:
+    // io_ev[0] there, the DMA into the staging buffer and the conversion, io_ev[1] when done.
+    int enqueue_vel_upload(const SceneHost& sh, uint32_t offset, uint64_t cnt, const float* vel3,
+                           cudaStream_t vel_stream);
     // set_state of every particle (when pos3 / vel3 are given), `count` substeps and get_state,
     // with one wait at the end; outputs in page-locked memory come from the last substep's
     // density pass (densities) and force pass (positions, velocities).
