@@ -419,7 +419,7 @@ int Model::enqueue_substep(cudaEvent_t* ev) {
     launch.defer_vel = false;
     if (cells_wait) {
         VFS_CUDA_TRY(cudaStreamWaitEvent(s, cells_wait, 0));
-        VFS_CUDA_TRY(launch_vel_records(n, sperm, vel[c], vel[o], aux, rec, s));
+        VFS_CUDA_TRY(launch_vel_records(n, sperm, stage + 3 * (size_t)n, vel[o], aux, rec, s));
     }
     if (ev) VFS_CUDA_TRY(cudaEventRecord(ev[5], s));
     VFS_CUDA_TRY(launch_force(launch, pos[o], vel[o], aux, rec, bnd, cell_scan, nbr, nbr_count, pos[c],
@@ -835,16 +835,14 @@ int Model::enqueue_set_state(uint32_t scene, const float* pos3, const float* vel
 
 int Model::enqueue_vel_upload(const SceneHost& sh, uint32_t offset, uint64_t cnt, const float* vel3,
                               cudaStream_t vel_stream) {
-    // By DMA (a copy engine, so the velocities move while the key, sort and later passes keep
-    // every SM busy), converted on the side stream; io_ev[1] marks them done.
+    // By DMA into the staging buffer (a copy engine, so the velocities move while the key, sort
+    // and later passes keep every SM busy); io_ev[1] marks them done. The substep's
+    // k_vel_records reads them there (packed float3 in slot order) by the sort's permutation.
     float* const vel_stage = stage + 3 * (size_t)n;
-    const unsigned blocks = (unsigned)((cnt + kIoBlock - 1) / kIoBlock);
     VFS_CUDA_TRY(cudaEventRecord(io_ev[0], stream));
     VFS_CUDA_TRY(cudaStreamWaitEvent(vel_stream, io_ev[0], 0));
-    VFS_CUDA_TRY(cudaMemcpyAsync(vel_stage, vel3, cnt * 12, cudaMemcpyHostToDevice, vel_stream));
-    k_expand_state<<<blocks, kIoBlock, 0, vel_stream>>>(sh.off + offset, (uint32_t)cnt, nullptr,
-                                                         vel_stage, pos[cur], vel[cur], aux);
-    VFS_CUDA_TRY(cudaGetLastError());
+    VFS_CUDA_TRY(cudaMemcpyAsync(vel_stage + 3 * ((size_t)sh.off + offset), vel3, cnt * 12,
+                                 cudaMemcpyHostToDevice, vel_stream));
     VFS_CUDA_TRY(cudaEventRecord(io_ev[1], vel_stream));
     return VFS_OK;
 }

@@ -212,9 +212,10 @@ cudaError_t launch_sort(uint32_t n, const SortConfig& sc, const SortScratch& scr
 // for the ids in x.w, and flags every scene of L with a particle that moved more than h skin / 2
 // since its list build.
 // The sorted velocities and the force records' velocity half of a substep whose cell and density
-// passes ran with StepLaunch::defer_vel: vel_out[i] = vel_in[perm[i]], rec[2i + 1] = (that
-// velocity, aux[i].y), the values those passes write otherwise.
-cudaError_t launch_vel_records(uint32_t n, const uint32_t* perm, const float4* vel_in,
+// passes ran with StepLaunch::defer_vel, from the uploaded velocities (packed float3 in slot
+// order, vel3): vel_out[i] = (vel3[perm[i]], 0), rec[2i + 1] = (that velocity, aux[i].y), the
+// values those passes write otherwise.
+cudaError_t launch_vel_records(uint32_t n, const uint32_t* perm, const float* vel3,
                                float4* vel_out, const float4* aux, float4* rec, cudaStream_t s);
 cudaError_t launch_cells_reorder(const StepLaunch& L, uint32_t n, const uint32_t* skeys, const uint32_t* perm,
                                  uint32_t* cell_scan, const float4* pos_in, const float4* vel_in,

@@ -2166,23 +2166,24 @@ cudaError_t launch_sort(uint32_t n, const SortConfig& sc, const SortScratch& scr
 
 namespace {
 __global__ void __launch_bounds__(256)
-    k_vel_records(uint32_t n, const uint32_t* __restrict__ perm, const float4* __restrict__ vel_in,
+    k_vel_records(uint32_t n, const uint32_t* __restrict__ perm, const float* __restrict__ vel3,
                   float4* __restrict__ vel_out, const float4* __restrict__ aux,
                   float4* __restrict__ rec) {
     const uint32_t i = blockIdx.x * 256u + threadIdx.x;
     if (i >= n) return;
     uint32_t src = perm[i];
     if (src >= n) src = i;  // only after a reported sort failure, as in the cell pass
-    const float4 v = __ldg(vel_in + src);
-    vel_out[i] = v;
-    rec[2 * (size_t)i + 1] = make_float4(v.x, v.y, v.z, __ldg(aux + i).y);
+    const float* v = vel3 + 3 * (size_t)src;
+    const float vx = __ldg(v), vy = __ldg(v + 1), vz = __ldg(v + 2);
+    vel_out[i] = make_float4(vx, vy, vz, 0.0f);
+    rec[2 * (size_t)i + 1] = make_float4(vx, vy, vz, __ldg(aux + i).y);
 }
 }  // namespace
 
-cudaError_t launch_vel_records(uint32_t n, const uint32_t* perm, const float4* vel_in,
+cudaError_t launch_vel_records(uint32_t n, const uint32_t* perm, const float* vel3,
                                float4* vel_out, const float4* aux, float4* rec, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
-    k_vel_records<<<(n + 255u) / 256u, 256, 0, s>>>(n, perm, vel_in, vel_out, aux, rec);
+    k_vel_records<<<(n + 255u) / 256u, 256, 0, s>>>(n, perm, vel3, vel_out, aux, rec);
     return cudaGetLastError();
 }
 
