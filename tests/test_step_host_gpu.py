@@ -61,6 +61,31 @@ def test_step_host_on_the_1m_scene_with_its_lists():
     assert fused.skin_builds() > 0
 
 
+def test_round_trips_of_the_models_own_state_keep_its_skin_lists():
+    """A frame loop that uploads the model's own state every substep renumbers the ids to the
+    slots each time (SetParticleState sets ids to offset + i), while the sort has moved particles
+    between slots. A whole-scene upload moves each slot's build index to the slot's new id, so
+    the skin lists stay in use and the loop steps exactly like plain substeps: a round trip that
+    fell back to the bucket walk would sum in another order and differ in the last bits."""
+    w = W.obstacle_1m()
+    plain, looped = W.build_model(w), W.build_model(w)
+    for m in (plain, looped):
+        m.substeps(120)  # falling at ~0.12 m/s: particles cross cells every substep
+    s = looped.copy_data_buffers()
+    n = w.n
+    bufs = {"positions": _pinned((n, 3)), "velocities": _pinned((n, 3)), "densities": _pinned((n,))}
+    bufs["positions"][:] = s["positions"]
+    bufs["velocities"][:] = s["velocities"]
+    b0, b1 = plain.skin_builds(), looped.skin_builds()
+    for _ in range(8):
+        plain.substeps(1)
+        looped.step_host(bufs["positions"], bufs["velocities"], 1, out=bufs)
+    a = plain.copy_data_buffers()
+    for k in ("positions", "velocities", "densities"):
+        assert np.array_equal(a[k], bufs[k]), k
+    assert plain.skin_builds() - b0 == looped.skin_builds() - b1
+
+
 def test_step_host_on_a_small_model():
     # 32,768 particles: the three-lane density pass; the force pass is the same kernel.
     w = W.dam_break_32k()

@@ -53,11 +53,15 @@ constexpr uint32_t kIoBlock = 256;
 // device's address space, or a device staging copy) to the float4 state. A block moves its
 // 256 records through shared memory, so every warp reads 128 contiguous bytes. Positions (with
 // the ids and the zeroed densities) and velocities are converted when their source is given, so
-// the two halves can run on different streams.
+// the two halves can run on different streams. With b_next (an upload of a whole scene while
+// every id is a different slot's), the build index of the particle each slot held is stored
+// under the slot's new id, read before the slot is overwritten.
 __global__ void __launch_bounds__(kIoBlock)
     k_expand_state(uint32_t offset, uint32_t count, const float* __restrict__ pos3,
                    const float* __restrict__ vel3, float4* __restrict__ pos,
-                   float4* __restrict__ vel, float4* __restrict__ aux) {
+                   float4* __restrict__ vel, float4* __restrict__ aux,
+                   const uint32_t* __restrict__ b_of_id, uint32_t* __restrict__ b_next,
+                   uint32_t n_ids) {
     __shared__ float s_p[3 * kIoBlock], s_v[3 * kIoBlock];
     const uint32_t base = blockIdx.x * kIoBlock, t = threadIdx.x;
     const uint32_t m = min(kIoBlock, count - base);
@@ -70,6 +74,10 @@ __global__ void __launch_bounds__(kIoBlock)
     if (t >= m) return;
     const uint32_t d = offset + base + t;
     if (pos3) {
+        if (b_next) {
+            const uint32_t old = __float_as_uint(pos[d].w);
+            b_next[d] = old < n_ids ? b_of_id[old] : 0u;
+        }
         pos[d] = make_float4(s_p[3 * t], s_p[3 * t + 1], s_p[3 * t + 2], __uint_as_float(d));
         aux[d].z = 0.0f;  // SetParticleState zeroes the densities it covers (model.cpp:146)
     }
@@ -381,7 +389,9 @@ int Model::enqueue_substep(cudaEvent_t* ev) {
     // pass itself, the velocities' upload queued behind it. Taken here, whatever returns below.
     const float* host_pos = keys_host_pos;
     const float* host_vel = keys_host_vel;
+    uint32_t* const host_b_next = host_pos && keys_host_remap ? skin.b_next : nullptr;
     keys_host_pos = keys_host_vel = nullptr;
+    keys_host_remap = false;
     if (ev) VFS_CUDA_TRY(cudaEventRecord(ev[0], s));
     // The sort scratch is zero here: zeroed when allocated and by every substep's cell pass.
     if (ev) VFS_CUDA_TRY(cudaEventRecord(ev[1], s));
@@ -389,9 +399,11 @@ int Model::enqueue_substep(cudaEvent_t* ev) {
     // a sort of those alone (count on the device), a merge with the rest.
     const SkinLists sk = active_skin();
     VFS_CUDA_TRY(launch_keys_delta(launch, pos[c], pkeys, keys, vals, moved, sc, sort_scratch, s,
-                                   host_pos, pos[c], aux));
+                                   host_pos, pos[c], aux, skin.b_of_id, host_b_next));
     if (host_pos) {
-        const int rc = enqueue_vel_upload(scenes[0], 0, n, host_vel, io_stream);
+        int rc = move_build_indices(host_b_next, 0, n);
+        if (rc) return rc;
+        rc = enqueue_vel_upload(scenes[0], 0, n, host_vel, io_stream);
         if (rc) return rc;
     }
     if (ev) VFS_CUDA_TRY(cudaEventRecord(ev[2], s));
@@ -500,6 +512,7 @@ Model::~Model() {
     cudaFree(skin.count);
     cudaFree(skin.x_build);
     cudaFree(skin.b_of_id);
+    cudaFree(skin.b_next);
     cudaFree(skin.xcur);
     cudaFree(skin.stale);
     cudaFree(skin.ctl);
@@ -605,7 +618,7 @@ int Model::init() {
     return refresh_params();
 }
 
-// Candidate lists with a skin, 224 bytes per particle. Three-lane (small) models do not use them,
+// Candidate lists with a skin, 228 bytes per particle. Three-lane (small) models do not use them,
 // and a model too large for them on this device runs without (every particle walks its buckets).
 int Model::alloc_skin() {
     if (n == 0 || planes_mode(n)) return VFS_OK;
@@ -616,6 +629,7 @@ int Model::alloc_skin() {
         cudaMalloc(&s.count, N * sizeof(uint32_t)) != cudaSuccess ||
         cudaMalloc(&s.x_build, N * sizeof(float4)) != cudaSuccess ||
         cudaMalloc(&s.b_of_id, N * sizeof(uint32_t)) != cudaSuccess ||
+        cudaMalloc(&s.b_next, N * sizeof(uint32_t)) != cudaSuccess ||
         cudaMalloc(&s.xcur, N * sizeof(float4)) != cudaSuccess ||
         cudaMalloc(&s.stale, scenes.size() * sizeof(uint32_t)) != cudaSuccess ||
         cudaMalloc(&s.ctl, scenes.size() * kSkinCtl * sizeof(uint32_t)) != cudaSuccess ||
@@ -627,6 +641,7 @@ int Model::alloc_skin() {
         cudaFree(s.count);
         cudaFree(s.x_build);
         cudaFree(s.b_of_id);
+        cudaFree(s.b_next);
         cudaFree(s.xcur);
         cudaFree(s.stale);
         cudaFree(s.ctl);
@@ -799,6 +814,13 @@ int Model::enqueue_set_state(uint32_t scene, const float* pos3, const float* vel
         return fail(VFS_ERR_CAPACITY, "offset + count exceeds the scene's particle count");
     if (cnt == 0) return VFS_OK;
     if (!pos3 || !vel3) return fail(VFS_ERR_INVALID_ARGUMENT, "pos and vel must not be NULL");
+    // The skin lists across the upload (see ids_unique): a whole scene's build indices follow
+    // its slots to their new ids; after part of a scene ids may repeat, and nothing is moved
+    // (the cell pass's displacement check then finds the lists stale).
+    const bool whole = offset == 0 && cnt == sh.n;
+    uint32_t* const b_next = whole && ids_unique ? skin.b_next : nullptr;
+    if (!whole) ids_unique = false;
+    else if (scenes.size() == 1) ids_unique = true;
     // Page-locked inputs are read by the conversion kernel itself (over NVLink-C2C on GB300);
     // pageable ones are copied into the staging buffer first.
     const float* sp = static_cast<const float*>(device_alias(pos3));
@@ -815,21 +837,35 @@ int Model::enqueue_set_state(uint32_t scene, const float* pos3, const float* vel
             sv = vel_stage;
         }
         k_expand_state<<<blocks, kIoBlock, 0, stream>>>(sh.off + offset, (uint32_t)cnt, sp, sv,
-                                                         pos[cur], vel[cur], aux);
-    } else if (sp != stage && scenes.size() == 1 && offset == 0 && cnt == sh.n) {
+                                                         pos[cur], vel[cur], aux, skin.b_of_id,
+                                                         b_next, n);
+        VFS_CUDA_TRY(cudaGetLastError());
+        return move_build_indices(b_next, sh.off, cnt);
+    } else if (sp != stage && scenes.size() == 1 && whole) {
         // Positions first, alone on the host link, read by the next substep's key pass itself
         // (the upload and the key arithmetic overlap); the velocities follow after that pass.
         keys_host_pos = sp;
         keys_host_vel = vel3;
+        keys_host_remap = b_next != nullptr;
         return VFS_OK;
     } else {
         // Positions first, alone on the host link; the velocities follow on the side stream.
         k_expand_state<<<blocks, kIoBlock, 0, stream>>>(sh.off + offset, (uint32_t)cnt, sp, nullptr,
-                                                         pos[cur], vel[cur], aux);
+                                                         pos[cur], vel[cur], aux, skin.b_of_id,
+                                                         b_next, n);
         VFS_CUDA_TRY(cudaGetLastError());
+        const int rc = move_build_indices(b_next, sh.off, cnt);
+        if (rc) return rc;
         return enqueue_vel_upload(sh, offset, cnt, vel3, vel_stream);
     }
-    VFS_CUDA_TRY(cudaGetLastError());
+}
+
+// The build indices an upload stored under the new ids of slots [off, off + cnt) (b_next, or
+// nothing to do when null) replace the old mapping there.
+int Model::move_build_indices(const uint32_t* b_next, uint32_t off, uint64_t cnt) {
+    if (!b_next || cnt == 0) return VFS_OK;
+    VFS_CUDA_TRY(cudaMemcpyAsync(skin.b_of_id + off, b_next + off, cnt * sizeof(uint32_t),
+                                 cudaMemcpyDeviceToDevice, stream));
     return VFS_OK;
 }
 

@@ -143,6 +143,8 @@ struct SkinLists {
     uint32_t* count = nullptr;    // per build index: list length, kSkinUsable when it can be summed
     float4* x_build = nullptr;    // per build index: position at the last build
     uint32_t* b_of_id = nullptr;  // per id: build index
+    uint32_t* b_next = nullptr;   // a whole-scene upload's b_of_id under the new ids (id = slot:
+                                  // the build index of the particle the slot held), copied back
     float4* xcur = nullptr;       // per build index: current position (x, y, z) and current sorted
                                   // index (w, as bits), written by the cell pass
     uint32_t* stale = nullptr;    // per scene: nonzero when some particle moved past h skin / 2
@@ -186,12 +188,14 @@ cudaError_t launch_digit_hist(const uint32_t* keys, uint32_t n, const SortConfig
 // (W = ceil(n / 32)), the moved (key, index) pairs compacted in index order, their digit
 // histograms, and the moved count in scr.mcount. host3 (a single scene only): the positions are
 // read from that page-locked packed float3 array instead, and stored into pos_out (= pos) as the
-// state upload stores them (id = slot, the densities in aux zeroed).
+// state upload stores them (id = slot, the densities in aux zeroed; with b_next, each slot's
+// old id's build index stored under its new id, b_next[slot] = b_of_id[old id]).
 cudaError_t launch_keys_delta(const StepLaunch& L, const float4* pos, const uint32_t* pkeys,
                               uint32_t* mkeys, uint32_t* midx, uint32_t* bits,
                               const SortConfig& sc, const SortScratch& scr, cudaStream_t s,
                               const float* host3 = nullptr, float4* pos_out = nullptr,
-                              float4* aux = nullptr);
+                              float4* aux = nullptr, const uint32_t* b_of_id = nullptr,
+                              uint32_t* b_next = nullptr);
 // Incremental sort, last pass: merge of the unmoved particles with the sorted moved ones into the
 // stable sort of all (key, index) pairs.
 cudaError_t launch_merge(uint32_t n, const uint32_t* pkeys, const uint32_t* bits,

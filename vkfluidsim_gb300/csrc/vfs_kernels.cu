@@ -1775,15 +1775,17 @@ __device__ __forceinline__ uint32_t particle_key(const StepLaunch& L, uint32_t i
 
 // kHostIn (a single scene's host round trip): the positions come from page-locked host memory,
 // packed float3 in slot order (host3, its device address), and the kernel also stores them as the
-// model's positions (pos_out, id = slot) and zeroes the densities, as the state upload does; the
-// tile's 12 KB are read into shared memory with coalesced loads first.
+// model's positions (pos_out, id = slot) and zeroes the densities, as the state upload does (with
+// b_next, the build index under each slot's old id is stored under its new id first); the tile's
+// 12 KB are read into shared memory with coalesced loads first.
 template <bool kBatch, bool kHostIn>
 __global__ void __launch_bounds__(256)
     k_keys_flags(StepLaunch L, const float4* __restrict__ pos, const uint32_t* __restrict__ pkeys,
                  uint32_t* __restrict__ bits, int passes, int digit_bits,
                  uint32_t* __restrict__ ghist, uint32_t* __restrict__ tile_cnt,
                  const float* __restrict__ host3, float4* __restrict__ pos_out,
-                 float4* __restrict__ aux) {
+                 float4* __restrict__ aux, const uint32_t* __restrict__ b_of_id,
+                 uint32_t* __restrict__ b_next) {
     __shared__ uint32_t s_h[kMaxSortPasses * kMaxSortBins];
     __shared__ uint32_t s_n[8];
     __shared__ float s_p[kHostIn ? 3 * kDeltaTile : 1];
@@ -1810,6 +1812,10 @@ __global__ void __launch_bounds__(256)
             if (kHostIn) {
                 const uint32_t l = 3u * ((uint32_t)k * 256u + (uint32_t)tid);
                 xs[k] = make_float4(s_p[l], s_p[l + 1u], s_p[l + 2u], __uint_as_float(i));
+                if (b_next) {
+                    const uint32_t old = __float_as_uint(pos_out[i].w);
+                    b_next[i] = old < L.total ? b_of_id[old] : 0u;
+                }
                 pos_out[i] = xs[k];
                 aux[i].z = 0.0f;
             } else {
@@ -2090,18 +2096,22 @@ size_t sort_scratch_words(const SortConfig& c) {
 cudaError_t launch_keys_delta(const StepLaunch& L, const float4* pos, const uint32_t* pkeys,
                               uint32_t* mkeys, uint32_t* midx, uint32_t* bits,
                               const SortConfig& sc, const SortScratch& scr, cudaStream_t s,
-                              const float* host3, float4* pos_out, float4* aux) {
+                              const float* host3, float4* pos_out, float4* aux,
+                              const uint32_t* b_of_id, uint32_t* b_next) {
     if (L.total == 0) return cudaSuccess;
     const uint32_t tiles = sc.delta_blocks, W = (L.total + 31u) >> 5;
     if (L.n_scenes > 1)
         k_keys_flags<true, false><<<tiles, 256, 0, s>>>(L, pos, pkeys, bits, sc.passes, sc.digit_bits,
-                                                        scr.ghist, scr.dstatus, nullptr, nullptr, nullptr);
+                                                        scr.ghist, scr.dstatus, nullptr, nullptr, nullptr,
+                                                        nullptr, nullptr);
     else if (host3)
         k_keys_flags<false, true><<<tiles, 256, 0, s>>>(L, pos, pkeys, bits, sc.passes, sc.digit_bits,
-                                                        scr.ghist, scr.dstatus, host3, pos_out, aux);
+                                                        scr.ghist, scr.dstatus, host3, pos_out, aux,
+                                                        b_of_id, b_next);
     else
         k_keys_flags<false, false><<<tiles, 256, 0, s>>>(L, pos, pkeys, bits, sc.passes, sc.digit_bits,
-                                                         scr.ghist, scr.dstatus, nullptr, nullptr, nullptr);
+                                                         scr.ghist, scr.dstatus, nullptr, nullptr, nullptr,
+                                                         nullptr, nullptr);
     if (tiles <= kFoldTiles) {
         if (L.n_scenes > 1)
             k_moved_compact<true, true><<<tiles, 256, 0, s>>>(L, pos, bits, scr.dstatus, mkeys, midx, scr.mcount);

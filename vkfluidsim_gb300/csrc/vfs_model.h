@@ -71,6 +71,10 @@ struct Model {
     uint32_t* nbr_count = nullptr;  // list length per particle
     SkinLists skin{};               // candidate lists with a skin (absent in three-lane mode)
     float skin_fraction = 0.05f;    // skin / h; 0 turns the lists off
+    // Every id is a different slot's (true from creation; an upload of part of a scene can
+    // repeat ids). While it holds, an upload of a whole scene moves each slot's build index to
+    // the slot's new id, so a host round trip of the model's own state keeps its skin lists.
+    bool ids_unique = true;
     float* stage = nullptr;         // 32 bytes per particle of host-transfer staging
     uint32_t* scratch = nullptr;
     size_t scratch_words = 0;
@@ -86,6 +90,7 @@ struct Model {
     // after that pass. Set by enqueue_set_state, taken by the next enqueue_substep.
     const float* keys_host_pos = nullptr;
     const float* keys_host_vel = nullptr;
+    bool keys_host_remap = false;  // that pass also moves the build indices (skin.b_next)
     // step_host's one-substep round trip through page-locked buffers, captured once per set of
     // buffers (host pointers and their device aliases) and replayed.
     cudaGraphExec_t host_graph = nullptr;
@@ -129,6 +134,7 @@ struct Model {
     // io_ev[0] there, the DMA into the staging buffer and the conversion, io_ev[1] when done.
     int enqueue_vel_upload(const SceneHost& sh, uint32_t offset, uint64_t cnt, const float* vel3,
                            cudaStream_t vel_stream);
+    int move_build_indices(const uint32_t* b_next, uint32_t off, uint64_t cnt);
     // set_state of every particle (when pos3 / vel3 are given), `count` substeps and get_state,
     // with one wait at the end; outputs in page-locked memory come from the last substep's
     // density pass (densities) and force pass (positions, velocities).
