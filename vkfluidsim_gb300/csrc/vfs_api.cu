@@ -733,9 +733,12 @@ int Model::step_host(const float* pos3, const float* vel3, int32_t count, float*
     if (fused && count == 1 && in_p && in_v && use_graph) {
         // The frame loop's case: one substep between a page-locked upload and read-back. The
         // sequence below (the upload, the velocities on the side stream, the substep with its
-        // host outputs) is captured once for this set of buffers and replayed as one graph.
-        const void* key[10] = {pos3, vel3, pos_out, vel_out, dens_out, in_p, in_v,
-                               ho.pos3, ho.vel3, ho.dens};
+        // host outputs) is captured once for this set of buffers and replayed as one graph. The
+        // graph either moves the build indices with the upload or not (ids_unique at capture),
+        // so a change of ids_unique captures again.
+        const void* key[11] = {pos3, vel3, pos_out, vel_out, dens_out, in_p, in_v,
+                               ho.pos3, ho.vel3, ho.dens,
+                               reinterpret_cast<const void*>((uintptr_t)ids_unique)};
         if (!host_graph || std::memcmp(key, host_graph_key, sizeof key) != 0) {
             if (host_graph) cudaGraphExecDestroy(host_graph);
             host_graph = nullptr;
@@ -766,6 +769,7 @@ int Model::step_host(const float* pos3, const float* vel3, int32_t count, float*
             std::memcpy(host_graph_key, key, sizeof key);
         }
         VFS_CUDA_TRY(cudaGraphLaunch(host_graph, stream));
+        ids_unique = true;  // the replayed upload set every id to its slot
         stepped = true;
         substeps_done += 1;
         return check_device();

@@ -94,7 +94,7 @@ struct Model {
     // step_host's one-substep round trip through page-locked buffers, captured once per set of
     // buffers (host pointers and their device aliases) and replayed.
     cudaGraphExec_t host_graph = nullptr;
-    const void* host_graph_key[10] = {};
+    const void* host_graph_key[11] = {};
     SceneParams* d_scenes = nullptr;   // batched launches: the scene table
     uint16_t* d_scene_of = nullptr;    // batched launches: scene id per particle
     DevObject* d_objects = nullptr;    // boundary objects of all scenes
