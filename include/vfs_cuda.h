@@ -158,7 +158,9 @@ int vfs_model_get_boundary_object(const vfs_model* m, uint32_t idx, vfs_boundary
 
 /* SetParticleState (src/models/model.h:77-81, model.cpp:139-147): writes count particles at
  * offset (count < 0: all from offset); densities of those particles are zeroed. ids are set to
- * offset + i. */
+ * offset + i. An upload of every particle keeps the model's candidate lists usable when the
+ * particles stay near the positions the slots held (a host round trip of the model's own
+ * state); an upload of part of the scene leaves them to be rebuilt. */
 int vfs_model_set_particle_state(vfs_model* m, const float* pos, const float* vel,
                                  uint32_t offset, int64_t count);
 /* SetParticlesInBox in Compact mode (src/models/model.cpp:117-137, 35-66): a lattice with
